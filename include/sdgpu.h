@@ -1,0 +1,181 @@
+/*
+ * sdgpu.h -- C ABI of libsdgpu.so, the GB300 (sm_103a) implementation of the
+ * blocked exact k-nearest-neighbour path of the R package sparseDist
+ * (gambalab/sparseDist): the column-pair distance slabs, the per-column
+ * top-k, the running per-row top-k, the SNN overlap weights and the SNN graph.
+ *
+ * Conventions
+ *  - Every entry point is extern "C", never throws, and returns an int status
+ *    (SDG_OK == 0).  sdg_last_error() returns the message of the calling
+ *    thread's last failure; messages reproduce the reference's error text.
+ *  - Sparse inputs are borrowed host pointers to the slots of an R dgCMatrix
+ *    (sdg_csc): p has ncol+1 entries, i / x have p[ncol] entries, row indices
+ *    ascending within each column.  Observations are the COLUMNS.
+ *  - Outputs are caller-allocated, column-major (R's layout): an n x k matrix
+ *    stores element (row r, column t) at [t * n + r].  Indices are 1-based.
+ *    Empty slots hold NA: INT32_MIN for indices (R's NA_integer_) and the bit
+ *    pattern 0x7FF00000000007A2 for values (R's NA_real_).
+ *  - `ncores` and `block_size` are validated exactly as the reference does and
+ *    never change a result; the GPU does not use them.
+ *  - Methods: see sdg_method.  "jaccard" is the caller's alias of SDG_BINARY.
+ *
+ * Each function's comment names the reference interface it replaces.
+ */
+#ifndef SDGPU_H
+#define SDGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+#define SDG_EXTERN extern "C"
+#else
+#define SDG_EXTERN extern
+#endif
+#define SDG_API SDG_EXTERN __attribute__((visibility("default")))
+
+typedef enum {
+  SDG_BINARY = 0,     /* Jaccard on the sparsity pattern */
+  SDG_COSINE = 1,
+  SDG_EUCLIDEAN = 2,
+  SDG_MANHATTAN = 3,
+  SDG_PEARSON = 4,
+  SDG_JS = 5          /* Jensen-Shannon distance sqrt(JSD) */
+} sdg_method;
+
+typedef enum {
+  SDG_OK = 0,
+  SDG_E_ARG = -1,          /* invalid argument (reference's validation text) */
+  SDG_E_NONFINITE = -2,    /* cosine / js input not finite (or js negative) */
+  SDG_E_ROWS = -3,         /* row dimensions differ */
+  SDG_E_NOCAND = -4,       /* "No candidate neighbours available." */
+  SDG_E_NOMEM = -5,        /* device or host allocation failed */
+  SDG_E_INDEX = -6,        /* SNN index out of range */
+  SDG_E_CUDA = -7,         /* CUDA runtime error */
+  SDG_E_UNSUPPORTED = -8,  /* outside this build's limits (message says which) */
+  SDG_E_CANCELLED = -9     /* sdg_ctx_cancel() was called */
+} sdg_status;
+
+/* Bits of *flags: the reference's k-clamp warnings ("k (K) exceeds the N
+ * available neighbours; returning N."), reported instead of printed. */
+enum { SDG_WARN_CLAMP_FWD = 1, SDG_WARN_CLAMP_REV = 2 };
+
+typedef struct {
+  int32_t nrow, ncol;
+  const int32_t* p;   /* ncol + 1 */
+  const int32_t* i;   /* p[ncol] */
+  const double* x;    /* p[ncol] */
+} sdg_csc;
+
+typedef struct sdg_ctx sdg_ctx;
+
+/* ---- context ------------------------------------------------------------ */
+
+/* Library version as 10000*major + 100*minor + patch. */
+SDG_API int sdg_version(void);
+
+/* Copies the calling thread's last error message into buf (NUL-terminated,
+ * truncated to len) and returns its full length. */
+SDG_API int sdg_last_error(char* buf, size_t len);
+
+/* One context per (thread, device): owns a CUDA stream and the device memory
+ * of in-flight work.  device < 0 selects the current device. */
+SDG_API int sdg_ctx_create(int device, sdg_ctx** out);
+SDG_API int sdg_ctx_destroy(sdg_ctx* ctx);
+
+/* Asks running work on ctx to stop at its next query tile; the call then
+ * returns SDG_E_CANCELLED.  Safe to call from another thread (this is what
+ * R_CheckUserInterrupt maps onto).  Cleared by sdg_ctx_reset_cancel(). */
+SDG_API int sdg_ctx_cancel(sdg_ctx* ctx);
+SDG_API int sdg_ctx_reset_cancel(sdg_ctx* ctx);
+
+/* ---- the reference's .Call kernels, one for one --------------------------- */
+
+/* Distance / similarity slab between the columns of m and m2:
+ * D is ncol(m) x ncol(m2), D(i, j) = method(column i of m, column j of m2).
+ * Replaces fastJacc2 / fastCosine2 / fastEuclidean2 / fastManhattan2 /
+ * fastCorr2 / fastJS2 (src/sparseDist.cpp:559, :967, :833, :734, :403, :1074;
+ * .Call stubs R/RcppExports.R:29-67).  dist selects 1 - similarity for
+ * binary / cosine / pearson and must be 1 for the other methods' kernels
+ * (which ignore it, as the reference does). */
+SDG_API int sdg_dist_cross(sdg_ctx* ctx, int method, int dist, const sdg_csc* m,
+                           const sdg_csc* m2, double* D);
+
+/* Per-column top-k of a dense block D (nrow x ncol, column-major).
+ * idx / dist are ncol x k.  self_row[b] is 0 or the 1-based row excluded for
+ * column b.  Replaces topKBlock (src/topK.cpp:66-149, R/RcppExports.R:77-79). */
+SDG_API int sdg_topk_block(sdg_ctx* ctx, const double* D, int64_t nrow, int64_t ncol,
+                           int k, int decreasing, const int32_t* self_row,
+                           int32_t* idx, double* dist);
+
+/* Folds block D (query columns col_offset .. col_offset+ncol-1, 0-based) into
+ * the running per-row top-k best_idx / best_val (nrow x k, updated in place).
+ * self_col[i] is 0 or the 1-based global query index excluded for row i.
+ * Replaces topKRowsAccum (src/topKRows.cpp:103-248, R/RcppExports.R:81-83). */
+SDG_API int sdg_topk_rows_accum(sdg_ctx* ctx, const double* D, int64_t nrow, int64_t ncol,
+                                int k, int decreasing, int32_t* best_idx, double* best_val,
+                                int32_t col_offset, const int32_t* self_col);
+
+/* Jaccard overlap of kNN neighbour sets: w (n x k) aligned with idx (n x k,
+ * 1-based, NA padded).  Replaces snnJaccard (src/snn.cpp:197-250,
+ * R/RcppExports.R:13-15). */
+SDG_API int sdg_snn_jaccard(sdg_ctx* ctx, const int32_t* idx, int32_t n, int32_t k,
+                            int include_self, double* w);
+
+/* ---- the fused paths (the R block loops move onto the GPU) ----------------- */
+
+/* sparseKNN(X, Y, k, method, dist, include_self, drop_degenerate, block_size):
+ * Y == NULL is the self-search.  idx / dist must hold ncol(X) * k values; the
+ * result is ncol(X) x k_eff with k_eff = *k_eff <= k after the reference's
+ * clamp (SDG_WARN_CLAMP_FWD set in *flags when it applied).  Replaces the
+ * block loop of R/sparseKNN.R:110-313 (slab .Call + topKBlock .Call per
+ * block). */
+SDG_API int sdg_knn(sdg_ctx* ctx, const sdg_csc* X, const sdg_csc* Y, int method, int dist,
+                    int k, int include_self, int drop_degenerate, int block_size, int ncores,
+                    int32_t* idx, double* dist_out, int* k_eff, int* flags);
+
+/* sparseKNNCross(X, Y, k, ...): forward (ncol(X) x k_fwd, indices into Y) and
+ * reverse (ncol(Y) x k_rev, indices into X), each clamped independently.
+ * fwd_* hold ncol(X) * k and rev_* hold ncol(Y) * k values.  Replaces
+ * R/sparseKNNCross.R:44-199 (slab + topKBlock + topKRowsAccum per block). */
+SDG_API int sdg_knn_cross(sdg_ctx* ctx, const sdg_csc* X, const sdg_csc* Y, int method,
+                          int dist, int k, int drop_degenerate, int block_size, int ncores,
+                          int32_t* fwd_idx, double* fwd_dist, int32_t* rev_idx,
+                          double* rev_dist, int* k_fwd, int* k_rev, int* flags);
+
+/* sparseSNN(idx, include_self, prune, symmetrise, edges = "knn") as the slots
+ * of the n x n dgCMatrix.  Call once with p == NULL to learn *nnz, then with
+ * p (n + 1), i and x (nnz each).  Replaces snnJaccard plus the Matrix
+ * assembly of R/sparseSNN.R:221-250. */
+SDG_API int sdg_snn_graph(sdg_ctx* ctx, const int32_t* idx, int32_t n, int32_t k,
+                          int include_self, double prune, int symmetrise, int64_t* nnz,
+                          int32_t* p, int32_t* i, double* x);
+
+/* ---- device-resident inputs (serving / batching) ---------------------------- */
+
+/* A CSC matrix uploaded once and kept in device memory, with its per-column
+ * data (norms, unit values, masks) computed on first use. */
+typedef struct sdg_matrix sdg_matrix;
+SDG_API int sdg_matrix_upload(sdg_ctx* ctx, const sdg_csc* M, sdg_matrix** out);
+SDG_API int sdg_matrix_free(sdg_matrix* M);
+
+/* sdg_knn over resident matrices; results are written to host buffers. */
+SDG_API int sdg_knn_resident(sdg_ctx* ctx, const sdg_matrix* X, const sdg_matrix* Y,
+                             int method, int dist, int k, int include_self,
+                             int drop_degenerate, int32_t* idx, double* dist_out,
+                             int* k_eff, int* flags);
+
+/* Statistics of the last sdg_knn* call on ctx (for profiling and tests):
+ * out[0] = pairs screened, out[1] = pairs re-ranked exactly, out[2] = queries
+ * whose candidate buffer overflowed (finished by the exact path), out[3] =
+ * kernels launched, out[4] = screening kernel time in microseconds (device
+ * events), out[5] = total device time in microseconds. */
+SDG_API int sdg_last_stats(sdg_ctx* ctx, int64_t* out, int n);
+
+/* Selects the candidate-generation engine for subsequent calls on ctx:
+ * 0 = automatic, 1 = exact FP64 slab for every pair, 2 = screened (FP32 /
+ * integer screen, exact FP64 re-rank).  Results are identical; only speed
+ * differs.  Used by tests to cross-check the two engines. */
+SDG_API int sdg_ctx_set_engine(sdg_ctx* ctx, int engine);
+
+#endif

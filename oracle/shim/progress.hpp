@@ -1,0 +1,2 @@
+// progress.hpp -- forwards to the project-written API shim (test infrastructure only).
+#include "sdg_shim.hpp"

@@ -1,0 +1,167 @@
+"""ctypes binding of libsdgpu.so (the C ABI declared in include/sdgpu.h).
+
+The library is the only compute path: if it is missing, or no CUDA device is
+present, every call raises; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsdgpu.so")
+
+SDG_OK = 0
+STATUS_NAMES = {-1: "SDG_E_ARG", -2: "SDG_E_NONFINITE", -3: "SDG_E_ROWS", -4: "SDG_E_NOCAND",
+                -5: "SDG_E_NOMEM", -6: "SDG_E_INDEX", -7: "SDG_E_CUDA", -8: "SDG_E_UNSUPPORTED",
+                -9: "SDG_E_CANCELLED"}
+WARN_CLAMP_FWD = 1
+WARN_CLAMP_REV = 2
+
+NA_INTEGER = np.int32(-(2 ** 31))
+NA_REAL_BITS = np.uint64(0x7FF00000000007A2)
+
+EXPORTED = ["sdg_version", "sdg_last_error", "sdg_ctx_create", "sdg_ctx_destroy", "sdg_ctx_cancel",
+            "sdg_ctx_reset_cancel", "sdg_dist_cross", "sdg_topk_block", "sdg_topk_rows_accum",
+            "sdg_snn_jaccard", "sdg_knn", "sdg_knn_cross", "sdg_snn_graph", "sdg_matrix_upload",
+            "sdg_matrix_free", "sdg_knn_resident", "sdg_last_stats", "sdg_ctx_set_engine"]
+
+
+class SdgError(RuntimeError):
+    """A failure reported by libsdgpu.so; ``code`` is the sdg_status value."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(message)
+        self.code = code
+        self.status = STATUS_NAMES.get(code, str(code))
+
+
+class CSC(C.Structure):
+    _fields_ = [("nrow", C.c_int32), ("ncol", C.c_int32),
+                ("p", C.POINTER(C.c_int32)), ("i", C.POINTER(C.c_int32)),
+                ("x", C.POINTER(C.c_double))]
+
+
+_lib = None
+_lib_lock = threading.Lock()
+
+
+def load() -> C.CDLL:
+    """Loads libsdgpu.so; raises if it has not been built."""
+    global _lib
+    with _lib_lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise ImportError("libsdgpu.so is not built (run `python -m sparsedist_gb300.build`); "
+                                  "there is no CPU fallback")
+            lib = C.CDLL(LIB_PATH)
+            v = C.c_void_p
+            lib.sdg_last_error.argtypes = [C.c_char_p, C.c_size_t]
+            lib.sdg_ctx_create.argtypes = [C.c_int, C.POINTER(v)]
+            lib.sdg_ctx_destroy.argtypes = [v]
+            lib.sdg_ctx_cancel.argtypes = [v]
+            lib.sdg_ctx_reset_cancel.argtypes = [v]
+            lib.sdg_ctx_set_engine.argtypes = [v, C.c_int]
+            lib.sdg_last_stats.argtypes = [v, v, C.c_int]
+            lib.sdg_dist_cross.argtypes = [v, C.c_int, C.c_int, v, v, v]
+            lib.sdg_topk_block.argtypes = [v, v, C.c_int64, C.c_int64, C.c_int, C.c_int, v, v, v]
+            lib.sdg_topk_rows_accum.argtypes = [v, v, C.c_int64, C.c_int64, C.c_int, C.c_int, v, v,
+                                                C.c_int32, v]
+            lib.sdg_snn_jaccard.argtypes = [v, v, C.c_int32, C.c_int32, C.c_int, v]
+            lib.sdg_snn_graph.argtypes = [v, v, C.c_int32, C.c_int32, C.c_int, C.c_double, C.c_int,
+                                          v, v, v, v]
+            lib.sdg_knn.argtypes = [v, v, v, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                    C.c_int, v, v, v, v]
+            lib.sdg_knn_cross.argtypes = [v, v, v, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                          C.c_int, v, v, v, v, v, v, v]
+            lib.sdg_matrix_upload.argtypes = [v, v, C.POINTER(v)]
+            lib.sdg_matrix_free.argtypes = [v]
+            lib.sdg_knn_resident.argtypes = [v, v, v, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                             v, v, v, v]
+            _lib = lib
+    return _lib
+
+
+def last_error() -> str:
+    lib = load()
+    buf = C.create_string_buffer(4096)
+    lib.sdg_last_error(buf, 4096)
+    return buf.value.decode()
+
+
+def check(status: int):
+    if status != SDG_OK:
+        raise SdgError(status, last_error())
+
+
+class Context:
+    """An sdg_ctx: one CUDA stream on one device."""
+
+    def __init__(self, device: int = -1):
+        lib = load()
+        h = C.c_void_p()
+        check(lib.sdg_ctx_create(int(device), C.byref(h)))
+        self.handle = h
+        self.lib = lib
+
+    def close(self):
+        if self.handle:
+            self.lib.sdg_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_engine(self, engine: int):
+        check(self.lib.sdg_ctx_set_engine(self.handle, int(engine)))
+
+    def cancel(self):
+        check(self.lib.sdg_ctx_cancel(self.handle))
+
+    def reset_cancel(self):
+        check(self.lib.sdg_ctx_reset_cancel(self.handle))
+
+    def stats(self):
+        out = np.zeros(8, np.int64)
+        check(self.lib.sdg_last_stats(self.handle, out.ctypes.data, 8))
+        return {"pairs_screened": int(out[0]), "pairs_exact": int(out[1]),
+                "overflow_queries": int(out[2]), "kernels": int(out[3]),
+                "screen_us": int(out[4]), "device_us": int(out[5])}
+
+
+_tls = threading.local()
+
+
+def default_context() -> Context:
+    ctx = getattr(_tls, "ctx", None)
+    if ctx is None:
+        ctx = Context()
+        _tls.ctx = ctx
+    return ctx
+
+
+class HeldCSC:
+    """Keeps contiguous int32/float64 CSC arrays alive behind a CSC struct."""
+
+    def __init__(self, nrow, ncol, p, i, x):
+        self.p = np.ascontiguousarray(p, dtype=np.int32)
+        self.i = np.ascontiguousarray(i, dtype=np.int32)
+        self.x = np.ascontiguousarray(x, dtype=np.float64)
+        self.nrow, self.ncol = int(nrow), int(ncol)
+        self.s = CSC(self.nrow, self.ncol, self.p.ctypes.data_as(C.POINTER(C.c_int32)),
+                     self.i.ctypes.data_as(C.POINTER(C.c_int32)),
+                     self.x.ctypes.data_as(C.POINTER(C.c_double)))
+
+    @property
+    def ref(self):
+        return C.byref(self.s)
+
+
+def na_real(shape) -> np.ndarray:
+    return np.full(shape, NA_REAL_BITS, dtype=np.uint64).view(np.float64)

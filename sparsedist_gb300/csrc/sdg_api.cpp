@@ -1,0 +1,767 @@
+// sdg_api.cpp -- the C ABI of libsdgpu.so (include/sdgpu.h) and the host-side
+// orchestration of the blocked kNN path: argument checks with the reference's
+// messages, uploads, per-column preparation, the k clamp, and the
+// candidate-generation engines (exact slab, or screen + exact re-rank).
+//
+// Reference behaviour restated here: R/sparseKNN.R:110-313 (sparseKNN),
+// R/sparseKNNCross.R:44-199 (sparseKNNCross), R/sparseSNN.R:120-250
+// (sparseSNN, edges = "knn") and the kernels' own checks in src/*.cpp.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/sdgpu.h"
+#include "sdg_kernels.h"
+#include "sdg_screen.h"
+
+using namespace sdg;
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+namespace {
+
+thread_local std::string g_err;
+
+struct Fail {
+  int code;
+};
+
+[[noreturn]] void fail(int code, const std::string& msg) {
+  g_err = msg;
+  throw Fail{code};
+}
+
+void cuda_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    fail(e == cudaErrorMemoryAllocation ? SDG_E_NOMEM : SDG_E_CUDA,
+         std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e));
+  }
+}
+#define CK(x) cuda_check((x), #x)
+
+const char* kMsgK = "'k' must be a positive integer no larger than .Machine$integer.max.";
+const char* kMsgBlock = "'block_size' must be a positive integer no larger than .Machine$integer.max.";
+const char* kMsgNcores = "'ncores' must be a non-negative integer no larger than .Machine$integer.max.";
+const char* kMsgCosine = "Cosine requires finite input (found NA, NaN or Inf).";
+const char* kMsgJS =
+    "fastJS2 requires finite, non-negative input (columns should be normalised to sum to 1 "
+    "for a true JS divergence).";
+
+const char* method_name(int m) {
+  static const char* names[] = {"binary", "cosine", "euclidean", "manhattan", "pearson", "js"};
+  return (m >= 0 && m <= 5) ? names[m] : "?";
+}
+
+void check_method(int method, int dist) {
+  if (method < 0 || method > 5) fail(SDG_E_ARG, "unknown method");
+  if ((method == EUCLIDEAN || method == MANHATTAN || method == JS) && !dist) {
+    // R/sparseKNN.R:168-171
+    fail(SDG_E_ARG, std::string("'dist = FALSE' is only meaningful for methods \"binary\", "
+                                "\"cosine\" and \"pearson\"; ") +
+                        method_name(method) + " has no similarity form.");
+  }
+}
+
+// R/sparseKNN.R:172-181
+bool decreasing_for(int method, int dist) {
+  return (method == BINARY || method == COSINE || method == PEARSON) ? !dist : false;
+}
+
+template <typename T>
+T* dalloc(size_t n, cudaStream_t s) {
+  void* p = nullptr;
+  CK(cudaMallocAsync(&p, std::max<size_t>(n, 1) * sizeof(T), s));
+  return static_cast<T*>(p);
+}
+
+// RAII holder for stream-ordered device allocations.
+struct DevBuf {
+  void* p = nullptr;
+  cudaStream_t s = nullptr;
+  DevBuf() {}
+  DevBuf(size_t bytes, cudaStream_t st) : s(st) { CK(cudaMallocAsync(&p, std::max<size_t>(bytes, 1), st)); }
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), s(o.s) { o.p = nullptr; }
+  DevBuf& operator=(DevBuf&& o) noexcept { release(); p = o.p; s = o.s; o.p = nullptr; return *this; }
+  ~DevBuf() { release(); }
+  void release() { if (p) cudaFreeAsync(p, s); p = nullptr; }
+  template <typename T> T* as() const { return static_cast<T*>(p); }
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// context and resident matrices
+// ---------------------------------------------------------------------------
+struct sdg_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::atomic<int> cancel{0};
+  int engine = 0;
+  int64_t stats[8] = {0};
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+struct sdg_matrix {
+  sdg_ctx* ctx = nullptr;
+  int32_t nrow = 0, ncol = 0;
+  int64_t nnz = 0;
+  DevBuf p, i, x;
+  DevBuf empty;                 // uint8 per column
+  int64_t n_empty = -1;
+  DevBuf uval, scale;           // cosine
+  int cos_status = 1;           // 1 = not computed, 0 = ok, <0 = error code
+  DevBuf s1, s2;                // pearson moments
+  bool have_moments = false;
+  int js_status = 1;
+  ScreenCache screen;           // per-method screening data (sdg_screen.h)
+
+  DevCsc dev() const {
+    DevCsc d;
+    d.nrow = nrow; d.ncol = ncol;
+    d.p = p.as<int64_t>(); d.i = i.as<int32_t>(); d.x = x.as<double>();
+    return d;
+  }
+};
+
+namespace {
+
+void check_csc_host(const sdg_csc* M, const char* name) {
+  if (!M) fail(SDG_E_ARG, std::string("'") + name + "' must be provided.");
+  if (M->nrow < 0 || M->ncol < 0) fail(SDG_E_ARG, std::string("invalid dimensions of '") + name + "'.");
+  if (M->ncol > 0 && !M->p) fail(SDG_E_ARG, std::string("invalid dgCMatrix '") + name + "': no column pointers.");
+  if (M->ncol > 0) {
+    if (M->p[0] != 0) fail(SDG_E_ARG, std::string("invalid dgCMatrix '") + name + "': p[0] != 0.");
+    for (int32_t j = 0; j < M->ncol; ++j)
+      if (M->p[j + 1] < M->p[j])
+        fail(SDG_E_ARG, std::string("invalid dgCMatrix '") + name + "': column pointers decrease.");
+  }
+}
+
+__attribute__((unused)) void sync(sdg_ctx* c) { CK(cudaStreamSynchronize(c->stream)); }
+
+// Row indices in range and strictly ascending within each column: checked on
+// the device before any kernel indexes by row.
+std::unique_ptr<sdg_matrix> upload(sdg_ctx* c, const sdg_csc* M, const char* name) {
+  check_csc_host(M, name);
+  auto m = std::make_unique<sdg_matrix>();
+  m->ctx = c;
+  m->nrow = M->nrow;
+  m->ncol = M->ncol;
+  m->nnz = M->ncol > 0 ? M->p[M->ncol] : 0;
+  cudaStream_t s = c->stream;
+  std::vector<int64_t> p64((size_t)m->ncol + 1, 0);
+  for (int32_t j = 0; j <= m->ncol && m->ncol > 0; ++j) p64[j] = M->p[j];
+  m->p = DevBuf(sizeof(int64_t) * p64.size(), s);
+  m->i = DevBuf(sizeof(int32_t) * (size_t)m->nnz, s);
+  m->x = DevBuf(sizeof(double) * (size_t)m->nnz, s);
+  CK(cudaMemcpyAsync(m->p.p, p64.data(), sizeof(int64_t) * p64.size(), cudaMemcpyHostToDevice, s));
+  if (m->nnz > 0) {
+    CK(cudaMemcpyAsync(m->i.p, M->i, sizeof(int32_t) * (size_t)m->nnz, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(m->x.p, M->x, sizeof(double) * (size_t)m->nnz, cudaMemcpyHostToDevice, s));
+  }
+  DevBuf err(sizeof(int), s);
+  CK(cudaMemsetAsync(err.p, 0, sizeof(int), s));
+  launch_check_rows(m->dev(), err.as<int>(), s);
+  int herr = 0;
+  CK(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (herr)
+    fail(SDG_E_ARG, std::string("invalid dgCMatrix '") + name +
+                        "': row indices must lie in [0, nrow) and ascend within each column.");
+  return m;
+}
+
+void ensure_empty(sdg_matrix* m) {
+  if (m->n_empty >= 0) return;
+  cudaStream_t s = m->ctx->stream;
+  m->empty = DevBuf((size_t)m->ncol, s);
+  launch_col_empty(m->dev(), m->empty.as<uint8_t>(), s);
+  std::vector<uint8_t> h((size_t)m->ncol);
+  if (m->ncol > 0)
+    CK(cudaMemcpyAsync(h.data(), m->empty.p, (size_t)m->ncol, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  int64_t n = 0;
+  for (uint8_t v : h) n += v;
+  m->n_empty = n;
+}
+
+void ensure_cosine(sdg_matrix* m) {
+  if (m->cos_status == 0) return;
+  if (m->cos_status < 0) fail(SDG_E_NONFINITE, kMsgCosine);
+  cudaStream_t s = m->ctx->stream;
+  m->uval = DevBuf(sizeof(double) * (size_t)m->nnz, s);
+  m->scale = DevBuf(sizeof(double) * (size_t)m->ncol, s);
+  DevBuf err(sizeof(int), s);
+  CK(cudaMemsetAsync(err.p, 0, sizeof(int), s));
+  launch_unit_csc(m->dev(), m->uval.as<double>(), m->scale.as<double>(), err.as<int>(), s);
+  int herr = 0;
+  CK(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  m->cos_status = herr ? SDG_E_NONFINITE : 0;
+  if (herr) fail(SDG_E_NONFINITE, kMsgCosine);
+}
+
+void ensure_moments(sdg_matrix* m) {
+  if (m->have_moments) return;
+  cudaStream_t s = m->ctx->stream;
+  m->s1 = DevBuf(sizeof(double) * (size_t)m->ncol, s);
+  m->s2 = DevBuf(sizeof(double) * (size_t)m->ncol, s);
+  launch_moments(m->dev(), m->s1.as<double>(), m->s2.as<double>(), s);
+  m->have_moments = true;
+}
+
+void ensure_js(sdg_matrix* m) {
+  if (m->js_status == 0) return;
+  if (m->js_status < 0) fail(SDG_E_NONFINITE, kMsgJS);
+  cudaStream_t s = m->ctx->stream;
+  DevBuf err(sizeof(int), s);
+  CK(cudaMemsetAsync(err.p, 0, sizeof(int), s));
+  launch_check_js(m->x.as<double>(), m->nnz, err.as<int>(), s);
+  int herr = 0;
+  CK(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  m->js_status = herr ? SDG_E_NONFINITE : 0;
+  if (herr) fail(SDG_E_NONFINITE, kMsgJS);
+}
+
+// Method-specific preparation of the reference-side (m) and query-side (m2)
+// matrices, in the order the reference raises its errors.
+void prepare(int method, sdg_matrix* ref, sdg_matrix* qry) {
+  if (method == COSINE) { ensure_cosine(ref); if (qry != ref) ensure_cosine(qry); }
+  else if (method == PEARSON) { ensure_moments(ref); if (qry != ref) ensure_moments(qry); }
+  else if (method == JS) { ensure_js(ref); if (qry != ref) ensure_js(qry); }
+}
+
+ColAux aux_of(const sdg_matrix* m) {
+  ColAux a;
+  a.empty = m->empty.as<uint8_t>();
+  a.uval = m->uval.as<double>();
+  a.scale = m->scale.as<double>();
+  a.s = m->s1.as<double>();
+  a.ss = m->s2.as<double>();
+  return a;
+}
+
+void check_cancel(sdg_ctx* c) {
+  if (c->cancel.load(std::memory_order_relaxed)) fail(SDG_E_CANCELLED, "Computation interrupted by the user.");
+}
+
+// ---------------------------------------------------------------------------
+// forward kNN on the device: result d_idx / d_val (nq x k, column-major)
+// ---------------------------------------------------------------------------
+struct KnnPlan {
+  int method = 0, dist = 1, k = 1;
+  bool decreasing = false;
+  bool selfmode = false, include_self = false;
+  const uint8_t* ref_mask = nullptr;   // degenerate reference columns (or null)
+  const uint8_t* qry_blank = nullptr;  // degenerate query columns (or null)
+};
+
+void exact_engine(sdg_ctx* c, const KnnPlan& P, sdg_matrix* ref, sdg_matrix* qry,
+                  int32_t* d_idx, double* d_val) {
+  cudaStream_t s = c->stream;
+  const int64_t nr = ref->ncol, nq = qry->ncol;
+  const int64_t budget = (int64_t)1 << 30;                 // slab bytes per chunk
+  int64_t B = std::max<int64_t>(1, std::min<int64_t>(nq, budget / std::max<int64_t>(1, nr * 8)));
+  DevBuf D(sizeof(double) * (size_t)(nr * B), s);
+  const ColAux ra = aux_of(ref), qa = aux_of(qry);
+  const double self_value =
+      (P.method == BINARY || P.method == COSINE || P.method == PEARSON) ? (P.dist ? 0.0 : 1.0) : 0.0;
+  for (int64_t q0 = 0; q0 < nq; q0 += B) {
+    check_cancel(c);
+    const int64_t nb = std::min(B, nq - q0);
+    launch_exact_slab(P.method, P.dist, ref->dev(), ra, qry->dev(), qa, q0, nb, P.ref_mask,
+                      P.selfmode && P.include_self, self_value, D.as<double>(), s);
+    SelectArgs a;
+    a.vals = D.as<double>();
+    a.seg_stride = nr; a.elem_stride = 1; a.len = nr; a.nseg = nb;
+    a.idx_base = 0;
+    a.skip_base = (P.selfmode && !P.include_self) ? q0 : -1;
+    a.seg_blank = P.qry_blank;
+    a.out_idx = d_idx; a.out_val = d_val; a.out_ld = nq; a.out_row0 = q0;
+    a.k = P.k; a.decreasing = P.decreasing;
+    launch_select(a, s);
+    c->stats[1] += nr * nb;
+    c->stats[3] += 2;
+  }
+  CK(cudaGetLastError());
+}
+
+int pick_engine(sdg_ctx* c, const KnnPlan& P, int64_t nr, int64_t nq) {
+  if (c->engine == 1) return 1;
+  if (!screen_supported(P.method, P.k)) return 1;
+  if (c->engine == 2) return 2;
+  // Small problems: the exact slab is already latency-bound.
+  return (nr * nq <= (int64_t)1 << 22) ? 1 : 2;
+}
+
+// sparseKNN core (R/sparseKNN.R:183-301) after argument checks.
+void knn_device(sdg_ctx* c, sdg_matrix* X, sdg_matrix* Y, int method, int dist, int k,
+                int include_self, int drop_degenerate, bool cross_side, int side,
+                int32_t* d_idx_out, double* d_val_out, int* k_eff, int* flags,
+                DevBuf* hold_idx, DevBuf* hold_val) {
+  const bool selfmode = (Y == nullptr);
+  sdg_matrix* ref = selfmode ? X : Y;
+  ensure_empty(ref);
+  ensure_empty(X);
+  int64_t avail = drop_degenerate ? (ref->ncol - ref->n_empty) : ref->ncol;
+  if (selfmode && !include_self) avail -= 1;
+  if (avail < 1) {
+    if (cross_side)
+      fail(SDG_E_NOCAND, std::string("No candidate neighbours available for the ") +
+                             (side == 0 ? "forward" : "reverse") + " direction.");
+    fail(SDG_E_NOCAND, "No candidate neighbours available.");
+  }
+  if (k > avail) {
+    *flags |= (side == 0) ? SDG_WARN_CLAMP_FWD : SDG_WARN_CLAMP_REV;
+    k = (int)avail;
+  }
+  *k_eff = k;
+  if (k > kMaxK)
+    fail(SDG_E_UNSUPPORTED, "k above " + std::to_string(kMaxK) +
+                                " neighbours is not supported by this build.");
+  prepare(method, ref, X);
+
+  KnnPlan P;
+  P.method = method; P.dist = dist; P.k = k; P.decreasing = decreasing_for(method, dist);
+  P.selfmode = selfmode; P.include_self = include_self != 0;
+  P.ref_mask = drop_degenerate ? ref->empty.as<uint8_t>() : nullptr;
+  P.qry_blank = drop_degenerate ? X->empty.as<uint8_t>() : nullptr;
+
+  cudaStream_t s = c->stream;
+  const int64_t nq = X->ncol;
+  int32_t* d_idx = d_idx_out;
+  double* d_val = d_val_out;
+  if (!d_idx) {
+    *hold_idx = DevBuf(sizeof(int32_t) * (size_t)(nq * k), s);
+    *hold_val = DevBuf(sizeof(double) * (size_t)(nq * k), s);
+    d_idx = hold_idx->as<int32_t>();
+    d_val = hold_val->as<double>();
+  }
+  const int eng = pick_engine(c, P, ref->ncol, nq);
+  if (eng == 2) {
+    ScreenRun r;
+    r.method = method; r.dist = dist; r.k = k; r.decreasing = P.decreasing;
+    r.selfmode = selfmode; r.include_self = P.include_self;
+    r.ref_mask = P.ref_mask; r.qry_blank = P.qry_blank;
+    screen_knn(c->stream, r, ref->dev(), aux_of(ref), &ref->screen, X->dev(), aux_of(X),
+               &X->screen, d_idx, d_val, c->stats, [c]() { check_cancel(c); });
+  } else {
+    exact_engine(c, P, ref, X, d_idx, d_val);
+  }
+}
+
+template <typename F>
+int guarded(F&& f) {
+  try {
+    f();
+    return SDG_OK;
+  } catch (const Fail& e) {
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    g_err = "out of host memory";
+    return SDG_E_NOMEM;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return SDG_E_CUDA;
+  } catch (...) {
+    g_err = "unknown failure";
+    return SDG_E_CUDA;
+  }
+}
+
+void check_counts(int k, int block_size, int ncores) {
+  if (k < 1) fail(SDG_E_ARG, kMsgK);
+  if (block_size < 1) fail(SDG_E_ARG, kMsgBlock);
+  if (ncores < 0) fail(SDG_E_ARG, kMsgNcores);
+}
+
+void begin_stats(sdg_ctx* c) {
+  std::memset(c->stats, 0, sizeof c->stats);
+  CK(cudaEventRecord(c->ev[0], c->stream));
+}
+void end_stats(sdg_ctx* c) {
+  CK(cudaEventRecord(c->ev[1], c->stream));
+  CK(cudaEventSynchronize(c->ev[1]));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
+  c->stats[5] = (int64_t)(ms * 1000.0f);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+SDG_API int sdg_version(void) { return 10000; }
+
+SDG_API int sdg_last_error(char* buf, size_t len) {
+  if (buf && len > 0) {
+    const size_t n = std::min(len - 1, g_err.size());
+    std::memcpy(buf, g_err.data(), n);
+    buf[n] = '\0';
+  }
+  return (int)g_err.size();
+}
+
+SDG_API int sdg_ctx_create(int device, sdg_ctx** out) {
+  return guarded([&] {
+    if (!out) fail(SDG_E_ARG, "out must not be NULL");
+    auto c = std::make_unique<sdg_ctx>();
+    if (device < 0) CK(cudaGetDevice(&device));
+    c->device = device;
+    CK(cudaSetDevice(device));
+    CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    for (auto& e : c->ev) CK(cudaEventCreate(&e));
+    *out = c.release();
+  });
+}
+
+SDG_API int sdg_ctx_destroy(sdg_ctx* c) {
+  if (!c) return SDG_OK;
+  cudaStreamSynchronize(c->stream);
+  for (auto& e : c->ev) if (e) cudaEventDestroy(e);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return SDG_OK;
+}
+
+SDG_API int sdg_ctx_cancel(sdg_ctx* c) {
+  if (!c) return SDG_E_ARG;
+  c->cancel.store(1);
+  return SDG_OK;
+}
+
+SDG_API int sdg_ctx_reset_cancel(sdg_ctx* c) {
+  if (!c) return SDG_E_ARG;
+  c->cancel.store(0);
+  return SDG_OK;
+}
+
+SDG_API int sdg_ctx_set_engine(sdg_ctx* c, int engine) {
+  if (!c || engine < 0 || engine > 2) { g_err = "invalid engine"; return SDG_E_ARG; }
+  c->engine = engine;
+  return SDG_OK;
+}
+
+SDG_API int sdg_last_stats(sdg_ctx* c, int64_t* out, int n) {
+  if (!c || !out) return SDG_E_ARG;
+  for (int t = 0; t < n && t < 8; ++t) out[t] = c->stats[t];
+  return SDG_OK;
+}
+
+SDG_API int sdg_dist_cross(sdg_ctx* c, int method, int dist, const sdg_csc* m, const sdg_csc* m2,
+                           double* D) {
+  return guarded([&] {
+    if (!c) fail(SDG_E_ARG, "ctx must not be NULL");
+    CK(cudaSetDevice(c->device));
+    if (method < 0 || method > 5) fail(SDG_E_ARG, "unknown method");
+    check_csc_host(m, "m");
+    check_csc_host(m2, "m2");
+    if (method == JS) {                              // src/sparseDist.cpp:1077-1081 first
+      auto a = upload(c, m, "m");
+      auto b = upload(c, m2, "m2");
+      ensure_js(a.get());
+      ensure_js(b.get());
+    }
+    if (m->nrow != m2->nrow)
+      fail(SDG_E_ROWS, "Mismatched row dimensions of m (" + std::to_string(m->nrow) +
+                           ") and m2 (" + std::to_string(m2->nrow) + ").");
+    auto a = upload(c, m, "m");
+    auto b = upload(c, m2, "m2");
+    prepare(method, a.get(), b.get());
+    cudaStream_t s = c->stream;
+    const int64_t nc = a->ncol, nc2 = b->ncol;
+    const int64_t budget = (int64_t)1 << 30;
+    const int64_t B = std::max<int64_t>(1, std::min<int64_t>(std::max<int64_t>(nc2, 1),
+                                                             budget / std::max<int64_t>(1, nc * 8)));
+    DevBuf Dd(sizeof(double) * (size_t)(nc * B), s);
+    for (int64_t q0 = 0; q0 < nc2; q0 += B) {
+      const int64_t nb = std::min(B, nc2 - q0);
+      launch_exact_slab(method, dist, a->dev(), aux_of(a.get()), b->dev(), aux_of(b.get()), q0,
+                        nb, nullptr, 0, 0.0, Dd.as<double>(), s);
+      CK(cudaGetLastError());
+      CK(cudaMemcpyAsync(D + q0 * nc, Dd.p, sizeof(double) * (size_t)(nc * nb),
+                         cudaMemcpyDeviceToHost, s));
+    }
+    CK(cudaStreamSynchronize(s));
+  });
+}
+
+SDG_API int sdg_topk_block(sdg_ctx* c, const double* D, int64_t nrow, int64_t ncol, int k,
+                           int decreasing, const int32_t* self_row, int32_t* idx, double* dist) {
+  return guarded([&] {
+    if (!c) fail(SDG_E_ARG, "ctx must not be NULL");
+    CK(cudaSetDevice(c->device));
+    if (k < 1) fail(SDG_E_ARG, "k must be >= 1.");
+    if (nrow < 0 || ncol < 0) fail(SDG_E_ARG, "invalid dimensions of D.");
+    std::vector<int64_t> skip((size_t)std::max<int64_t>(ncol, 1), -1);
+    for (int64_t b = 0; b < ncol; ++b) {
+      const int32_t sr = self_row ? self_row[b] : 0;
+      if (sr == NA_INT || sr < 0 || (int64_t)sr > nrow)
+        fail(SDG_E_ARG, "self_row entries must be 0 or valid 1-based rows of D.");
+      skip[(size_t)b] = sr > 0 ? sr - 1 : -1;
+    }
+    if (k > kMaxK)
+      fail(SDG_E_UNSUPPORTED, "k above " + std::to_string(kMaxK) + " is not supported by this build.");
+    if (ncol == 0) return;
+    cudaStream_t s = c->stream;
+    DevBuf dD(sizeof(double) * (size_t)(nrow * ncol), s), dskip(sizeof(int64_t) * (size_t)ncol, s);
+    DevBuf di(sizeof(int32_t) * (size_t)(ncol * k), s), dv(sizeof(double) * (size_t)(ncol * k), s);
+    if (nrow > 0) CK(cudaMemcpyAsync(dD.p, D, sizeof(double) * (size_t)(nrow * ncol), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dskip.p, skip.data(), sizeof(int64_t) * (size_t)ncol, cudaMemcpyHostToDevice, s));
+    SelectArgs a;
+    a.vals = dD.as<double>(); a.seg_stride = nrow; a.elem_stride = 1; a.len = nrow; a.nseg = ncol;
+    a.skip_arr = dskip.as<int64_t>();
+    a.out_idx = di.as<int32_t>(); a.out_val = dv.as<double>(); a.out_ld = ncol; a.out_row0 = 0;
+    a.k = k; a.decreasing = decreasing != 0;
+    launch_select(a, s);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(idx, di.p, sizeof(int32_t) * (size_t)(ncol * k), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(dist, dv.p, sizeof(double) * (size_t)(ncol * k), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+  });
+}
+
+SDG_API int sdg_topk_rows_accum(sdg_ctx* c, const double* D, int64_t nrow, int64_t ncol, int k,
+                                int decreasing, int32_t* best_idx, double* best_val,
+                                int32_t col_offset, const int32_t* self_col) {
+  return guarded([&] {
+    if (!c) fail(SDG_E_ARG, "ctx must not be NULL");
+    CK(cudaSetDevice(c->device));
+    if (k < 1) fail(SDG_E_ARG, "k must be >= 1.");
+    if (col_offset < 0) fail(SDG_E_ARG, "col_offset must be >= 0.");
+    if (nrow < 0 || ncol < 0) fail(SDG_E_ARG, "invalid dimensions of D.");
+    std::vector<int64_t> skip((size_t)std::max<int64_t>(nrow, 1), -1);
+    for (int64_t r = 0; r < nrow; ++r) {
+      const int32_t sc = self_col ? self_col[r] : 0;
+      if (sc == NA_INT || sc < 0)
+        fail(SDG_E_ARG, "self_col entries must be 0 or a positive 1-based query index.");
+      skip[(size_t)r] = sc > 0 ? (int64_t)sc - 1 : -1;
+    }
+    if (k > kMaxK)
+      fail(SDG_E_UNSUPPORTED, "k above " + std::to_string(kMaxK) + " is not supported by this build.");
+    if (nrow == 0) return;
+    cudaStream_t s = c->stream;
+    DevBuf dD(sizeof(double) * (size_t)std::max<int64_t>(nrow * ncol, 1), s);
+    DevBuf dskip(sizeof(int64_t) * (size_t)nrow, s);
+    DevBuf di(sizeof(int32_t) * (size_t)(nrow * k), s), dv(sizeof(double) * (size_t)(nrow * k), s);
+    if (ncol > 0) CK(cudaMemcpyAsync(dD.p, D, sizeof(double) * (size_t)(nrow * ncol), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dskip.p, skip.data(), sizeof(int64_t) * (size_t)nrow, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(di.p, best_idx, sizeof(int32_t) * (size_t)(nrow * k), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dv.p, best_val, sizeof(double) * (size_t)(nrow * k), cudaMemcpyHostToDevice, s));
+    SelectArgs a;
+    a.vals = dD.as<double>(); a.seg_stride = 1; a.elem_stride = nrow; a.len = ncol; a.nseg = nrow;
+    a.idx_base = col_offset;
+    a.skip_arr = dskip.as<int64_t>();
+    a.seed_idx = di.as<int32_t>(); a.seed_val = dv.as<double>(); a.seed_ld = nrow;
+    a.out_idx = di.as<int32_t>(); a.out_val = dv.as<double>(); a.out_ld = nrow; a.out_row0 = 0;
+    a.k = k; a.decreasing = decreasing != 0;
+    launch_select(a, s);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(best_idx, di.p, sizeof(int32_t) * (size_t)(nrow * k), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(best_val, dv.p, sizeof(double) * (size_t)(nrow * k), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+  });
+}
+
+namespace {
+void snn_weights_device(sdg_ctx* c, const int32_t* idx, int32_t n, int32_t k, int include_self,
+                        DevBuf* d_idx, DevBuf* d_w) {
+  if (n < 1 || k < 1) fail(SDG_E_ARG, "'idx' must have at least one row and column.");
+  cudaStream_t s = c->stream;
+  const int64_t total = (int64_t)n * k;
+  *d_idx = DevBuf(sizeof(int32_t) * (size_t)total, s);
+  *d_w = DevBuf(sizeof(double) * (size_t)total, s);
+  CK(cudaMemcpyAsync(d_idx->p, idx, sizeof(int32_t) * (size_t)total, cudaMemcpyHostToDevice, s));
+  DevBuf err(sizeof(int), s);
+  CK(cudaMemsetAsync(err.p, 0, sizeof(int), s));
+  launch_snn_check(d_idx->as<int32_t>(), n, k, err.as<int>(), s);
+  int herr = 0;
+  CK(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (herr)
+    fail(SDG_E_INDEX, "'idx' entries must be NA or 1-based row indices in [1, nrow(idx)].");
+  DevBuf sets(sizeof(int32_t) * (size_t)n * ((size_t)k + 1), s), sizes(sizeof(int32_t) * (size_t)n, s);
+  launch_snn_sets(d_idx->as<int32_t>(), n, k, include_self, sets.as<int32_t>(), sizes.as<int32_t>(), s);
+  launch_snn_weights(d_idx->as<int32_t>(), n, k, sets.as<int32_t>(), sizes.as<int32_t>(),
+                     d_w->as<double>(), s);
+  CK(cudaGetLastError());
+}
+}  // namespace
+
+SDG_API int sdg_snn_jaccard(sdg_ctx* c, const int32_t* idx, int32_t n, int32_t k, int include_self,
+                            double* w) {
+  return guarded([&] {
+    if (!c) fail(SDG_E_ARG, "ctx must not be NULL");
+    CK(cudaSetDevice(c->device));
+    DevBuf di, dw;
+    snn_weights_device(c, idx, n, k, include_self, &di, &dw);
+    CK(cudaMemcpyAsync(w, dw.p, sizeof(double) * (size_t)n * k, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  });
+}
+
+SDG_API int sdg_snn_graph(sdg_ctx* c, const int32_t* idx, int32_t n, int32_t k, int include_self,
+                          double prune, int symmetrise, int64_t* nnz, int32_t* p, int32_t* i,
+                          double* x) {
+  return guarded([&] {
+    if (!c) fail(SDG_E_ARG, "ctx must not be NULL");
+    if (!nnz) fail(SDG_E_ARG, "nnz must not be NULL");
+    CK(cudaSetDevice(c->device));
+    if (!(prune >= 0.0 && prune <= 1.0))
+      fail(SDG_E_ARG, "'prune' must be a finite number between 0 and 1.");
+    DevBuf di, dw;
+    snn_weights_device(c, idx, n, k, include_self, &di, &dw);
+    int32_t *dp = nullptr, *drow = nullptr;
+    double* dx = nullptr;
+    int64_t m = 0;
+    const int st = snn_graph_build(di.as<int32_t>(), dw.as<double>(), n, k, prune, symmetrise, &m,
+                                   &dp, &drow, &dx, c->stream);
+    if (st) cuda_check((cudaError_t)st, "snn_graph_build");
+    DevBuf hp, hi, hx;
+    hp.p = dp; hp.s = c->stream;
+    hi.p = drow; hi.s = c->stream;
+    hx.p = dx; hx.s = c->stream;
+    *nnz = m;
+    if (p) {
+      CK(cudaMemcpyAsync(p, dp, sizeof(int32_t) * ((size_t)n + 1), cudaMemcpyDeviceToHost, c->stream));
+      if (m > 0) {
+        CK(cudaMemcpyAsync(i, drow, sizeof(int32_t) * (size_t)m, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(x, dx, sizeof(double) * (size_t)m, cudaMemcpyDeviceToHost, c->stream));
+      }
+    }
+    CK(cudaStreamSynchronize(c->stream));
+  });
+}
+
+SDG_API int sdg_knn(sdg_ctx* c, const sdg_csc* X, const sdg_csc* Y, int method, int dist, int k,
+                    int include_self, int drop_degenerate, int block_size, int ncores,
+                    int32_t* idx, double* dist_out, int* k_eff, int* flags) {
+  return guarded([&] {
+    if (!c || !idx || !dist_out || !k_eff || !flags) fail(SDG_E_ARG, "NULL argument");
+    CK(cudaSetDevice(c->device));
+    *flags = 0;
+    check_counts(k, block_size, ncores);
+    check_method(method, dist);
+    check_csc_host(X, "X");
+    if (X->ncol < 1) fail(SDG_E_ARG, "'X' must have at least one column.");
+    if (Y) {
+      check_csc_host(Y, "Y");
+      if (X->nrow != Y->nrow) fail(SDG_E_ROWS, "'X' and 'Y' must have the same number of rows.");
+    }
+    begin_stats(c);
+    auto xm = upload(c, X, "X");
+    std::unique_ptr<sdg_matrix> ym;
+    if (Y) ym = upload(c, Y, "Y");
+    DevBuf hi, hv;
+    knn_device(c, xm.get(), ym.get(), method, dist, k, include_self, drop_degenerate, false, 0,
+               nullptr, nullptr, k_eff, flags, &hi, &hv);
+    const size_t cnt = (size_t)xm->ncol * (size_t)*k_eff;
+    CK(cudaMemcpyAsync(idx, hi.p, sizeof(int32_t) * cnt, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(dist_out, hv.p, sizeof(double) * cnt, cudaMemcpyDeviceToHost, c->stream));
+    end_stats(c);
+  });
+}
+
+SDG_API int sdg_knn_cross(sdg_ctx* c, const sdg_csc* X, const sdg_csc* Y, int method, int dist,
+                          int k, int drop_degenerate, int block_size, int ncores,
+                          int32_t* fwd_idx, double* fwd_dist, int32_t* rev_idx, double* rev_dist,
+                          int* k_fwd, int* k_rev, int* flags) {
+  return guarded([&] {
+    if (!c || !fwd_idx || !fwd_dist || !rev_idx || !rev_dist || !k_fwd || !k_rev || !flags)
+      fail(SDG_E_ARG, "NULL argument");
+    CK(cudaSetDevice(c->device));
+    *flags = 0;
+    if (!Y)
+      fail(SDG_E_ARG, "'Y' is required. For a single matrix use sparseKNN(), which already "
+                      "exploits symmetry via the full/diag arguments.");
+    check_counts(k, block_size, ncores);
+    check_method(method, dist);
+    check_csc_host(X, "X");
+    check_csc_host(Y, "Y");
+    if (X->nrow != Y->nrow) fail(SDG_E_ROWS, "'X' and 'Y' must have the same number of rows.");
+    if (X->ncol < 1) fail(SDG_E_ARG, "'X' must have at least one column.");
+    if (Y->ncol < 1) fail(SDG_E_ARG, "'Y' must have at least one column.");
+    begin_stats(c);
+    auto xm = upload(c, X, "X");
+    auto ym = upload(c, Y, "Y");
+    // Both clamps are decided before any work (R/sparseKNNCross.R:117-127).
+    ensure_empty(xm.get());
+    ensure_empty(ym.get());
+    const int64_t av_f = drop_degenerate ? ym->ncol - ym->n_empty : ym->ncol;
+    const int64_t av_r = drop_degenerate ? xm->ncol - xm->n_empty : xm->ncol;
+    if (av_f < 1) fail(SDG_E_NOCAND, "No candidate neighbours available for the forward direction.");
+    if (av_r < 1) fail(SDG_E_NOCAND, "No candidate neighbours available for the reverse direction.");
+    // forward == sparseKNN(X, Y); reverse == sparseKNN(Y, X): every kernel is
+    // bit-for-bit symmetric in its two columns (R/sparseKNNCross.R:33-40).
+    DevBuf fi, fv, ri, rv;
+    knn_device(c, xm.get(), ym.get(), method, dist, k, 0, drop_degenerate, true, 0, nullptr,
+               nullptr, k_fwd, flags, &fi, &fv);
+    knn_device(c, ym.get(), xm.get(), method, dist, k, 0, drop_degenerate, true, 1, nullptr,
+               nullptr, k_rev, flags, &ri, &rv);
+    const size_t cf = (size_t)xm->ncol * (size_t)*k_fwd, cr = (size_t)ym->ncol * (size_t)*k_rev;
+    CK(cudaMemcpyAsync(fwd_idx, fi.p, sizeof(int32_t) * cf, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(fwd_dist, fv.p, sizeof(double) * cf, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(rev_idx, ri.p, sizeof(int32_t) * cr, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(rev_dist, rv.p, sizeof(double) * cr, cudaMemcpyDeviceToHost, c->stream));
+    end_stats(c);
+  });
+}
+
+SDG_API int sdg_matrix_upload(sdg_ctx* c, const sdg_csc* M, sdg_matrix** out) {
+  return guarded([&] {
+    if (!c || !out) fail(SDG_E_ARG, "NULL argument");
+    CK(cudaSetDevice(c->device));
+    auto m = upload(c, M, "M");
+    ensure_empty(m.get());
+    *out = m.release();
+  });
+}
+
+SDG_API int sdg_matrix_free(sdg_matrix* M) {
+  if (!M) return SDG_OK;
+  cudaSetDevice(M->ctx->device);
+  cudaStream_t s = M->ctx->stream;
+  screen_cache_free(&M->screen, s);
+  delete M;
+  cudaStreamSynchronize(s);
+  return SDG_OK;
+}
+
+SDG_API int sdg_knn_resident(sdg_ctx* c, const sdg_matrix* X, const sdg_matrix* Y, int method,
+                             int dist, int k, int include_self, int drop_degenerate, int32_t* idx,
+                             double* dist_out, int* k_eff, int* flags) {
+  return guarded([&] {
+    if (!c || !X || !idx || !dist_out || !k_eff || !flags) fail(SDG_E_ARG, "NULL argument");
+    CK(cudaSetDevice(c->device));
+    *flags = 0;
+    if (k < 1) fail(SDG_E_ARG, kMsgK);
+    check_method(method, dist);
+    if (X->ncol < 1) fail(SDG_E_ARG, "'X' must have at least one column.");
+    if (Y && X->nrow != Y->nrow) fail(SDG_E_ROWS, "'X' and 'Y' must have the same number of rows.");
+    begin_stats(c);
+    DevBuf hi, hv;
+    knn_device(c, const_cast<sdg_matrix*>(X), const_cast<sdg_matrix*>(Y), method, dist, k,
+               include_self, drop_degenerate, false, 0, nullptr, nullptr, k_eff, flags, &hi, &hv);
+    const size_t cnt = (size_t)X->ncol * (size_t)*k_eff;
+    CK(cudaMemcpyAsync(idx, hi.p, sizeof(int32_t) * cnt, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(dist_out, hv.p, sizeof(double) * cnt, cudaMemcpyDeviceToHost, c->stream));
+    end_stats(c);
+  });
+}
+
+}  // extern "C"

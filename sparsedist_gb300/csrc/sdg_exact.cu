@@ -1,0 +1,281 @@
+// sdg_exact.cu -- exact FP64 column-pair values, in the reference's order.
+//
+// Compiled with -fmad=false and written with __dadd_rn / __dmul_rn: no
+// multiply-add is ever fused, so each value is the IEEE double the reference
+// computes (sequential sums in ascending row order).  These kernels produce
+// every distance this library returns; the FP32 screen only decides which
+// pairs need one.
+#include <cmath>
+
+#include "sdg_kernels.h"
+
+namespace sdg {
+namespace {
+
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+
+// ---- per-column preparation -------------------------------------------------
+
+// R/sparseKNN.R:214-220: colSums(abs(M)) == 0 with NA treated as non-empty.
+__global__ void k_col_empty(DevCsc M, uint8_t* empty) {
+  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (j >= M.ncol) return;
+  uint8_t e = 1;
+  for (int64_t a = M.p[j]; a < M.p[j + 1]; ++a)
+    if (!(M.x[a] == 0.0)) { e = 0; break; }
+  empty[j] = e;
+}
+
+// unit_csc: src/sparseDist.cpp:246-284 (dnrm2-style scaled sum of squares).
+__global__ void k_unit_csc(DevCsc M, double* uval, double* scale_out, int* err) {
+  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (j >= M.ncol) return;
+  double scale = 0.0, ssq = 1.0;
+  const int64_t a0 = M.p[j], a1 = M.p[j + 1];
+  for (int64_t a = a0; a < a1; ++a) {
+    const double v = M.x[a];
+    if (!isfinite(v)) { atomicOr(err, 1); return; }
+    if (v == 0.0) continue;
+    const double av = fabs(v);
+    if (scale < av) { const double r = scale / av; ssq = dadd(1.0, dmul(dmul(ssq, r), r)); scale = av; }
+    else            { const double r = av / scale; ssq = dadd(ssq, dmul(r, r)); }
+  }
+  const double sq = sqrt(ssq);
+  scale_out[j] = scale;
+  for (int64_t a = a0; a < a1; ++a)
+    uval[a] = (scale == 0.0) ? 0.0 : ((M.x[a]) / scale) / sq;
+}
+
+__global__ void k_moments(DevCsc M, double* sum, double* sumsq) {
+  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (j >= M.ncol) return;
+  double s = 0.0, ss = 0.0;
+  for (int64_t a = M.p[j]; a < M.p[j + 1]; ++a) {
+    const double v = M.x[a];
+    s = dadd(s, v);
+    ss = dadd(ss, dmul(v, v));
+  }
+  sum[j] = s;
+  sumsq[j] = ss;
+}
+
+// fastJS2 input check: src/sparseDist.cpp:1077-1081.
+__global__ void k_check_js(const double* x, int64_t nnz, int* err) {
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < nnz;
+       a += (int64_t)gridDim.x * blockDim.x) {
+    const double v = x[a];
+    if (!isfinite(v) || v < 0.0) { atomicOr(err, 1); return; }
+  }
+}
+
+// ---- exact pair values ---------------------------------------------------------
+
+// jacc_common / jacc_value: src/sparseDist.cpp:535-556
+__device__ double pair_binary(const DevCsc& A, int32_t i, const DevCsc& B, int32_t j, bool dist) {
+  int64_t a = A.p[i], ae = A.p[i + 1], b = B.p[j], be = B.p[j + 1];
+  const double ni = (double)(ae - a), nj = (double)(be - b);
+  int64_t common = 0;
+  while (a < ae && b < be) {
+    const int32_t ra = __ldg(A.i + a), rb = __ldg(B.i + b);
+    common += (ra == rb);
+    a += (ra <= rb);
+    b += (rb <= ra);
+  }
+  const double c = (double)common;
+  const double denom = dsub(dadd(ni, nj), c);
+  const double sim = (denom > 0.0) ? (c / denom) : 1.0;
+  return dist ? dsub(1.0, sim) : sim;
+}
+
+// unit_dot / unit_cosine: src/sparseDist.cpp:287-331
+__device__ double pair_cosine(const DevCsc& A, const ColAux& aa, int32_t i, const DevCsc& B,
+                              const ColAux& ba, int32_t j, bool dist) {
+  const bool ea = (aa.scale[i] == 0.0), eb = (ba.scale[j] == 0.0);
+  double c;
+  if (ea || eb) {
+    c = (ea && eb) ? 1.0 : 0.0;
+  } else {
+    int64_t a = A.p[i], ae = A.p[i + 1], b = B.p[j], be = B.p[j + 1];
+    double s = 0.0;
+    while (a < ae && b < be) {
+      const int32_t ra = __ldg(A.i + a), rb = __ldg(B.i + b);
+      if (ra == rb) { s = dadd(s, dmul(aa.uval[a], ba.uval[b])); ++a; ++b; }
+      else if (ra < rb) { ++a; }
+      else { ++b; }
+    }
+    c = s;
+    if (!(c == c)) c = 0.0;
+    else if (c > 1.0) c = 1.0;
+    else if (c < -1.0) c = -1.0;
+  }
+  return dist ? dsub(1.0, c) : c;
+}
+
+// fastEuclidean2 pair loop: src/sparseDist.cpp:855-871
+__device__ double pair_euclidean(const DevCsc& A, int32_t i, const DevCsc& B, int32_t j) {
+  int64_t a = A.p[i], ae = A.p[i + 1], b = B.p[j], be = B.p[j + 1];
+  double num = 0.0;
+  while (a < ae && b < be) {
+    const int32_t ra = __ldg(A.i + a), rb = __ldg(B.i + b);
+    if (ra == rb) {
+      const double diff = dsub(A.x[a], B.x[b]); num = dadd(num, dmul(diff, diff)); ++a; ++b;
+    } else if (ra < rb) {
+      num = dadd(num, dmul(A.x[a], A.x[a])); ++a;
+    } else {
+      num = dadd(num, dmul(B.x[b], B.x[b])); ++b;
+    }
+  }
+  for (; a < ae; ++a) num = dadd(num, dmul(A.x[a], A.x[a]));
+  for (; b < be; ++b) num = dadd(num, dmul(B.x[b], B.x[b]));
+  return sqrt(num);
+}
+
+// fastManhattan2 pair loop: src/sparseDist.cpp:755-772
+__device__ double pair_manhattan(const DevCsc& A, int32_t i, const DevCsc& B, int32_t j) {
+  int64_t a = A.p[i], ae = A.p[i + 1], b = B.p[j], be = B.p[j + 1];
+  double num = 0.0;
+  while (a < ae && b < be) {
+    const int32_t ra = __ldg(A.i + a), rb = __ldg(B.i + b);
+    if (ra == rb) { num = dadd(num, fabs(dsub(A.x[a], B.x[b]))); ++a; ++b; }
+    else if (ra < rb) { num = dadd(num, fabs(A.x[a])); ++a; }
+    else { num = dadd(num, fabs(B.x[b])); ++b; }
+  }
+  for (; a < ae; ++a) num = dadd(num, fabs(A.x[a]));
+  for (; b < be; ++b) num = dadd(num, fabs(B.x[b]));
+  return num;
+}
+
+// fastCorr2 (src/sparseDist.cpp:424-431) with arma::cor in the single-pass
+// vector form: sums in ascending row order over stored entries.
+__device__ double pair_pearson(const DevCsc& A, const ColAux& aa, int32_t i, const DevCsc& B,
+                               const ColAux& ba, int32_t j, bool dist) {
+  int64_t a = A.p[i], ae = A.p[i + 1], b = B.p[j], be = B.p[j + 1];
+  double sab = 0.0;
+  while (a < ae && b < be) {
+    const int32_t ra = __ldg(A.i + a), rb = __ldg(B.i + b);
+    if (ra == rb) { sab = dadd(sab, dmul(A.x[a], B.x[b])); ++a; ++b; }
+    else if (ra < rb) { ++a; }
+    else { ++b; }
+  }
+  const double N = (double)A.nrow;
+  const double norm = (A.nrow > 1) ? dsub(N, 1.0) : 1.0;
+  const double cov = dsub(sab, dmul(aa.s[i], ba.s[j]) / N) / norm;
+  const double va = dsub(aa.ss[i], dmul(aa.s[i], aa.s[i]) / N) / norm;
+  const double vb = dsub(ba.ss[j], dmul(ba.s[j], ba.s[j]) / N) / norm;
+  double c = cov / dmul(sqrt(va), sqrt(vb));
+  if (!isfinite(c)) c = 0.0;
+  if (c > 1.0) c = 1.0;
+  if (c < -1.0) c = -1.0;
+  return dist ? dsub(1.0, c) : c;
+}
+
+// fastJS2 (src/sparseDist.cpp:1099-1108, xlogx :206-210): per row
+// ((xlogx(P)+xlogx(Q)) - xlogx(P+Q)) + (P+Q)*log 2, summed into an even-row and
+// an odd-row accumulator; rows where P and Q are both 0 add +0 and are skipped.
+__device__ __forceinline__ double xlogx(double x) {
+  const double r = dmul(x, log(x));
+  return isnan(r) ? 0.0 : r;
+}
+
+__device__ double pair_js(const DevCsc& A, int32_t i, const DevCsc& B, int32_t j) {
+  const double log2v = 0.69314718055994530942;   // log(2.0), correctly rounded
+  int64_t a = A.p[i], ae = A.p[i + 1], b = B.p[j], be = B.p[j + 1];
+  double acc0 = 0.0, acc1 = 0.0;
+  while (a < ae || b < be) {
+    int32_t r;
+    double P = 0.0, Q = 0.0;
+    const int32_t ra = (a < ae) ? __ldg(A.i + a) : INT32_MAX;
+    const int32_t rb = (b < be) ? __ldg(B.i + b) : INT32_MAX;
+    if (ra < rb) { r = ra; P = A.x[a]; ++a; }
+    else if (rb < ra) { r = rb; Q = B.x[b]; ++b; }
+    else { r = ra; P = A.x[a]; Q = B.x[b]; ++a; ++b; }
+    const double PQ = dadd(P, Q);
+    const double t = dadd(dsub(dadd(xlogx(P), xlogx(Q)), xlogx(PQ)), dmul(PQ, log2v));
+    if (r & 1) acc1 = dadd(acc1, t); else acc0 = dadd(acc0, t);
+  }
+  const double v = dmul(0.5, dadd(acc0, acc1));
+  return (v > 0.0) ? sqrt(v) : 0.0;
+}
+
+__device__ __forceinline__ double pair_value(int method, bool dist, const DevCsc& A,
+                                             const ColAux& aa, int32_t i, const DevCsc& B,
+                                             const ColAux& ba, int32_t j) {
+  switch (method) {
+    case BINARY: return pair_binary(A, i, B, j, dist);
+    case COSINE: return pair_cosine(A, aa, i, B, ba, j, dist);
+    case EUCLIDEAN: return pair_euclidean(A, i, B, j);
+    case MANHATTAN: return pair_manhattan(A, i, B, j);
+    case PEARSON: return pair_pearson(A, aa, i, B, ba, j, dist);
+    default: return pair_js(A, i, B, j);
+  }
+}
+
+__global__ void k_exact_slab(int method, int dist, DevCsc ref, ColAux ra, DevCsc qry, ColAux qa,
+                             int64_t q0, const uint8_t* ref_mask, int restore_self,
+                             double self_value, double* D) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t b = blockIdx.y;
+  if (i >= ref.ncol) return;
+  const int64_t q = q0 + b;
+  double v;
+  if (ref_mask && ref_mask[i]) v = na_real();
+  else if (restore_self && i == q) v = self_value;
+  else v = pair_value(method, dist != 0, ref, ra, (int32_t)i, qry, qa, (int32_t)q);
+  D[b * (int64_t)ref.ncol + i] = v;
+}
+
+__global__ void k_exact_pairs(int method, int dist, DevCsc ref, ColAux ra, DevCsc qry,
+                              ColAux qa, const int32_t* ref_idx, const int32_t* qry_idx,
+                              int64_t npairs, double* out) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= npairs) return;
+  out[t] = pair_value(method, dist != 0, ref, ra, ref_idx[t], qry, qa, qry_idx[t]);
+}
+
+inline unsigned blocks_for(int64_t n, int threads) {
+  return (unsigned)((n + threads - 1) / threads);
+}
+
+}  // namespace
+
+void launch_col_empty(const DevCsc& M, uint8_t* empty, cudaStream_t s) {
+  if (M.ncol > 0) k_col_empty<<<blocks_for(M.ncol, 256), 256, 0, s>>>(M, empty);
+}
+void launch_unit_csc(const DevCsc& M, double* uval, double* scale, int* err, cudaStream_t s) {
+  if (M.ncol > 0) k_unit_csc<<<blocks_for(M.ncol, 128), 128, 0, s>>>(M, uval, scale, err);
+}
+void launch_moments(const DevCsc& M, double* sum, double* sumsq, cudaStream_t s) {
+  if (M.ncol > 0) k_moments<<<blocks_for(M.ncol, 128), 128, 0, s>>>(M, sum, sumsq);
+}
+void launch_check_js(const double* x, int64_t nnz, int* err, cudaStream_t s) {
+  if (nnz > 0) {
+    unsigned g = blocks_for(nnz, 256);
+    if (g > 152u * 16u) g = 152u * 16u;
+    k_check_js<<<g, 256, 0, s>>>(x, nnz, err);
+  }
+}
+
+void launch_exact_slab(int method, int dist, const DevCsc& ref, const ColAux& ra,
+                       const DevCsc& qry, const ColAux& qa, int64_t q0, int64_t nb,
+                       const uint8_t* ref_mask, int restore_self, double self_value,
+                       double* D, cudaStream_t s) {
+  if (ref.ncol == 0 || nb == 0) return;
+  for (int64_t b0 = 0; b0 < nb; b0 += 65535) {            // gridDim.y limit
+    const int64_t cnt = (nb - b0 < 65535) ? nb - b0 : 65535;
+    dim3 grid(blocks_for(ref.ncol, 128), (unsigned)cnt);
+    k_exact_slab<<<grid, 128, 0, s>>>(method, dist, ref, ra, qry, qa, q0 + b0, ref_mask,
+                                      restore_self, self_value, D + b0 * (int64_t)ref.ncol);
+  }
+}
+
+void launch_exact_pairs(int method, int dist, const DevCsc& ref, const ColAux& ra,
+                        const DevCsc& qry, const ColAux& qa, const int32_t* ref_idx,
+                        const int32_t* qry_idx, int64_t npairs, double* out, cudaStream_t s) {
+  if (npairs > 0)
+    k_exact_pairs<<<blocks_for(npairs, 128), 128, 0, s>>>(method, dist, ref, ra, qry, qa,
+                                                           ref_idx, qry_idx, npairs, out);
+}
+
+}  // namespace sdg

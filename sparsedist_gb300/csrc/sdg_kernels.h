@@ -1,0 +1,78 @@
+// sdg_kernels.h -- host-side launchers of the CUDA kernels (implemented in the
+// .cu files of this directory), called by the orchestration in sdg_api.cpp.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "sdg_common.cuh"
+
+namespace sdg {
+
+// ---- sdg_exact.cu: per-column preparation and exact FP64 pair values --------
+void launch_col_empty(const DevCsc& M, uint8_t* empty, cudaStream_t s);
+void launch_unit_csc(const DevCsc& M, double* uval, double* scale, int* err, cudaStream_t s);
+void launch_moments(const DevCsc& M, double* sum, double* sumsq, cudaStream_t s);
+void launch_check_js(const double* x, int64_t nnz, int* err, cudaStream_t s);
+
+// Exact values of every pair (ref column i, query column q0 + b) for
+// b < nb into D (nb columns of length ref.ncol).  Masked reference columns
+// (ref_mask[i] != 0) get NaN; with restore_self, the self position i == q0 + b
+// gets self_value (R/sparseKNN.R:270-279).
+void launch_exact_slab(int method, int dist, const DevCsc& ref, const ColAux& ra,
+                       const DevCsc& qry, const ColAux& qa, int64_t q0, int64_t nb,
+                       const uint8_t* ref_mask, int restore_self, double self_value,
+                       double* D, cudaStream_t s);
+
+// Exact values of listed pairs: out[t] = value(ref col ref_idx[t], query col
+// qry_idx[t]).
+void launch_exact_pairs(int method, int dist, const DevCsc& ref, const ColAux& ra,
+                        const DevCsc& qry, const ColAux& qa, const int32_t* ref_idx,
+                        const int32_t* qry_idx, int64_t npairs, double* out, cudaStream_t s);
+
+// ---- sdg_select.cu: exact top-k selection --------------------------------------
+
+// One "segment" per output row: candidates are vals[seg*seg_stride +
+// t*elem_stride] for t < len with global index idx_base + t.  Skipped: non-
+// finite values, elem_mask[t] != 0, and the global index skip_base + seg when
+// skip_base >= 0 or skip_arr[seg] (0-based global, < 0 = none) when given.
+// Optional seeds (1-based idx / values, column-major with leading dim seed_ld,
+// read up to the first NA) join the candidates.  The k best under
+// (value asc|desc, index asc) are written best-first, NA padded, to
+// out_idx / out_val at [t * out_ld + out_row0 + seg]; rows with
+// seg_blank[out_row0 + seg] != 0 are written all-NA.
+struct SelectArgs {
+  const double* vals = nullptr;
+  int64_t seg_stride = 0, elem_stride = 1, len = 0, nseg = 0;
+  int64_t idx_base = 0;
+  const uint8_t* elem_mask = nullptr;
+  int64_t skip_base = -1;
+  const int64_t* skip_arr = nullptr;
+  const int32_t* seed_idx = nullptr;
+  const double* seed_val = nullptr;
+  int64_t seed_ld = 0;
+  const uint8_t* seg_blank = nullptr;
+  int32_t* out_idx = nullptr;
+  double* out_val = nullptr;
+  int64_t out_ld = 0, out_row0 = 0;
+  int k = 1;
+  int decreasing = 0;
+};
+constexpr int kMaxK = 1024;   // largest k the selection kernels hold on chip
+void launch_select(const SelectArgs& a, cudaStream_t s);
+
+// ---- sdg_snn.cu: SNN weights and graph ------------------------------------------
+void launch_snn_check(const int32_t* idx, int32_t n, int32_t k, int* err, cudaStream_t s);
+// sets: n x (k+1) scratch, sizes: n
+void launch_snn_sets(const int32_t* idx, int32_t n, int32_t k, int include_self,
+                     int32_t* sets, int32_t* sizes, cudaStream_t s);
+void launch_snn_weights(const int32_t* idx, int32_t n, int32_t k, const int32_t* sets,
+                        const int32_t* sizes, double* w, cudaStream_t s);
+// Graph assembly: returns nnz through *nnz_host (synchronises the stream).
+// Buffers are allocated from the stream-ordered pool and returned; the caller
+// frees them with cudaFreeAsync.
+int snn_graph_build(const int32_t* d_idx, const double* d_w, int32_t n, int32_t k,
+                    double prune, int symmetrise, int64_t* nnz_host, int32_t** d_p,
+                    int32_t** d_i, double** d_x, cudaStream_t s);
+
+}  // namespace sdg

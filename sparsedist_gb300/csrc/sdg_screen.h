@@ -1,0 +1,44 @@
+// sdg_screen.h -- the screened candidate engine: an FP32 / integer screen over
+// every (query, reference) pair with a rigorous error bound, a candidate list
+// per query column, and an exact FP64 re-rank of the candidates (sdg_exact.cu)
+// followed by the exact top-k (sdg_select.cu).
+#pragma once
+
+#include <cstdint>
+#include <functional>
+
+#include "sdg_common.cuh"
+
+namespace sdg {
+
+// Screening data derived from one matrix for one method, kept with the
+// matrix so that a resident reference pays for it once.
+struct ScreenCache {
+  int method = -1;
+  void* blob = nullptr;      // one device allocation holding the arrays below
+  float* fval = nullptr;     // per stored entry: value the screen multiplies
+  float* cnorm = nullptr;    // per column: norm term of the method
+};
+
+struct ScreenRun {
+  int method = 0, dist = 1, k = 1;
+  bool decreasing = false, selfmode = false, include_self = false;
+  const uint8_t* ref_mask = nullptr;
+  const uint8_t* qry_blank = nullptr;
+};
+
+bool screen_supported(int method, int k);
+
+// Returns 0, a cudaError_t value, or -9 when cancelled.  stats: see
+// sdg_last_stats in include/sdgpu.h.
+int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColAux& ra,
+               ScreenCache* rc, const DevCsc& qry, const ColAux& qa, ScreenCache* qc,
+               int32_t* d_idx, double* d_val, int64_t* stats,
+               const std::function<void()>& check_cancel);
+
+void screen_cache_free(ScreenCache* c, cudaStream_t s);
+
+// Device check used at upload: rows in [0, nrow) and strictly ascending.
+void launch_check_rows(const DevCsc& M, int* err, cudaStream_t s);
+
+}  // namespace sdg

@@ -1,0 +1,124 @@
+// sdg_select.cu -- exact top-k selection under the reference's comparator.
+//
+// One warp owns one output row ("segment") and keeps its k best candidates in
+// shared memory as a list sorted best-first on the key (order_key(value),
+// index).  The comparator is a strict total order, so the result is the top-k
+// of the candidate set whatever order candidates arrive in: it equals the
+// bounded-heap results of topKBlock (src/topK.cpp:104-131) and of
+// topKRowsAccum's strictly-better replacement (src/topKRows.cpp:201-228).
+#include "sdg_kernels.h"
+
+namespace sdg {
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+__device__ __forceinline__ bool less_key(uint64_t ka, int32_t ia, uint64_t kb, int32_t ib) {
+  return ka < kb || (ka == kb && ia < ib);
+}
+
+// Warp-cooperative insertion of the lanes' candidates into the sorted list.
+__device__ __forceinline__ void insert_batch(bool valid, uint64_t key, int32_t gidx,
+                                             uint64_t* lk, int32_t* li, int& n, int K,
+                                             int lane) {
+  bool pass = valid;
+  if (n == K) pass = pass && less_key(key, gidx, lk[K - 1], li[K - 1]);
+  unsigned m = __ballot_sync(FULL, pass);
+  while (m) {
+    const int src = __ffs(m) - 1;
+    m &= m - 1;
+    const uint64_t kk = __shfl_sync(FULL, key, src);
+    const int32_t ii = __shfl_sync(FULL, gidx, src);
+    if (n == K && !less_key(kk, ii, lk[K - 1], li[K - 1])) continue;
+    int lo = 0, hi = n;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (less_key(lk[mid], li[mid], kk, ii)) lo = mid + 1; else hi = mid;
+    }
+    const int last = (n < K) ? n : K - 1;            // [lo, last) moves right by one
+    if (last > lo) {
+      for (int c = (last - 1) >> 5; c >= (lo >> 5); --c) {
+        const int e = c * 32 + lane;
+        const bool mv = (e >= lo && e < last);
+        uint64_t tk = 0;
+        int32_t ti = 0;
+        if (mv) { tk = lk[e]; ti = li[e]; }
+        __syncwarp();
+        if (mv) { lk[e + 1] = tk; li[e + 1] = ti; }
+        __syncwarp();
+      }
+    }
+    if (lane == 0) { lk[lo] = kk; li[lo] = ii; }
+    __syncwarp();
+    if (n < K) ++n;
+  }
+}
+
+__global__ void k_select(SelectArgs a) {
+  extern __shared__ unsigned char smem[];
+  const int warps = blockDim.x >> 5;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t seg = (int64_t)blockIdx.x * warps + warp;
+  if (seg >= a.nseg) return;                         // uniform per warp
+  const int K = a.k;
+  uint64_t* lk = reinterpret_cast<uint64_t*>(smem) + (int64_t)warp * K;
+  int32_t* li = reinterpret_cast<int32_t*>(reinterpret_cast<uint64_t*>(smem) + (int64_t)warps * K) +
+                (int64_t)warp * K;
+  const bool dec = a.decreasing != 0;
+  const int64_t row = a.out_row0 + seg;
+  int n = 0;
+
+  const bool blank = a.seg_blank && a.seg_blank[row];
+  if (!blank) {
+    if (a.seed_idx) {
+      // Carried state: slots fill left to right, read up to the first NA.
+      for (int t0 = 0; t0 < K; t0 += 32) {
+        const int t = t0 + lane;
+        int32_t gi = NA_INT;
+        double v = 0.0;
+        if (t < K) { gi = a.seed_idx[(int64_t)t * a.seed_ld + row]; v = a.seed_val[(int64_t)t * a.seed_ld + row]; }
+        const bool bad = (t < K) && (gi == NA_INT || gi <= 0);
+        const unsigned bm = __ballot_sync(FULL, bad);
+        const int lim = bm ? (__ffs(bm) - 1) : 32;
+        const bool ok = (lane < lim) && (t < K);
+        insert_batch(ok, ok ? order_key(v, dec) : 0, ok ? gi - 1 : 0, lk, li, n, K, lane);
+        if (bm) break;
+      }
+    }
+    const int64_t skip = (a.skip_base >= 0) ? a.skip_base + seg
+                         : (a.skip_arr ? a.skip_arr[seg] : (int64_t)-1);
+    const double* base = a.vals + seg * a.seg_stride;
+    for (int64_t t0 = 0; t0 < a.len; t0 += 32) {
+      const int64_t t = t0 + lane;
+      bool ok = t < a.len;
+      uint64_t key = 0;
+      int32_t g = 0;
+      if (ok) {
+        const double v = base[t * a.elem_stride];
+        const int64_t gg = a.idx_base + t;
+        ok = isfinite(v) && gg != skip && !(a.elem_mask && a.elem_mask[t]);
+        key = order_key(v, dec);
+        g = (int32_t)gg;
+      }
+      insert_batch(ok, key, g, lk, li, n, K, lane);
+    }
+  }
+  for (int t = lane; t < K; t += 32) {
+    const int64_t at = (int64_t)t * a.out_ld + row;
+    if (t < n) { a.out_idx[at] = li[t] + 1; a.out_val[at] = key_value(lk[t], dec); }
+    else       { a.out_idx[at] = NA_INT;    a.out_val[at] = na_real(); }
+  }
+}
+
+}  // namespace
+
+void launch_select(const SelectArgs& a, cudaStream_t s) {
+  if (a.nseg <= 0) return;
+  int warps = 8;
+  while (warps > 1 && (size_t)warps * a.k * 12 > 48 * 1024) warps >>= 1;
+  const size_t smem = (size_t)warps * a.k * 12;
+  const int64_t blocks = (a.nseg + warps - 1) / warps;
+  k_select<<<(unsigned)blocks, warps * 32, smem, s>>>(a);
+}
+
+}  // namespace sdg
