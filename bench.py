@@ -1,0 +1,345 @@
+#!/usr/bin/env python
+"""bench.py -- kNN query columns per second of sparseKNN on GB300.
+
+Workload (configuration 2, "plain sparse kNN at scale"): a 30,000 x 200,000
+CSC float64 log-count matrix (per-column nnz ~ lognormal, mean 1,800, sdlog
+0.6; rows weighted by lognormal(0, 1.5) means; values log1p of NB(2) counts),
+generated seeded on the GPU (sparsedist_gb300/synth.py).  The reference
+matrix stays resident in HBM.  One step = one block of B query columns of
+that matrix searched against all 200,000 reference columns, cosine, k = 20,
+i.e. one block of sparseKNN(X[, block], X) -- the unit of the reference's
+own block loop (R/sparseKNN.R:248-294).
+
+* value: query columns / s with inputs resident in HBM (CUDA events on the
+  library's stream, which is torch's current stream).
+* e2e:   the same through the C ABI with host buffers: per step the query
+  block's CSC arrays are copied host -> device from pinned memory and the
+  idx / dist results device -> host, inside the timed region.
+* roofline: the bounding kernel's algorithmic bytes per launch over its
+  average CUDA-event duration (per-launch figure of the path: 12 bytes per
+  stored entry touched per evaluated pair, plus 12 bytes per output slot).
+* cpu_baseline: the reference's algorithm on this machine's host cores (the
+  oracle port, OpenMP over all cores) on one block of 256 query columns
+  against the full reference.
+
+--impl reference times that CPU implementation alone, on the same workload.
+Multi-GPU (torchrun): each rank searches its own query blocks against its
+own replica of the reference (query-column sharding, no collective on the
+data path); value = all ranks' columns / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METHOD_CODES = {"binary": 0, "cosine": 1, "euclidean": 2, "manhattan": 3, "pearson": 4, "js": 5}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--method", default="cosine")
+    ap.add_argument("--k", type=int, default=20)
+    ap.add_argument("--block", type=int, default=4096, help="query columns per step")
+    ap.add_argument("--ncol", type=int, default=200000)
+    ap.add_argument("--nrow", type=int, default=30000)
+    ap.add_argument("--mean-nnz", type=float, default=1800.0)
+    ap.add_argument("--engine", type=int, default=0, help="0 auto, 1 exact slab, 2 screened")
+    ap.add_argument("--cpu-cols", type=int, default=256, help="query columns of the CPU sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                      "--format=csv,noheader,nounits"], capture_output=True,
+                                     text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([s.strip() for s in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        sm = [float(s[1]) for s in self.samples if len(s) >= 9 and s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if len(s) >= 9 and s[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            if len(s) >= 9:
+                for n, v in zip(names, s[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(self.samples)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def make_workload(args, device):
+    from sparsedist_gb300 import synth
+    p, i, x = synth.logcount_csc(nrow=args.nrow, ncol=args.ncol, mean_nnz=args.mean_nnz, seed=2,
+                                 device=device)
+    return p, i, x
+
+
+def block_arrays(p, i, x, c0, c1):
+    a, b = int(p[c0]), int(p[c1])
+    return (p[c0:c1 + 1] - a).astype(np.int32), i[a:b], x[a:b]
+
+
+def bytes_alg(p, c0, c1, nnz_ref, ncol_ref, k, method):
+    """Per-launch algorithmic bytes: s * (nr * NNZ_Q + nq * NNZ_R) + nq * k * 12."""
+    s = 4 if method == "binary" else 12
+    nq = c1 - c0
+    nnz_q = int(p[c1]) - int(p[c0])
+    return s * (ncol_ref * nnz_q + nq * nnz_ref) + nq * k * 12
+
+
+def cpu_baseline(p, i, x, nrow, ncol, method, k, cols, threads):
+    import scipy.sparse as sp
+    from oracle import build as obuild
+    from oracle.pyoracle import Oracle
+    obuild.build_oracle()
+    orc = Oracle(threads=threads)
+    ref = sp.csc_matrix((x, i, p), shape=(nrow, ncol))
+    qp, qi, qx = block_arrays(p, i, x, 0, cols)
+    Q = sp.csc_matrix((qx, qi, qp), shape=(nrow, cols))
+    t0 = time.perf_counter()
+    orc.knn(Q, ref, k=k, method=method, block_size=256)
+    dt = time.perf_counter() - t0
+    return cols / dt, dt
+
+
+def run_reference(args):
+    """--impl reference: the reference's algorithm on the host cores."""
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    device = "cuda" if torch.cuda.is_available() else "cpu"
+    p, i, x = make_workload(args, device)
+    threads = os.cpu_count() or 1
+    cols = args.cpu_cols
+    for _ in range(args.warmup):
+        cpu_baseline(p, i, x, args.nrow, args.ncol, args.method, args.k, cols, threads)
+    t = 0.0
+    for _ in range(args.steps):
+        _, dt = cpu_baseline(p, i, x, args.nrow, args.ncol, args.method, args.k, cols, threads)
+        t += dt
+    v = cols * args.steps / t
+    print(json.dumps({
+        "impl": "reference", "metric": "kNN query columns/s (sparseKNN cosine k=20, config 2)",
+        "value": v, "unit": "columns/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000 * t / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(args, cols),
+        "cpu_baseline": {"value": v, "unit": "columns/s", "cores": threads, "kind": "port",
+                         "sample": "%d query columns x %d reference columns per step" % (cols, args.ncol)},
+        "e2e": {"value": v, "unit": "columns/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+
+
+def workload_config(args, block):
+    return {"workload": "config 2: sparseKNN(X[, block], X) on a resident %dx%d log-count CSC "
+                        "(nnz/col lognormal mean %.0f), %s, k=%d" % (args.nrow, args.ncol,
+                                                                    args.mean_nnz, args.method, args.k),
+            "nrow": args.nrow, "ncol": args.ncol, "query_block": block, "method": args.method,
+            "k": args.k, "l2": "inputs larger than L2: the 4.3 GB reference is streamed every step"}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+
+    from sparsedist_gb300 import _lib
+    p, i, x = make_workload(args, "cuda")
+    nnz_ref = int(p[-1])
+    ctx = _lib.Context(local)
+    ctx.set_engine(args.engine)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    lib = ctx.lib
+    ref = _lib.Resident(ctx, args.nrow, args.ncol, p, i, x)
+
+    B, K, W, k = args.block, args.steps, args.warmup, args.k
+    method = METHOD_CODES[args.method]
+    nblocks = args.ncol // B
+    steps = [((rank * (K + W) + s) % nblocks) * B for s in range(W + K)]
+    queries = [_lib.Resident(ctx, args.nrow, B, *block_arrays(p, i, x, c0, c0 + B)) for c0 in steps]
+    d_idx = torch.empty(B * k, dtype=torch.int32, device="cuda")
+    d_val = torch.empty(B * k, dtype=torch.float64, device="cuda")
+    keff = np.zeros(1, np.int32)
+    flags = np.zeros(1, np.int32)
+
+    def step(q):
+        _lib.check(lib.sdg_knn_resident_device(ctx.handle, q.handle, ref.handle, method, 1, k, 0, 1,
+                                               d_idx.data_ptr(), d_val.data_ptr(),
+                                               keff.ctypes.data, flags.ctypes.data))
+
+    for s in range(W):
+        step(queries[s])
+    torch.cuda.synchronize()
+    ctx.kernel_time()                      # reset
+    stats_launches = 0
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for s in range(K):
+            step(queries[W + s])
+        e1.record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    kms, klaunch = ctx.kernel_time()
+    stats_launches = ctx.stats()["kernels"]
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = world * B * K / (ms_max / 1000.0)
+
+    # roofline of the bounding kernel (per launch)
+    alg = np.mean([bytes_alg(p, c0, c0 + B, nnz_ref, args.ncol, k, args.method) for c0 in steps[W:]])
+    launches_per_step = max(1, klaunch // max(K, 1))
+    per_launch_ms = kms / max(klaunch, 1)
+    achieved = (alg / launches_per_step) / (per_launch_ms / 1000.0) / 1e9 if klaunch else None
+    peak, peak_kind = measured_peaks()
+
+    # end to end through the C ABI with host buffers (pinned)
+    e2e = None
+    if not args.no_e2e:
+        hq = []
+        for c0 in steps:
+            bp, bi, bx = block_arrays(p, i, x, c0, c0 + B)
+            pins = []
+            for a in (bp, bi, bx):
+                t_ = torch.empty(a.shape, dtype={np.int32: torch.int32, np.float64: torch.float64}[a.dtype.type],
+                                 pin_memory=True)
+                t_.numpy()[:] = a
+                pins.append(t_)
+            hq.append(pins)
+        h_idx = torch.empty(B * k, dtype=torch.int32, pin_memory=True)
+        h_val = torch.empty(B * k, dtype=torch.float64, pin_memory=True)
+
+        def e2e_step(pins):
+            held = _lib.HeldCSC(args.nrow, B, pins[0].numpy(), pins[1].numpy(), pins[2].numpy())
+            h = __import__("ctypes").c_void_p()
+            _lib.check(lib.sdg_matrix_upload(ctx.handle, held.ref, __import__("ctypes").byref(h)))
+            _lib.check(lib.sdg_knn_resident(ctx.handle, h, ref.handle, method, 1, k, 0, 1,
+                                            h_idx.data_ptr(), h_val.data_ptr(), keff.ctypes.data,
+                                            flags.ctypes.data))
+            lib.sdg_matrix_free(h)
+
+        for s in range(W):
+            e2e_step(hq[s])
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for s in range(K):
+            e2e_step(hq[W + s])
+        torch.cuda.synchronize()
+        et = torch.tensor([time.perf_counter() - t0], dtype=torch.float64, device="cuda")
+        if world > 1:
+            dist.all_reduce(et, op=dist.ReduceOp.MAX)
+        h2d = int(np.mean([sum(a.numel() * a.element_size() for a in pins) for pins in hq[W:]]))
+        e2e = {"value": world * B * K / float(et.item()), "unit": "columns/s",
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": B * k * 12}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        v, dt = cpu_baseline(p, i, x, args.nrow, args.ncol, args.method, k, args.cpu_cols, threads)
+        cpu = {"value": v, "unit": "columns/s", "cores": threads, "kind": "port",
+               "sample": "%d query columns x %d reference columns (one reference block), %.1f s"
+                         % (args.cpu_cols, args.ncol, dt)}
+
+    if rank == 0:
+        st = ctx.stats()
+        line = {
+            "metric": "kNN query columns/s (sparseKNN cosine k=20, config 2)",
+            "value": value, "unit": "columns/s", "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(args, B) | {"parallelism": "query-column shards x%d" % world,
+                                                  "nnz": nnz_ref, "engine": args.engine},
+            "e2e": e2e,
+            "gpu_launches": int(stats_launches) * K,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": (achieved / peak) if achieved else None, "traffic": None,
+                         "peak_kind": peak_kind, "kernel_ms_per_launch": per_launch_ms,
+                         "alg_bytes_per_launch": alg / launches_per_step},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "stats_last_call": st,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -165,12 +165,32 @@ SDG_API int sdg_knn_resident(sdg_ctx* ctx, const sdg_matrix* X, const sdg_matrix
                              int drop_degenerate, int32_t* idx, double* dist_out,
                              int* k_eff, int* flags);
 
+/* As sdg_knn_resident, with idx / dist_out in DEVICE memory (caller
+ * allocated, ncol(X) * k each); nothing is copied back and the call returns
+ * once the work is queued on the context's stream (stream order). */
+SDG_API int sdg_knn_resident_device(sdg_ctx* ctx, const sdg_matrix* X, const sdg_matrix* Y,
+                                    int method, int dist, int k, int include_self,
+                                    int drop_degenerate, int32_t* idx, double* dist_out,
+                                    int* k_eff, int* flags);
+
+/* Makes ctx launch its work on the caller's CUDA stream (a cudaStream_t
+ * passed as void*; NULL restores the context's own stream), so that a host
+ * framework can order and time the library's kernels on its stream. */
+SDG_API int sdg_ctx_set_stream(sdg_ctx* ctx, void* stream);
+
 /* Statistics of the last sdg_knn* call on ctx (for profiling and tests):
  * out[0] = pairs screened, out[1] = pairs re-ranked exactly, out[2] = queries
  * whose candidate buffer overflowed (finished by the exact path), out[3] =
  * kernels launched, out[4] = screening kernel time in microseconds (device
  * events), out[5] = total device time in microseconds. */
 SDG_API int sdg_last_stats(sdg_ctx* ctx, int64_t* out, int n);
+
+/* Device time of the kernel that bounds the kNN path (the pair-value slab of
+ * the exact engine, the screen of the screened engine), accumulated with
+ * CUDA events on the context's stream over every sdg_knn* call since the
+ * previous sdg_kernel_time call: *ms is the total, *launches the number of
+ * launches.  Synchronises with the last recorded launch and resets. */
+SDG_API int sdg_kernel_time(sdg_ctx* ctx, double* ms, int64_t* launches);
 
 /* Selects the candidate-generation engine for subsequent calls on ctx:
  * 0 = automatic, 1 = exact FP64 slab for every pair, 2 = screened (FP32 /

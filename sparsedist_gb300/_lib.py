@@ -27,7 +27,8 @@ NA_REAL_BITS = np.uint64(0x7FF00000000007A2)
 EXPORTED = ["sdg_version", "sdg_last_error", "sdg_ctx_create", "sdg_ctx_destroy", "sdg_ctx_cancel",
             "sdg_ctx_reset_cancel", "sdg_dist_cross", "sdg_topk_block", "sdg_topk_rows_accum",
             "sdg_snn_jaccard", "sdg_knn", "sdg_knn_cross", "sdg_snn_graph", "sdg_matrix_upload",
-            "sdg_matrix_free", "sdg_knn_resident", "sdg_last_stats", "sdg_ctx_set_engine"]
+            "sdg_matrix_free", "sdg_knn_resident", "sdg_knn_resident_device", "sdg_ctx_set_stream",
+            "sdg_last_stats", "sdg_ctx_set_engine", "sdg_kernel_time"]
 
 
 class SdgError(RuntimeError):
@@ -81,6 +82,9 @@ def load() -> C.CDLL:
             lib.sdg_matrix_free.argtypes = [v]
             lib.sdg_knn_resident.argtypes = [v, v, v, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                              v, v, v, v]
+            lib.sdg_knn_resident_device.argtypes = lib.sdg_knn_resident.argtypes
+            lib.sdg_ctx_set_stream.argtypes = [v, v]
+            lib.sdg_kernel_time.argtypes = [v, v, v]
             _lib = lib
     return _lib
 
@@ -121,11 +125,23 @@ class Context:
     def set_engine(self, engine: int):
         check(self.lib.sdg_ctx_set_engine(self.handle, int(engine)))
 
+    def set_stream(self, stream_ptr):
+        """Launch on the caller's CUDA stream (an integer cudaStream_t, e.g.
+        torch.cuda.current_stream().cuda_stream); None restores the own stream."""
+        check(self.lib.sdg_ctx_set_stream(self.handle, C.c_void_p(stream_ptr) if stream_ptr else None))
+
     def cancel(self):
         check(self.lib.sdg_ctx_cancel(self.handle))
 
     def reset_cancel(self):
         check(self.lib.sdg_ctx_reset_cancel(self.handle))
+
+    def kernel_time(self):
+        """(total ms, launches) of the bounding kernel since the last call."""
+        ms = np.zeros(1, np.float64)
+        n = np.zeros(1, np.int64)
+        check(self.lib.sdg_kernel_time(self.handle, ms.ctypes.data, n.ctypes.data))
+        return float(ms[0]), int(n[0])
 
     def stats(self):
         out = np.zeros(8, np.int64)
@@ -161,6 +177,29 @@ class HeldCSC:
     @property
     def ref(self):
         return C.byref(self.s)
+
+
+class Resident:
+    """An sdg_matrix: a CSC matrix kept in device memory (sdg_matrix_upload)."""
+
+    def __init__(self, ctx: Context, nrow, ncol, p, i, x):
+        self.ctx = ctx
+        held = HeldCSC(nrow, ncol, p, i, x)
+        h = C.c_void_p()
+        check(ctx.lib.sdg_matrix_upload(ctx.handle, held.ref, C.byref(h)))
+        self.handle = h
+        self.nrow, self.ncol = int(nrow), int(ncol)
+
+    def free(self):
+        if self.handle:
+            self.ctx.lib.sdg_matrix_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
 
 
 def na_real(shape) -> np.ndarray:

@@ -94,7 +94,13 @@ struct DevBuf {
   DevBuf(DevBuf&& o) noexcept : p(o.p), s(o.s) { o.p = nullptr; }
   DevBuf& operator=(DevBuf&& o) noexcept { release(); p = o.p; s = o.s; o.p = nullptr; return *this; }
   ~DevBuf() { release(); }
-  void release() { if (p) cudaFreeAsync(p, s); p = nullptr; }
+  // Buffers owned by a resident matrix outlive any one stream: they are
+  // released with the synchronous cudaFree (which also frees pool memory).
+  void detach() { s = nullptr; }
+  void release() {
+    if (p) { if (s) cudaFreeAsync(p, s); else cudaFree(p); }
+    p = nullptr;
+  }
   template <typename T> T* as() const { return static_cast<T*>(p); }
 };
 
@@ -105,12 +111,52 @@ struct DevBuf {
 // ---------------------------------------------------------------------------
 struct sdg_ctx {
   int device = 0;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;       // where work is launched
+  cudaStream_t own_stream = nullptr;   // the context's own stream
   std::atomic<int> cancel{0};
   int engine = 0;
   int64_t stats[8] = {0};
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  // event pairs bracketing the bounding kernel's launches (sdg_kernel_time)
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> tev;
+  size_t tev_used = 0;
+  double tev_folded_ms = 0.0;
+  int64_t tev_launches = 0;
 };
+
+namespace {
+
+void fold_kernel_times(sdg_ctx* c) {
+  if (c->tev_used == 0) return;
+  CK(cudaEventSynchronize(c->tev[c->tev_used - 1].second));
+  for (size_t t = 0; t < c->tev_used; ++t) {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, c->tev[t].first, c->tev[t].second));
+    c->tev_folded_ms += ms;
+  }
+  c->tev_used = 0;
+}
+
+}  // namespace
+
+// Brackets one launch of the bounding kernel (see sdg_kernel_time).
+void sdg_time_begin(sdg_ctx* c) {
+  if (c->tev_used == c->tev.size()) {
+    if (c->tev.size() >= 1024) fold_kernel_times(c);
+    else {
+      cudaEvent_t a, b;
+      CK(cudaEventCreate(&a));
+      CK(cudaEventCreate(&b));
+      c->tev.emplace_back(a, b);
+    }
+  }
+  CK(cudaEventRecord(c->tev[c->tev_used].first, c->stream));
+}
+void sdg_time_end(sdg_ctx* c) {
+  CK(cudaEventRecord(c->tev[c->tev_used].second, c->stream));
+  ++c->tev_used;
+  ++c->tev_launches;
+}
 
 struct sdg_matrix {
   sdg_ctx* ctx = nullptr;
@@ -125,6 +171,11 @@ struct sdg_matrix {
   bool have_moments = false;
   int js_status = 1;
   ScreenCache screen;           // per-method screening data (sdg_screen.h)
+
+  ~sdg_matrix() {
+    if (ctx) cudaStreamSynchronize(ctx->stream);
+    for (DevBuf* b : {&p, &i, &x, &empty, &uval, &scale, &s1, &s2}) b->detach();
+  }
 
   DevCsc dev() const {
     DevCsc d;
@@ -281,8 +332,10 @@ void exact_engine(sdg_ctx* c, const KnnPlan& P, sdg_matrix* ref, sdg_matrix* qry
   for (int64_t q0 = 0; q0 < nq; q0 += B) {
     check_cancel(c);
     const int64_t nb = std::min(B, nq - q0);
+    sdg_time_begin(c);
     launch_exact_slab(P.method, P.dist, ref->dev(), ra, qry->dev(), qa, q0, nb, P.ref_mask,
                       P.selfmode && P.include_self, self_value, D.as<double>(), s);
+    sdg_time_end(c);
     SelectArgs a;
     a.vals = D.as<double>();
     a.seg_stride = nr; a.elem_stride = 1; a.len = nr; a.nseg = nb;
@@ -424,7 +477,8 @@ SDG_API int sdg_ctx_create(int device, sdg_ctx** out) {
     if (device < 0) CK(cudaGetDevice(&device));
     c->device = device;
     CK(cudaSetDevice(device));
-    CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
+    c->stream = c->own_stream;
     for (auto& e : c->ev) CK(cudaEventCreate(&e));
     *out = c.release();
   });
@@ -434,7 +488,8 @@ SDG_API int sdg_ctx_destroy(sdg_ctx* c) {
   if (!c) return SDG_OK;
   cudaStreamSynchronize(c->stream);
   for (auto& e : c->ev) if (e) cudaEventDestroy(e);
-  cudaStreamDestroy(c->stream);
+  for (auto& pr : c->tev) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
+  cudaStreamDestroy(c->own_stream);
   delete c;
   return SDG_OK;
 }
@@ -451,10 +506,31 @@ SDG_API int sdg_ctx_reset_cancel(sdg_ctx* c) {
   return SDG_OK;
 }
 
+SDG_API int sdg_ctx_set_stream(sdg_ctx* c, void* stream) {
+  return guarded([&] {
+    if (!c) fail(SDG_E_ARG, "ctx must not be NULL");
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    c->stream = stream ? static_cast<cudaStream_t>(stream) : c->own_stream;
+  });
+}
+
 SDG_API int sdg_ctx_set_engine(sdg_ctx* c, int engine) {
   if (!c || engine < 0 || engine > 2) { g_err = "invalid engine"; return SDG_E_ARG; }
   c->engine = engine;
   return SDG_OK;
+}
+
+SDG_API int sdg_kernel_time(sdg_ctx* c, double* ms, int64_t* launches) {
+  return guarded([&] {
+    if (!c || !ms || !launches) fail(SDG_E_ARG, "NULL argument");
+    CK(cudaSetDevice(c->device));
+    fold_kernel_times(c);
+    *ms = c->tev_folded_ms;
+    *launches = c->tev_launches;
+    c->tev_folded_ms = 0.0;
+    c->tev_launches = 0;
+  });
 }
 
 SDG_API int sdg_last_stats(sdg_ctx* c, int64_t* out, int n) {
@@ -736,10 +812,30 @@ SDG_API int sdg_matrix_free(sdg_matrix* M) {
   if (!M) return SDG_OK;
   cudaSetDevice(M->ctx->device);
   cudaStream_t s = M->ctx->stream;
-  screen_cache_free(&M->screen, s);
-  delete M;
   cudaStreamSynchronize(s);
+  screen_cache_free(&M->screen, s);
+  cudaStreamSynchronize(s);
+  delete M;
   return SDG_OK;
+}
+
+SDG_API int sdg_knn_resident_device(sdg_ctx* c, const sdg_matrix* X, const sdg_matrix* Y,
+                                    int method, int dist, int k, int include_self,
+                                    int drop_degenerate, int32_t* idx, double* dist_out,
+                                    int* k_eff, int* flags) {
+  return guarded([&] {
+    if (!c || !X || !idx || !dist_out || !k_eff || !flags) fail(SDG_E_ARG, "NULL argument");
+    CK(cudaSetDevice(c->device));
+    *flags = 0;
+    if (k < 1) fail(SDG_E_ARG, kMsgK);
+    check_method(method, dist);
+    if (X->ncol < 1) fail(SDG_E_ARG, "'X' must have at least one column.");
+    if (Y && X->nrow != Y->nrow) fail(SDG_E_ROWS, "'X' and 'Y' must have the same number of rows.");
+    std::memset(c->stats, 0, sizeof c->stats);
+    knn_device(c, const_cast<sdg_matrix*>(X), const_cast<sdg_matrix*>(Y), method, dist, k,
+               include_self, drop_degenerate, false, 0, idx, dist_out, k_eff, flags, nullptr,
+               nullptr);
+  });
 }
 
 SDG_API int sdg_knn_resident(sdg_ctx* c, const sdg_matrix* X, const sdg_matrix* Y, int method,

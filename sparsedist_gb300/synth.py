@@ -1,0 +1,70 @@
+"""Seeded synthetic inputs with the shapes and value distributions of the
+benchmark configurations (the reference's own bench reads 10x PBMC downloads,
+bench/R/03-datasets.R:56-71, which are not available offline; these stand in
+for them).
+
+* ``uniform_csc``: nrow x ncol CSC, a uniform random pattern of exactly
+  round(density * nrow * ncol) positions, |N(0,1)| values (configuration 1:
+  2,000 x 10,000 at 2%).
+* ``logcount_csc``: single-cell-like log counts (configuration 2: 30,000 x
+  200,000): per-column nnz ~ lognormal(log(mean_nnz) - sdlog^2/2, sdlog)
+  clipped to [1, nrow]; rows drawn without replacement with probability
+  proportional to row means mu_r ~ lognormal(0, row_sdlog) (exponential-race
+  sampling); values log1p(NB(size 2, mean mu_r * s_c)) with column scales
+  s_c ~ lognormal(0, col_sdlog); zero counts are dropped, so no explicit zeros
+  are stored.  Generated on the GPU with torch (seeded), returned as host
+  numpy CSC arrays.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+
+def uniform_csc(nrow, ncol, density, seed=0):
+    import scipy.sparse as sp
+    rng = np.random.default_rng(seed)
+    M = sp.random(nrow, ncol, density=density, format="csc", random_state=rng,
+                  data_rvs=lambda n: np.abs(rng.standard_normal(n)))
+    M.sort_indices()
+    return M
+
+
+def logcount_csc(nrow=30000, ncol=200000, mean_nnz=1800.0, sdlog=0.6, row_sdlog=1.5,
+                 col_sdlog=0.5, seed=0, device="cuda", chunk=1024):
+    """Returns (p int32[ncol+1], i int32[nnz], x float64[nnz]) on the host."""
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed))
+    f64 = torch.float64
+    mu = torch.exp(torch.randn(nrow, generator=g, device=device, dtype=f64) * row_sdlog)
+    meanlog = math.log(mean_nnz) - sdlog * sdlog / 2.0
+    nnz_c = torch.exp(meanlog + sdlog * torch.randn(ncol, generator=g, device=device, dtype=f64))
+    nnz_c = torch.clamp(torch.round(nnz_c), 1, nrow).to(torch.int64)
+    s_c = torch.exp(col_sdlog * torch.randn(ncol, generator=g, device=device, dtype=f64))
+    inv_mu = (1.0 / mu)[None, :]
+    p = np.zeros(ncol + 1, np.int64)
+    rows_parts, vals_parts = [], []
+    for c0 in range(0, ncol, chunk):
+        c1 = min(ncol, c0 + chunk)
+        b = c1 - c0
+        u = torch.rand(b, nrow, generator=g, device=device, dtype=f64)
+        key = -torch.log1p(-u) * inv_mu                  # Exp(1) / mu_r: smallest keys win
+        kth = torch.sort(key, dim=1).values.gather(1, (nnz_c[c0:c1] - 1)[:, None])
+        mask = key <= kth
+        cols, rows = mask.nonzero(as_tuple=True)         # column-major: col, then row ascending
+        mean = mu[rows] * s_c[c0 + cols]
+        lam = torch._standard_gamma(torch.full_like(mean, 2.0), generator=g) * (mean / 2.0)
+        cnt = torch.poisson(lam, generator=g)
+        keep = cnt > 0
+        cols, rows, cnt = cols[keep], rows[keep], cnt[keep]
+        vals = torch.log1p(cnt)
+        per_col = torch.bincount(cols, minlength=b).cpu().numpy()
+        p[c0 + 1:c1 + 1] = per_col
+        rows_parts.append(rows.to(torch.int32).cpu().numpy())
+        vals_parts.append(vals.cpu().numpy())
+    p = np.cumsum(p)
+    if p[-1] >= 2 ** 31:
+        raise ValueError("nnz exceeds the dgCMatrix limit of 2^31 - 1")
+    return p.astype(np.int32), np.concatenate(rows_parts), np.concatenate(vals_parts)
