@@ -319,19 +319,25 @@ struct KnnPlan {
   const uint8_t* qry_blank = nullptr;  // degenerate query columns (or null)
 };
 
+double self_value_for(const KnnPlan& P) {
+  // R/sparseKNN.R:270-279
+  return (P.method == BINARY || P.method == COSINE || P.method == PEARSON) ? (P.dist ? 0.0 : 1.0)
+                                                                           : 0.0;
+}
+
+// Exact FP64 slab + exact top-k for query columns [q_lo, q_hi).
 void exact_engine(sdg_ctx* c, const KnnPlan& P, sdg_matrix* ref, sdg_matrix* qry,
-                  int32_t* d_idx, double* d_val) {
+                  int32_t* d_idx, double* d_val, int64_t q_lo, int64_t q_hi) {
   cudaStream_t s = c->stream;
   const int64_t nr = ref->ncol, nq = qry->ncol;
   const int64_t budget = (int64_t)1 << 30;                 // slab bytes per chunk
-  int64_t B = std::max<int64_t>(1, std::min<int64_t>(nq, budget / std::max<int64_t>(1, nr * 8)));
+  int64_t B = std::max<int64_t>(1, std::min<int64_t>(q_hi - q_lo, budget / std::max<int64_t>(1, nr * 8)));
   DevBuf D(sizeof(double) * (size_t)(nr * B), s);
   const ColAux ra = aux_of(ref), qa = aux_of(qry);
-  const double self_value =
-      (P.method == BINARY || P.method == COSINE || P.method == PEARSON) ? (P.dist ? 0.0 : 1.0) : 0.0;
-  for (int64_t q0 = 0; q0 < nq; q0 += B) {
+  const double self_value = self_value_for(P);
+  for (int64_t q0 = q_lo; q0 < q_hi; q0 += B) {
     check_cancel(c);
-    const int64_t nb = std::min(B, nq - q0);
+    const int64_t nb = std::min(B, q_hi - q0);
     sdg_time_begin(c);
     launch_exact_slab(P.method, P.dist, ref->dev(), ra, qry->dev(), qa, q0, nb, P.ref_mask,
                       P.selfmode && P.include_self, self_value, D.as<double>(), s);
@@ -351,9 +357,9 @@ void exact_engine(sdg_ctx* c, const KnnPlan& P, sdg_matrix* ref, sdg_matrix* qry
   CK(cudaGetLastError());
 }
 
-int pick_engine(sdg_ctx* c, const KnnPlan& P, int64_t nr, int64_t nq) {
+int pick_engine(sdg_ctx* c, const KnnPlan& P, int32_t nrow, int64_t nr, int64_t nq) {
   if (c->engine == 1) return 1;
-  if (!screen_supported(P.method, P.k)) return 1;
+  if (!screen_supported(P.method, P.k) || !screen_fits(nrow)) return 1;
   if (c->engine == 2) return 2;
   // Small problems: the exact slab is already latency-bound.
   return (nr * nq <= (int64_t)1 << 22) ? 1 : 2;
@@ -402,16 +408,24 @@ void knn_device(sdg_ctx* c, sdg_matrix* X, sdg_matrix* Y, int method, int dist, 
     d_idx = hold_idx->as<int32_t>();
     d_val = hold_val->as<double>();
   }
-  const int eng = pick_engine(c, P, ref->ncol, nq);
+  const int eng = pick_engine(c, P, ref->nrow, ref->ncol, nq);
   if (eng == 2) {
     ScreenRun r;
     r.method = method; r.dist = dist; r.k = k; r.decreasing = P.decreasing;
     r.selfmode = selfmode; r.include_self = P.include_self;
+    r.self_value = self_value_for(P);
     r.ref_mask = P.ref_mask; r.qry_blank = P.qry_blank;
-    screen_knn(c->stream, r, ref->dev(), aux_of(ref), &ref->screen, X->dev(), aux_of(X),
-               &X->screen, d_idx, d_val, c->stats, [c]() { check_cancel(c); });
+    r.qry_empty = X->empty.as<uint8_t>();
+    ScreenHooks h;
+    h.check_cancel = [c]() { check_cancel(c); };
+    h.time_begin = [c]() { sdg_time_begin(c); };
+    h.time_end = [c]() { sdg_time_end(c); };
+    h.exact_range = [&](int64_t q0, int64_t n) { exact_engine(c, P, ref, X, d_idx, d_val, q0, q0 + n); };
+    const int st = screen_knn(c->stream, r, ref->dev(), aux_of(ref), &ref->screen, X->dev(),
+                              aux_of(X), &X->screen, d_idx, d_val, c->stats, h);
+    if (st) cuda_check((cudaError_t)st, "screen_knn");
   } else {
-    exact_engine(c, P, ref, X, d_idx, d_val);
+    exact_engine(c, P, ref, X, d_idx, d_val, 0, nq);
   }
 }
 

@@ -234,6 +234,20 @@ __global__ void k_exact_pairs(int method, int dist, DevCsc ref, ColAux ra, DevCs
   out[t] = pair_value(method, dist != 0, ref, ra, ref_idx[t], qry, qa, qry_idx[t]);
 }
 
+// Candidate pairs of the screened engine: slots with ref_idx < 0 are unused;
+// with restore_self the self pair (ref == query) takes self_value.
+__global__ void k_exact_pairs_sparse(int method, int dist, DevCsc ref, ColAux ra, DevCsc qry,
+                                     ColAux qa, const int32_t* ref_idx, const int32_t* qry_idx,
+                                     int64_t npairs, int restore_self, double self_value,
+                                     double* out) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= npairs) return;
+  const int32_t c = ref_idx[t], q = qry_idx[t];
+  if (c < 0 || q < 0) return;
+  out[t] = (restore_self && c == q) ? self_value
+                                    : pair_value(method, dist != 0, ref, ra, c, qry, qa, q);
+}
+
 inline unsigned blocks_for(int64_t n, int threads) {
   return (unsigned)((n + threads - 1) / threads);
 }
@@ -276,6 +290,15 @@ void launch_exact_pairs(int method, int dist, const DevCsc& ref, const ColAux& r
   if (npairs > 0)
     k_exact_pairs<<<blocks_for(npairs, 128), 128, 0, s>>>(method, dist, ref, ra, qry, qa,
                                                            ref_idx, qry_idx, npairs, out);
+}
+
+void launch_exact_pairs_sparse(int method, int dist, const DevCsc& ref, const ColAux& ra,
+                               const DevCsc& qry, const ColAux& qa, const int32_t* ref_idx,
+                               const int32_t* qry_idx, int64_t npairs, int restore_self,
+                               double self_value, double* out, cudaStream_t s) {
+  if (npairs > 0)
+    k_exact_pairs_sparse<<<blocks_for(npairs, 128), 128, 0, s>>>(
+        method, dist, ref, ra, qry, qa, ref_idx, qry_idx, npairs, restore_self, self_value, out);
 }
 
 }  // namespace sdg

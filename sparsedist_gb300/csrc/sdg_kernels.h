@@ -30,6 +30,13 @@ void launch_exact_pairs(int method, int dist, const DevCsc& ref, const ColAux& r
                         const DevCsc& qry, const ColAux& qa, const int32_t* ref_idx,
                         const int32_t* qry_idx, int64_t npairs, double* out, cudaStream_t s);
 
+// Candidate pairs (screened engine): slots with ref_idx < 0 are skipped; with
+// restore_self the self pair takes self_value.
+void launch_exact_pairs_sparse(int method, int dist, const DevCsc& ref, const ColAux& ra,
+                               const DevCsc& qry, const ColAux& qa, const int32_t* ref_idx,
+                               const int32_t* qry_idx, int64_t npairs, int restore_self,
+                               double self_value, double* out, cudaStream_t s);
+
 // ---- sdg_select.cu: exact top-k selection --------------------------------------
 
 // One "segment" per output row: candidates are vals[seg*seg_stride +
@@ -57,6 +64,12 @@ struct SelectArgs {
   int64_t out_ld = 0, out_row0 = 0;
   int k = 1;
   int decreasing = 0;
+  // Candidate lists: when cand is set, element t of segment seg has global
+  // index cand[seg * cand_ld + t] and the segment's length is cand_count[seg]
+  // (len is then ignored).
+  const int32_t* cand = nullptr;
+  const int32_t* cand_count = nullptr;
+  int64_t cand_ld = 0;
 };
 constexpr int kMaxK = 1024;   // largest k the selection kernels hold on chip
 void launch_select(const SelectArgs& a, cudaStream_t s);

@@ -1,10 +1,58 @@
 // sdg_screen.cu -- the screened candidate engine (see sdg_screen.h).
+//
+// GB300 executes FP64 at roughly 1/70 of its FP32 rate, so evaluating every
+// column pair exactly in FP64 (as the reference does on the CPU) is bound by
+// the FP64 pipe.  This engine evaluates every pair in FP32 instead, with a
+// rigorous per-pair error bound E, and re-ranks in exact FP64 only the pairs
+// whose optimistic bound can still reach the k-th best pessimistic bound:
+//
+//   keep (q, c)  iff  key(q, c) + E(q, c) >= T_q - margin,
+//   T_q = k-th largest of key(q, c') - E(q, c') over eligible c'.
+//
+// Every member of the exact top-k (ties included) satisfies the test, so the
+// exact re-rank over the kept pairs returns exactly the reference's result.
+// A query whose kept set exceeds the candidate capacity is finished by the
+// exact slab engine instead.
+//
+// Screen kernel layout: one CTA of 512 threads holds a tile of up to 16 query
+// columns in shared memory as a row-indexed table -- mask16[r] (which tile
+// queries store row r), off16[r] (offset of row r's values within its 64-row
+// group), gbase[g] (offset of group g) and vals[] (the tile's values, row-major
+// then by query).  Each lane then walks one reference column (reference
+// columns are visited in descending-nnz order so the 32 lanes of a warp do
+// similar work), looks each stored row up in the table and accumulates 16
+// FP32 screen values in registers.  Work items (tile, reference part) are
+// handed out part-major by an atomic counter, so the 152 SMs stream the same
+// reference part at the same time and it is read from HBM about once.
+#include <cub/device/device_radix_sort.cuh>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
 #include "sdg_kernels.h"
 #include "sdg_screen.h"
 
 namespace sdg {
 namespace {
 
+constexpr int QT = 16;               // queries per tile
+constexpr int SCREEN_THREADS = 512;
+constexpr int SELECT_WARPS = 8;
+// dynamic shared memory of the screen kernel: the 227 KB per-CTA maximum less
+// room for its static shared memory
+constexpr size_t kSmemMax = 227 * 1024 - 1024;
+constexpr float U32 = 5.9604644775390625e-8f;   // 2^-24
+
+inline unsigned blocks_for(int64_t n, int threads) {
+  return (unsigned)((n + threads - 1) / threads);
+}
+
+#define SK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return (int)e_; } while (0)
+
+// ---------------------------------------------------------------------------
+// validation used at upload
+// ---------------------------------------------------------------------------
 __global__ void k_check_rows(DevCsc M, int* err) {
   const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (j >= M.ncol) return;
@@ -16,18 +64,573 @@ __global__ void k_check_rows(DevCsc M, int* err) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// per-matrix screening data
+// ---------------------------------------------------------------------------
+// fval: the value the screen multiplies (unit value for cosine, raw value for
+// euclidean / manhattan, 1 for binary); cnorm: sum of squares (euclidean) or
+// of magnitudes (manhattan), accumulated in FP64 then rounded; nnz per column.
+__global__ void k_screen_prep(DevCsc M, int method, const double* uval, float* fval, float* cnorm,
+                              int32_t* nnz) {
+  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (j >= M.ncol) return;
+  double acc = 0.0;
+  const int64_t a0 = M.p[j], a1 = M.p[j + 1];
+  for (int64_t a = a0; a < a1; ++a) {
+    const double v = M.x[a];
+    float f;
+    if (method == COSINE) f = (float)uval[a];
+    else if (method == BINARY) f = 1.0f;
+    else f = (float)v;
+    fval[a] = f;
+    if (method == EUCLIDEAN) acc += v * v;
+    else if (method == MANHATTAN) acc += fabs(v);
+  }
+  cnorm[j] = (float)acc;
+  nnz[j] = (int32_t)(a1 - a0);
+}
+
+__global__ void k_iota_neg_nnz(const int32_t* nnz, int64_t n, uint32_t* keys, int32_t* ids) {
+  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  keys[j] = 0x7fffffffu - (uint32_t)nnz[j];   // ascending key = descending nnz
+  ids[j] = (int32_t)j;
+}
+
+// ---------------------------------------------------------------------------
+// the screen kernel
+// ---------------------------------------------------------------------------
+struct ScreenArgs {
+  int method;
+  int32_t nrow;
+  int groups;                 // ceil(nrow / 64)
+  int vcap;                   // tile value capacity (floats)
+  // reference
+  const int64_t* rp; const int32_t* ri; const float* rv;
+  const int32_t* rperm;       // position -> reference column
+  int64_t nr;
+  // queries (columns of the query matrix)
+  const int64_t* qp; const int32_t* qi; const float* qv;
+  const int32_t* tile_q;      // first local query of each tile
+  const int32_t* tile_n;      // queries in each tile
+  int64_t q_begin;            // local query 0 = query column q_begin
+  int ntiles, nparts;
+  int64_t part_len;
+  float* S;                   // S[qlocal * nr + pos]
+  int* work;                  // work counter
+};
+
+__device__ __forceinline__ void accumulate(int method, float (&acc)[QT], uint32_t m, uint32_t base,
+                                           float v, const float* __restrict__ vals) {
+  if (method == MANHATTAN) {
+#pragma unroll
+    for (int j = 0; j < QT; ++j) {
+      if (m & (1u << j)) {
+        const float q = vals[base];
+        acc[j] += (fabsf(v) + fabsf(q)) - fabsf(v - q);
+        ++base;
+      }
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < QT; ++j) {
+      if (m & (1u << j)) {
+        acc[j] = fmaf(v, vals[base], acc[j]);
+        ++base;
+      }
+    }
+  }
+}
+
+template <int METHOD_KIND>   // 0: product, 1: manhattan
+__global__ void __launch_bounds__(SCREEN_THREADS, 1) k_screen(ScreenArgs A) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int nrow_pad = (A.nrow + 1) & ~1;
+  uint16_t* mask = reinterpret_cast<uint16_t*>(smem);
+  uint16_t* off = mask + nrow_pad;
+  uint32_t* gbase = reinterpret_cast<uint32_t*>(off + nrow_pad);
+  float* vals = reinterpret_cast<float*>(gbase + A.groups + 1);
+  __shared__ int s_item;
+  const int tid = threadIdx.x;
+  const int method = METHOD_KIND == 1 ? (int)MANHATTAN : (int)COSINE;
+  int cur_tile = -1;
+
+  for (;;) {
+    __syncthreads();
+    if (tid == 0) s_item = atomicAdd(A.work, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= A.ntiles * A.nparts) break;
+    const int part = item / A.ntiles, tile = item % A.ntiles;
+    const int tq0 = A.tile_q[tile], tn = A.tile_n[tile];
+
+    if (tile != cur_tile) {
+      // -- build the tile's row table --------------------------------------
+      uint32_t* mask32 = reinterpret_cast<uint32_t*>(mask);
+      for (int w = tid; w < nrow_pad / 2; w += SCREEN_THREADS) mask32[w] = 0u;
+      __syncthreads();
+      for (int j = 0; j < tn; ++j) {
+        const int64_t q = A.q_begin + tq0 + j;
+        const int64_t e0 = A.qp[q], e1 = A.qp[q + 1];
+        for (int64_t e = e0 + tid; e < e1; e += SCREEN_THREADS) {
+          const int32_t r = A.qi[e];
+          atomicOr(&mask32[r >> 1], 1u << (((r & 1) << 4) + j));
+        }
+      }
+      __syncthreads();
+      for (int g = tid; g < A.groups; g += SCREEN_THREADS) {
+        uint32_t run = 0;
+        const int r0 = g * 64, r1 = min(A.nrow, r0 + 64);
+        for (int r = r0; r < r1; ++r) { off[r] = (uint16_t)run; run += __popc((uint32_t)mask[r]); }
+        gbase[g] = run;
+      }
+      __syncthreads();
+      if (tid < 32) {                                   // exclusive scan of group sums
+        uint32_t carry = 0;
+        for (int g0 = 0; g0 < A.groups; g0 += 32) {
+          const int g = g0 + tid;
+          const uint32_t v = (g < A.groups) ? gbase[g] : 0u;
+          uint32_t x = v;
+#pragma unroll
+          for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+            if (tid >= d) x += y;
+          }
+          if (g < A.groups) gbase[g] = carry + x - v;
+          carry += __shfl_sync(0xffffffffu, x, 31);
+        }
+      }
+      __syncthreads();
+      for (int j = 0; j < tn; ++j) {
+        const int64_t q = A.q_begin + tq0 + j;
+        const int64_t e0 = A.qp[q], e1 = A.qp[q + 1];
+        const uint32_t below = (1u << j) - 1u;
+        for (int64_t e = e0 + tid; e < e1; e += SCREEN_THREADS) {
+          const int32_t r = A.qi[e];
+          const uint32_t pos = gbase[r >> 6] + off[r] + __popc((uint32_t)mask[r] & below);
+          if (pos < (uint32_t)A.vcap) vals[pos] = A.qv[e];
+        }
+      }
+      __syncthreads();
+      cur_tile = tile;
+    }
+
+    // -- stream the part's reference columns: one column per lane ----------
+    const int64_t p0 = (int64_t)part * A.part_len;
+    const int64_t p1 = min(A.nr, p0 + A.part_len);
+    for (int64_t pos = p0 + tid; pos < p1; pos += SCREEN_THREADS) {
+      const int32_t c = A.rperm[pos];
+      float acc[QT];
+#pragma unroll
+      for (int j = 0; j < QT; ++j) acc[j] = 0.f;
+      int64_t e = A.rp[c];
+      const int64_t e1 = A.rp[c + 1];
+      for (; e < e1 && (e & 3); ++e) {
+        const int32_t r = __ldg(A.ri + e);
+        const uint32_t m = mask[r];
+        if (m) accumulate(method, acc, m, gbase[r >> 6] + off[r], __ldg(A.rv + e), vals);
+      }
+      for (; e + 4 <= e1; e += 4) {
+        const int4 r4 = __ldg(reinterpret_cast<const int4*>(A.ri + e));
+        const float4 v4 = __ldg(reinterpret_cast<const float4*>(A.rv + e));
+        uint32_t m;
+        m = mask[r4.x]; if (m) accumulate(method, acc, m, gbase[r4.x >> 6] + off[r4.x], v4.x, vals);
+        m = mask[r4.y]; if (m) accumulate(method, acc, m, gbase[r4.y >> 6] + off[r4.y], v4.y, vals);
+        m = mask[r4.z]; if (m) accumulate(method, acc, m, gbase[r4.z >> 6] + off[r4.z], v4.z, vals);
+        m = mask[r4.w]; if (m) accumulate(method, acc, m, gbase[r4.w >> 6] + off[r4.w], v4.w, vals);
+      }
+      for (; e < e1; ++e) {
+        const int32_t r = __ldg(A.ri + e);
+        const uint32_t m = mask[r];
+        if (m) accumulate(method, acc, m, gbase[r >> 6] + off[r], __ldg(A.rv + e), vals);
+      }
+#pragma unroll
+      for (int j = 0; j < QT; ++j)
+        if (j < tn) A.S[(int64_t)(tq0 + j) * A.nr + pos] = acc[j];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// screen select: per query, the k-th pessimistic bound and the kept pairs
+// ---------------------------------------------------------------------------
+struct SelectScreenArgs {
+  int method, k;
+  const float* S;
+  int64_t nr;
+  const int32_t* rperm;
+  const int32_t* rnnz; const float* rnorm;
+  const int32_t* qnnz; const float* qnorm;   // indexed by query column
+  const uint8_t* ref_mask;                   // eligible reference columns
+  const uint8_t* qry_blank;                  // query rows written all-NA
+  const uint8_t* qry_force_exact;            // queries the screen cannot bound
+  int64_t q_begin, nq;                       // local queries of this chunk
+  int selfmode, include_self;                // self search: query q == reference q
+  int cap;
+  int32_t* cand;                             // [qlocal * cap + t] reference column
+  int32_t* count;                            // kept pairs per query (capped)
+  int32_t* overflow;                         // 1 = finish with the exact engine
+};
+
+// Larger key = better.  E bounds |key_fp32 - key_exact| (see the file header
+// and DESIGN notes of each method).
+__device__ __forceinline__ void key_and_bound(int method, float s, int32_t nq_, float Nq, int32_t nc_,
+                                              float Nc, float& key, float& err) {
+  const float n = (float)min(nq_, nc_);
+  if (method == COSINE) {
+    key = s;
+    err = (n + 40.f) * U32 * 1.01f + 1e-12f;
+  } else if (method == EUCLIDEAN) {
+    const float T = Nq + Nc;
+    key = 2.f * s - T;
+    err = ((n + 46.f) * U32 * 1.01f + 1e-12f) * T + 1e-30f;
+  } else if (method == MANHATTAN) {
+    const float T = Nq + Nc;
+    key = s - T;
+    err = ((n + 46.f) * U32 * 1.01f + 1e-12f) * T + 1e-30f;
+  } else {                                   // BINARY: s is the exact count
+    const float denom = (float)(nq_ + nc_) - s;
+    key = (denom > 0.f) ? s / denom : 1.f;
+    err = key * (4.f * U32) + 1e-30f;
+  }
+}
+
+__global__ void k_screen_select(SelectScreenArgs A) {
+  extern __shared__ float lists[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t ql = (int64_t)blockIdx.x * SELECT_WARPS + warp;
+  if (ql >= A.nq) return;
+  const int64_t q = A.q_begin + ql;
+  float* lst = lists + warp * A.k;
+  const int K = A.k;
+  if ((A.qry_blank && A.qry_blank[q]) ) {
+    if (lane == 0) { A.count[ql] = 0; A.overflow[ql] = 0; }
+    return;
+  }
+  if (A.qry_force_exact && A.qry_force_exact[q]) {
+    if (lane == 0) { A.count[ql] = 0; A.overflow[ql] = 1; }
+    return;
+  }
+  const int32_t nq_ = A.qnnz[q];
+  const float Nq = A.qnorm ? A.qnorm[q] : 0.f;
+  const float* Srow = A.S + ql * A.nr;
+  const int64_t self_c = A.selfmode ? q : -1;
+  int n = 0;
+  // pass 1: the k largest pessimistic keys
+  for (int64_t p0 = 0; p0 < A.nr; p0 += 32) {
+    const int64_t pos = p0 + lane;
+    float lo = -INFINITY;
+    bool ok = pos < A.nr;
+    if (ok) {
+      const int32_t c = A.rperm[pos];
+      if (A.ref_mask && A.ref_mask[c]) ok = false;
+      else if (c == self_c) {
+        if (A.include_self) lo = INFINITY; else ok = false;
+      } else {
+        float key, err;
+        key_and_bound(A.method, Srow[pos], nq_, Nq, A.rnnz[c], A.rnorm ? A.rnorm[c] : 0.f, key, err);
+        lo = key - err;
+      }
+    }
+    bool pass = ok && (n < K || lo > lst[K - 1]);
+    unsigned m = __ballot_sync(0xffffffffu, pass);
+    while (m) {
+      const int src = __ffs(m) - 1;
+      m &= m - 1;
+      const float v = __shfl_sync(0xffffffffu, lo, src);
+      if (n == K && !(v > lst[K - 1])) continue;
+      int lo_i = 0, hi_i = n;                       // first index with lst[i] < v
+      while (lo_i < hi_i) { const int mid = (lo_i + hi_i) >> 1; if (lst[mid] >= v) lo_i = mid + 1; else hi_i = mid; }
+      const int last = (n < K) ? n : K - 1;
+      if (last > lo_i) {
+        for (int cch = (last - 1) >> 5; cch >= (lo_i >> 5); --cch) {
+          const int e = cch * 32 + lane;
+          const bool mv = (e >= lo_i && e < last);
+          float t = 0.f;
+          if (mv) t = lst[e];
+          __syncwarp();
+          if (mv) lst[e + 1] = t;
+          __syncwarp();
+        }
+      }
+      if (lane == 0) lst[lo_i] = v;
+      __syncwarp();
+      if (n < K) ++n;
+    }
+  }
+  const float T = (n == K) ? lst[K - 1] : -INFINITY;
+  const float margin = (T == -INFINITY || T == INFINITY) ? 0.f : fabsf(T) * (8.f * U32) + 1e-30f;
+  // pass 2: keep every pair whose optimistic key reaches T
+  int cnt = 0;
+  bool over = false;
+  int32_t* out = A.cand + ql * (int64_t)A.cap;
+  for (int64_t p0 = 0; p0 < A.nr && !over; p0 += 32) {
+    const int64_t pos = p0 + lane;
+    bool keep = false;
+    int32_t c = -1;
+    if (pos < A.nr) {
+      c = A.rperm[pos];
+      if (A.ref_mask && A.ref_mask[c]) keep = false;
+      else if (c == self_c) keep = A.include_self != 0;
+      else {
+        float key, err;
+        key_and_bound(A.method, Srow[pos], nq_, Nq, A.rnnz[c], A.rnorm ? A.rnorm[c] : 0.f, key, err);
+        keep = (key + err) >= T - margin;
+      }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    const int rank = __popc(m & ((1u << lane) - 1u));
+    if (keep && cnt + rank < A.cap) out[cnt + rank] = c;
+    cnt += __popc(m);
+    if (cnt > A.cap) over = true;
+  }
+  if (lane == 0) {
+    A.count[ql] = over ? 0 : cnt;
+    A.overflow[ql] = over ? 1 : 0;
+  }
+}
+
+__global__ void k_exact_candidates_prep(const int32_t* count, int64_t nq, int cap, int32_t* qidx,
+                                        const int32_t* cand, int32_t* ridx, int64_t q_begin) {
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= nq * cap) return;
+  const int64_t ql = s / cap, t = s % cap;
+  if (t < count[ql]) { qidx[s] = (int32_t)(q_begin + ql); ridx[s] = cand[s]; }
+  else { qidx[s] = -1; ridx[s] = -1; }
+}
+
 }  // namespace
 
 void launch_check_rows(const DevCsc& M, int* err, cudaStream_t s) {
-  if (M.ncol > 0) k_check_rows<<<(unsigned)((M.ncol + 127) / 128), 128, 0, s>>>(M, err);
+  if (M.ncol > 0) k_check_rows<<<blocks_for(M.ncol, 128), 128, 0, s>>>(M, err);
 }
 
-bool screen_supported(int, int) { return false; }
+bool screen_supported(int method, int k) {
+  return (method == BINARY || method == COSINE || method == EUCLIDEAN || method == MANHATTAN) &&
+         k >= 1 && k <= 1024;
+}
 
-int screen_knn(cudaStream_t, const ScreenRun&, const DevCsc&, const ColAux&, ScreenCache*,
-               const DevCsc&, const ColAux&, ScreenCache*, int32_t*, double*, int64_t*,
-               const std::function<void()>&) {
-  return (int)cudaErrorNotSupported;
+static size_t table_bytes(int32_t nrow) {
+  const size_t nrow_pad = (size_t)((nrow + 1) & ~1);
+  const size_t groups = (size_t)(nrow + 63) / 64;
+  return nrow_pad * 4 + (groups + 1) * 4;
+}
+
+bool screen_fits(int32_t nrow) {
+  return nrow < (1 << 24) && table_bytes(nrow) + 4096 * 4 <= kSmemMax;
+}
+
+static int ensure_cache(ScreenCache* c, int method, const DevCsc& M, const ColAux& aux,
+                        cudaStream_t s) {
+  const int family = method;
+  if (c->method == family) return 0;
+  if (c->blob) { SK(cudaFreeAsync(c->blob, s)); *c = ScreenCache(); }
+  const int64_t nnz = M.ncol > 0 ? -1 : 0;
+  (void)nnz;
+  int64_t h_nnz = 0;
+  if (M.ncol > 0) SK(cudaMemcpyAsync(&h_nnz, M.p + M.ncol, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  SK(cudaStreamSynchronize(s));
+  const size_t bytes = sizeof(float) * ((size_t)h_nnz + 4) + sizeof(float) * ((size_t)M.ncol + 4) +
+                       sizeof(int32_t) * ((size_t)M.ncol + 4) * 2 + 64;
+  SK(cudaMallocAsync(&c->blob, bytes, s));
+  char* b = static_cast<char*>(c->blob);
+  c->fval = reinterpret_cast<float*>(b);
+  b += sizeof(float) * ((size_t)h_nnz + 4);
+  c->cnorm = reinterpret_cast<float*>(b);
+  b += sizeof(float) * ((size_t)M.ncol + 4);
+  c->nnz = reinterpret_cast<int32_t*>(b);
+  b += sizeof(int32_t) * ((size_t)M.ncol + 4);
+  c->perm = reinterpret_cast<int32_t*>(b);
+  c->nnz_total = h_nnz;
+  if (M.ncol > 0) {
+    k_screen_prep<<<blocks_for(M.ncol, 128), 128, 0, s>>>(M, method, aux.uval, c->fval, c->cnorm,
+                                                           c->nnz);
+    // descending-nnz order of the columns (radix sort on 32-bit keys)
+    uint32_t *k_in = nullptr, *k_out = nullptr;
+    int32_t* ids = nullptr;
+    void* tmp = nullptr;
+    size_t tb = 0;
+    SK(cudaMallocAsync(&k_in, sizeof(uint32_t) * M.ncol, s));
+    SK(cudaMallocAsync(&k_out, sizeof(uint32_t) * M.ncol, s));
+    SK(cudaMallocAsync(&ids, sizeof(int32_t) * M.ncol, s));
+    k_iota_neg_nnz<<<blocks_for(M.ncol, 256), 256, 0, s>>>(c->nnz, M.ncol, k_in, ids);
+    SK(cub::DeviceRadixSort::SortPairs(nullptr, tb, k_in, k_out, ids, c->perm, (int)M.ncol, 0, 32, s));
+    SK(cudaMallocAsync(&tmp, tb + 16, s));
+    SK(cub::DeviceRadixSort::SortPairs(tmp, tb, k_in, k_out, ids, c->perm, (int)M.ncol, 0, 32, s));
+    SK(cudaFreeAsync(tmp, s));
+    SK(cudaFreeAsync(k_in, s));
+    SK(cudaFreeAsync(k_out, s));
+    SK(cudaFreeAsync(ids, s));
+  }
+  SK(cudaGetLastError());
+  c->method = family;
+  return 0;
+}
+
+int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColAux& ra,
+               ScreenCache* rc, const DevCsc& qry, const ColAux& qa, ScreenCache* qc,
+               int32_t* d_idx, double* d_val, int64_t* stats, const ScreenHooks& hooks) {
+  SK((cudaError_t)ensure_cache(rc, r.method, ref, ra, s));
+  SK((cudaError_t)ensure_cache(qc, r.method, qry, qa, s));
+  const int64_t nr = ref.ncol, nq = qry.ncol;
+  const int32_t nrow = ref.nrow;
+  const size_t tbytes = table_bytes(nrow);
+  const int vcap = (int)std::min<size_t>((kSmemMax - tbytes - 256) / 4, 1u << 20);
+  const int groups = (nrow + 63) / 64;
+
+  // host copy of the query column sizes (tile formation)
+  std::vector<int32_t> hq_nnz((size_t)nq);
+  SK(cudaMemcpyAsync(hq_nnz.data(), qc->nnz, sizeof(int32_t) * nq, cudaMemcpyDeviceToHost, s));
+  std::vector<uint8_t> h_blank;
+  if (r.qry_blank) {
+    h_blank.resize((size_t)nq);
+    SK(cudaMemcpyAsync(h_blank.data(), r.qry_blank, (size_t)nq, cudaMemcpyDeviceToHost, s));
+  }
+  SK(cudaStreamSynchronize(s));
+
+  // queries per screen pass: the FP32 slab S is chunk x nr floats
+  const int64_t sbudget = (int64_t)4 << 30;
+  const int64_t chunk = std::max<int64_t>(QT, std::min<int64_t>(nq, sbudget / (4 * std::max<int64_t>(nr, 1))));
+  const int cap = std::max(256, std::min(8192, 16 * r.k + 64));
+
+  float* S = nullptr;
+  int32_t *cand = nullptr, *count = nullptr, *over = nullptr, *qidx = nullptr, *ridx = nullptr;
+  int32_t *tile_q = nullptr, *tile_n = nullptr;
+  int* work = nullptr;
+  double* rvals = nullptr;
+  uint8_t* force = nullptr;
+  const int64_t cslots = chunk * (int64_t)cap;
+  SK(cudaMallocAsync(&S, sizeof(float) * (size_t)(chunk * nr + 4), s));
+  SK(cudaMallocAsync(&cand, sizeof(int32_t) * (size_t)cslots, s));
+  SK(cudaMallocAsync(&count, sizeof(int32_t) * (size_t)chunk, s));
+  SK(cudaMallocAsync(&over, sizeof(int32_t) * (size_t)chunk, s));
+  SK(cudaMallocAsync(&qidx, sizeof(int32_t) * (size_t)cslots, s));
+  SK(cudaMallocAsync(&ridx, sizeof(int32_t) * (size_t)cslots, s));
+  SK(cudaMallocAsync(&rvals, sizeof(double) * (size_t)cslots, s));
+  SK(cudaMallocAsync(&tile_q, sizeof(int32_t) * (size_t)(chunk + 1), s));
+  SK(cudaMallocAsync(&tile_n, sizeof(int32_t) * (size_t)(chunk + 1), s));
+  SK(cudaMallocAsync(&work, sizeof(int), s));
+  // cosine cannot bound an all-zero query (its convention value is not a dot
+  // product): such queries go to the exact engine.
+  if (r.method == COSINE && r.qry_empty) force = const_cast<uint8_t*>(r.qry_empty);
+
+  const size_t smem = tbytes + (size_t)vcap * 4 + 64;
+  static bool attr_set[2] = {false, false};
+  if (!attr_set[0]) {
+    SK(cudaFuncSetAttribute(k_screen<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax));
+    SK(cudaFuncSetAttribute(k_screen<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax));
+    attr_set[0] = true;
+  }
+  int nsm = 152;
+  {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  }
+
+  std::vector<int> overflow_queries;
+  for (int64_t q0 = 0; q0 < nq; q0 += chunk) {
+    hooks.check_cancel();
+    const int64_t nb = std::min(chunk, nq - q0);
+    // tiles: up to QT consecutive queries whose values fit the table
+    std::vector<int32_t> tq, tn;
+    int64_t j = 0;
+    while (j < nb) {
+      int n = 0;
+      int64_t vals = 0;
+      while (j + n < nb && n < QT) {
+        const int64_t add = hq_nnz[(size_t)(q0 + j + n)];
+        if (n > 0 && vals + add > vcap) break;
+        vals += add;
+        ++n;
+      }
+      if (vals > vcap) {                        // a single query too large for the table
+        overflow_queries.push_back((int)(q0 + j));
+        // leave its S rows unused: it is finished by the exact engine
+      }
+      tq.push_back((int32_t)j);
+      tn.push_back(vals > vcap ? 0 : n);
+      j += n;
+    }
+    const int ntiles = (int)tq.size();
+    SK(cudaMemcpyAsync(tile_q, tq.data(), sizeof(int32_t) * ntiles, cudaMemcpyHostToDevice, s));
+    SK(cudaMemcpyAsync(tile_n, tn.data(), sizeof(int32_t) * ntiles, cudaMemcpyHostToDevice, s));
+    SK(cudaMemsetAsync(work, 0, sizeof(int), s));
+    // reference parts: a part's screen data should stay in L2 while all SMs read it
+    const int64_t ref_bytes = (rc->nnz_total + 1) * 8;
+    int nparts = (int)std::max<int64_t>(1, (ref_bytes + (48ll << 20) - 1) / (48ll << 20));
+    nparts = std::max(nparts, (2 * nsm + ntiles - 1) / ntiles);
+    nparts = (int)std::min<int64_t>(nparts, std::max<int64_t>(1, nr / 64));
+    const int64_t part_len = (nr + nparts - 1) / nparts;
+
+    ScreenArgs A;
+    A.method = r.method; A.nrow = nrow; A.groups = groups; A.vcap = vcap;
+    A.rp = ref.p; A.ri = ref.i; A.rv = rc->fval; A.rperm = rc->perm; A.nr = nr;
+    A.qp = qry.p; A.qi = qry.i; A.qv = qc->fval;
+    A.tile_q = tile_q; A.tile_n = tile_n; A.q_begin = q0; A.ntiles = ntiles; A.nparts = nparts;
+    A.part_len = part_len; A.S = S; A.work = work;
+    const int grid = std::min<int64_t>((int64_t)nsm, (int64_t)ntiles * nparts);
+    hooks.time_begin();
+    if (r.method == MANHATTAN) k_screen<1><<<grid, SCREEN_THREADS, smem, s>>>(A);
+    else k_screen<0><<<grid, SCREEN_THREADS, smem, s>>>(A);
+    hooks.time_end();
+    SK(cudaGetLastError());
+
+    SelectScreenArgs B;
+    B.method = r.method; B.k = r.k; B.S = S; B.nr = nr; B.rperm = rc->perm;
+    B.rnnz = rc->nnz; B.rnorm = (r.method == EUCLIDEAN || r.method == MANHATTAN) ? rc->cnorm : nullptr;
+    B.qnnz = qc->nnz; B.qnorm = (r.method == EUCLIDEAN || r.method == MANHATTAN) ? qc->cnorm : nullptr;
+    B.ref_mask = r.ref_mask; B.qry_blank = r.qry_blank; B.qry_force_exact = force;
+    B.q_begin = q0; B.nq = nb; B.selfmode = r.selfmode; B.include_self = r.include_self;
+    B.cap = cap; B.cand = cand; B.count = count; B.overflow = over;
+    const size_t ssmem = sizeof(float) * (size_t)SELECT_WARPS * r.k;
+    if (ssmem > 48 * 1024)
+      SK(cudaFuncSetAttribute(k_screen_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssmem));
+    k_screen_select<<<blocks_for(nb, SELECT_WARPS), SELECT_WARPS * 32, ssmem, s>>>(B);
+    SK(cudaGetLastError());
+
+    // exact FP64 values of the kept pairs, then the exact top-k
+    k_exact_candidates_prep<<<blocks_for(nb * cap, 256), 256, 0, s>>>(count, nb, cap, qidx, cand,
+                                                                        ridx, q0);
+    launch_exact_pairs_sparse(r.method, r.dist, ref, ra, qry, qa, ridx, qidx, nb * cap, r.selfmode &&
+                              r.include_self, r.self_value, rvals, s);
+    SelectArgs sa;
+    sa.vals = rvals; sa.seg_stride = cap; sa.elem_stride = 1; sa.nseg = nb;
+    sa.cand = cand; sa.cand_count = count; sa.cand_ld = cap;
+    sa.seg_blank = r.qry_blank;
+    sa.out_idx = d_idx; sa.out_val = d_val; sa.out_ld = nq; sa.out_row0 = q0;
+    sa.k = r.k; sa.decreasing = r.decreasing;
+    launch_select(sa, s);
+    SK(cudaGetLastError());
+
+    std::vector<int32_t> h_over((size_t)nb), h_count((size_t)nb);
+    SK(cudaMemcpyAsync(h_over.data(), over, sizeof(int32_t) * nb, cudaMemcpyDeviceToHost, s));
+    SK(cudaMemcpyAsync(h_count.data(), count, sizeof(int32_t) * nb, cudaMemcpyDeviceToHost, s));
+    SK(cudaStreamSynchronize(s));
+    for (int64_t t = 0; t < nb; ++t) {
+      if (h_over[(size_t)t]) overflow_queries.push_back((int)(q0 + t));
+      stats[1] += h_count[(size_t)t];
+    }
+    stats[0] += nb * nr;
+    stats[3] += 5;
+  }
+  std::sort(overflow_queries.begin(), overflow_queries.end());
+  overflow_queries.erase(std::unique(overflow_queries.begin(), overflow_queries.end()),
+                         overflow_queries.end());
+  stats[2] += (int64_t)overflow_queries.size();
+  SK(cudaFreeAsync(S, s)); SK(cudaFreeAsync(cand, s)); SK(cudaFreeAsync(count, s));
+  SK(cudaFreeAsync(over, s)); SK(cudaFreeAsync(qidx, s)); SK(cudaFreeAsync(ridx, s));
+  SK(cudaFreeAsync(rvals, s)); SK(cudaFreeAsync(tile_q, s)); SK(cudaFreeAsync(tile_n, s));
+  SK(cudaFreeAsync(work, s));
+  // queries the screen could not bound: the exact slab engine, run by runs
+  size_t a = 0;
+  while (a < overflow_queries.size()) {
+    size_t b = a + 1;
+    while (b < overflow_queries.size() && overflow_queries[b] == overflow_queries[b - 1] + 1) ++b;
+    hooks.exact_range(overflow_queries[a], (int64_t)(b - a));
+    a = b;
+  }
+  return 0;
 }
 
 void screen_cache_free(ScreenCache* c, cudaStream_t s) {

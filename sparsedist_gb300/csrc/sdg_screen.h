@@ -18,23 +18,34 @@ struct ScreenCache {
   void* blob = nullptr;      // one device allocation holding the arrays below
   float* fval = nullptr;     // per stored entry: value the screen multiplies
   float* cnorm = nullptr;    // per column: norm term of the method
+  int32_t* nnz = nullptr;    // per column: stored entries
+  int32_t* perm = nullptr;   // columns in descending-nnz order
+  int64_t nnz_total = 0;
 };
 
 struct ScreenRun {
   int method = 0, dist = 1, k = 1;
   bool decreasing = false, selfmode = false, include_self = false;
-  const uint8_t* ref_mask = nullptr;
-  const uint8_t* qry_blank = nullptr;
+  double self_value = 0.0;                 // restored self value (include_self)
+  const uint8_t* ref_mask = nullptr;       // excluded reference columns
+  const uint8_t* qry_blank = nullptr;      // query rows written all-NA
+  const uint8_t* qry_empty = nullptr;      // all-zero query columns
+};
+
+struct ScreenHooks {
+  std::function<void()> check_cancel;
+  std::function<void()> time_begin, time_end;        // bracket the screen kernel
+  std::function<void(int64_t, int64_t)> exact_range;  // finish queries [q0, q0+n) exactly
 };
 
 bool screen_supported(int method, int k);
+bool screen_fits(int32_t nrow);
 
-// Returns 0, a cudaError_t value, or -9 when cancelled.  stats: see
-// sdg_last_stats in include/sdgpu.h.
+// Returns 0 or a cudaError_t value; exceptions thrown by the hooks propagate.
+// stats: see sdg_last_stats in include/sdgpu.h.
 int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColAux& ra,
                ScreenCache* rc, const DevCsc& qry, const ColAux& qa, ScreenCache* qc,
-               int32_t* d_idx, double* d_val, int64_t* stats,
-               const std::function<void()>& check_cancel);
+               int32_t* d_idx, double* d_val, int64_t* stats, const ScreenHooks& hooks);
 
 void screen_cache_free(ScreenCache* c, cudaStream_t s);
 

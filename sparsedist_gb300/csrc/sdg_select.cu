@@ -88,14 +88,16 @@ __global__ void k_select(SelectArgs a) {
     const int64_t skip = (a.skip_base >= 0) ? a.skip_base + seg
                          : (a.skip_arr ? a.skip_arr[seg] : (int64_t)-1);
     const double* base = a.vals + seg * a.seg_stride;
-    for (int64_t t0 = 0; t0 < a.len; t0 += 32) {
+    const int64_t len = a.cand ? (int64_t)a.cand_count[seg] : a.len;
+    const int32_t* cidx = a.cand ? a.cand + seg * a.cand_ld : nullptr;
+    for (int64_t t0 = 0; t0 < len; t0 += 32) {
       const int64_t t = t0 + lane;
-      bool ok = t < a.len;
+      bool ok = t < len;
       uint64_t key = 0;
       int32_t g = 0;
       if (ok) {
         const double v = base[t * a.elem_stride];
-        const int64_t gg = a.idx_base + t;
+        const int64_t gg = cidx ? (int64_t)cidx[t] : a.idx_base + t;
         ok = isfinite(v) && gg != skip && !(a.elem_mask && a.elem_mask[t]);
         key = order_key(v, dec);
         g = (int32_t)gg;
