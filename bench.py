@@ -244,10 +244,12 @@ def main():
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
+        torch.cuda.nvtx.range_push("sdg_timed")      # ncu --nvtx-include sdg_timed/
         e0.record(stream)
         for s in range(K):
             step(queries[W + s])
         e1.record(stream)
+        torch.cuda.nvtx.range_pop()
         torch.cuda.synchronize()
     if world > 1:
         dist.barrier()

@@ -493,6 +493,13 @@ SDG_API int sdg_ctx_create(int device, sdg_ctx** out) {
     CK(cudaSetDevice(device));
     CK(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
     c->stream = c->own_stream;
+    // Keep freed pool memory mapped: the per-call slabs (up to a few GB) are
+    // re-allocated on every call and would otherwise be unmapped and mapped
+    // again at each synchronisation.
+    cudaMemPool_t pool;
+    CK(cudaDeviceGetDefaultMemPool(&pool, device));
+    uint64_t keep = UINT64_MAX;
+    CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
     for (auto& e : c->ev) CK(cudaEventCreate(&e));
     *out = c.release();
   });

@@ -28,23 +28,69 @@ __global__ void k_col_empty(DevCsc M, uint8_t* empty) {
   empty[j] = e;
 }
 
-// unit_csc: src/sparseDist.cpp:246-284 (dnrm2-style scaled sum of squares).
-__global__ void k_unit_csc(DevCsc M, double* uval, double* scale_out, int* err) {
-  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+// unit_csc: src/sparseDist.cpp:246-284, the dnrm2-style recurrence
+//   if (scale < a) { r = scale / a; ssq = 1 + ssq * r * r; scale = a; }
+//   else           { r = a / scale; ssq += r * r; }
+// over the non-zero entries, then u = (x / scale) / sqrt(ssq).  One warp per
+// column: the running scale is a prefix maximum, so every ratio r (and its
+// branch) is computed in parallel; only the sum-of-squares update is a serial
+// chain, run by lane 0 in the reference's order and expression form, so the
+// result is bit-identical to the reference's sequential loop.
+__global__ void k_unit_csc_warp(DevCsc M, double* uval, double* scale_out, int* err) {
+  __shared__ double s_r[8][32];
+  __shared__ int s_f[8][32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t j = blockIdx.x * (int64_t)(blockDim.x >> 5) + warp;
   if (j >= M.ncol) return;
-  double scale = 0.0, ssq = 1.0;
   const int64_t a0 = M.p[j], a1 = M.p[j + 1];
-  for (int64_t a = a0; a < a1; ++a) {
-    const double v = M.x[a];
-    if (!isfinite(v)) { atomicOr(err, 1); return; }
-    if (v == 0.0) continue;
-    const double av = fabs(v);
-    if (scale < av) { const double r = scale / av; ssq = dadd(1.0, dmul(dmul(ssq, r), r)); scale = av; }
-    else            { const double r = av / scale; ssq = dadd(ssq, dmul(r, r)); }
+  double scale = 0.0, ssq = 1.0;
+  bool bad = false;
+  for (int64_t c0 = a0; c0 < a1; c0 += 32) {
+    const int64_t a = c0 + lane;
+    double av = 0.0;
+    bool nz = false;
+    if (a < a1) {
+      const double v = M.x[a];
+      if (!isfinite(v)) bad = true;
+      nz = (v != 0.0);
+      av = fabs(v);
+    }
+    // exclusive prefix max of the magnitudes (scale before this element)
+    double incl = nz ? av : 0.0;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const double y = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl = fmax(incl, y);
+    }
+    double prev = __shfl_up_sync(0xffffffffu, incl, 1);
+    if (lane == 0) prev = 0.0;
+    prev = fmax(prev, scale);
+    int flag = 0;                  // 0: skip (zero), 1: new maximum, 2: below maximum
+    double r = 0.0;
+    if (nz) {
+      if (prev < av) { flag = 1; r = prev / av; }
+      else { flag = 2; r = av / prev; }
+    }
+    s_r[warp][lane] = r;
+    s_f[warp][lane] = flag;
+    __syncwarp();
+    if (lane == 0) {
+      const int n = (int)((a1 - c0) < 32 ? (a1 - c0) : 32);
+      for (int t = 0; t < n; ++t) {
+        const int f = s_f[warp][t];
+        const double rr = s_r[warp][t];
+        if (f == 1) ssq = dadd(1.0, dmul(dmul(ssq, rr), rr));
+        else if (f == 2) ssq = dadd(ssq, dmul(rr, rr));
+      }
+    }
+    __syncwarp();
+    scale = fmax(scale, __shfl_sync(0xffffffffu, incl, 31));
   }
+  if (__any_sync(0xffffffffu, bad)) { if (lane == 0) atomicOr(err, 1); return; }
+  ssq = __shfl_sync(0xffffffffu, ssq, 0);
   const double sq = sqrt(ssq);
-  scale_out[j] = scale;
-  for (int64_t a = a0; a < a1; ++a)
+  if (lane == 0) scale_out[j] = scale;
+  for (int64_t a = a0 + lane; a < a1; a += 32)
     uval[a] = (scale == 0.0) ? 0.0 : ((M.x[a]) / scale) / sq;
 }
 
@@ -248,6 +294,101 @@ __global__ void k_exact_pairs_sparse(int method, int dist, DevCsc ref, ColAux ra
                                     : pair_value(method, dist != 0, ref, ra, c, qry, qa, q);
 }
 
+// Match-only methods (binary, cosine, pearson): the value depends on the rows
+// both columns store, summed in ascending row order.  One warp per query row
+// of the candidate table: for each candidate, lanes take 32 consecutive
+// entries of the shorter column and binary-search them in the longer one; the
+// matched products are then added by lane 0 in ascending row order, so the sum
+// is the reference's sequential sum bit for bit.
+__device__ double warp_match_value(int method, bool dist, const DevCsc& A, const ColAux& aa,
+                                   int32_t i, const DevCsc& B, const ColAux& ba, int32_t j,
+                                   int lane) {
+  const int64_t ia0 = A.p[i], ia1 = A.p[i + 1], jb0 = B.p[j], jb1 = B.p[j + 1];
+  if (method == COSINE) {
+    const bool ea = (aa.scale[i] == 0.0), eb = (ba.scale[j] == 0.0);
+    if (ea || eb) { const double c = (ea && eb) ? 1.0 : 0.0; return dist ? dsub(1.0, c) : c; }
+  }
+  const bool a_short = (ia1 - ia0) <= (jb1 - jb0);
+  const int32_t* si = a_short ? A.i : B.i;
+  const int32_t* li = a_short ? B.i : A.i;
+  const int64_t s0 = a_short ? ia0 : jb0, s1 = a_short ? ia1 : jb1;
+  int64_t l0 = a_short ? jb0 : ia0;
+  const int64_t l1 = a_short ? jb1 : ia1;
+  const double* av = (method == COSINE) ? aa.uval : A.x;
+  const double* bv = (method == COSINE) ? ba.uval : B.x;
+  double sum = 0.0;
+  int64_t common = 0;
+  for (int64_t c0 = s0; c0 < s1 && l0 < l1; c0 += 32) {
+    const int64_t s = c0 + lane;
+    bool hit = false;
+    double prod = 0.0;
+    int64_t lb = l1;
+    if (s < s1) {
+      const int32_t r = __ldg(si + s);
+      int64_t lo = l0, hi = l1;                        // first index with row >= r
+      while (lo < hi) { const int64_t mid = (lo + hi) >> 1; if (__ldg(li + mid) < r) lo = mid + 1; else hi = mid; }
+      lb = lo;
+      if (lo < l1 && __ldg(li + lo) == r) {
+        hit = true;
+        if (method != BINARY) {
+          const int64_t ea_ = a_short ? s : lo, eb_ = a_short ? lo : s;
+          prod = dmul(av[ea_], bv[eb_]);
+        }
+      }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, hit);
+    common += __popc(m);
+    if (method != BINARY) {
+      for (int t = 0; t < 32; ++t) {
+        const double p = __shfl_sync(0xffffffffu, prod, t);
+        if ((m >> t) & 1u) sum = dadd(sum, p);
+      }
+    }
+    l0 = __shfl_sync(0xffffffffu, lb, 31);
+  }
+  if (method == BINARY) {
+    const double ni = (double)(ia1 - ia0), nj = (double)(jb1 - jb0), c = (double)common;
+    const double denom = dsub(dadd(ni, nj), c);
+    const double sim = (denom > 0.0) ? (c / denom) : 1.0;
+    return dist ? dsub(1.0, sim) : sim;
+  }
+  if (method == COSINE) {
+    double c = sum;
+    if (!(c == c)) c = 0.0;
+    else if (c > 1.0) c = 1.0;
+    else if (c < -1.0) c = -1.0;
+    return dist ? dsub(1.0, c) : c;
+  }
+  // pearson
+  const double N = (double)A.nrow;
+  const double norm = (A.nrow > 1) ? dsub(N, 1.0) : 1.0;
+  const double cov = dsub(sum, dmul(aa.s[i], ba.s[j]) / N) / norm;
+  const double va = dsub(aa.ss[i], dmul(aa.s[i], aa.s[i]) / N) / norm;
+  const double vb = dsub(ba.ss[j], dmul(ba.s[j], ba.s[j]) / N) / norm;
+  double c = cov / dmul(sqrt(va), sqrt(vb));
+  if (!isfinite(c)) c = 0.0;
+  if (c > 1.0) c = 1.0;
+  if (c < -1.0) c = -1.0;
+  return dist ? dsub(1.0, c) : c;
+}
+
+__global__ void k_rerank_warp(int method, int dist, DevCsc ref, ColAux ra, DevCsc qry, ColAux qa,
+                              const int32_t* cand, const int32_t* count, int cap, int64_t nq_local,
+                              int64_t q_begin, int restore_self, double self_value, double* out) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t ql = blockIdx.x * (int64_t)(blockDim.x >> 5) + warp;
+  if (ql >= nq_local) return;
+  const int32_t q = (int32_t)(q_begin + ql);
+  const int n = count[ql];
+  for (int t = 0; t < n; ++t) {
+    const int32_t c = cand[ql * cap + t];
+    double v;
+    if (restore_self && c == q) v = self_value;
+    else v = warp_match_value(method, dist != 0, ref, ra, c, qry, qa, q, lane);
+    if (lane == 0) out[ql * cap + t] = v;
+  }
+}
+
 inline unsigned blocks_for(int64_t n, int threads) {
   return (unsigned)((n + threads - 1) / threads);
 }
@@ -258,7 +399,7 @@ void launch_col_empty(const DevCsc& M, uint8_t* empty, cudaStream_t s) {
   if (M.ncol > 0) k_col_empty<<<blocks_for(M.ncol, 256), 256, 0, s>>>(M, empty);
 }
 void launch_unit_csc(const DevCsc& M, double* uval, double* scale, int* err, cudaStream_t s) {
-  if (M.ncol > 0) k_unit_csc<<<blocks_for(M.ncol, 128), 128, 0, s>>>(M, uval, scale, err);
+  if (M.ncol > 0) k_unit_csc_warp<<<blocks_for(M.ncol, 8), 256, 0, s>>>(M, uval, scale, err);
 }
 void launch_moments(const DevCsc& M, double* sum, double* sumsq, cudaStream_t s) {
   if (M.ncol > 0) k_moments<<<blocks_for(M.ncol, 128), 128, 0, s>>>(M, sum, sumsq);
@@ -290,6 +431,20 @@ void launch_exact_pairs(int method, int dist, const DevCsc& ref, const ColAux& r
   if (npairs > 0)
     k_exact_pairs<<<blocks_for(npairs, 128), 128, 0, s>>>(method, dist, ref, ra, qry, qa,
                                                            ref_idx, qry_idx, npairs, out);
+}
+
+bool rerank_warp_supported(int method) {
+  return method == BINARY || method == COSINE || method == PEARSON;
+}
+
+void launch_rerank_warp(int method, int dist, const DevCsc& ref, const ColAux& ra,
+                        const DevCsc& qry, const ColAux& qa, const int32_t* cand,
+                        const int32_t* count, int cap, int64_t nq_local, int64_t q_begin,
+                        int restore_self, double self_value, double* out, cudaStream_t s) {
+  if (nq_local > 0)
+    k_rerank_warp<<<blocks_for(nq_local, 8), 256, 0, s>>>(method, dist, ref, ra, qry, qa, cand,
+                                                          count, cap, nq_local, q_begin,
+                                                          restore_self, self_value, out);
 }
 
 void launch_exact_pairs_sparse(int method, int dist, const DevCsc& ref, const ColAux& ra,

@@ -37,6 +37,14 @@ void launch_exact_pairs_sparse(int method, int dist, const DevCsc& ref, const Co
                                const int32_t* qry_idx, int64_t npairs, int restore_self,
                                double self_value, double* out, cudaStream_t s);
 
+// Warp-cooperative exact values of a candidate table (cand[ql * cap + t] for
+// t < count[ql]) for the match-only methods (binary, cosine, pearson).
+bool rerank_warp_supported(int method);
+void launch_rerank_warp(int method, int dist, const DevCsc& ref, const ColAux& ra,
+                        const DevCsc& qry, const ColAux& qa, const int32_t* cand,
+                        const int32_t* count, int cap, int64_t nq_local, int64_t q_begin,
+                        int restore_self, double self_value, double* out, cudaStream_t s);
+
 // ---- sdg_select.cu: exact top-k selection --------------------------------------
 
 // One "segment" per output row: candidates are vals[seg*seg_stride +

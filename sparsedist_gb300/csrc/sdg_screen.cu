@@ -15,10 +15,10 @@
 // exact slab engine instead.
 //
 // Screen kernel layout: one CTA of 512 threads holds a tile of up to 16 query
-// columns in shared memory as a row-indexed table -- mask16[r] (which tile
-// queries store row r), off16[r] (offset of row r's values within its 64-row
-// group), gbase[g] (offset of group g) and vals[] (the tile's values, row-major
-// then by query).  Each lane then walks one reference column (reference
+// columns in shared memory as a row-indexed table -- one 32-bit word per row,
+// row[r] = (mask16 << 16) | off16 (mask16: which tile queries store row r;
+// off16: where row r's values start in vals[]) -- and vals[] (the tile's
+// values, row-major then by query).  Each lane then walks one reference column (reference
 // columns are visited in descending-nnz order so the 32 lanes of a warp do
 // similar work), looks each stored row up in the table and accumulates 16
 // FP32 screen values in registers.  Work items (tile, reference part) are
@@ -142,16 +142,21 @@ __device__ __forceinline__ void accumulate(int method, float (&acc)[QT], uint32_
   }
 }
 
+__device__ __forceinline__ void accumulate_word(int method, float (&acc)[QT], uint32_t w, float v,
+                                                const float* __restrict__ vals) {
+  const uint32_t m = w >> 16;
+  if (m) accumulate(method, acc, m, w & 0xffffu, v, vals);   // rows outside the tile: skip
+}
+
 template <int METHOD_KIND>   // 0: product, 1: manhattan
 __global__ void __launch_bounds__(SCREEN_THREADS, 1) k_screen(ScreenArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int nrow_pad = (A.nrow + 1) & ~1;
-  uint16_t* mask = reinterpret_cast<uint16_t*>(smem);
-  uint16_t* off = mask + nrow_pad;
-  uint32_t* gbase = reinterpret_cast<uint32_t*>(off + nrow_pad);
-  float* vals = reinterpret_cast<float*>(gbase + A.groups + 1);
+  // row[r] = (mask16 << 16) | offset of row r's first value in vals[]
+  uint32_t* row = reinterpret_cast<uint32_t*>(smem);
+  float* vals = reinterpret_cast<float*>(row + A.nrow);
   __shared__ int s_item;
-  const int tid = threadIdx.x;
+  __shared__ uint32_t s_warp[SCREEN_THREADS / 32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int method = METHOD_KIND == 1 ? (int)MANHATTAN : (int)COSINE;
   int cur_tile = -1;
 
@@ -166,39 +171,44 @@ __global__ void __launch_bounds__(SCREEN_THREADS, 1) k_screen(ScreenArgs A) {
 
     if (tile != cur_tile) {
       // -- build the tile's row table --------------------------------------
-      uint32_t* mask32 = reinterpret_cast<uint32_t*>(mask);
-      for (int w = tid; w < nrow_pad / 2; w += SCREEN_THREADS) mask32[w] = 0u;
+      for (int r = tid; r < A.nrow; r += SCREEN_THREADS) row[r] = 0u;
       __syncthreads();
       for (int j = 0; j < tn; ++j) {
         const int64_t q = A.q_begin + tq0 + j;
         const int64_t e0 = A.qp[q], e1 = A.qp[q + 1];
-        for (int64_t e = e0 + tid; e < e1; e += SCREEN_THREADS) {
-          const int32_t r = A.qi[e];
-          atomicOr(&mask32[r >> 1], 1u << (((r & 1) << 4) + j));
-        }
+        for (int64_t e = e0 + tid; e < e1; e += SCREEN_THREADS)
+          atomicOr(&row[A.qi[e]], 1u << (16 + j));
       }
       __syncthreads();
-      for (int g = tid; g < A.groups; g += SCREEN_THREADS) {
-        uint32_t run = 0;
-        const int r0 = g * 64, r1 = min(A.nrow, r0 + 64);
-        for (int r = r0; r < r1; ++r) { off[r] = (uint16_t)run; run += __popc((uint32_t)mask[r]); }
-        gbase[g] = run;
-      }
-      __syncthreads();
-      if (tid < 32) {                                   // exclusive scan of group sums
-        uint32_t carry = 0;
-        for (int g0 = 0; g0 < A.groups; g0 += 32) {
-          const int g = g0 + tid;
-          const uint32_t v = (g < A.groups) ? gbase[g] : 0u;
-          uint32_t x = v;
+      // exclusive scan of popc(mask) over rows: contiguous row ranges per thread
+      const int per = (A.nrow + SCREEN_THREADS - 1) / SCREEN_THREADS;
+      const int r0 = tid * per, r1 = min(A.nrow, r0 + per);
+      uint32_t sum = 0;
+      for (int r = r0; r < r1; ++r) sum += __popc(row[r] >> 16);
+      uint32_t x = sum;
 #pragma unroll
-          for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
-            if (tid >= d) x += y;
-          }
-          if (g < A.groups) gbase[g] = carry + x - v;
-          carry += __shfl_sync(0xffffffffu, x, 31);
+      for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+        if (lane >= d) x += y;
+      }
+      if (lane == 31) s_warp[warp] = x;
+      __syncthreads();
+      if (warp == 0) {
+        const uint32_t v = (lane < SCREEN_THREADS / 32) ? s_warp[lane] : 0u;
+        uint32_t t = v;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const uint32_t y = __shfl_up_sync(0xffffffffu, t, d);
+          if (lane >= d) t += y;
         }
+        if (lane < SCREEN_THREADS / 32) s_warp[lane] = t - v;
+      }
+      __syncthreads();
+      uint32_t run = s_warp[warp] + x - sum;
+      for (int r = r0; r < r1; ++r) {
+        const uint32_t w = row[r];
+        row[r] = (w & 0xffff0000u) | (run & 0xffffu);
+        run += __popc(w >> 16);
       }
       __syncthreads();
       for (int j = 0; j < tn; ++j) {
@@ -206,8 +216,8 @@ __global__ void __launch_bounds__(SCREEN_THREADS, 1) k_screen(ScreenArgs A) {
         const int64_t e0 = A.qp[q], e1 = A.qp[q + 1];
         const uint32_t below = (1u << j) - 1u;
         for (int64_t e = e0 + tid; e < e1; e += SCREEN_THREADS) {
-          const int32_t r = A.qi[e];
-          const uint32_t pos = gbase[r >> 6] + off[r] + __popc((uint32_t)mask[r] & below);
+          const uint32_t w = row[A.qi[e]];
+          const uint32_t pos = (w & 0xffffu) + __popc((w >> 16) & below);
           if (pos < (uint32_t)A.vcap) vals[pos] = A.qv[e];
         }
       }
@@ -225,25 +235,27 @@ __global__ void __launch_bounds__(SCREEN_THREADS, 1) k_screen(ScreenArgs A) {
       for (int j = 0; j < QT; ++j) acc[j] = 0.f;
       int64_t e = A.rp[c];
       const int64_t e1 = A.rp[c + 1];
-      for (; e < e1 && (e & 3); ++e) {
-        const int32_t r = __ldg(A.ri + e);
-        const uint32_t m = mask[r];
-        if (m) accumulate(method, acc, m, gbase[r >> 6] + off[r], __ldg(A.rv + e), vals);
+      for (; e < e1 && (e & 3); ++e)
+        accumulate_word(method, acc, row[__ldg(A.ri + e)], __ldg(A.rv + e), vals);
+      if (e + 4 <= e1) {
+        int4 rn = __ldg(reinterpret_cast<const int4*>(A.ri + e));
+        float4 vn = __ldg(reinterpret_cast<const float4*>(A.rv + e));
+        for (; e + 4 <= e1; e += 4) {
+          const int4 r4 = rn;
+          const float4 v4 = vn;
+          if (e + 8 <= e1) {                            // prefetch the next group
+            rn = __ldg(reinterpret_cast<const int4*>(A.ri + e + 4));
+            vn = __ldg(reinterpret_cast<const float4*>(A.rv + e + 4));
+          }
+          const uint32_t w0 = row[r4.x], w1 = row[r4.y], w2 = row[r4.z], w3 = row[r4.w];
+          accumulate_word(method, acc, w0, v4.x, vals);
+          accumulate_word(method, acc, w1, v4.y, vals);
+          accumulate_word(method, acc, w2, v4.z, vals);
+          accumulate_word(method, acc, w3, v4.w, vals);
+        }
       }
-      for (; e + 4 <= e1; e += 4) {
-        const int4 r4 = __ldg(reinterpret_cast<const int4*>(A.ri + e));
-        const float4 v4 = __ldg(reinterpret_cast<const float4*>(A.rv + e));
-        uint32_t m;
-        m = mask[r4.x]; if (m) accumulate(method, acc, m, gbase[r4.x >> 6] + off[r4.x], v4.x, vals);
-        m = mask[r4.y]; if (m) accumulate(method, acc, m, gbase[r4.y >> 6] + off[r4.y], v4.y, vals);
-        m = mask[r4.z]; if (m) accumulate(method, acc, m, gbase[r4.z >> 6] + off[r4.z], v4.z, vals);
-        m = mask[r4.w]; if (m) accumulate(method, acc, m, gbase[r4.w >> 6] + off[r4.w], v4.w, vals);
-      }
-      for (; e < e1; ++e) {
-        const int32_t r = __ldg(A.ri + e);
-        const uint32_t m = mask[r];
-        if (m) accumulate(method, acc, m, gbase[r >> 6] + off[r], __ldg(A.rv + e), vals);
-      }
+      for (; e < e1; ++e)
+        accumulate_word(method, acc, row[__ldg(A.ri + e)], __ldg(A.rv + e), vals);
 #pragma unroll
       for (int j = 0; j < QT; ++j)
         if (j < tn) A.S[(int64_t)(tq0 + j) * A.nr + pos] = acc[j];
@@ -410,11 +422,7 @@ bool screen_supported(int method, int k) {
          k >= 1 && k <= 1024;
 }
 
-static size_t table_bytes(int32_t nrow) {
-  const size_t nrow_pad = (size_t)((nrow + 1) & ~1);
-  const size_t groups = (size_t)(nrow + 63) / 64;
-  return nrow_pad * 4 + (groups + 1) * 4;
-}
+static size_t table_bytes(int32_t nrow) { return (size_t)nrow * 4 + 16; }
 
 bool screen_fits(int32_t nrow) {
   return nrow < (1 << 24) && table_bytes(nrow) + 4096 * 4 <= kSmemMax;
@@ -475,7 +483,8 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
   const int64_t nr = ref.ncol, nq = qry.ncol;
   const int32_t nrow = ref.nrow;
   const size_t tbytes = table_bytes(nrow);
-  const int vcap = (int)std::min<size_t>((kSmemMax - tbytes - 256) / 4, 1u << 20);
+  // row offsets are 16-bit: a tile holds at most 65,535 values
+  const int vcap = (int)std::min<size_t>((kSmemMax - tbytes - 256) / 4, 65535);
   const int groups = (nrow + 63) / 64;
 
   // host copy of the query column sizes (tile formation)
@@ -558,7 +567,7 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
     SK(cudaMemsetAsync(work, 0, sizeof(int), s));
     // reference parts: a part's screen data should stay in L2 while all SMs read it
     const int64_t ref_bytes = (rc->nnz_total + 1) * 8;
-    int nparts = (int)std::max<int64_t>(1, (ref_bytes + (48ll << 20) - 1) / (48ll << 20));
+    int nparts = (int)std::max<int64_t>(1, (ref_bytes + (96ll << 20) - 1) / (96ll << 20));
     nparts = std::max(nparts, (2 * nsm + ntiles - 1) / ntiles);
     nparts = (int)std::min<int64_t>(nparts, std::max<int64_t>(1, nr / 64));
     const int64_t part_len = (nr + nparts - 1) / nparts;
@@ -590,10 +599,15 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
     SK(cudaGetLastError());
 
     // exact FP64 values of the kept pairs, then the exact top-k
-    k_exact_candidates_prep<<<blocks_for(nb * cap, 256), 256, 0, s>>>(count, nb, cap, qidx, cand,
-                                                                        ridx, q0);
-    launch_exact_pairs_sparse(r.method, r.dist, ref, ra, qry, qa, ridx, qidx, nb * cap, r.selfmode &&
-                              r.include_self, r.self_value, rvals, s);
+    if (rerank_warp_supported(r.method)) {
+      launch_rerank_warp(r.method, r.dist, ref, ra, qry, qa, cand, count, cap, nb, q0,
+                         r.selfmode && r.include_self, r.self_value, rvals, s);
+    } else {
+      k_exact_candidates_prep<<<blocks_for(nb * cap, 256), 256, 0, s>>>(count, nb, cap, qidx,
+                                                                          cand, ridx, q0);
+      launch_exact_pairs_sparse(r.method, r.dist, ref, ra, qry, qa, ridx, qidx, nb * cap,
+                                r.selfmode && r.include_self, r.self_value, rvals, s);
+    }
     SelectArgs sa;
     sa.vals = rvals; sa.seg_stride = cap; sa.elem_stride = 1; sa.nseg = nb;
     sa.cand = cand; sa.cand_count = count; sa.cand_ld = cap;
