@@ -29,7 +29,31 @@ using namespace sdg;
 // ---------------------------------------------------------------------------
 namespace {
 
-thread_local std::string g_err;
+// The calling thread's last error message, in a fixed buffer so that setting
+// it never allocates.
+struct ErrBuf {
+  char text[1024] = {0};
+  size_t len = 0;
+  void set(const char* s, size_t n) {
+    n = std::min(n, sizeof(text) - 1);
+    std::memcpy(text, s, n);
+    text[n] = '\0';
+    len = n;
+  }
+  ErrBuf& operator=(const std::string& s) { set(s.data(), s.size()); return *this; }
+  ErrBuf& operator=(const char* s) { set(s, std::strlen(s)); return *this; }
+  size_t size() const { return len; }
+  const char* data() const { return text; }
+};
+thread_local ErrBuf g_err;
+
+}  // namespace
+
+namespace sdg {
+void set_error(const char* msg) { g_err = msg; }
+}  // namespace sdg
+
+namespace {
 
 struct Fail {
   int code;

@@ -9,6 +9,9 @@
 
 namespace sdg {
 
+// Sets the calling thread's error message (sdg_last_error); never allocates.
+void set_error(const char* msg);
+
 // ---- sdg_exact.cu: per-column preparation and exact FP64 pair values --------
 void launch_col_empty(const DevCsc& M, uint8_t* empty, cudaStream_t s);
 void launch_unit_csc(const DevCsc& M, double* uval, double* scale, int* err, cudaStream_t s);

@@ -10,6 +10,7 @@
 #include <cub/device/device_select.cuh>
 
 #include "sdg_kernels.h"
+#include "sdg_snn_core.cuh"
 
 namespace sdg {
 namespace {
@@ -18,66 +19,25 @@ inline unsigned blocks_for(int64_t n, int threads) {
   return (unsigned)((n + threads - 1) / threads);
 }
 
-// copy_indices range check: src/snn.cpp:94-108
 __global__ void k_snn_check(const int32_t* idx, int64_t total, int32_t n, int* err) {
   for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < total;
        a += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t v = idx[a];
-    if (v != NA_INT && (v < 1 || v > n)) { atomicOr(err, 1); return; }
+    if (snn_index_bad(idx[a], n)) { atomicOr(err, 1); return; }
   }
 }
 
-// build_sets: src/snn.cpp:119-141
 __global__ void k_snn_sets(const int32_t* idx, int32_t n, int32_t k, int include_self,
                            int32_t* sets, int32_t* sizes) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  int32_t* S = sets + i * (int64_t)(k + 1);
-  int c = 0;
-  if (include_self) S[c++] = (int32_t)i;
-  for (int32_t t = 0; t < k; ++t) {
-    const int32_t v = idx[(int64_t)t * n + i];
-    if (v == NA_INT) continue;
-    if (v - 1 != i) S[c++] = v - 1;
-  }
-  for (int a = 1; a < c; ++a) {                       // insertion sort (c <= k + 1)
-    const int32_t x = S[a];
-    int b = a - 1;
-    while (b >= 0 && S[b] > x) { S[b + 1] = S[b]; --b; }
-    S[b + 1] = x;
-  }
-  int u = 0;
-  for (int a = 0; a < c; ++a)
-    if (u == 0 || S[u - 1] != S[a]) S[u++] = S[a];
-  sizes[i] = u;
+  sizes[i] = snn_build_set(idx, n, k, include_self, i, sets + i * (int64_t)(k + 1));
 }
 
-// per-slot weight: src/snn.cpp:224-242, inter_size :73-82, jaccard_from_counts :179-181
 __global__ void k_snn_weights(const int32_t* idx, int32_t n, int32_t k, const int32_t* sets,
                               const int32_t* sizes, double* w) {
   const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (a >= (int64_t)n * k) return;
-  const int64_t i = a % n;
-  const int32_t v = idx[a];
-  double out = na_real();
-  const int32_t ni = sizes[i];
-  if (v != NA_INT && ni > 0) {
-    const int64_t j = v - 1;
-    const int32_t nj = sizes[j];
-    if (nj > 0) {
-      const int32_t* Si = sets + i * (int64_t)(k + 1);
-      const int32_t* Sj = sets + j * (int64_t)(k + 1);
-      int64_t c = 0, x = 0, y = 0;
-      while (x < ni && y < nj) {
-        const int32_t p = Si[x], q = Sj[y];
-        if (p < q) ++x;
-        else if (q < p) ++y;
-        else { ++c; ++x; ++y; }
-      }
-      out = (double)c / (double)((int64_t)ni + nj - c);
-    }
-  }
-  w[a] = out;
+  w[a] = snn_weight(idx, n, k, sets, sizes, a);
 }
 
 // keep <- !is.na(w) & !is.na(idx) & (w > prune)  (R/sparseSNN.R:226); each kept
