@@ -28,7 +28,7 @@ EXPORTED = ["sdg_version", "sdg_last_error", "sdg_ctx_create", "sdg_ctx_destroy"
             "sdg_ctx_reset_cancel", "sdg_dist_cross", "sdg_topk_block", "sdg_topk_rows_accum",
             "sdg_snn_jaccard", "sdg_knn", "sdg_knn_cross", "sdg_snn_graph", "sdg_matrix_upload",
             "sdg_matrix_free", "sdg_knn_resident", "sdg_knn_resident_device", "sdg_ctx_set_stream",
-            "sdg_last_stats", "sdg_ctx_set_engine", "sdg_kernel_time"]
+            "sdg_last_stats", "sdg_ctx_set_engine", "sdg_kernel_time", "sdg_knn_block"]
 
 
 class SdgError(RuntimeError):
@@ -84,6 +84,8 @@ def load() -> C.CDLL:
                                              v, v, v, v]
             lib.sdg_knn_resident_device.argtypes = lib.sdg_knn_resident.argtypes
             lib.sdg_ctx_set_stream.argtypes = [v, v]
+            lib.sdg_knn_block.argtypes = [v, v, v, C.c_int64, C.c_int64, C.c_int, C.c_int, C.c_int,
+                                          C.c_int, C.c_int, v, v, C.c_int, v, v]
             lib.sdg_kernel_time.argtypes = [v, v, v]
             _lib = lib
     return _lib

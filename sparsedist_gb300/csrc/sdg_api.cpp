@@ -341,6 +341,8 @@ struct KnnPlan {
   bool selfmode = false, include_self = false;
   const uint8_t* ref_mask = nullptr;   // degenerate reference columns (or null)
   const uint8_t* qry_blank = nullptr;  // degenerate query columns (or null)
+  // result row of query column q: q - out_first, leading dimension out_ld
+  int64_t out_first = 0, out_ld = 0;
 };
 
 double self_value_for(const KnnPlan& P) {
@@ -371,8 +373,8 @@ void exact_engine(sdg_ctx* c, const KnnPlan& P, sdg_matrix* ref, sdg_matrix* qry
     a.seg_stride = nr; a.elem_stride = 1; a.len = nr; a.nseg = nb;
     a.idx_base = 0;
     a.skip_base = (P.selfmode && !P.include_self) ? q0 : -1;
-    a.seg_blank = P.qry_blank;
-    a.out_idx = d_idx; a.out_val = d_val; a.out_ld = nq; a.out_row0 = q0;
+    a.seg_blank = P.qry_blank ? P.qry_blank + P.out_first : nullptr;
+    a.out_idx = d_idx; a.out_val = d_val; a.out_ld = P.out_ld; a.out_row0 = q0 - P.out_first;
     a.k = P.k; a.decreasing = P.decreasing;
     launch_select(a, s);
     c->stats[1] += nr * nb;
@@ -390,10 +392,12 @@ int pick_engine(sdg_ctx* c, const KnnPlan& P, int32_t nrow, int64_t nr, int64_t 
 }
 
 // sparseKNN core (R/sparseKNN.R:183-301) after argument checks.
+// Computes rows [q_lo, q_hi) (q_hi < 0: all) of the result, laid out as a
+// (q_hi - q_lo) x k column-major matrix.
 void knn_device(sdg_ctx* c, sdg_matrix* X, sdg_matrix* Y, int method, int dist, int k,
                 int include_self, int drop_degenerate, bool cross_side, int side,
                 int32_t* d_idx_out, double* d_val_out, int* k_eff, int* flags,
-                DevBuf* hold_idx, DevBuf* hold_val) {
+                DevBuf* hold_idx, DevBuf* hold_val, int64_t q_lo = 0, int64_t q_hi = -1) {
   const bool selfmode = (Y == nullptr);
   sdg_matrix* ref = selfmode ? X : Y;
   ensure_empty(ref);
@@ -423,7 +427,12 @@ void knn_device(sdg_ctx* c, sdg_matrix* X, sdg_matrix* Y, int method, int dist, 
   P.qry_blank = drop_degenerate ? X->empty.as<uint8_t>() : nullptr;
 
   cudaStream_t s = c->stream;
-  const int64_t nq = X->ncol;
+  const int64_t nq_all = X->ncol;
+  if (q_hi < 0) q_hi = nq_all;
+  if (q_lo < 0 || q_hi > nq_all || q_lo >= q_hi) fail(SDG_E_ARG, "invalid query column range");
+  const int64_t nq = q_hi - q_lo;
+  P.out_first = q_lo;
+  P.out_ld = nq;
   int32_t* d_idx = d_idx_out;
   double* d_val = d_val_out;
   if (!d_idx) {
@@ -440,6 +449,7 @@ void knn_device(sdg_ctx* c, sdg_matrix* X, sdg_matrix* Y, int method, int dist, 
     r.self_value = self_value_for(P);
     r.ref_mask = P.ref_mask; r.qry_blank = P.qry_blank;
     r.qry_empty = X->empty.as<uint8_t>();
+    r.q_lo = q_lo; r.q_hi = q_hi; r.out_first = q_lo; r.out_ld = nq;
     ScreenHooks h;
     h.check_cancel = [c]() { check_cancel(c); };
     h.time_begin = [c]() { sdg_time_begin(c); };
@@ -449,7 +459,7 @@ void knn_device(sdg_ctx* c, sdg_matrix* X, sdg_matrix* Y, int method, int dist, 
                               aux_of(X), &X->screen, d_idx, d_val, c->stats, h);
     if (st) cuda_check((cudaError_t)st, "screen_knn");
   } else {
-    exact_engine(c, P, ref, X, d_idx, d_val, 0, nq);
+    exact_engine(c, P, ref, X, d_idx, d_val, q_lo, q_hi);
   }
 }
 
@@ -795,6 +805,32 @@ SDG_API int sdg_knn(sdg_ctx* c, const sdg_csc* X, const sdg_csc* Y, int method, 
     CK(cudaMemcpyAsync(idx, hi.p, sizeof(int32_t) * cnt, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(dist_out, hv.p, sizeof(double) * cnt, cudaMemcpyDeviceToHost, c->stream));
     end_stats(c);
+  });
+}
+
+SDG_API int sdg_knn_block(sdg_ctx* c, const sdg_matrix* X, const sdg_matrix* Y, int64_t q0,
+                          int64_t nq, int method, int dist, int k, int include_self,
+                          int drop_degenerate, int32_t* idx, double* dist_out, int device_out,
+                          int* k_eff, int* flags) {
+  return guarded([&] {
+    if (!c || !X || !idx || !dist_out || !k_eff || !flags) fail(SDG_E_ARG, "NULL argument");
+    CK(cudaSetDevice(c->device));
+    *flags = 0;
+    if (k < 1) fail(SDG_E_ARG, kMsgK);
+    check_method(method, dist);
+    if (Y && X->nrow != Y->nrow) fail(SDG_E_ROWS, "'X' and 'Y' must have the same number of rows.");
+    if (q0 < 0 || nq < 1 || q0 + nq > X->ncol) fail(SDG_E_ARG, "invalid query column range");
+    std::memset(c->stats, 0, sizeof c->stats);
+    DevBuf hi, hv;
+    knn_device(c, const_cast<sdg_matrix*>(X), const_cast<sdg_matrix*>(Y), method, dist, k,
+               include_self, drop_degenerate, false, 0, device_out ? idx : nullptr,
+               device_out ? dist_out : nullptr, k_eff, flags, &hi, &hv, q0, q0 + nq);
+    if (!device_out) {
+      const size_t cnt = (size_t)nq * (size_t)*k_eff;
+      CK(cudaMemcpyAsync(idx, hi.p, sizeof(int32_t) * cnt, cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaMemcpyAsync(dist_out, hv.p, sizeof(double) * cnt, cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaStreamSynchronize(c->stream));
+    }
   });
 }
 

@@ -490,16 +490,14 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
   // host copy of the query column sizes (tile formation)
   std::vector<int32_t> hq_nnz((size_t)nq);
   SK(cudaMemcpyAsync(hq_nnz.data(), qc->nnz, sizeof(int32_t) * nq, cudaMemcpyDeviceToHost, s));
-  std::vector<uint8_t> h_blank;
-  if (r.qry_blank) {
-    h_blank.resize((size_t)nq);
-    SK(cudaMemcpyAsync(h_blank.data(), r.qry_blank, (size_t)nq, cudaMemcpyDeviceToHost, s));
-  }
   SK(cudaStreamSynchronize(s));
+  const int64_t q_lo = r.q_lo, q_hi = (r.q_hi < 0) ? nq : r.q_hi;
+  const int64_t out_ld = (r.out_ld < 0) ? nq : r.out_ld;
 
   // queries per screen pass: the FP32 slab S is chunk x nr floats
   const int64_t sbudget = (int64_t)4 << 30;
-  const int64_t chunk = std::max<int64_t>(QT, std::min<int64_t>(nq, sbudget / (4 * std::max<int64_t>(nr, 1))));
+  const int64_t chunk = std::max<int64_t>(
+      QT, std::min<int64_t>(std::max<int64_t>(q_hi - q_lo, 1), sbudget / (4 * std::max<int64_t>(nr, 1))));
   const int cap = std::max(256, std::min(8192, 16 * r.k + 64));
 
   float* S = nullptr;
@@ -538,9 +536,9 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
   }
 
   std::vector<int> overflow_queries;
-  for (int64_t q0 = 0; q0 < nq; q0 += chunk) {
+  for (int64_t q0 = q_lo; q0 < q_hi; q0 += chunk) {
     hooks.check_cancel();
-    const int64_t nb = std::min(chunk, nq - q0);
+    const int64_t nb = std::min(chunk, q_hi - q0);
     // tiles: up to QT consecutive queries whose values fit the table
     std::vector<int32_t> tq, tn;
     int64_t j = 0;
@@ -611,8 +609,8 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
     SelectArgs sa;
     sa.vals = rvals; sa.seg_stride = cap; sa.elem_stride = 1; sa.nseg = nb;
     sa.cand = cand; sa.cand_count = count; sa.cand_ld = cap;
-    sa.seg_blank = r.qry_blank;
-    sa.out_idx = d_idx; sa.out_val = d_val; sa.out_ld = nq; sa.out_row0 = q0;
+    sa.seg_blank = r.qry_blank ? r.qry_blank + r.out_first : nullptr;
+    sa.out_idx = d_idx; sa.out_val = d_val; sa.out_ld = out_ld; sa.out_row0 = q0 - r.out_first;
     sa.k = r.k; sa.decreasing = r.decreasing;
     launch_select(sa, s);
     SK(cudaGetLastError());

@@ -30,6 +30,10 @@ struct ScreenRun {
   const uint8_t* ref_mask = nullptr;       // excluded reference columns
   const uint8_t* qry_blank = nullptr;      // query rows written all-NA
   const uint8_t* qry_empty = nullptr;      // all-zero query columns
+  // query columns [q_lo, q_hi) of the query matrix (q_hi < 0: all); result
+  // row of query q is q - out_first in an output with leading dimension
+  // out_ld (< 0: the query count)
+  int64_t q_lo = 0, q_hi = -1, out_first = 0, out_ld = -1;
 };
 
 struct ScreenHooks {
