@@ -165,6 +165,17 @@ SDG_API int sdg_knn_resident(sdg_ctx* ctx, const sdg_matrix* X, const sdg_matrix
                              int drop_degenerate, int32_t* idx, double* dist_out,
                              int* k_eff, int* flags);
 
+/* Rows q0 .. q0+nq-1 of sparseKNN(X, Y, ...) over resident matrices: one
+ * block of the reference's block loop (R/sparseKNN.R:248-294) with the
+ * whole search's semantics -- self-exclusion by global column index and the
+ * k clamp over the whole reference -- so that ranks or streams can each take
+ * a share of the query columns.  idx / dist_out hold nq * k values (column-
+ * major nq x k_eff); device_out selects device (1) or host (0) buffers. */
+SDG_API int sdg_knn_block(sdg_ctx* ctx, const sdg_matrix* X, const sdg_matrix* Y, int64_t q0,
+                          int64_t nq, int method, int dist, int k, int include_self,
+                          int drop_degenerate, int32_t* idx, double* dist_out, int device_out,
+                          int* k_eff, int* flags);
+
 /* As sdg_knn_resident, with idx / dist_out in DEVICE memory (caller
  * allocated, ncol(X) * k each); nothing is copied back and the call returns
  * once the work is queued on the context's stream (stream order). */
