@@ -122,6 +122,23 @@ SDG_API int sdg_topk_rows_accum(sdg_ctx* ctx, const double* D, int64_t nrow, int
 SDG_API int sdg_snn_jaccard(sdg_ctx* ctx, const int32_t* idx, int32_t n, int32_t k,
                             int include_self, double* w);
 
+/* sdg_snn_jaccard for callers that cannot allocate device memory on their
+ * call path (a host framework that owns the GPU's memory through its own
+ * allocator, or a thread that must not call cudaMalloc / cudaFree because
+ * they synchronise the device).  No counterpart in the reference.
+ *
+ * idx (n x k int32, column-major, 1-based, NA = INT32_MIN) and w (n x k
+ * double) are DEVICE pointers owned by the caller; stream is a cudaStream_t
+ * (NULL = the legacy default stream).  The neighbour sets live in a fixed
+ * 32 MiB array compiled into the library (held by every GPU that loads it,
+ * until exit): a call is rejected with SDG_E_UNSUPPORTED unless
+ * n * (k + 2) + 1 <= 8,388,608.  Nothing is allocated.  The first call on a
+ * device looks up the array's device address (make it before any stream
+ * capture).  The call synchronises `stream` once, to read the index check.
+ * All calls share the array: calls whose work overlaps on the GPU race. */
+SDG_API int sdg_snn_jaccard_noalloc(const int32_t* idx, int32_t n, int32_t k, int include_self,
+                                    double* w, void* stream);
+
 /* ---- the fused paths (the R block loops move onto the GPU) ----------------- */
 
 /* sparseKNN(X, Y, k, method, dist, include_self, drop_degenerate, block_size):

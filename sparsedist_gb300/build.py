@@ -31,6 +31,7 @@ UNITS = [
     ("sdg_select.cu", []),
     ("sdg_snn.cu", []),
     ("sdg_screen.cu", []),
+    ("sdg_noalloc.cu", []),
     ("sdg_api.cpp", []),
 ]
 
