@@ -182,6 +182,35 @@ SDG_API int sdg_knn_resident(sdg_ctx* ctx, const sdg_matrix* X, const sdg_matrix
                              int drop_degenerate, int32_t* idx, double* dist_out,
                              int* k_eff, int* flags);
 
+/* ---- serving: continuous batching against a resident reference -------------
+ * A server keeps `ref` resident (with the per-column data of `methods`
+ * prepared up front), admits submitted query matrices while one of max_slots
+ * slots is free and their device-memory estimate (query, screen slab share,
+ * candidate table, results) fits mem_budget bytes, packs admitted requests
+ * that share (method, dist, drop_degenerate) into one engine pass, and runs
+ * passes on `workers` threads, each with its own stream, so work from
+ * requests arriving while others run overlaps on the device.  A request's
+ * result is sparseKNN(Q, ref, ...) exactly, alone or in any mix.  No
+ * counterpart in the reference (its serving path is this library's own). */
+typedef struct sdg_server sdg_server;
+SDG_API int sdg_server_create(sdg_ctx* ctx, const sdg_matrix* ref, int workers, int max_slots,
+                              int64_t mem_budget, const int* methods, int nmethods,
+                              sdg_server** out);
+SDG_API int sdg_server_submit(sdg_server* server, const sdg_csc* Q, int method, int dist, int k,
+                              int drop_degenerate, int64_t* request_id);
+/* 0 when the request finished, 1 on timeout (timeout_ms < 0 waits forever). */
+SDG_API int sdg_server_wait(sdg_server* server, int64_t request_id, int timeout_ms);
+/* Copies a finished request's ncol(Q) x k_eff result and releases it. */
+SDG_API int sdg_server_result(sdg_server* server, int64_t request_id, int32_t* idx,
+                              double* dist_out, int* k_eff, int* flags);
+/* Cancels a request that has not started (0); 1 if it is already running. */
+SDG_API int sdg_server_cancel(sdg_server* server, int64_t request_id);
+/* out[0..8]: completed requests, completed columns, p50 / p99 / mean latency
+ * (s, submit to completion), columns/s, batches, bytes admitted, requests
+ * waiting for admission. */
+SDG_API int sdg_server_stats(sdg_server* server, double* out, int n);
+SDG_API int sdg_server_destroy(sdg_server* server);
+
 /* Rows q0 .. q0+nq-1 of sparseKNN(X, Y, ...) over resident matrices: one
  * block of the reference's block loop (R/sparseKNN.R:248-294) with the
  * whole search's semantics -- self-exclusion by global column index and the

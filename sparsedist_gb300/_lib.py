@@ -28,7 +28,9 @@ EXPORTED = ["sdg_version", "sdg_last_error", "sdg_ctx_create", "sdg_ctx_destroy"
             "sdg_ctx_reset_cancel", "sdg_dist_cross", "sdg_topk_block", "sdg_topk_rows_accum",
             "sdg_snn_jaccard", "sdg_knn", "sdg_knn_cross", "sdg_snn_graph", "sdg_matrix_upload",
             "sdg_matrix_free", "sdg_knn_resident", "sdg_knn_resident_device", "sdg_ctx_set_stream",
-            "sdg_last_stats", "sdg_ctx_set_engine", "sdg_kernel_time", "sdg_knn_block"]
+            "sdg_last_stats", "sdg_ctx_set_engine", "sdg_kernel_time", "sdg_knn_block",
+            "sdg_server_create", "sdg_server_submit", "sdg_server_wait", "sdg_server_result",
+            "sdg_server_cancel", "sdg_server_stats", "sdg_server_destroy"]
 
 
 class SdgError(RuntimeError):
@@ -84,6 +86,14 @@ def load() -> C.CDLL:
                                              v, v, v, v]
             lib.sdg_knn_resident_device.argtypes = lib.sdg_knn_resident.argtypes
             lib.sdg_ctx_set_stream.argtypes = [v, v]
+            lib.sdg_server_create.argtypes = [v, v, C.c_int, C.c_int, C.c_int64, v, C.c_int,
+                                              C.POINTER(v)]
+            lib.sdg_server_submit.argtypes = [v, v, C.c_int, C.c_int, C.c_int, C.c_int, v]
+            lib.sdg_server_wait.argtypes = [v, C.c_int64, C.c_int]
+            lib.sdg_server_result.argtypes = [v, C.c_int64, v, v, v, v]
+            lib.sdg_server_cancel.argtypes = [v, C.c_int64]
+            lib.sdg_server_stats.argtypes = [v, v, C.c_int]
+            lib.sdg_server_destroy.argtypes = [v]
             lib.sdg_knn_block.argtypes = [v, v, v, C.c_int64, C.c_int64, C.c_int, C.c_int, C.c_int,
                                           C.c_int, C.c_int, v, v, C.c_int, v, v]
             lib.sdg_kernel_time.argtypes = [v, v, v]
@@ -200,6 +210,63 @@ class Resident:
     def __del__(self):
         try:
             self.free()
+        except Exception:
+            pass
+
+
+class Server:
+    """sdg_server: continuous-batching kNN service against a resident reference."""
+
+    def __init__(self, ctx: Context, ref: Resident, workers=2, max_slots=64,
+                 mem_budget=120 << 30, methods=(1,)):
+        self.ctx, self.ref = ctx, ref
+        m = np.ascontiguousarray(methods, dtype=np.int32)
+        h = C.c_void_p()
+        check(ctx.lib.sdg_server_create(ctx.handle, ref.handle, int(workers), int(max_slots),
+                                        int(mem_budget), m.ctypes.data, len(m), C.byref(h)))
+        self.handle = h
+        self.lib = ctx.lib
+        self._held = {}
+
+    def submit(self, nrow, ncol, p, i, x, method=1, dist=True, k=10, drop_degenerate=True):
+        held = HeldCSC(nrow, ncol, p, i, x)
+        rid = C.c_int64()
+        check(self.lib.sdg_server_submit(self.handle, held.ref, int(method), int(bool(dist)), int(k),
+                                         int(bool(drop_degenerate)), C.byref(rid)))
+        self._held[rid.value] = (ncol, k)
+        return rid.value
+
+    def wait(self, rid, timeout_ms=-1):
+        st = self.lib.sdg_server_wait(self.handle, C.c_int64(rid), int(timeout_ms))
+        if st < 0:
+            check(st)
+        return st == 0
+
+    def result(self, rid):
+        ncol, k = self._held.pop(rid)
+        idx = np.empty(ncol * k, np.int32)
+        dst = np.empty(ncol * k, np.float64)
+        ke, fl = C.c_int(), C.c_int()
+        check(self.lib.sdg_server_result(self.handle, C.c_int64(rid), idx.ctypes.data,
+                                         dst.ctypes.data, C.byref(ke), C.byref(fl)))
+        e = ke.value
+        return idx[:ncol * e].reshape(e, ncol).T.copy(), dst[:ncol * e].reshape(e, ncol).T.copy(), fl.value
+
+    def stats(self):
+        out = np.zeros(9, np.float64)
+        check(self.lib.sdg_server_stats(self.handle, out.ctypes.data, 9))
+        keys = ["completed", "columns", "p50_s", "p99_s", "mean_s", "columns_per_s", "batches",
+                "bytes_admitted", "waiting"]
+        return dict(zip(keys, out.tolist()))
+
+    def close(self):
+        if self.handle:
+            self.lib.sdg_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
         except Exception:
             pass
 

@@ -194,7 +194,7 @@ struct sdg_matrix {
   DevBuf s1, s2;                // pearson moments
   bool have_moments = false;
   int js_status = 1;
-  ScreenCache screen;           // per-method screening data (sdg_screen.h)
+  ScreenCache screen[4];        // screening data per method (sdg_screen.h), binary..manhattan
 
   ~sdg_matrix() {
     if (ctx) cudaStreamSynchronize(ctx->stream);
@@ -455,8 +455,8 @@ void knn_device(sdg_ctx* c, sdg_matrix* X, sdg_matrix* Y, int method, int dist, 
     h.time_begin = [c]() { sdg_time_begin(c); };
     h.time_end = [c]() { sdg_time_end(c); };
     h.exact_range = [&](int64_t q0, int64_t n) { exact_engine(c, P, ref, X, d_idx, d_val, q0, q0 + n); };
-    const int st = screen_knn(c->stream, r, ref->dev(), aux_of(ref), &ref->screen, X->dev(),
-                              aux_of(X), &X->screen, d_idx, d_val, c->stats, h);
+    const int st = screen_knn(c->stream, r, ref->dev(), aux_of(ref), &ref->screen[method], X->dev(),
+                              aux_of(X), &X->screen[method], d_idx, d_val, c->stats, h);
     if (st) cuda_check((cudaError_t)st, "screen_knn");
   } else {
     exact_engine(c, P, ref, X, d_idx, d_val, q_lo, q_hi);
@@ -894,7 +894,7 @@ SDG_API int sdg_matrix_free(sdg_matrix* M) {
   cudaSetDevice(M->ctx->device);
   cudaStream_t s = M->ctx->stream;
   cudaStreamSynchronize(s);
-  screen_cache_free(&M->screen, s);
+  for (auto& sc : M->screen) screen_cache_free(&sc, s);
   cudaStreamSynchronize(s);
   delete M;
   return SDG_OK;
@@ -939,6 +939,359 @@ SDG_API int sdg_knn_resident(sdg_ctx* c, const sdg_matrix* X, const sdg_matrix* 
     CK(cudaMemcpyAsync(dist_out, hv.p, sizeof(double) * cnt, cudaMemcpyDeviceToHost, c->stream));
     end_stats(c);
   });
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Serving: a resident reference, continuous batching, memory-budget admission
+// ===========================================================================
+//
+// Requests (query matrices of any column count, method, dist and k) are
+// admitted while a slot is free and their device-memory estimate fits the
+// budget; admitted requests that share (method, dist, drop_degenerate) are
+// packed column-wise into one query matrix and searched in one pass of the
+// engine at the largest k among them (the top-k at k_max, cut to each
+// request's k, IS its top-k under the reference's total order).  Several
+// worker threads, each with its own context and stream, run batches
+// concurrently, so a request that arrives while others run is admitted and
+// packed into the next batch as soon as memory and a slot free up.  Every
+// query column's result depends only on that column and the reference, so a
+// request's result is the same alone and in any mix.
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+
+namespace {
+
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct Request {
+  int64_t id = 0;
+  int method = 0, dist = 1, k = 1, drop = 1;
+  int32_t nrow = 0, ncol = 0;
+  std::vector<int32_t> p, i;
+  std::vector<double> x;
+  std::vector<int32_t> idx;
+  std::vector<double> val;
+  int k_eff = 0, flags = 0, status = SDG_OK;
+  std::string err;
+  int64_t mem = 0;
+  double t_submit = 0, t_start = 0, t_done = 0;
+  enum State { PENDING, ADMITTED, RUNNING, DONE, CANCELLED } state = PENDING;
+};
+
+}  // namespace
+
+struct sdg_server {
+  sdg_matrix* ref = nullptr;
+  int device = 0;
+  int64_t budget = 0, in_use = 0;
+  int max_slots = 1, active = 0;
+  int64_t max_batch_cols = 8192;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<Request*> pending, admitted;
+  std::unordered_map<int64_t, std::unique_ptr<Request>> reqs;
+  int64_t next_id = 1;
+  bool stop = false;
+  std::vector<std::thread> workers;
+  std::vector<sdg_ctx*> ctxs;
+  std::vector<double> latencies;          // completed requests, seconds
+  int64_t done_cols = 0, batches = 0;
+  double t_first = 0, t_last = 0;
+};
+
+namespace {
+
+// Device memory a request needs while it runs: its query CSC, its share of
+// the FP32 screen slab (capped by the engine's per-pass slab), the candidate
+// table and exact values, and the result buffers.
+int64_t request_mem(const sdg_server* S, int64_t ncol, int64_t nnz, int k) {
+  const int64_t nr = S->ref->ncol;
+  const int64_t slab_cols = std::min<int64_t>(ncol, std::max<int64_t>(16, ((int64_t)4 << 30) / (4 * std::max<int64_t>(nr, 1))));
+  const int64_t cap = std::max(256, std::min(8192, 16 * k + 64));
+  return nnz * 12 + (ncol + 1) * 8 + slab_cols * nr * 4 + ncol * cap * 24 + ncol * (int64_t)k * 12;
+}
+
+void admit_locked(sdg_server* S) {
+  while (!S->pending.empty()) {
+    Request* r = S->pending.front();
+    if (r->state == Request::CANCELLED) { S->pending.pop_front(); continue; }
+    if (S->active >= S->max_slots) break;
+    if (S->in_use + r->mem > S->budget && S->active > 0) break;   // always admit one
+    S->pending.pop_front();
+    r->state = Request::ADMITTED;
+    S->in_use += r->mem;
+    ++S->active;
+    S->admitted.push_back(r);
+  }
+}
+
+void run_batch(sdg_server* S, sdg_ctx* c, std::vector<Request*>& batch) {
+  // pack the requests' columns into one dgCMatrix
+  sdg_csc Q;
+  std::vector<int32_t> p(1, 0), i;
+  std::vector<double> x;
+  int kmax = 1;
+  for (Request* r : batch) {
+    const int32_t base = p.back();
+    for (int32_t j = 0; j < r->ncol; ++j) p.push_back(base + r->p[j + 1]);
+    i.insert(i.end(), r->i.begin(), r->i.end());
+    x.insert(x.end(), r->x.begin(), r->x.end());
+    kmax = std::max(kmax, r->k);
+  }
+  Q.nrow = S->ref->nrow;
+  Q.ncol = (int32_t)(p.size() - 1);
+  Q.p = p.data(); Q.i = i.data(); Q.x = x.data();
+  const Request* r0 = batch.front();
+  int st = guarded([&] {
+    auto qm = upload(c, &Q, "X");
+    DevBuf hi, hv;
+    int k_eff = 0, flags = 0;
+    knn_device(c, qm.get(), S->ref, r0->method, r0->dist, kmax, 0, r0->drop, false, 0, nullptr,
+               nullptr, &k_eff, &flags, &hi, &hv);
+    std::vector<int32_t> idx((size_t)Q.ncol * k_eff);
+    std::vector<double> val((size_t)Q.ncol * k_eff);
+    CK(cudaMemcpyAsync(idx.data(), hi.p, sizeof(int32_t) * idx.size(), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(val.data(), hv.p, sizeof(double) * val.size(), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    // k_eff here is min(kmax, available); each request keeps min(k, available)
+    const int avail_k = k_eff;
+    int64_t col0 = 0;
+    for (Request* r : batch) {
+      const int ke = std::min(r->k, avail_k);
+      r->k_eff = ke;
+      r->flags = (r->k > ke) ? SDG_WARN_CLAMP_FWD : 0;
+      r->idx.resize((size_t)r->ncol * ke);
+      r->val.resize((size_t)r->ncol * ke);
+      for (int t = 0; t < ke; ++t)
+        for (int32_t j = 0; j < r->ncol; ++j) {
+          r->idx[(size_t)t * r->ncol + j] = idx[(size_t)t * Q.ncol + col0 + j];
+          r->val[(size_t)t * r->ncol + j] = val[(size_t)t * Q.ncol + col0 + j];
+        }
+      col0 += r->ncol;
+    }
+  });
+  const std::string err = st == SDG_OK ? std::string() : std::string(g_err.data(), g_err.size());
+  const double t = now_s();
+  std::lock_guard<std::mutex> lock(S->mu);
+  for (Request* r : batch) {
+    r->status = st;
+    r->err = err;
+    r->t_done = t;
+    r->state = Request::DONE;
+    S->in_use -= r->mem;
+    --S->active;
+    S->latencies.push_back(r->t_done - r->t_submit);
+    S->done_cols += r->ncol;
+  }
+  ++S->batches;
+  S->t_last = t;
+  admit_locked(S);
+  S->cv_done.notify_all();
+  S->cv_work.notify_all();
+}
+
+void worker_main(sdg_server* S, sdg_ctx* c) {
+  cudaSetDevice(S->device);
+  for (;;) {
+    std::vector<Request*> batch;
+    {
+      std::unique_lock<std::mutex> lock(S->mu);
+      S->cv_work.wait(lock, [&] { return S->stop || !S->admitted.empty(); });
+      if (S->stop && S->admitted.empty()) return;
+      // the oldest admitted request decides the group; take every admitted
+      // request of that group, oldest first, up to the batch column limit
+      Request* head = S->admitted.front();
+      int64_t cols = 0;
+      for (auto it = S->admitted.begin(); it != S->admitted.end();) {
+        Request* r = *it;
+        if (r->state == Request::CANCELLED) { it = S->admitted.erase(it); continue; }
+        const bool same = r->method == head->method && r->dist == head->dist && r->drop == head->drop;
+        if (same && (batch.empty() || cols + r->ncol <= S->max_batch_cols)) {
+          batch.push_back(r);
+          cols += r->ncol;
+          r->state = Request::RUNNING;
+          r->t_start = now_s();
+          it = S->admitted.erase(it);
+        } else {
+          ++it;
+        }
+      }
+    }
+    if (!batch.empty()) run_batch(S, c, batch);
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+SDG_API int sdg_server_create(sdg_ctx* ctx, const sdg_matrix* ref, int workers, int max_slots,
+                              int64_t mem_budget, const int* methods, int nmethods,
+                              sdg_server** out) {
+  return guarded([&] {
+    if (!ctx || !ref || !out || workers < 1 || max_slots < 1 || mem_budget <= 0)
+      fail(SDG_E_ARG, "invalid server arguments");
+    CK(cudaSetDevice(ctx->device));
+    auto S = std::make_unique<sdg_server>();
+    S->ref = const_cast<sdg_matrix*>(ref);
+    S->device = ctx->device;
+    S->budget = mem_budget;
+    S->max_slots = max_slots;
+    // Prepare everything the served methods read from the reference now, so
+    // that the workers only ever read it: masks, unit values, screen data.
+    ensure_empty(S->ref);
+    const int saved_engine = ctx->engine;
+    for (int t = 0; t < nmethods; ++t) {
+      const int m = methods[t];
+      check_method(m, 1);
+      sdg_csc one;
+      std::vector<int64_t> hp(2);
+      CK(cudaMemcpy(hp.data(), S->ref->p.p, sizeof(int64_t) * 2, cudaMemcpyDeviceToHost));
+      std::vector<int32_t> pi = {0, (int32_t)(hp[1] - hp[0])}, ii((size_t)std::max<int64_t>(1, hp[1] - hp[0]));
+      std::vector<double> xx(ii.size(), 1.0);
+      if (hp[1] > hp[0]) {
+        CK(cudaMemcpy(ii.data(), S->ref->i.as<int32_t>() + hp[0], sizeof(int32_t) * (hp[1] - hp[0]), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(xx.data(), S->ref->x.as<double>() + hp[0], sizeof(double) * (hp[1] - hp[0]), cudaMemcpyDeviceToHost));
+      }
+      one.nrow = S->ref->nrow; one.ncol = 1; one.p = pi.data(); one.i = ii.data(); one.x = xx.data();
+      auto q = upload(ctx, &one, "X");
+      DevBuf hi, hv;
+      int ke = 0, fl = 0;
+      ctx->engine = screen_supported(m, 1) ? 2 : 1;
+      knn_device(ctx, q.get(), S->ref, m, 1, 1, 0, 1, false, 0, nullptr, nullptr, &ke, &fl, &hi, &hv);
+      CK(cudaStreamSynchronize(ctx->stream));
+    }
+    ctx->engine = saved_engine;
+    for (int w = 0; w < workers; ++w) {
+      sdg_ctx* c = nullptr;
+      const int st = sdg_ctx_create(S->device, &c);
+      if (st != SDG_OK) fail(st, std::string(g_err.data(), g_err.size()));
+      S->ctxs.push_back(c);
+    }
+    S->t_first = now_s();
+    sdg_server* raw = S.get();
+    for (sdg_ctx* c : S->ctxs) S->workers.emplace_back(worker_main, raw, c);
+    *out = S.release();
+  });
+}
+
+SDG_API int sdg_server_submit(sdg_server* S, const sdg_csc* Q, int method, int dist, int k,
+                              int drop_degenerate, int64_t* id) {
+  return guarded([&] {
+    if (!S || !id) fail(SDG_E_ARG, "NULL argument");
+    if (k < 1) fail(SDG_E_ARG, kMsgK);
+    check_method(method, dist);
+    check_csc_host(Q, "X");
+    if (Q->ncol < 1) fail(SDG_E_ARG, "'X' must have at least one column.");
+    if (Q->nrow != S->ref->nrow) fail(SDG_E_ROWS, "'X' and 'Y' must have the same number of rows.");
+    auto r = std::make_unique<Request>();
+    r->method = method; r->dist = dist; r->k = k; r->drop = drop_degenerate ? 1 : 0;
+    r->nrow = Q->nrow; r->ncol = Q->ncol;
+    r->p.assign(Q->p, Q->p + Q->ncol + 1);
+    r->i.assign(Q->i, Q->i + Q->p[Q->ncol]);
+    r->x.assign(Q->x, Q->x + Q->p[Q->ncol]);
+    r->mem = request_mem(S, Q->ncol, Q->p[Q->ncol], k);
+    r->t_submit = now_s();
+    std::lock_guard<std::mutex> lock(S->mu);
+    r->id = S->next_id++;
+    *id = r->id;
+    S->pending.push_back(r.get());
+    S->reqs.emplace(r->id, std::move(r));
+    admit_locked(S);
+    S->cv_work.notify_all();
+  });
+}
+
+SDG_API int sdg_server_wait(sdg_server* S, int64_t id, int timeout_ms) {
+  if (!S) return SDG_E_ARG;
+  std::unique_lock<std::mutex> lock(S->mu);
+  auto it = S->reqs.find(id);
+  if (it == S->reqs.end()) { g_err = "unknown request"; return SDG_E_ARG; }
+  Request* r = it->second.get();
+  auto done = [&] { return r->state == Request::DONE || r->state == Request::CANCELLED; };
+  if (timeout_ms < 0) S->cv_done.wait(lock, done);
+  else if (!S->cv_done.wait_for(lock, std::chrono::milliseconds(timeout_ms), done)) return 1;
+  return SDG_OK;
+}
+
+SDG_API int sdg_server_result(sdg_server* S, int64_t id, int32_t* idx, double* dist_out,
+                              int* k_eff, int* flags) {
+  if (!S || !k_eff || !flags) return SDG_E_ARG;
+  std::unique_ptr<Request> r;
+  {
+    std::lock_guard<std::mutex> lock(S->mu);
+    auto it = S->reqs.find(id);
+    if (it == S->reqs.end()) { g_err = "unknown request"; return SDG_E_ARG; }
+    if (it->second->state != Request::DONE) { g_err = "request not finished"; return SDG_E_ARG; }
+    r = std::move(it->second);
+    S->reqs.erase(it);
+  }
+  if (r->status != SDG_OK) { g_err = r->err; return r->status; }
+  *k_eff = r->k_eff;
+  *flags = r->flags;
+  if (idx) std::memcpy(idx, r->idx.data(), sizeof(int32_t) * r->idx.size());
+  if (dist_out) std::memcpy(dist_out, r->val.data(), sizeof(double) * r->val.size());
+  return SDG_OK;
+}
+
+SDG_API int sdg_server_cancel(sdg_server* S, int64_t id) {
+  if (!S) return SDG_E_ARG;
+  std::lock_guard<std::mutex> lock(S->mu);
+  auto it = S->reqs.find(id);
+  if (it == S->reqs.end()) { g_err = "unknown request"; return SDG_E_ARG; }
+  Request* r = it->second.get();
+  if (r->state == Request::PENDING || r->state == Request::ADMITTED) {
+    if (r->state == Request::ADMITTED) { S->in_use -= r->mem; --S->active; }
+    r->state = Request::CANCELLED;
+    r->status = SDG_E_CANCELLED;
+    r->err = "Computation interrupted by the user.";
+    admit_locked(S);
+    S->cv_done.notify_all();
+    S->cv_work.notify_all();
+    return SDG_OK;
+  }
+  return 1;   // already running or finished: the result will be delivered
+}
+
+// out[0] completed requests, [1] completed columns, [2] p50 latency (s),
+// [3] p99 latency (s), [4] mean latency (s), [5] columns/s since creation,
+// [6] batches run, [7] bytes admitted now, [8] requests waiting for admission.
+SDG_API int sdg_server_stats(sdg_server* S, double* out, int n) {
+  if (!S || !out) return SDG_E_ARG;
+  std::lock_guard<std::mutex> lock(S->mu);
+  std::vector<double> l = S->latencies;
+  std::sort(l.begin(), l.end());
+  auto pct = [&](double q) { return l.empty() ? 0.0 : l[std::min(l.size() - 1, (size_t)(q * (l.size() - 1) + 0.5))]; };
+  double mean = 0;
+  for (double v : l) mean += v;
+  mean = l.empty() ? 0 : mean / l.size();
+  const double span = std::max(1e-9, S->t_last - S->t_first);
+  const double vals[9] = {(double)l.size(), (double)S->done_cols, pct(0.5), pct(0.99), mean,
+                          S->done_cols / span, (double)S->batches, (double)S->in_use,
+                          (double)S->pending.size()};
+  for (int t = 0; t < n && t < 9; ++t) out[t] = vals[t];
+  return SDG_OK;
+}
+
+SDG_API int sdg_server_destroy(sdg_server* S) {
+  if (!S) return SDG_OK;
+  {
+    std::lock_guard<std::mutex> lock(S->mu);
+    S->stop = true;
+  }
+  S->cv_work.notify_all();
+  for (auto& t : S->workers) t.join();
+  for (sdg_ctx* c : S->ctxs) sdg_ctx_destroy(c);
+  delete S;
+  return SDG_OK;
 }
 
 }  // extern "C"
