@@ -61,6 +61,12 @@ def parse():
     ap.add_argument("--cpu-cols", type=int, default=256, help="query columns of the CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--config", default="c2", choices=["c2", "c1", "serve"],
+                    help="c2: the default line (configuration 2); c1: the CPU-runnable "
+                         "configuration 1; serve: configuration 5, the serving loop")
+    ap.add_argument("--serve-ref-cols", type=int, default=1000000)
+    ap.add_argument("--serve-requests", type=int, default=80)
+    ap.add_argument("--serve-util", type=float, default=0.75)
     return ap.parse_args()
 
 
@@ -194,8 +200,135 @@ def workload_config(args, block):
             "k": args.k, "l2": "inputs larger than L2: the 4.3 GB reference is streamed every step"}
 
 
+def run_c1(args):
+    """Configuration 1: 2,000 x 10,000 CSC, 2 % uniform pattern, |N(0,1)|
+    values; sparseKNN binary and cosine (k = 15, self-search), then
+    sparseSNN(prune = 1/15, symmetrise = TRUE), through the Python API (host
+    buffers in and out), against the CPU port on all host cores."""
+    import torch
+    import sparsedist_gb300 as sdg
+    from sparsedist_gb300 import synth
+    from oracle import build as obuild
+    from oracle.pyoracle import Oracle
+    X = synth.uniform_csc(2000, 10000, 0.02, seed=1)
+    obuild.build_oracle()
+    orc = Oracle(threads=os.cpu_count() or 1)
+    out = {}
+    for method in ("binary", "cosine"):
+        for _ in range(args.warmup):
+            sdg.sparseKNN(X, k=15, method=method, verbose=False)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            nn = sdg.sparseKNN(X, k=15, method=method, verbose=False)
+        gpu_s = (time.perf_counter() - t0) / args.steps
+        t0 = time.perf_counter()
+        ref = orc.knn(X, k=15, method=method)
+        cpu_s = time.perf_counter() - t0
+        same = bool(np.array_equal(nn["idx"], ref[0]) and
+                    np.array_equal(nn["dist"].view(np.uint64), ref[1].view(np.uint64)))
+        out[method] = {"gpu_columns_per_s": 10000 / gpu_s, "gpu_ms": 1000 * gpu_s,
+                       "cpu_columns_per_s": 10000 / cpu_s, "cpu_s": cpu_s, "identical": same}
+    t0 = time.perf_counter()
+    g = sdg.sparseSNN(nn, prune=1 / 15, verbose=False)
+    out["snn_ms"] = 1000 * (time.perf_counter() - t0)
+    out["snn_nnz"] = int(g.nnz)
+    print(json.dumps({"metric": "kNN query columns/s, configuration 1 (e2e through the Python API)",
+                      "config": {"workload": "2000x10000 CSC, 2% uniform, |N(0,1)|, k=15, self-search"},
+                      "cores": os.cpu_count(), "results": out}))
+
+
+def run_serve(args):
+    """Configuration 5: a resident 30,000 x serve_ref_cols log-count reference
+    (configuration 2's generator), Poisson arrivals of query matrices with
+    1..4,096 columns (log-uniform), methods cycling cosine / binary /
+    euclidean, k in {10, 20, 50}, admission under a 120 GB budget; reports
+    p50 / p99 latency (submit to completion) and columns/s."""
+    import threading
+    import torch
+    from sparsedist_gb300 import _lib, synth
+    nr = args.serve_ref_cols
+    t0 = time.perf_counter()
+    p, i, x = synth.logcount_csc(nrow=30000, ncol=nr, mean_nnz=1800, seed=3, device="cuda",
+                                 keep_on_device=True)
+    ctx = _lib.Context()
+    ref = _lib.Resident.from_device(ctx, 30000, nr, p, i, x)
+    nnz = int(p[-1].item())
+    del p, i, x
+    torch.cuda.empty_cache()
+    qp, qi, qx = synth.logcount_csc(nrow=30000, ncol=20000, mean_nnz=1800, seed=4, device="cuda")
+    gen_s = time.perf_counter() - t0
+    codes = {"cosine": 1, "binary": 0, "euclidean": 2}
+    srv = _lib.Server(ctx, ref, workers=2, max_slots=64, mem_budget=120 << 30,
+                      methods=list(codes.values()))
+    rng = np.random.default_rng(7)
+    n = args.serve_requests
+    sizes = np.clip(np.exp(rng.uniform(0, np.log(4096), n)).astype(int), 1, 4096)
+    starts = rng.integers(0, 20000 - 4096, n)
+    methods = [["cosine", "binary", "euclidean"][r % 3] for r in range(n)]
+    ks = rng.choice([10, 20, 50], n)
+
+    def block(c0, m):
+        a, b = int(qp[c0]), int(qp[c0 + m])
+        return (qp[c0:c0 + m + 1] - a).astype(np.int32), qi[a:b], qx[a:b]
+
+    # service rate with the GPU otherwise idle: one mid-size request per method
+    cal = 0.0
+    cal_cols = 0
+    for meth in codes:
+        bp, bi, bx = block(0, 512)
+        s0 = time.perf_counter()
+        rid = srv.submit(30000, 512, bp, bi, bx, codes[meth], True, 20)
+        srv.wait(rid)
+        srv.result(rid)
+        cal += time.perf_counter() - s0
+        cal_cols += 512
+    service_cols_per_s = cal_cols / cal
+    rate = args.serve_util * service_cols_per_s / float(np.mean(sizes))
+    gaps = rng.exponential(1.0 / rate, n)
+    srv_stats0 = srv.stats()
+    ids = []
+
+    def submitter():
+        for r in range(n):
+            time.sleep(gaps[r])
+            bp, bi, bx = block(int(starts[r]), int(sizes[r]))
+            ids.append(srv.submit(30000, int(sizes[r]), bp, bi, bx, codes[methods[r]], True,
+                                  int(ks[r])))
+
+    t_start = time.perf_counter()
+    th = threading.Thread(target=submitter)
+    th.start()
+    th.join()
+    for rid in ids:
+        srv.wait(rid)
+        srv.result(rid)
+    wall = time.perf_counter() - t_start
+    st = srv.stats()
+    # latencies of the Poisson requests only (drop the calibration requests)
+    print(json.dumps({
+        "metric": "served kNN columns/s + p50/p99 latency, configuration 5",
+        "value": float(sizes.sum()) / wall, "unit": "columns/s",
+        "p50_latency_s": st["p50_s"], "p99_latency_s": st["p99_s"], "mean_latency_s": st["mean_s"],
+        "requests": n, "columns": int(sizes.sum()), "batches": int(st["batches"] - srv_stats0["batches"]),
+        "arrival_rate_per_s": rate, "idle_service_columns_per_s": service_cols_per_s,
+        "target_utilisation": args.serve_util, "wall_s": wall, "setup_s": gen_s,
+        "config": {"workload": "resident 30000x%d log-count reference (nnz %d), Poisson arrivals, "
+                               "1..4096 columns log-uniform, cosine/binary/euclidean, k in "
+                               "{10,20,50}, 120 GB admission budget" % (nr, nnz)},
+        "note": "latency percentiles include the 3 calibration requests"}))
+    srv.close()
+    ref.free()
+
+
 def main():
     args = parse()
+    if args.config == "c1":
+        run_c1(args)
+        return
+    if args.config == "serve":
+        run_serve(args)
+        return
     if args.impl == "reference":
         run_reference(args)
         return

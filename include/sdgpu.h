@@ -175,6 +175,10 @@ SDG_API int sdg_snn_graph(sdg_ctx* ctx, const int32_t* idx, int32_t n, int32_t k
 typedef struct sdg_matrix sdg_matrix;
 SDG_API int sdg_matrix_upload(sdg_ctx* ctx, const sdg_csc* M, sdg_matrix** out);
 SDG_API int sdg_matrix_free(sdg_matrix* M);
+/* As sdg_matrix_upload from dgCMatrix slots that already live in device
+ * memory (int32 p / i, double x; copied device to device). */
+SDG_API int sdg_matrix_upload_device(sdg_ctx* ctx, int32_t nrow, int32_t ncol, const int32_t* p,
+                                     const int32_t* i, const double* x, sdg_matrix** out);
 
 /* sdg_knn over resident matrices; results are written to host buffers. */
 SDG_API int sdg_knn_resident(sdg_ctx* ctx, const sdg_matrix* X, const sdg_matrix* Y,

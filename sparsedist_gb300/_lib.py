@@ -30,7 +30,8 @@ EXPORTED = ["sdg_version", "sdg_last_error", "sdg_ctx_create", "sdg_ctx_destroy"
             "sdg_matrix_free", "sdg_knn_resident", "sdg_knn_resident_device", "sdg_ctx_set_stream",
             "sdg_last_stats", "sdg_ctx_set_engine", "sdg_kernel_time", "sdg_knn_block",
             "sdg_server_create", "sdg_server_submit", "sdg_server_wait", "sdg_server_result",
-            "sdg_server_cancel", "sdg_server_stats", "sdg_server_destroy"]
+            "sdg_server_cancel", "sdg_server_stats", "sdg_server_destroy",
+            "sdg_matrix_upload_device"]
 
 
 class SdgError(RuntimeError):
@@ -86,6 +87,7 @@ def load() -> C.CDLL:
                                              v, v, v, v]
             lib.sdg_knn_resident_device.argtypes = lib.sdg_knn_resident.argtypes
             lib.sdg_ctx_set_stream.argtypes = [v, v]
+            lib.sdg_matrix_upload_device.argtypes = [v, C.c_int32, C.c_int32, v, v, v, C.POINTER(v)]
             lib.sdg_server_create.argtypes = [v, v, C.c_int, C.c_int, C.c_int64, v, C.c_int,
                                               C.POINTER(v)]
             lib.sdg_server_submit.argtypes = [v, v, C.c_int, C.c_int, C.c_int, C.c_int, v]
@@ -201,6 +203,19 @@ class Resident:
         check(ctx.lib.sdg_matrix_upload(ctx.handle, held.ref, C.byref(h)))
         self.handle = h
         self.nrow, self.ncol = int(nrow), int(ncol)
+
+    @classmethod
+    def from_device(cls, ctx: Context, nrow, ncol, d_p, d_i, d_x):
+        """From dgCMatrix slots in device memory (torch tensors: int32 p / i,
+        float64 x); copied device to device."""
+        self = cls.__new__(cls)
+        self.ctx = ctx
+        h = C.c_void_p()
+        check(ctx.lib.sdg_matrix_upload_device(ctx.handle, int(nrow), int(ncol), d_p.data_ptr(),
+                                               d_i.data_ptr(), d_x.data_ptr(), C.byref(h)))
+        self.handle = h
+        self.nrow, self.ncol = int(nrow), int(ncol)
+        return self
 
     def free(self):
         if self.handle:

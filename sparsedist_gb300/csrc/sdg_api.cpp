@@ -242,8 +242,8 @@ std::unique_ptr<sdg_matrix> upload(sdg_ctx* c, const sdg_csc* M, const char* nam
   m->x = DevBuf(sizeof(double) * (size_t)m->nnz, s);
   CK(cudaMemcpyAsync(m->p.p, p64.data(), sizeof(int64_t) * p64.size(), cudaMemcpyHostToDevice, s));
   if (m->nnz > 0) {
-    CK(cudaMemcpyAsync(m->i.p, M->i, sizeof(int32_t) * (size_t)m->nnz, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(m->x.p, M->x, sizeof(double) * (size_t)m->nnz, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(m->i.p, M->i, sizeof(int32_t) * (size_t)m->nnz, cudaMemcpyDefault, s));
+    CK(cudaMemcpyAsync(m->x.p, M->x, sizeof(double) * (size_t)m->nnz, cudaMemcpyDefault, s));
   }
   DevBuf err(sizeof(int), s);
   CK(cudaMemsetAsync(err.p, 0, sizeof(int), s));
@@ -884,6 +884,21 @@ SDG_API int sdg_matrix_upload(sdg_ctx* c, const sdg_csc* M, sdg_matrix** out) {
     if (!c || !out) fail(SDG_E_ARG, "NULL argument");
     CK(cudaSetDevice(c->device));
     auto m = upload(c, M, "M");
+    ensure_empty(m.get());
+    *out = m.release();
+  });
+}
+
+SDG_API int sdg_matrix_upload_device(sdg_ctx* c, int32_t nrow, int32_t ncol, const int32_t* d_p,
+                                     const int32_t* d_i, const double* d_x, sdg_matrix** out) {
+  return guarded([&] {
+    if (!c || !out || ncol < 0 || (ncol > 0 && !d_p)) fail(SDG_E_ARG, "NULL argument");
+    CK(cudaSetDevice(c->device));
+    std::vector<int32_t> hp((size_t)ncol + 1, 0);
+    if (ncol > 0)
+      CK(cudaMemcpy(hp.data(), d_p, sizeof(int32_t) * hp.size(), cudaMemcpyDefault));
+    sdg_csc M{nrow, ncol, hp.data(), d_i, d_x};
+    auto m = upload(c, &M, "M");
     ensure_empty(m.get());
     *out = m.release();
   });

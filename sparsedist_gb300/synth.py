@@ -32,8 +32,9 @@ def uniform_csc(nrow, ncol, density, seed=0):
 
 
 def logcount_csc(nrow=30000, ncol=200000, mean_nnz=1800.0, sdlog=0.6, row_sdlog=1.5,
-                 col_sdlog=0.5, seed=0, device="cuda", chunk=1024):
-    """Returns (p int32[ncol+1], i int32[nnz], x float64[nnz]) on the host."""
+                 col_sdlog=0.5, seed=0, device="cuda", chunk=1024, keep_on_device=False):
+    """Returns (p int32[ncol+1], i int32[nnz], x float64[nnz]) on the host, or,
+    with keep_on_device, as torch tensors on ``device`` (p included)."""
     import torch
     g = torch.Generator(device=device)
     g.manual_seed(int(seed))
@@ -62,9 +63,16 @@ def logcount_csc(nrow=30000, ncol=200000, mean_nnz=1800.0, sdlog=0.6, row_sdlog=
         vals = torch.log1p(cnt)
         per_col = torch.bincount(cols, minlength=b).cpu().numpy()
         p[c0 + 1:c1 + 1] = per_col
-        rows_parts.append(rows.to(torch.int32).cpu().numpy())
-        vals_parts.append(vals.cpu().numpy())
+        if keep_on_device:
+            rows_parts.append(rows.to(torch.int32))
+            vals_parts.append(vals)
+        else:
+            rows_parts.append(rows.to(torch.int32).cpu().numpy())
+            vals_parts.append(vals.cpu().numpy())
     p = np.cumsum(p)
     if p[-1] >= 2 ** 31:
         raise ValueError("nnz exceeds the dgCMatrix limit of 2^31 - 1")
+    if keep_on_device:
+        return (torch.from_numpy(p.astype(np.int32)).to(device), torch.cat(rows_parts),
+                torch.cat(vals_parts))
     return p.astype(np.int32), np.concatenate(rows_parts), np.concatenate(vals_parts)
