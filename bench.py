@@ -61,10 +61,11 @@ def parse():
     ap.add_argument("--cpu-cols", type=int, default=256, help="query columns of the CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--config", default="c2", choices=["c2", "c1", "serve"],
+    ap.add_argument("--config", default="c2", choices=["c2", "c1", "c3", "serve"],
                     help="c2: the default line (configuration 2); c1: the CPU-runnable "
                          "configuration 1; serve: configuration 5, the serving loop")
     ap.add_argument("--serve-ref-cols", type=int, default=1000000)
+    ap.add_argument("--c3-cols", type=int, default=2000000)
     ap.add_argument("--serve-requests", type=int, default=80)
     ap.add_argument("--serve-util", type=float, default=0.75)
     return ap.parse_args()
@@ -321,8 +322,97 @@ def run_serve(args):
     ref.free()
 
 
+def run_c3(args):
+    """Configuration 3: 256 x 2,000,000 FP32 embeddings (i.i.d. N(0,1) mixed
+    with 1,000 Gaussian clusters, sigma 0.3, plus 1 % near duplicates at 1e-6),
+    cosine and euclidean self-search, k = 20, in blocks of 1,024 query columns:
+    the BF16 tensor-core screen + exact FP64 re-rank against the plain FP32
+    path, with idx identity and distance error checked against the exact FP64
+    engine on a sample of query columns."""
+    import ctypes as C
+    import torch
+    from sparsedist_gb300 import _lib, synth
+    d, n, B, k = 256, args.c3_cols, 1024, 20
+    X = synth.dense_embeddings(d=d, n=n, seed=5)
+    ctx = _lib.Context()
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    h = C.c_void_p()
+    _lib.check(ctx.lib.sdg_dense_upload(ctx.handle, X.data_ptr(), d, n, C.byref(h)))
+    d_idx = torch.empty(B * k, dtype=torch.int32, device="cuda")
+    d_val = torch.empty(B * k, dtype=torch.float64, device="cuda")
+    ke, fl = np.zeros(1, np.int32), np.zeros(1, np.int32)
+    res = {}
+    for method, code in (("cosine", 1), ("euclidean", 2)):
+        for mode, name in ((0, "bf16_screen_fp64_rerank"), (1, "plain_fp32")):
+            def step(s):
+                _lib.check(ctx.lib.sdg_dense_knn_block(ctx.handle, h, (s * B) % (n - B), B, code, k,
+                                                       mode, d_idx.data_ptr(), d_val.data_ptr(), 1,
+                                                       ke.ctypes.data, fl.ctypes.data))
+            for s in range(args.warmup):
+                step(s)
+            torch.cuda.synchronize()
+            ctx.kernel_time()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for s in range(args.steps):
+                step(args.warmup + s)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / args.steps
+            gemm_ms, launches = ctx.kernel_time()
+            flops = 2.0 * d * B * n
+            res["%s/%s" % (method, name)] = {"columns_per_s": B / (ms / 1000.0), "ms_per_block": ms,
+                                             "gemm_ms": gemm_ms / max(launches, 1),
+                                             "gemm_tflops": flops / (gemm_ms / max(launches, 1) / 1000.0) / 1e12}
+        res["%s/speedup_bf16_vs_fp32" % method] = (res["%s/bf16_screen_fp64_rerank" % method]["columns_per_s"] /
+                                                   res["%s/plain_fp32" % method]["columns_per_s"])
+    # correctness on a sample of query columns: the exact FP64 engine on the same data
+    qs = 16
+    A = X.double()                                        # (n, d)
+    p = torch.arange(0, (n + 1) * d, d, dtype=torch.int32, device="cuda")
+    rows = torch.arange(d, dtype=torch.int32, device="cuda").repeat(n)
+    full = _lib.Resident.from_device(ctx, d, n, p, rows, A.reshape(-1))
+    qp = torch.arange(0, (qs + 1) * d, d, dtype=torch.int32, device="cuda")
+    qsamp = _lib.Resident.from_device(ctx, d, qs, qp, rows[:qs * d], A[:qs].reshape(-1))
+    ctx.set_engine(1)
+    check = {}
+    for method, code in (("cosine", 1), ("euclidean", 2)):
+        wi = np.empty(qs * (k + 1), np.int32)
+        wd = np.empty(qs * (k + 1), np.float64)
+        _lib.check(ctx.lib.sdg_knn_resident(ctx.handle, qsamp.handle, full.handle, code, 1, k + 1, 0, 1,
+                                            wi.ctypes.data, wd.ctypes.data, ke.ctypes.data,
+                                            fl.ctypes.data))
+        wi = wi.reshape(k + 1, qs).T
+        wd = wd.reshape(k + 1, qs).T
+        for mode, name in ((0, "bf16_screen_fp64_rerank"), (1, "plain_fp32")):
+            gi = np.empty(qs * k, np.int32)
+            gd = np.empty(qs * k, np.float64)
+            _lib.check(ctx.lib.sdg_dense_knn_block(ctx.handle, h, 0, qs, code, k, mode, gi.ctypes.data,
+                                                   gd.ctypes.data, 0, ke.ctypes.data, fl.ctypes.data))
+            gi = gi.reshape(k, qs).T
+            gd = gd.reshape(k, qs).T
+            same, err = 0, 0.0
+            for q in range(qs):
+                keep = wi[q] != q + 1                     # the cross form includes the query itself
+                ri, rd = wi[q][keep][:k], wd[q][keep][:k]
+                same += int(np.array_equal(gi[q], ri))
+                err = max(err, float(np.max(np.abs(gd[q] - rd))))
+            check["%s/%s" % (method, name)] = {"rows_with_identical_idx": same, "rows": qs,
+                                               "max_abs_distance_error_vs_fp64": err}
+    ctx.set_engine(0)
+    print(json.dumps({"metric": "dense kNN query columns/s, configuration 3 (k=20, 1,024-query blocks)",
+                      "config": {"workload": "256x%d FP32 embeddings: N(0,1) + 1000 clusters (sigma 0.3) "
+                                             "+ 1%% near duplicates (1e-6)" % n},
+                      "results": res, "check_vs_fp64_engine": check}))
+    ctx.lib.sdg_dense_free(h)
+
+
 def main():
     args = parse()
+    if args.config == "c3":
+        run_c3(args)
+        return
     if args.config == "c1":
         run_c1(args)
         return

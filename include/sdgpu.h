@@ -186,6 +186,23 @@ SDG_API int sdg_knn_resident(sdg_ctx* ctx, const sdg_matrix* X, const sdg_matrix
                              int drop_degenerate, int32_t* idx, double* dist_out,
                              int* k_eff, int* flags);
 
+/* ---- dense embedding columns (BF16 tensor-core screen, exact FP64 re-rank) --
+ * X is d x n FP32, column-major (host or device pointer), each column one
+ * embedding.  sdg_dense_knn_block returns rows q0 .. q0+nq-1 of the
+ * self-search sparseKNN(X, k, method) (include_self = FALSE,
+ * drop_degenerate = TRUE) for cosine (dist) or euclidean.  mode 0: BF16
+ * tensor-core screen with a rigorous bound and exact FP64 re-rank (the
+ * reference's idx and distances); mode 1: the plain FP32 path (FP32 GEMM,
+ * top-k on FP32 values, no re-rank).  No counterpart in the reference, whose
+ * dense inputs are coerced to dgCMatrix (R/sparseKNN.R:194-200); the FP64
+ * values are those sparseKNN computes on the same data. */
+typedef struct sdg_dense sdg_dense;
+SDG_API int sdg_dense_upload(sdg_ctx* ctx, const float* X, int32_t d, int64_t n, sdg_dense** out);
+SDG_API int sdg_dense_free(sdg_dense* D);
+SDG_API int sdg_dense_knn_block(sdg_ctx* ctx, const sdg_dense* D, int64_t q0, int64_t nq,
+                                int method, int k, int mode, int32_t* idx, double* dist_out,
+                                int device_out, int* k_eff, int* flags);
+
 /* ---- serving: continuous batching against a resident reference -------------
  * A server keeps `ref` resident (with the per-column data of `methods`
  * prepared up front), admits submitted query matrices while one of max_slots

@@ -31,7 +31,7 @@ EXPORTED = ["sdg_version", "sdg_last_error", "sdg_ctx_create", "sdg_ctx_destroy"
             "sdg_last_stats", "sdg_ctx_set_engine", "sdg_kernel_time", "sdg_knn_block",
             "sdg_server_create", "sdg_server_submit", "sdg_server_wait", "sdg_server_result",
             "sdg_server_cancel", "sdg_server_stats", "sdg_server_destroy",
-            "sdg_matrix_upload_device"]
+            "sdg_matrix_upload_device", "sdg_dense_upload", "sdg_dense_free", "sdg_dense_knn_block"]
 
 
 class SdgError(RuntimeError):
@@ -87,6 +87,10 @@ def load() -> C.CDLL:
                                              v, v, v, v]
             lib.sdg_knn_resident_device.argtypes = lib.sdg_knn_resident.argtypes
             lib.sdg_ctx_set_stream.argtypes = [v, v]
+            lib.sdg_dense_upload.argtypes = [v, v, C.c_int32, C.c_int64, C.POINTER(v)]
+            lib.sdg_dense_free.argtypes = [v]
+            lib.sdg_dense_knn_block.argtypes = [v, v, C.c_int64, C.c_int64, C.c_int, C.c_int, C.c_int,
+                                                v, v, C.c_int, v, v]
             lib.sdg_matrix_upload_device.argtypes = [v, C.c_int32, C.c_int32, v, v, v, C.POINTER(v)]
             lib.sdg_server_create.argtypes = [v, v, C.c_int, C.c_int, C.c_int64, v, C.c_int,
                                               C.POINTER(v)]

@@ -32,6 +32,7 @@ UNITS = [
     ("sdg_snn.cu", []),
     ("sdg_screen.cu", []),
     ("sdg_noalloc.cu", []),
+    ("sdg_dense.cu", []),
     ("sdg_api.cpp", []),
 ]
 
@@ -67,7 +68,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
         objs = [f.result() for f in futs]
     if force or not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
         tmp = LIB + ".tmp"
-        cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs]
+        cudalib = os.path.join(os.path.dirname(os.path.dirname(nvcc())), "lib64")
+        cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcublas",
+               "-Xlinker", "-rpath", "-Xlinker", cudalib]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed: %s\n%s\n%s" % (" ".join(cmd), r.stdout, r.stderr))

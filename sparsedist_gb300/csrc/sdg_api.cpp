@@ -163,6 +163,12 @@ void fold_kernel_times(sdg_ctx* c) {
 
 }  // namespace
 
+namespace sdg {
+cudaStream_t ctx_stream(sdg_ctx* c) { return c->stream; }
+int ctx_device(sdg_ctx* c) { return c->device; }
+void ctx_add_overflow(sdg_ctx* c, int64_t n) { c->stats[2] += n; }
+}  // namespace sdg
+
 // Brackets one launch of the bounding kernel (see sdg_kernel_time).
 void sdg_time_begin(sdg_ctx* c) {
   if (c->tev_used == c->tev.size()) {

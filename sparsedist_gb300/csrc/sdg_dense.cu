@@ -1,0 +1,412 @@
+// sdg_dense.cu -- kNN over dense embedding columns (configuration 3).
+//
+// Columns are dense (d values each).  A cosine / euclidean slab between
+// dense columns is a true contraction, so the screen runs on the tensor
+// cores: BF16 GEMM tiles with FP32 accumulation (cuBLAS GemmEx) write the
+// screen slab S[q][r] = <col q, col r>; the select kernel keeps every
+// reference whose optimistic bound reaches the k-th pessimistic bound (the
+// BF16 rounding bound below); the kept pairs are re-ranked in exact FP64 with
+// the reference's arithmetic (unit_csc normalisation and a sequential dot for
+// cosine, a sequential sum of squared differences for euclidean), so the
+// returned idx and distances are those of sparseKNN on the same data.
+//
+// The plain path (mode 1) is the FP32 baseline: an FP32 SGEMM on the CUDA
+// cores and the top-k taken directly on the FP32 values (no re-rank).
+//
+// BF16 bound: every input is rounded to BF16 (relative error <= 2^-9), so a
+// product has relative error <= 2^-8 + 2^-18, and the FP32 accumulation of d
+// products adds at most d * 2^-22 relative (a conservative allowance for the
+// tensor cores' accumulation); with S|x_i y_i| <= |x| |y|:
+//   cosine    (unit vectors):  |S - S_exact| <= 0.0040 + d * 2^-22
+//   euclidean (2S - Nq - Nr):  2 (0.0040 + d * 2^-22) sqrt(Nq Nr) + 2^-20 (Nq + Nr)
+#include <cublas_v2.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "../../include/sdgpu.h"
+#include "sdg_kernels.h"
+
+struct sdg_dense {
+  int device = 0;
+  int32_t d = 0;
+  int64_t n = 0;
+  double* x64 = nullptr;          // d x n column-major
+  double* u64 = nullptr;          // unit columns (unit_csc on the dense column)
+  float* x32 = nullptr;
+  float* u32 = nullptr;
+  __nv_bfloat16* xb = nullptr;
+  __nv_bfloat16* ub = nullptr;
+  float* norm2 = nullptr;         // sum of squares (FP64, rounded)
+  double* scale = nullptr;        // unit_csc scale (0 = empty column)
+  uint8_t* empty = nullptr;
+  int64_t* pview = nullptr;       // column offsets j * d, for the CSC kernels
+  int64_t n_empty = 0;
+  cublasHandle_t blas = nullptr;
+};
+
+namespace sdg {
+namespace {
+
+constexpr int DSEL_WARPS = 8;
+
+inline unsigned blocks_for(int64_t n, int threads) {
+  return (unsigned)((n + threads - 1) / threads);
+}
+
+__global__ void k_dense_prep(int32_t d, int64_t n, const float* x32, double* x64, float* norm2,
+                             uint8_t* empty, int64_t* pview, int* err) {
+  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (j > n) return;
+  pview[j] = j * d;
+  if (j == n) return;
+  double s = 0.0;
+  uint8_t e = 1;
+  for (int32_t r = 0; r < d; ++r) {
+    const float v = x32[j * d + r];
+    if (!isfinite(v)) atomicOr(err, 1);
+    if (v != 0.f) e = 0;
+    const double dv = (double)v;
+    x64[j * d + r] = dv;
+    s += dv * dv;
+  }
+  norm2[j] = (float)s;
+  empty[j] = e;
+}
+
+__global__ void k_dense_cast(int64_t total, const double* u64, const float* x32, float* u32,
+                             __nv_bfloat16* ub, __nv_bfloat16* xb) {
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < total;
+       a += (int64_t)gridDim.x * blockDim.x) {
+    const float u = (float)u64[a];
+    u32[a] = u;
+    ub[a] = __float2bfloat16_rn(u);
+    xb[a] = __float2bfloat16_rn(x32[a]);
+  }
+}
+
+struct DenseSelArgs {
+  int method, k, mode;           // mode 0: BF16 bound, 1: plain FP32 (no bound)
+  const float* S;                // S[ql * n + r]
+  int64_t n, q0, nq;
+  int32_t d;
+  const float* norm2;
+  const uint8_t* empty;
+  int cap;
+  int32_t* cand;
+  int32_t* count;
+  int32_t* overflow;
+};
+
+__device__ __forceinline__ void dense_key(int method, int mode, int32_t d, float s, float Nq, float Nr,
+                                          float& key, float& err) {
+  const float rel = 0.0040f + (float)d * 2.384185791015625e-7f;   // 2^-22
+  if (method == COSINE) {
+    key = s;
+    err = mode == 0 ? rel : 0.f;
+  } else {
+    key = 2.f * s - (Nq + Nr);
+    err = mode == 0 ? 2.f * rel * sqrtf(Nq * Nr) + 9.5367431640625e-7f * (Nq + Nr) + 1e-30f : 0.f;
+  }
+}
+
+// per query: T = k-th largest (key - err), keep every r with key + err >= T
+__global__ void k_dense_select(DenseSelArgs A) {
+  extern __shared__ float lists[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t ql = (int64_t)blockIdx.x * DSEL_WARPS + warp;
+  if (ql >= A.nq) return;
+  const int64_t q = A.q0 + ql;
+  float* lst = lists + warp * A.k;
+  const int K = A.k;
+  if (A.empty[q]) {                        // degenerate query: all-NA row
+    if (lane == 0) { A.count[ql] = 0; A.overflow[ql] = 0; }
+    return;
+  }
+  const float Nq = A.norm2[q];
+  const float* Srow = A.S + ql * A.n;
+  int n = 0;
+  for (int64_t p0 = 0; p0 < A.n; p0 += 32) {
+    const int64_t r = p0 + lane;
+    float lo = -INFINITY;
+    bool ok = r < A.n && r != q && !A.empty[r];
+    if (ok) {
+      float key, err;
+      dense_key(A.method, A.mode, A.d, Srow[r], Nq, A.norm2[r], key, err);
+      lo = key - err;
+    }
+    const bool pass = ok && (n < K || lo > lst[K - 1]);
+    unsigned m = __ballot_sync(0xffffffffu, pass);
+    while (m) {
+      const int src = __ffs(m) - 1;
+      m &= m - 1;
+      const float v = __shfl_sync(0xffffffffu, lo, src);
+      if (n == K && !(v > lst[K - 1])) continue;
+      int a = 0, b = n;
+      while (a < b) { const int mid = (a + b) >> 1; if (lst[mid] >= v) a = mid + 1; else b = mid; }
+      const int last = (n < K) ? n : K - 1;
+      if (last > a) {
+        for (int c = (last - 1) >> 5; c >= (a >> 5); --c) {
+          const int e = c * 32 + lane;
+          const bool mv = (e >= a && e < last);
+          float t = 0.f;
+          if (mv) t = lst[e];
+          __syncwarp();
+          if (mv) lst[e + 1] = t;
+          __syncwarp();
+        }
+      }
+      if (lane == 0) lst[a] = v;
+      __syncwarp();
+      if (n < K) ++n;
+    }
+  }
+  const float T = (n == K) ? lst[K - 1] : -INFINITY;
+  const float margin = (T == -INFINITY) ? 0.f : fabsf(T) * 4.76837158203125e-7f + 1e-30f;
+  int cnt = 0;
+  bool over = false;
+  int32_t* out = A.cand + ql * (int64_t)A.cap;
+  for (int64_t p0 = 0; p0 < A.n && !over; p0 += 32) {
+    const int64_t r = p0 + lane;
+    bool keep = false;
+    if (r < A.n && r != q && !A.empty[r]) {
+      float key, err;
+      dense_key(A.method, A.mode, A.d, Srow[r], Nq, A.norm2[r], key, err);
+      keep = (key + err) >= T - margin;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    const int rank = __popc(m & ((1u << lane) - 1u));
+    if (keep && cnt + rank < A.cap) out[cnt + rank] = (int32_t)r;
+    cnt += __popc(m);
+    if (cnt > A.cap) over = true;
+  }
+  if (lane == 0) { A.count[ql] = over ? 0 : cnt; A.overflow[ql] = over ? 1 : 0; }
+}
+
+// Exact FP64 value of each kept pair, in the reference's arithmetic; in the
+// plain mode the FP32 value of the slab instead.
+__global__ void k_dense_values(int method, int mode, int32_t d, const double* x64, const double* u64,
+                               const float* S, int64_t n, const float* norm2, const int32_t* cand,
+                               const int32_t* count, int cap, int64_t q0, int64_t nq, double* out) {
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= nq * cap) return;
+  const int64_t ql = s / cap, t = s % cap;
+  if (t >= count[ql]) return;
+  const int64_t q = q0 + ql, r = cand[s];
+  if (mode == 1) {
+    const float sv = S[ql * n + r];
+    out[s] = (method == COSINE) ? (double)(1.f - fminf(1.f, fmaxf(-1.f, sv)))
+                                : (double)sqrtf(fmaxf(0.f, norm2[q] + norm2[r] - 2.f * sv));
+    return;
+  }
+  if (method == COSINE) {
+    // unit_dot / unit_cosine (src/sparseDist.cpp:287-331), reference column first
+    const double* a = u64 + r * d;
+    const double* b = u64 + q * d;
+    double acc = 0.0;
+    for (int32_t k = 0; k < d; ++k) acc = __dadd_rn(acc, __dmul_rn(a[k], b[k]));
+    double c = acc;
+    if (!(c == c)) c = 0.0;
+    else if (c > 1.0) c = 1.0;
+    else if (c < -1.0) c = -1.0;
+    out[s] = __dsub_rn(1.0, c);
+  } else {
+    // fastEuclidean2's pair loop with every row stored (src/sparseDist.cpp:855-871)
+    const double* a = x64 + r * d;
+    const double* b = x64 + q * d;
+    double num = 0.0;
+    for (int32_t k = 0; k < d; ++k) {
+      const double diff = __dsub_rn(a[k], b[k]);
+      num = __dadd_rn(num, __dmul_rn(diff, diff));
+    }
+    out[s] = sqrt(num);
+  }
+}
+
+// exact FP64 values of one query against every reference (overflow fallback)
+__global__ void k_dense_exact_row(int method, int32_t d, const double* x64, const double* u64,
+                                  const uint8_t* empty, int64_t n, int64_t q, double* out) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  if (r == q || empty[r]) { out[r] = na_real(); return; }
+  double acc = 0.0;
+  if (method == COSINE) {
+    for (int32_t k = 0; k < d; ++k) acc = __dadd_rn(acc, __dmul_rn(u64[r * d + k], u64[q * d + k]));
+    double c = acc;
+    if (!(c == c)) c = 0.0; else if (c > 1.0) c = 1.0; else if (c < -1.0) c = -1.0;
+    out[r] = __dsub_rn(1.0, c);
+  } else {
+    for (int32_t k = 0; k < d; ++k) {
+      const double diff = __dsub_rn(x64[r * d + k], x64[q * d + k]);
+      acc = __dadd_rn(acc, __dmul_rn(diff, diff));
+    }
+    out[r] = sqrt(acc);
+  }
+}
+
+int fail_with(int code, const char* msg) { set_error(msg); return code; }
+int cuda_fail(cudaError_t e) {
+  set_error(cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? SDG_E_NOMEM : SDG_E_CUDA;
+}
+#define DK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return cuda_fail(e_); } while (0)
+#define DB(x) do { cublasStatus_t b_ = (x); if (b_ != CUBLAS_STATUS_SUCCESS) return fail_with(SDG_E_CUDA, "cuBLAS call failed"); } while (0)
+
+}  // namespace
+}  // namespace sdg
+
+using namespace sdg;
+
+extern "C" {
+
+SDG_API int sdg_dense_upload(sdg_ctx* ctx, const float* X, int32_t d, int64_t n, sdg_dense** out) {
+  if (!ctx || !X || !out || d < 1 || n < 1) return fail_with(SDG_E_ARG, "invalid dense upload arguments");
+  cudaStream_t s = ctx_stream(ctx);
+  DK(cudaSetDevice(ctx_device(ctx)));
+  auto D = new sdg_dense();
+  D->device = ctx_device(ctx);
+  D->d = d;
+  D->n = n;
+  const size_t tot = (size_t)d * (size_t)n;
+  int* err = nullptr;
+  DK(cudaMalloc(&D->x64, tot * 8)); DK(cudaMalloc(&D->u64, tot * 8));
+  DK(cudaMalloc(&D->x32, tot * 4)); DK(cudaMalloc(&D->u32, tot * 4));
+  DK(cudaMalloc(&D->xb, tot * 2)); DK(cudaMalloc(&D->ub, tot * 2));
+  DK(cudaMalloc(&D->norm2, n * 4)); DK(cudaMalloc(&D->scale, n * 8));
+  DK(cudaMalloc(&D->empty, n)); DK(cudaMalloc(&D->pview, (n + 1) * 8));
+  DK(cudaMalloc(&err, sizeof(int)));
+  DK(cudaMemsetAsync(err, 0, sizeof(int), s));
+  DK(cudaMemcpyAsync(D->x32, X, tot * 4, cudaMemcpyDefault, s));
+  k_dense_prep<<<blocks_for(n + 1, 128), 128, 0, s>>>(d, n, D->x32, D->x64, D->norm2, D->empty,
+                                                      D->pview, err);
+  DevCsc M;
+  M.nrow = d; M.ncol = (int32_t)n; M.p = D->pview; M.i = nullptr; M.x = D->x64;
+  launch_unit_csc(M, D->u64, D->scale, err, s);
+  k_dense_cast<<<152 * 16, 256, 0, s>>>((int64_t)tot, D->u64, D->x32, D->u32, D->ub, D->xb);
+  int herr = 0;
+  std::vector<uint8_t> he((size_t)n);
+  DK(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  DK(cudaMemcpyAsync(he.data(), D->empty, (size_t)n, cudaMemcpyDeviceToHost, s));
+  DK(cudaStreamSynchronize(s));
+  cudaFree(err);
+  for (uint8_t v : he) D->n_empty += v;
+  if (herr) { sdg_dense_free(D); return fail_with(SDG_E_NONFINITE, "Cosine requires finite input (found NA, NaN or Inf)."); }
+  DB(cublasCreate(&D->blas));
+  *out = D;
+  return SDG_OK;
+}
+
+SDG_API int sdg_dense_free(sdg_dense* D) {
+  if (!D) return SDG_OK;
+  cudaSetDevice(D->device);
+  cudaDeviceSynchronize();
+  for (void* p : {(void*)D->x64, (void*)D->u64, (void*)D->x32, (void*)D->u32, (void*)D->xb,
+                  (void*)D->ub, (void*)D->norm2, (void*)D->scale, (void*)D->empty, (void*)D->pview})
+    if (p) cudaFree(p);
+  if (D->blas) cublasDestroy(D->blas);
+  delete D;
+  return SDG_OK;
+}
+
+SDG_API int sdg_dense_knn_block(sdg_ctx* ctx, const sdg_dense* D, int64_t q0, int64_t nq,
+                                int method, int k, int mode, int32_t* idx, double* dist_out,
+                                int device_out, int* k_eff, int* flags) {
+  if (!ctx || !D || !idx || !dist_out || !k_eff || !flags) return fail_with(SDG_E_ARG, "NULL argument");
+  if (method != COSINE && method != EUCLIDEAN) return fail_with(SDG_E_UNSUPPORTED, "dense kNN supports cosine and euclidean");
+  if (mode != 0 && mode != 1) return fail_with(SDG_E_ARG, "mode must be 0 (BF16 screen) or 1 (plain FP32)");
+  if (k < 1) return fail_with(SDG_E_ARG, "'k' must be a positive integer no larger than .Machine$integer.max.");
+  if (q0 < 0 || nq < 1 || q0 + nq > D->n) return fail_with(SDG_E_ARG, "invalid query column range");
+  DK(cudaSetDevice(D->device));
+  cudaStream_t s = ctx_stream(ctx);
+  *flags = 0;
+  const int64_t avail = D->n - D->n_empty - 1;        // self-search, include_self = FALSE
+  if (avail < 1) return fail_with(SDG_E_NOCAND, "No candidate neighbours available.");
+  if (k > avail) { k = (int)avail; *flags |= SDG_WARN_CLAMP_FWD; }
+  if (k > kMaxK) return fail_with(SDG_E_UNSUPPORTED, "k above 1024 is not supported by this build.");
+  *k_eff = k;
+  const int64_t n = D->n;
+  const int cap = std::max(512, std::min(16384, 64 * k + 256));
+  const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(nq, ((int64_t)8 << 30) / (4 * n)));
+  float* S = nullptr;
+  int32_t *cand = nullptr, *count = nullptr, *over = nullptr, *o_idx = idx;
+  double *vals = nullptr, *o_val = dist_out, *row = nullptr;
+  DK(cudaMallocAsync(&S, sizeof(float) * (size_t)(chunk * n), s));
+  DK(cudaMallocAsync(&cand, sizeof(int32_t) * (size_t)(chunk * cap), s));
+  DK(cudaMallocAsync(&count, sizeof(int32_t) * (size_t)chunk, s));
+  DK(cudaMallocAsync(&over, sizeof(int32_t) * (size_t)chunk, s));
+  DK(cudaMallocAsync(&vals, sizeof(double) * (size_t)(chunk * cap), s));
+  if (!device_out) {
+    DK(cudaMallocAsync(&o_idx, sizeof(int32_t) * (size_t)(nq * k), s));
+    DK(cudaMallocAsync(&o_val, sizeof(double) * (size_t)(nq * k), s));
+  }
+  DB(cublasSetStream(D->blas, s));
+  const float one = 1.f, zero = 0.f;
+  std::vector<int64_t> overflow;
+  for (int64_t c0 = q0; c0 < q0 + nq; c0 += chunk) {
+    const int64_t nb = std::min(chunk, q0 + nq - c0);
+    // S (n x nb, column-major) = R^T Q: S[ql * n + r] = <col r, col c0 + ql>
+    sdg_time_begin(ctx);
+    if (mode == 0) {
+      const __nv_bfloat16* M = (method == COSINE) ? D->ub : D->xb;
+      DB(cublasGemmEx(D->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)n, (int)nb, D->d, &one, M,
+                      CUDA_R_16BF, D->d, M + (size_t)c0 * D->d, CUDA_R_16BF, D->d, &zero, S,
+                      CUDA_R_32F, (int)n, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT));
+    } else {
+      const float* M = (method == COSINE) ? D->u32 : D->x32;
+      DB(cublasSgemm(D->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)n, (int)nb, D->d, &one, M, D->d,
+                     M + (size_t)c0 * D->d, D->d, &zero, S, (int)n));
+    }
+    sdg_time_end(ctx);
+    DenseSelArgs A;
+    A.method = method; A.k = k; A.mode = mode; A.S = S; A.n = n; A.q0 = c0; A.nq = nb; A.d = D->d;
+    A.norm2 = D->norm2; A.empty = D->empty; A.cap = cap; A.cand = cand; A.count = count;
+    A.overflow = over;
+    const size_t smem = sizeof(float) * (size_t)DSEL_WARPS * k;
+    if (smem > 48 * 1024)
+      DK(cudaFuncSetAttribute(k_dense_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_dense_select<<<blocks_for(nb, DSEL_WARPS), DSEL_WARPS * 32, smem, s>>>(A);
+    k_dense_values<<<blocks_for(nb * cap, 128), 128, 0, s>>>(method, mode, D->d, D->x64, D->u64, S, n,
+                                                              D->norm2, cand, count, cap, c0, nb, vals);
+    SelectArgs sa;
+    sa.vals = vals; sa.seg_stride = cap; sa.elem_stride = 1; sa.nseg = nb;
+    sa.cand = cand; sa.cand_count = count; sa.cand_ld = cap;
+    sa.seg_blank = D->empty + q0;          // rows are relative to q0
+    sa.out_idx = o_idx; sa.out_val = o_val; sa.out_ld = nq; sa.out_row0 = c0 - q0;
+    sa.k = k; sa.decreasing = 0;
+    launch_select(sa, s);
+    DK(cudaGetLastError());
+    std::vector<int32_t> h_over((size_t)nb);
+    DK(cudaMemcpyAsync(h_over.data(), over, sizeof(int32_t) * nb, cudaMemcpyDeviceToHost, s));
+    DK(cudaStreamSynchronize(s));
+    for (int64_t t = 0; t < nb; ++t) if (h_over[(size_t)t]) overflow.push_back(c0 + t);
+  }
+  if (!overflow.empty()) {
+    DK(cudaMallocAsync(&row, sizeof(double) * (size_t)n, s));
+    for (int64_t q : overflow) {
+      k_dense_exact_row<<<blocks_for(n, 256), 256, 0, s>>>(method, D->d, D->x64, D->u64, D->empty,
+                                                            n, q, row);
+      SelectArgs sa;
+      sa.vals = row; sa.seg_stride = 0; sa.elem_stride = 1; sa.len = n; sa.nseg = 1;
+      sa.seg_blank = D->empty + q0;
+      sa.out_idx = o_idx; sa.out_val = o_val; sa.out_ld = nq; sa.out_row0 = q - q0;
+      sa.k = k; sa.decreasing = 0;
+      launch_select(sa, s);
+    }
+    DK(cudaGetLastError());
+  }
+  if (!device_out) {
+    DK(cudaMemcpyAsync(idx, o_idx, sizeof(int32_t) * (size_t)(nq * k), cudaMemcpyDeviceToHost, s));
+    DK(cudaMemcpyAsync(dist_out, o_val, sizeof(double) * (size_t)(nq * k), cudaMemcpyDeviceToHost, s));
+  }
+  DK(cudaFreeAsync(S, s)); DK(cudaFreeAsync(cand, s)); DK(cudaFreeAsync(count, s));
+  DK(cudaFreeAsync(over, s)); DK(cudaFreeAsync(vals, s));
+  if (row) DK(cudaFreeAsync(row, s));
+  if (!device_out) { DK(cudaFreeAsync(o_idx, s)); DK(cudaFreeAsync(o_val, s)); }
+  DK(cudaStreamSynchronize(s));
+  ctx_add_overflow(ctx, (int64_t)overflow.size());
+  return SDG_OK;
+}
+
+}  // extern "C"

@@ -7,10 +7,20 @@
 
 #include "sdg_common.cuh"
 
+struct sdg_ctx;
+// Bracket one launch of the bounding kernel (sdg_kernel_time).
+void sdg_time_begin(sdg_ctx* c);
+void sdg_time_end(sdg_ctx* c);
+
 namespace sdg {
 
 // Sets the calling thread's error message (sdg_last_error); never allocates.
 void set_error(const char* msg);
+
+// Context accessors for the translation units outside sdg_api.cpp.
+cudaStream_t ctx_stream(sdg_ctx* c);
+int ctx_device(sdg_ctx* c);
+void ctx_add_overflow(sdg_ctx* c, int64_t n);
 
 // ---- sdg_exact.cu: per-column preparation and exact FP64 pair values --------
 void launch_col_empty(const DevCsc& M, uint8_t* empty, cudaStream_t s);

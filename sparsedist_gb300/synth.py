@@ -31,6 +31,28 @@ def uniform_csc(nrow, ncol, density, seed=0):
     return M
 
 
+def dense_embeddings(d=256, n=2000000, centres=1000, sigma=0.3, cluster_frac=0.5, dup_frac=0.01,
+                     eps=1e-6, seed=0, device="cuda"):
+    """Configuration 3's embeddings as a torch float32 tensor of shape (n, d)
+    (i.e. d x n column-major): a share of i.i.d. N(0,1) columns, the rest drawn
+    around one of ``centres`` N(0,1) centres with N(0, sigma^2) noise, then
+    ``dup_frac`` of the columns replaced by a copy of another column plus
+    N(0, eps^2) noise (near duplicates)."""
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed))
+    X = torch.randn(n, d, generator=g, device=device, dtype=torch.float32)
+    C = torch.randn(centres, d, generator=g, device=device, dtype=torch.float32)
+    member = torch.rand(n, generator=g, device=device) < cluster_frac
+    which = torch.randint(0, centres, (n,), generator=g, device=device)
+    X = torch.where(member[:, None], C[which] + sigma * X, X)
+    ndup = int(dup_frac * n)
+    dst = torch.randperm(n, generator=g, device=device)[:ndup]
+    src = torch.randint(0, n, (ndup,), generator=g, device=device)
+    X[dst] = X[src] + eps * torch.randn(ndup, d, generator=g, device=device)
+    return X.contiguous()
+
+
 def logcount_csc(nrow=30000, ncol=200000, mean_nnz=1800.0, sdlog=0.6, row_sdlog=1.5,
                  col_sdlog=0.5, seed=0, device="cuda", chunk=1024, keep_on_device=False):
     """Returns (p int32[ncol+1], i int32[nnz], x float64[nnz]) on the host, or,
