@@ -361,8 +361,11 @@ def run_c3(args):
             torch.cuda.synchronize()
             ms = e0.elapsed_time(e1) / args.steps
             gemm_ms, launches = ctx.kernel_time()
+            st = ctx.stats()                              # the last block's counters
             flops = 2.0 * d * B * n
             res["%s/%s" % (method, name)] = {"columns_per_s": B / (ms / 1000.0), "ms_per_block": ms,
+                                             "candidates_per_query": st["pairs_exact"] / B,
+                                             "overflow_queries": st["overflow_queries"],
                                              "gemm_ms": gemm_ms / max(launches, 1),
                                              "gemm_tflops": flops / (gemm_ms / max(launches, 1) / 1000.0) / 1e12}
         res["%s/speedup_bf16_vs_fp32" % method] = (res["%s/bf16_screen_fp64_rerank" % method]["columns_per_s"] /

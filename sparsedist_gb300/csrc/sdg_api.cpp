@@ -167,6 +167,8 @@ namespace sdg {
 cudaStream_t ctx_stream(sdg_ctx* c) { return c->stream; }
 int ctx_device(sdg_ctx* c) { return c->device; }
 void ctx_add_overflow(sdg_ctx* c, int64_t n) { c->stats[2] += n; }
+void ctx_stats_add(sdg_ctx* c, int slot, int64_t n) { if (slot >= 0 && slot < 8) c->stats[slot] += n; }
+void ctx_stats_reset(sdg_ctx* c) { std::memset(c->stats, 0, sizeof c->stats); }
 }  // namespace sdg
 
 // Brackets one launch of the bounding kernel (see sdg_kernel_time).

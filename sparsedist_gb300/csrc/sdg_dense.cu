@@ -87,13 +87,27 @@ __global__ void k_dense_cast(int64_t total, const double* u64, const float* x32,
   }
 }
 
+// A query's scan over the n references is split into segments of DSEG
+// references, one warp per (query, segment), so that the slab is streamed at
+// full bandwidth: (1) each warp keeps the top k of its segment's pessimistic
+// keys (key - err); (2) one warp per query merges the segments' lists into
+// the exact k-th largest pessimistic key T (the top k of a union is the top k
+// of the parts' top k); (3) each warp keeps every reference of its segment
+// whose optimistic key reaches T - margin, appended to the query's candidate
+// list with one atomic per 32 x 4 references.
+constexpr int DSEG = 32768;
+
 struct DenseSelArgs {
   int method, k, mode;           // mode 0: BF16 bound, 1: plain FP32 (no bound)
-  const float* S;                // S[ql * n + r]
+  const float* S;                // S[ql * ldS + r]
+  int64_t ldS;                   // multiple of 4 (float4 rows)
   int64_t n, q0, nq;
   int32_t d;
-  const float* norm2;
-  const uint8_t* empty;
+  const float* norm2;            // padded to ldS entries
+  const uint8_t* empty;          // padded to ldS entries (padding = 1)
+  int nseg;
+  float* segtop;                 // [ql][seg][k], best first, -inf padded
+  float* cut;                    // [ql]: T - margin
   int cap;
   int32_t* cand;
   int32_t* count;
@@ -112,83 +126,168 @@ __device__ __forceinline__ void dense_key(int method, int mode, int32_t d, float
   }
 }
 
-// per query: T = k-th largest (key - err), keep every r with key + err >= T
-__global__ void k_dense_select(DenseSelArgs A) {
+// Warp-cooperative insertion of the lanes flagged in m (value v on each lane)
+// into lst[0..n), kept sorted descending and at most K long.
+__device__ __forceinline__ void warp_insert_desc(float* lst, int K, int& n, unsigned m, float v, int lane) {
+  while (m) {
+    const int src = __ffs(m) - 1;
+    m &= m - 1;
+    const float x = __shfl_sync(0xffffffffu, v, src);
+    if (n == K && !(x > lst[K - 1])) continue;
+    int a = 0, b = n;
+    while (a < b) { const int mid = (a + b) >> 1; if (lst[mid] >= x) a = mid + 1; else b = mid; }
+    const int last = (n < K) ? n : K - 1;
+    if (last > a) {
+      for (int c = (last - 1) >> 5; c >= (a >> 5); --c) {
+        const int e = c * 32 + lane;
+        const bool mv = (e >= a && e < last);
+        float t = 0.f;
+        if (mv) t = lst[e];
+        __syncwarp();
+        if (mv) lst[e + 1] = t;
+        __syncwarp();
+      }
+    }
+    if (lane == 0) lst[a] = x;
+    __syncwarp();
+    if (n < K) ++n;
+  }
+}
+
+// The four references r0..r0+3 of one lane: their pessimistic (lo) and
+// optimistic (hi) keys, -inf where the reference is not a candidate.
+__device__ __forceinline__ void dense_keys4(const DenseSelArgs& A, int64_t q, float Nq, const float* Srow,
+                                            int64_t r0, float lo[4], float hi[4]) {
+  const float4 s4 = *reinterpret_cast<const float4*>(Srow + r0);
+  const uchar4 e4 = *reinterpret_cast<const uchar4*>(A.empty + r0);
+  float4 n4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (A.method != COSINE) n4 = *reinterpret_cast<const float4*>(A.norm2 + r0);
+  const float sv[4] = {s4.x, s4.y, s4.z, s4.w};
+  const float nv[4] = {n4.x, n4.y, n4.z, n4.w};
+  const uint8_t ev[4] = {e4.x, e4.y, e4.z, e4.w};
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int64_t r = r0 + j;
+    lo[j] = hi[j] = -INFINITY;
+    if (r < A.n && r != q && !ev[j]) {
+      float key, err;
+      dense_key(A.method, A.mode, A.d, sv[j], Nq, nv[j], key, err);
+      lo[j] = key - err;
+      hi[j] = key + err;
+    }
+  }
+}
+
+// (1) top k of each (query, segment)'s pessimistic keys
+__global__ void k_dense_segtop(DenseSelArgs A) {
+  extern __shared__ float lists[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t ql = (int64_t)blockIdx.x * DSEL_WARPS + warp;
+  const int seg = blockIdx.y;
+  if (ql >= A.nq) return;
+  const int64_t q = A.q0 + ql;
+  const int K = A.k;
+  float* lst = lists + warp * K;
+  int n = 0;
+  if (!A.empty[q]) {
+    const float Nq = A.norm2[q];
+    const float* Srow = A.S + ql * A.ldS;
+    const int64_t r_end = min(A.n, (int64_t)(seg + 1) * DSEG);
+    float thr = -INFINITY;                       // lst[K - 1] once the list is full
+    for (int64_t p0 = (int64_t)seg * DSEG; p0 < r_end; p0 += 128) {
+      float lo[4], hi[4];
+      dense_keys4(A, q, Nq, Srow, p0 + 4 * lane, lo, hi);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const unsigned m = __ballot_sync(0xffffffffu, lo[j] > -INFINITY && (n < K || lo[j] > thr));
+        if (m) {
+          warp_insert_desc(lst, K, n, m, lo[j], lane);
+          if (n == K) thr = lst[K - 1];
+        }
+      }
+    }
+  }
+  float* out = A.segtop + (ql * A.nseg + seg) * (int64_t)K;
+  for (int t = lane; t < K; t += 32) out[t] = t < n ? lst[t] : -INFINITY;
+}
+
+// (2) per query: T = k-th largest pessimistic key over all segments
+__global__ void k_dense_thresh(DenseSelArgs A) {
   extern __shared__ float lists[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t ql = (int64_t)blockIdx.x * DSEL_WARPS + warp;
   if (ql >= A.nq) return;
-  const int64_t q = A.q0 + ql;
-  float* lst = lists + warp * A.k;
   const int K = A.k;
-  if (A.empty[q]) {                        // degenerate query: all-NA row
-    if (lane == 0) { A.count[ql] = 0; A.overflow[ql] = 0; }
-    return;
-  }
-  const float Nq = A.norm2[q];
-  const float* Srow = A.S + ql * A.n;
+  float* lst = lists + warp * K;
+  const float* in = A.segtop + ql * A.nseg * (int64_t)K;
+  const int64_t tot = (int64_t)A.nseg * K;
   int n = 0;
-  for (int64_t p0 = 0; p0 < A.n; p0 += 32) {
-    const int64_t r = p0 + lane;
-    float lo = -INFINITY;
-    bool ok = r < A.n && r != q && !A.empty[r];
-    if (ok) {
-      float key, err;
-      dense_key(A.method, A.mode, A.d, Srow[r], Nq, A.norm2[r], key, err);
-      lo = key - err;
-    }
-    const bool pass = ok && (n < K || lo > lst[K - 1]);
-    unsigned m = __ballot_sync(0xffffffffu, pass);
-    while (m) {
-      const int src = __ffs(m) - 1;
-      m &= m - 1;
-      const float v = __shfl_sync(0xffffffffu, lo, src);
-      if (n == K && !(v > lst[K - 1])) continue;
-      int a = 0, b = n;
-      while (a < b) { const int mid = (a + b) >> 1; if (lst[mid] >= v) a = mid + 1; else b = mid; }
-      const int last = (n < K) ? n : K - 1;
-      if (last > a) {
-        for (int c = (last - 1) >> 5; c >= (a >> 5); --c) {
-          const int e = c * 32 + lane;
-          const bool mv = (e >= a && e < last);
-          float t = 0.f;
-          if (mv) t = lst[e];
-          __syncwarp();
-          if (mv) lst[e + 1] = t;
-          __syncwarp();
-        }
-      }
-      if (lane == 0) lst[a] = v;
-      __syncwarp();
-      if (n < K) ++n;
-    }
+  for (int64_t p0 = 0; p0 < tot; p0 += 32) {
+    const float v = p0 + lane < tot ? in[p0 + lane] : -INFINITY;
+    const unsigned m = __ballot_sync(0xffffffffu, v > -INFINITY && (n < K || v > lst[K - 1]));
+    if (m) warp_insert_desc(lst, K, n, m, v, lane);
   }
-  const float T = (n == K) ? lst[K - 1] : -INFINITY;
-  const float margin = (T == -INFINITY) ? 0.f : fabsf(T) * 4.76837158203125e-7f + 1e-30f;
-  int cnt = 0;
-  bool over = false;
+  if (lane == 0) {
+    const float T = (n == K) ? lst[K - 1] : -INFINITY;
+    const float margin = (T == -INFINITY) ? 0.f : fabsf(T) * 4.76837158203125e-7f + 1e-30f;
+    A.cut[ql] = T - margin;
+    A.count[ql] = 0;
+  }
+}
+
+// (3) keep every reference of the segment whose optimistic key reaches the cut
+__global__ void k_dense_keep(DenseSelArgs A) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t ql = (int64_t)blockIdx.x * DSEL_WARPS + warp;
+  const int seg = blockIdx.y;
+  if (ql >= A.nq) return;
+  const int64_t q = A.q0 + ql;
+  if (A.empty[q]) return;
+  const float Nq = A.norm2[q];
+  const float cut = A.cut[ql];
+  const float* Srow = A.S + ql * A.ldS;
   int32_t* out = A.cand + ql * (int64_t)A.cap;
-  for (int64_t p0 = 0; p0 < A.n && !over; p0 += 32) {
-    const int64_t r = p0 + lane;
-    bool keep = false;
-    if (r < A.n && r != q && !A.empty[r]) {
-      float key, err;
-      dense_key(A.method, A.mode, A.d, Srow[r], Nq, A.norm2[r], key, err);
-      keep = (key + err) >= T - margin;
+  const int64_t r_end = min(A.n, (int64_t)(seg + 1) * DSEG);
+  for (int64_t p0 = (int64_t)seg * DSEG; p0 < r_end; p0 += 128) {
+    float lo[4], hi[4];
+    dense_keys4(A, q, Nq, Srow, p0 + 4 * lane, lo, hi);
+    int mine = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) mine += (hi[j] > -INFINITY && hi[j] >= cut);
+    int incl = mine;                              // warp inclusive scan of the lanes' counts
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
     }
-    const unsigned m = __ballot_sync(0xffffffffu, keep);
-    const int rank = __popc(m & ((1u << lane) - 1u));
-    if (keep && cnt + rank < A.cap) out[cnt + rank] = (int32_t)r;
-    cnt += __popc(m);
-    if (cnt > A.cap) over = true;
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    if (total == 0) continue;
+    int base = 0;
+    if (lane == 31) base = atomicAdd(A.count + ql, total);
+    base = __shfl_sync(0xffffffffu, base, 31) + incl - mine;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (hi[j] > -INFINITY && hi[j] >= cut) {
+        if (base < A.cap) out[base] = (int32_t)(p0 + 4 * lane + j);
+        ++base;
+      }
+    }
   }
-  if (lane == 0) { A.count[ql] = over ? 0 : cnt; A.overflow[ql] = over ? 1 : 0; }
+}
+
+// overflowing queries drop their list (they are finished by the exact row path)
+__global__ void k_dense_overflow(int64_t nq, int cap, int32_t* count, int32_t* overflow) {
+  const int64_t ql = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (ql >= nq) return;
+  const bool over = count[ql] > cap;
+  overflow[ql] = over ? 1 : 0;
+  if (over) count[ql] = 0;
 }
 
 // Exact FP64 value of each kept pair, in the reference's arithmetic; in the
 // plain mode the FP32 value of the slab instead.
 __global__ void k_dense_values(int method, int mode, int32_t d, const double* x64, const double* u64,
-                               const float* S, int64_t n, const float* norm2, const int32_t* cand,
+                               const float* S, int64_t ldS, const float* norm2, const int32_t* cand,
                                const int32_t* count, int cap, int64_t q0, int64_t nq, double* out) {
   const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= nq * cap) return;
@@ -196,7 +295,7 @@ __global__ void k_dense_values(int method, int mode, int32_t d, const double* x6
   if (t >= count[ql]) return;
   const int64_t q = q0 + ql, r = cand[s];
   if (mode == 1) {
-    const float sv = S[ql * n + r];
+    const float sv = S[ql * ldS + r];
     out[s] = (method == COSINE) ? (double)(1.f - fminf(1.f, fmaxf(-1.f, sv)))
                                 : (double)sqrtf(fmaxf(0.f, norm2[q] + norm2[r] - 2.f * sv));
     return;
@@ -274,8 +373,11 @@ SDG_API int sdg_dense_upload(sdg_ctx* ctx, const float* X, int32_t d, int64_t n,
   DK(cudaMalloc(&D->x64, tot * 8)); DK(cudaMalloc(&D->u64, tot * 8));
   DK(cudaMalloc(&D->x32, tot * 4)); DK(cudaMalloc(&D->u32, tot * 4));
   DK(cudaMalloc(&D->xb, tot * 2)); DK(cudaMalloc(&D->ub, tot * 2));
-  DK(cudaMalloc(&D->norm2, n * 4)); DK(cudaMalloc(&D->scale, n * 8));
-  DK(cudaMalloc(&D->empty, n)); DK(cudaMalloc(&D->pview, (n + 1) * 8));
+  const int64_t npad = (n + 127) / 128 * 128;       // float4 / uchar4 reads past n stay in bounds
+  DK(cudaMalloc(&D->norm2, npad * 4)); DK(cudaMalloc(&D->scale, n * 8));
+  DK(cudaMalloc(&D->empty, npad)); DK(cudaMalloc(&D->pview, (n + 1) * 8));
+  DK(cudaMemsetAsync(D->norm2, 0, npad * 4, s));
+  DK(cudaMemsetAsync(D->empty, 1, npad, s));
   DK(cudaMalloc(&err, sizeof(int)));
   DK(cudaMemsetAsync(err, 0, sizeof(int), s));
   DK(cudaMemcpyAsync(D->x32, X, tot * 4, cudaMemcpyDefault, s));
@@ -328,11 +430,16 @@ SDG_API int sdg_dense_knn_block(sdg_ctx* ctx, const sdg_dense* D, int64_t q0, in
   *k_eff = k;
   const int64_t n = D->n;
   const int cap = std::max(512, std::min(16384, 64 * k + 256));
-  const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(nq, ((int64_t)8 << 30) / (4 * n)));
+  const int64_t ldS = (n + 127) / 128 * 128;
+  const int nseg = (int)((n + DSEG - 1) / DSEG);
+  const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(nq, ((int64_t)8 << 30) / (4 * ldS)));
   float* S = nullptr;
+  float *segtop = nullptr, *cut = nullptr;
   int32_t *cand = nullptr, *count = nullptr, *over = nullptr, *o_idx = idx;
   double *vals = nullptr, *o_val = dist_out, *row = nullptr;
-  DK(cudaMallocAsync(&S, sizeof(float) * (size_t)(chunk * n), s));
+  DK(cudaMallocAsync(&S, sizeof(float) * (size_t)(chunk * ldS), s));
+  DK(cudaMallocAsync(&segtop, sizeof(float) * (size_t)(chunk * nseg * k), s));
+  DK(cudaMallocAsync(&cut, sizeof(float) * (size_t)chunk, s));
   DK(cudaMallocAsync(&cand, sizeof(int32_t) * (size_t)(chunk * cap), s));
   DK(cudaMallocAsync(&count, sizeof(int32_t) * (size_t)chunk, s));
   DK(cudaMallocAsync(&over, sizeof(int32_t) * (size_t)chunk, s));
@@ -344,30 +451,35 @@ SDG_API int sdg_dense_knn_block(sdg_ctx* ctx, const sdg_dense* D, int64_t q0, in
   DB(cublasSetStream(D->blas, s));
   const float one = 1.f, zero = 0.f;
   std::vector<int64_t> overflow;
+  ctx_stats_reset(ctx);
+  ctx_stats_add(ctx, 0, n * nq);                      // pairs screened
   for (int64_t c0 = q0; c0 < q0 + nq; c0 += chunk) {
     const int64_t nb = std::min(chunk, q0 + nq - c0);
-    // S (n x nb, column-major) = R^T Q: S[ql * n + r] = <col r, col c0 + ql>
+    // S (n x nb, column-major, leading dimension ldS) = R^T Q:
+    // S[ql * ldS + r] = <col r, col c0 + ql>
     sdg_time_begin(ctx);
     if (mode == 0) {
       const __nv_bfloat16* M = (method == COSINE) ? D->ub : D->xb;
       DB(cublasGemmEx(D->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)n, (int)nb, D->d, &one, M,
                       CUDA_R_16BF, D->d, M + (size_t)c0 * D->d, CUDA_R_16BF, D->d, &zero, S,
-                      CUDA_R_32F, (int)n, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT));
+                      CUDA_R_32F, (int)ldS, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT));
     } else {
       const float* M = (method == COSINE) ? D->u32 : D->x32;
       DB(cublasSgemm(D->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)n, (int)nb, D->d, &one, M, D->d,
-                     M + (size_t)c0 * D->d, D->d, &zero, S, (int)n));
+                     M + (size_t)c0 * D->d, D->d, &zero, S, (int)ldS));
     }
     sdg_time_end(ctx);
     DenseSelArgs A;
-    A.method = method; A.k = k; A.mode = mode; A.S = S; A.n = n; A.q0 = c0; A.nq = nb; A.d = D->d;
-    A.norm2 = D->norm2; A.empty = D->empty; A.cap = cap; A.cand = cand; A.count = count;
-    A.overflow = over;
-    const size_t smem = sizeof(float) * (size_t)DSEL_WARPS * k;
-    if (smem > 48 * 1024)
-      DK(cudaFuncSetAttribute(k_dense_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_dense_select<<<blocks_for(nb, DSEL_WARPS), DSEL_WARPS * 32, smem, s>>>(A);
-    k_dense_values<<<blocks_for(nb * cap, 128), 128, 0, s>>>(method, mode, D->d, D->x64, D->u64, S, n,
+    A.method = method; A.k = k; A.mode = mode; A.S = S; A.ldS = ldS; A.n = n; A.q0 = c0; A.nq = nb;
+    A.d = D->d; A.norm2 = D->norm2; A.empty = D->empty; A.nseg = nseg; A.segtop = segtop; A.cut = cut;
+    A.cap = cap; A.cand = cand; A.count = count; A.overflow = over;
+    const size_t smem = sizeof(float) * (size_t)DSEL_WARPS * k;     // <= 32 KB (k <= 1024)
+    const dim3 grid(blocks_for(nb, DSEL_WARPS), (unsigned)nseg);
+    k_dense_segtop<<<grid, DSEL_WARPS * 32, smem, s>>>(A);
+    k_dense_thresh<<<blocks_for(nb, DSEL_WARPS), DSEL_WARPS * 32, smem, s>>>(A);
+    k_dense_keep<<<grid, DSEL_WARPS * 32, 0, s>>>(A);
+    k_dense_overflow<<<blocks_for(nb, 256), 256, 0, s>>>(nb, cap, count, over);
+    k_dense_values<<<blocks_for(nb * cap, 128), 128, 0, s>>>(method, mode, D->d, D->x64, D->u64, S, ldS,
                                                               D->norm2, cand, count, cap, c0, nb, vals);
     SelectArgs sa;
     sa.vals = vals; sa.seg_stride = cap; sa.elem_stride = 1; sa.nseg = nb;
@@ -377,10 +489,14 @@ SDG_API int sdg_dense_knn_block(sdg_ctx* ctx, const sdg_dense* D, int64_t q0, in
     sa.k = k; sa.decreasing = 0;
     launch_select(sa, s);
     DK(cudaGetLastError());
-    std::vector<int32_t> h_over((size_t)nb);
+    std::vector<int32_t> h_over((size_t)nb), h_count((size_t)nb);
     DK(cudaMemcpyAsync(h_over.data(), over, sizeof(int32_t) * nb, cudaMemcpyDeviceToHost, s));
+    DK(cudaMemcpyAsync(h_count.data(), count, sizeof(int32_t) * nb, cudaMemcpyDeviceToHost, s));
     DK(cudaStreamSynchronize(s));
-    for (int64_t t = 0; t < nb; ++t) if (h_over[(size_t)t]) overflow.push_back(c0 + t);
+    for (int64_t t = 0; t < nb; ++t) {
+      if (h_over[(size_t)t]) overflow.push_back(c0 + t);
+      ctx_stats_add(ctx, 1, h_over[(size_t)t] ? n : h_count[(size_t)t]);   // pairs valued exactly
+    }
   }
   if (!overflow.empty()) {
     DK(cudaMallocAsync(&row, sizeof(double) * (size_t)n, s));
@@ -401,6 +517,7 @@ SDG_API int sdg_dense_knn_block(sdg_ctx* ctx, const sdg_dense* D, int64_t q0, in
     DK(cudaMemcpyAsync(dist_out, o_val, sizeof(double) * (size_t)(nq * k), cudaMemcpyDeviceToHost, s));
   }
   DK(cudaFreeAsync(S, s)); DK(cudaFreeAsync(cand, s)); DK(cudaFreeAsync(count, s));
+  DK(cudaFreeAsync(segtop, s)); DK(cudaFreeAsync(cut, s));
   DK(cudaFreeAsync(over, s)); DK(cudaFreeAsync(vals, s));
   if (row) DK(cudaFreeAsync(row, s));
   if (!device_out) { DK(cudaFreeAsync(o_idx, s)); DK(cudaFreeAsync(o_val, s)); }

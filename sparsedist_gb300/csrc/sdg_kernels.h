@@ -21,6 +21,9 @@ void set_error(const char* msg);
 cudaStream_t ctx_stream(sdg_ctx* c);
 int ctx_device(sdg_ctx* c);
 void ctx_add_overflow(sdg_ctx* c, int64_t n);
+// slot t of the per-call statistics (sdg_last_stats); reset clears all eight
+void ctx_stats_add(sdg_ctx* c, int slot, int64_t n);
+void ctx_stats_reset(sdg_ctx* c);
 
 // ---- sdg_exact.cu: per-column preparation and exact FP64 pair values --------
 void launch_col_empty(const DevCsc& M, uint8_t* empty, cudaStream_t s);

@@ -40,3 +40,37 @@ def test_bf16_screen_with_exact_rerank_equals_oracle(method, code):
     agree = np.mean(plain[0] == want[0])
     assert agree > 0.5                                                   # reported, not required
     torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("method,code", [("cosine", 1), ("euclidean", 2)])
+def test_bf16_screen_many_segments_and_zero_columns(method, code):
+    """70,001 references (three 32,768-reference segments, the last one ragged
+    and not a multiple of 128) and a query block that starts mid-matrix; two
+    all-zero columns (one query, one reference) are degenerate: the query's row
+    is all NA and the reference is never returned.  The oracle's two-matrix
+    search with k + 1 neighbours, minus each query's own column, is the
+    self-search result."""
+    import ctypes as C
+    import torch
+    from sparsedist_gb300 import _lib, synth
+    d, n, q0, nq, k = 32, 70001, 1000, 64, 10
+    X = synth.dense_embeddings(d=d, n=n, centres=50, seed=7)
+    X[q0 + 5] = 0.0
+    X[40000] = 0.0
+    ctx = _lib.Context()
+    h = C.c_void_p()
+    _lib.check(ctx.lib.sdg_dense_upload(ctx.handle, X.data_ptr(), d, n, C.byref(h)))
+    got = dense_knn(ctx, h, q0, nq, code, k, 0)
+    ctx.lib.sdg_dense_free(h)
+    A = sp.csc_matrix(X.double().cpu().numpy().T)
+    wi, wd, _ = OracleBackend().knn(A[:, q0:q0 + nq], A, k=k + 1, method=method)
+    for t in range(nq):
+        if t == 5:
+            assert np.all(got[0][t] == np.iinfo(np.int32).min)
+            assert np.all(np.isnan(got[1][t]))
+            continue
+        keep = wi[t] != q0 + t + 1
+        assert same_bits(got[0][t], wi[t][keep][:k]), t
+        assert same_bits(got[1][t], wd[t][keep][:k]), t
+        assert 40001 not in got[0][t]
+    torch.cuda.synchronize()
