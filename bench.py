@@ -66,6 +66,7 @@ def parse():
                          "configuration 1; serve: configuration 5, the serving loop")
     ap.add_argument("--serve-ref-cols", type=int, default=1000000)
     ap.add_argument("--c3-cols", type=int, default=2000000)
+    ap.add_argument("--c3-block", type=int, default=4096)
     ap.add_argument("--serve-requests", type=int, default=80)
     ap.add_argument("--serve-util", type=float, default=0.75)
     return ap.parse_args()
@@ -325,14 +326,14 @@ def run_serve(args):
 def run_c3(args):
     """Configuration 3: 256 x 2,000,000 FP32 embeddings (i.i.d. N(0,1) mixed
     with 1,000 Gaussian clusters, sigma 0.3, plus 1 % near duplicates at 1e-6),
-    cosine and euclidean self-search, k = 20, in blocks of 1,024 query columns:
+    cosine and euclidean self-search, k = 20, in blocks of --c3-block (4,096) query columns:
     the BF16 tensor-core screen + exact FP64 re-rank against the plain FP32
     path, with idx identity and distance error checked against the exact FP64
     engine on a sample of query columns."""
     import ctypes as C
     import torch
     from sparsedist_gb300 import _lib, synth
-    d, n, B, k = 256, args.c3_cols, 1024, 20
+    d, n, B, k = 256, args.c3_cols, args.c3_block, 20
     X = synth.dense_embeddings(d=d, n=n, seed=5)
     ctx = _lib.Context()
     stream = torch.cuda.current_stream()
@@ -344,7 +345,8 @@ def run_c3(args):
     ke, fl = np.zeros(1, np.int32), np.zeros(1, np.int32)
     res = {}
     for method, code in (("cosine", 1), ("euclidean", 2)):
-        for mode, name in ((0, "bf16_screen_fp64_rerank"), (1, "plain_fp32")):
+        for mode, name in ((0, "bf16_tcgen05_fused_fp64_rerank"), (2, "bf16_cublas_slab_fp64_rerank"),
+                           (1, "plain_fp32")):
             def step(s):
                 _lib.check(ctx.lib.sdg_dense_knn_block(ctx.handle, h, (s * B) % (n - B), B, code, k,
                                                        mode, d_idx.data_ptr(), d_val.data_ptr(), 1,
@@ -368,7 +370,7 @@ def run_c3(args):
                                              "overflow_queries": st["overflow_queries"],
                                              "gemm_ms": gemm_ms / max(launches, 1),
                                              "gemm_tflops": flops / (gemm_ms / max(launches, 1) / 1000.0) / 1e12}
-        res["%s/speedup_bf16_vs_fp32" % method] = (res["%s/bf16_screen_fp64_rerank" % method]["columns_per_s"] /
+        res["%s/speedup_bf16_vs_fp32" % method] = (res["%s/bf16_tcgen05_fused_fp64_rerank" % method]["columns_per_s"] /
                                                    res["%s/plain_fp32" % method]["columns_per_s"])
     # correctness on a sample of query columns: the exact FP64 engine on the same data
     qs = 16
@@ -388,7 +390,8 @@ def run_c3(args):
                                             fl.ctypes.data))
         wi = wi.reshape(k + 1, qs).T
         wd = wd.reshape(k + 1, qs).T
-        for mode, name in ((0, "bf16_screen_fp64_rerank"), (1, "plain_fp32")):
+        for mode, name in ((0, "bf16_tcgen05_fused_fp64_rerank"), (2, "bf16_cublas_slab_fp64_rerank"),
+                           (1, "plain_fp32")):
             gi = np.empty(qs * k, np.int32)
             gd = np.empty(qs * k, np.float64)
             _lib.check(ctx.lib.sdg_dense_knn_block(ctx.handle, h, 0, qs, code, k, mode, gi.ctypes.data,
@@ -404,7 +407,7 @@ def run_c3(args):
             check["%s/%s" % (method, name)] = {"rows_with_identical_idx": same, "rows": qs,
                                                "max_abs_distance_error_vs_fp64": err}
     ctx.set_engine(0)
-    print(json.dumps({"metric": "dense kNN query columns/s, configuration 3 (k=20, 1,024-query blocks)",
+    print(json.dumps({"metric": "dense kNN query columns/s, configuration 3 (k=20, %d-query blocks)" % B,
                       "config": {"workload": "256x%d FP32 embeddings: N(0,1) + 1000 clusters (sigma 0.3) "
                                              "+ 1%% near duplicates (1e-6)" % n},
                       "results": res, "check_vs_fp64_engine": check}))

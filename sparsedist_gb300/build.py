@@ -33,6 +33,7 @@ UNITS = [
     ("sdg_screen.cu", []),
     ("sdg_noalloc.cu", []),
     ("sdg_dense.cu", []),
+    ("sdg_dense_tc.cu", []),
     ("sdg_api.cpp", []),
 ]
 

@@ -19,33 +19,12 @@
 // tensor cores' accumulation); with S|x_i y_i| <= |x| |y|:
 //   cosine    (unit vectors):  |S - S_exact| <= 0.0040 + d * 2^-22
 //   euclidean (2S - Nq - Nr):  2 (0.0040 + d * 2^-22) sqrt(Nq Nr) + 2^-20 (Nq + Nr)
-#include <cublas_v2.h>
-#include <cuda_bf16.h>
-
 #include <algorithm>
 #include <cmath>
 #include <vector>
 
 #include "../../include/sdgpu.h"
-#include "sdg_kernels.h"
-
-struct sdg_dense {
-  int device = 0;
-  int32_t d = 0;
-  int64_t n = 0;
-  double* x64 = nullptr;          // d x n column-major
-  double* u64 = nullptr;          // unit columns (unit_csc on the dense column)
-  float* x32 = nullptr;
-  float* u32 = nullptr;
-  __nv_bfloat16* xb = nullptr;
-  __nv_bfloat16* ub = nullptr;
-  float* norm2 = nullptr;         // sum of squares (FP64, rounded)
-  double* scale = nullptr;        // unit_csc scale (0 = empty column)
-  uint8_t* empty = nullptr;
-  int64_t* pview = nullptr;       // column offsets j * d, for the CSC kernels
-  int64_t n_empty = 0;
-  cublasHandle_t blas = nullptr;
-};
+#include "sdg_dense.h"
 
 namespace sdg {
 namespace {
@@ -113,18 +92,6 @@ struct DenseSelArgs {
   int32_t* count;
   int32_t* overflow;
 };
-
-__device__ __forceinline__ void dense_key(int method, int mode, int32_t d, float s, float Nq, float Nr,
-                                          float& key, float& err) {
-  const float rel = 0.0040f + (float)d * 2.384185791015625e-7f;   // 2^-22
-  if (method == COSINE) {
-    key = s;
-    err = mode == 0 ? rel : 0.f;
-  } else {
-    key = 2.f * s - (Nq + Nr);
-    err = mode == 0 ? 2.f * rel * sqrtf(Nq * Nr) + 9.5367431640625e-7f * (Nq + Nr) + 1e-30f : 0.f;
-  }
-}
 
 // Warp-cooperative insertion of the lanes flagged in m (value v on each lane)
 // into lst[0..n), kept sorted descending and at most K long.
@@ -228,9 +195,7 @@ __global__ void k_dense_thresh(DenseSelArgs A) {
     if (m) warp_insert_desc(lst, K, n, m, v, lane);
   }
   if (lane == 0) {
-    const float T = (n == K) ? lst[K - 1] : -INFINITY;
-    const float margin = (T == -INFINITY) ? 0.f : fabsf(T) * 4.76837158203125e-7f + 1e-30f;
-    A.cut[ql] = T - margin;
+    A.cut[ql] = dense_cut((n == K) ? lst[K - 1] : -INFINITY);
     A.count[ql] = 0;
   }
 }
@@ -374,6 +339,8 @@ SDG_API int sdg_dense_upload(sdg_ctx* ctx, const float* X, int32_t d, int64_t n,
   DK(cudaMalloc(&D->x32, tot * 4)); DK(cudaMalloc(&D->u32, tot * 4));
   DK(cudaMalloc(&D->xb, tot * 2)); DK(cudaMalloc(&D->ub, tot * 2));
   const int64_t npad = (n + 127) / 128 * 128;       // float4 / uchar4 reads past n stay in bounds
+  D->npad = npad;
+  D->dpad = (d + 63) / 64 * 64;
   DK(cudaMalloc(&D->norm2, npad * 4)); DK(cudaMalloc(&D->scale, n * 8));
   DK(cudaMalloc(&D->empty, npad)); DK(cudaMalloc(&D->pview, (n + 1) * 8));
   DK(cudaMemsetAsync(D->norm2, 0, npad * 4, s));
@@ -387,6 +354,19 @@ SDG_API int sdg_dense_upload(sdg_ctx* ctx, const float* X, int32_t d, int64_t n,
   M.nrow = d; M.ncol = (int32_t)n; M.p = D->pview; M.i = nullptr; M.x = D->x64;
   launch_unit_csc(M, D->u64, D->scale, err, s);
   k_dense_cast<<<152 * 16, 256, 0, s>>>((int64_t)tot, D->u64, D->x32, D->u32, D->ub, D->xb);
+  if (D->dpad == d) {
+    D->ubp = D->ub;
+    D->xbp = D->xb;
+  } else {                                          // rows d..dpad-1 of the padded copies are zero
+    const size_t ptot = (size_t)D->dpad * (size_t)n;
+    DK(cudaMalloc(&D->ubp, ptot * 2)); DK(cudaMalloc(&D->xbp, ptot * 2));
+    DK(cudaMemset2DAsync(D->ubp, (size_t)D->dpad * 2, 0, (size_t)D->dpad * 2, (size_t)n, s));
+    DK(cudaMemset2DAsync(D->xbp, (size_t)D->dpad * 2, 0, (size_t)D->dpad * 2, (size_t)n, s));
+    DK(cudaMemcpy2DAsync(D->ubp, (size_t)D->dpad * 2, D->ub, (size_t)d * 2, (size_t)d * 2, (size_t)n,
+                         cudaMemcpyDeviceToDevice, s));
+    DK(cudaMemcpy2DAsync(D->xbp, (size_t)D->dpad * 2, D->xb, (size_t)d * 2, (size_t)d * 2, (size_t)n,
+                         cudaMemcpyDeviceToDevice, s));
+  }
   int herr = 0;
   std::vector<uint8_t> he((size_t)n);
   DK(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -404,6 +384,8 @@ SDG_API int sdg_dense_free(sdg_dense* D) {
   if (!D) return SDG_OK;
   cudaSetDevice(D->device);
   cudaDeviceSynchronize();
+  if (D->ubp && D->ubp != D->ub) cudaFree(D->ubp);
+  if (D->xbp && D->xbp != D->xb) cudaFree(D->xbp);
   for (void* p : {(void*)D->x64, (void*)D->u64, (void*)D->x32, (void*)D->u32, (void*)D->xb,
                   (void*)D->ub, (void*)D->norm2, (void*)D->scale, (void*)D->empty, (void*)D->pview})
     if (p) cudaFree(p);
@@ -417,7 +399,8 @@ SDG_API int sdg_dense_knn_block(sdg_ctx* ctx, const sdg_dense* D, int64_t q0, in
                                 int device_out, int* k_eff, int* flags) {
   if (!ctx || !D || !idx || !dist_out || !k_eff || !flags) return fail_with(SDG_E_ARG, "NULL argument");
   if (method != COSINE && method != EUCLIDEAN) return fail_with(SDG_E_UNSUPPORTED, "dense kNN supports cosine and euclidean");
-  if (mode != 0 && mode != 1) return fail_with(SDG_E_ARG, "mode must be 0 (BF16 screen) or 1 (plain FP32)");
+  if (mode < 0 || mode > 2)
+    return fail_with(SDG_E_ARG, "mode must be 0 (BF16 screen), 1 (plain FP32) or 2 (BF16 slab screen)");
   if (k < 1) return fail_with(SDG_E_ARG, "'k' must be a positive integer no larger than .Machine$integer.max.");
   if (q0 < 0 || nq < 1 || q0 + nq > D->n) return fail_with(SDG_E_ARG, "invalid query column range");
   DK(cudaSetDevice(D->device));
@@ -430,16 +413,23 @@ SDG_API int sdg_dense_knn_block(sdg_ctx* ctx, const sdg_dense* D, int64_t q0, in
   *k_eff = k;
   const int64_t n = D->n;
   const int cap = std::max(512, std::min(16384, 64 * k + 256));
+  // mode 0 runs the fused tensor-core screen where it applies (no slab in
+  // HBM), else the BF16 slab screen of mode 2; smode is the bound in force
+  const bool fused = mode == 0 && tc_screen_supported(D, method, k);
+  const int smode = (mode == 1) ? 1 : 0;
   const int64_t ldS = (n + 127) / 128 * 128;
   const int nseg = (int)((n + DSEG - 1) / DSEG);
-  const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(nq, ((int64_t)8 << 30) / (4 * ldS)));
+  const int64_t chunk = fused ? std::min<int64_t>(nq, 65536)
+                              : std::max<int64_t>(1, std::min<int64_t>(nq, ((int64_t)8 << 30) / (4 * ldS)));
   float* S = nullptr;
   float *segtop = nullptr, *cut = nullptr;
   int32_t *cand = nullptr, *count = nullptr, *over = nullptr, *o_idx = idx;
   double *vals = nullptr, *o_val = dist_out, *row = nullptr;
-  DK(cudaMallocAsync(&S, sizeof(float) * (size_t)(chunk * ldS), s));
-  DK(cudaMallocAsync(&segtop, sizeof(float) * (size_t)(chunk * nseg * k), s));
-  DK(cudaMallocAsync(&cut, sizeof(float) * (size_t)chunk, s));
+  if (!fused) {
+    DK(cudaMallocAsync(&S, sizeof(float) * (size_t)(chunk * ldS), s));
+    DK(cudaMallocAsync(&segtop, sizeof(float) * (size_t)(chunk * nseg * k), s));
+    DK(cudaMallocAsync(&cut, sizeof(float) * (size_t)chunk, s));
+  }
   DK(cudaMallocAsync(&cand, sizeof(int32_t) * (size_t)(chunk * cap), s));
   DK(cudaMallocAsync(&count, sizeof(int32_t) * (size_t)chunk, s));
   DK(cudaMallocAsync(&over, sizeof(int32_t) * (size_t)chunk, s));
@@ -455,10 +445,14 @@ SDG_API int sdg_dense_knn_block(sdg_ctx* ctx, const sdg_dense* D, int64_t q0, in
   ctx_stats_add(ctx, 0, n * nq);                      // pairs screened
   for (int64_t c0 = q0; c0 < q0 + nq; c0 += chunk) {
     const int64_t nb = std::min(chunk, q0 + nq - c0);
+    if (fused) {
+      const int st = tc_screen(ctx, D, method, k, c0, nb, cand, count, over, cap, s);
+      if (st != SDG_OK) return st;
+    } else {
     // S (n x nb, column-major, leading dimension ldS) = R^T Q:
     // S[ql * ldS + r] = <col r, col c0 + ql>
     sdg_time_begin(ctx);
-    if (mode == 0) {
+    if (smode == 0) {
       const __nv_bfloat16* M = (method == COSINE) ? D->ub : D->xb;
       DB(cublasGemmEx(D->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)n, (int)nb, D->d, &one, M,
                       CUDA_R_16BF, D->d, M + (size_t)c0 * D->d, CUDA_R_16BF, D->d, &zero, S,
@@ -470,7 +464,7 @@ SDG_API int sdg_dense_knn_block(sdg_ctx* ctx, const sdg_dense* D, int64_t q0, in
     }
     sdg_time_end(ctx);
     DenseSelArgs A;
-    A.method = method; A.k = k; A.mode = mode; A.S = S; A.ldS = ldS; A.n = n; A.q0 = c0; A.nq = nb;
+    A.method = method; A.k = k; A.mode = smode; A.S = S; A.ldS = ldS; A.n = n; A.q0 = c0; A.nq = nb;
     A.d = D->d; A.norm2 = D->norm2; A.empty = D->empty; A.nseg = nseg; A.segtop = segtop; A.cut = cut;
     A.cap = cap; A.cand = cand; A.count = count; A.overflow = over;
     const size_t smem = sizeof(float) * (size_t)DSEL_WARPS * k;     // <= 32 KB (k <= 1024)
@@ -479,7 +473,8 @@ SDG_API int sdg_dense_knn_block(sdg_ctx* ctx, const sdg_dense* D, int64_t q0, in
     k_dense_thresh<<<blocks_for(nb, DSEL_WARPS), DSEL_WARPS * 32, smem, s>>>(A);
     k_dense_keep<<<grid, DSEL_WARPS * 32, 0, s>>>(A);
     k_dense_overflow<<<blocks_for(nb, 256), 256, 0, s>>>(nb, cap, count, over);
-    k_dense_values<<<blocks_for(nb * cap, 128), 128, 0, s>>>(method, mode, D->d, D->x64, D->u64, S, ldS,
+    }
+    k_dense_values<<<blocks_for(nb * cap, 128), 128, 0, s>>>(method, smode, D->d, D->x64, D->u64, S, ldS,
                                                               D->norm2, cand, count, cap, c0, nb, vals);
     SelectArgs sa;
     sa.vals = vals; sa.seg_stride = cap; sa.elem_stride = 1; sa.nseg = nb;
@@ -516,8 +511,10 @@ SDG_API int sdg_dense_knn_block(sdg_ctx* ctx, const sdg_dense* D, int64_t q0, in
     DK(cudaMemcpyAsync(idx, o_idx, sizeof(int32_t) * (size_t)(nq * k), cudaMemcpyDeviceToHost, s));
     DK(cudaMemcpyAsync(dist_out, o_val, sizeof(double) * (size_t)(nq * k), cudaMemcpyDeviceToHost, s));
   }
-  DK(cudaFreeAsync(S, s)); DK(cudaFreeAsync(cand, s)); DK(cudaFreeAsync(count, s));
-  DK(cudaFreeAsync(segtop, s)); DK(cudaFreeAsync(cut, s));
+  if (S) DK(cudaFreeAsync(S, s));
+  if (segtop) DK(cudaFreeAsync(segtop, s));
+  if (cut) DK(cudaFreeAsync(cut, s));
+  DK(cudaFreeAsync(cand, s)); DK(cudaFreeAsync(count, s));
   DK(cudaFreeAsync(over, s)); DK(cudaFreeAsync(vals, s));
   if (row) DK(cudaFreeAsync(row, s));
   if (!device_out) { DK(cudaFreeAsync(o_idx, s)); DK(cudaFreeAsync(o_val, s)); }

@@ -1,7 +1,8 @@
-"""Dense embedding columns (configuration 3's path): the BF16 tensor-core
-screen with the exact FP64 re-rank must return the oracle's sparseKNN result
-on the same data bit for bit (idx and distances), near-duplicate columns
-included; the plain FP32 path is only reported (its recall is not exact)."""
+"""Dense embedding columns (configuration 3's path): both BF16 screens (mode 0,
+the fused tcgen05 kernel; mode 2, the cuBLAS slab) with the exact FP64 re-rank
+must return the oracle's sparseKNN result on the same data bit for bit (idx
+and distances), near-duplicate columns included; the plain FP32 path (mode 1)
+is only reported (its recall is not exact)."""
 import numpy as np
 import pytest
 import scipy.sparse as sp
@@ -22,8 +23,9 @@ def dense_knn(ctx, D, q0, nq, method, k, mode):
     return idx[:nq * e].reshape(e, nq).T.copy(), dst[:nq * e].reshape(e, nq).T.copy()
 
 
+@pytest.mark.parametrize("mode", [0, 2])
 @pytest.mark.parametrize("method,code", [("cosine", 1), ("euclidean", 2)])
-def test_bf16_screen_with_exact_rerank_equals_oracle(method, code):
+def test_bf16_screen_with_exact_rerank_equals_oracle(method, code, mode):
     import ctypes as C
     import torch
     from sparsedist_gb300 import _lib, synth
@@ -31,7 +33,7 @@ def test_bf16_screen_with_exact_rerank_equals_oracle(method, code):
     ctx = _lib.Context()
     h = C.c_void_p()
     _lib.check(ctx.lib.sdg_dense_upload(ctx.handle, X.data_ptr(), 64, 3000, C.byref(h)))
-    got = dense_knn(ctx, h, 0, 3000, code, 15, 0)
+    got = dense_knn(ctx, h, 0, 3000, code, 15, mode)
     plain = dense_knn(ctx, h, 0, 3000, code, 15, 1)
     ctx.lib.sdg_dense_free(h)
     A = X.double().cpu().numpy().T                                       # d x n
@@ -42,25 +44,28 @@ def test_bf16_screen_with_exact_rerank_equals_oracle(method, code):
     torch.cuda.synchronize()
 
 
+@pytest.mark.parametrize("k", [10, 20, 30])
+@pytest.mark.parametrize("mode", [0, 2])
 @pytest.mark.parametrize("method,code", [("cosine", 1), ("euclidean", 2)])
-def test_bf16_screen_many_segments_and_zero_columns(method, code):
+def test_bf16_screen_many_segments_and_zero_columns(method, code, mode, k):
     """70,001 references (three 32,768-reference segments, the last one ragged
     and not a multiple of 128) and a query block that starts mid-matrix; two
     all-zero columns (one query, one reference) are degenerate: the query's row
     is all NA and the reference is never returned.  The oracle's two-matrix
     search with k + 1 neighbours, minus each query's own column, is the
-    self-search result."""
+    self-search result.  k = 10, 20, 30 use the fused kernel's 16-, 24- and
+    32-long lists."""
     import ctypes as C
     import torch
     from sparsedist_gb300 import _lib, synth
-    d, n, q0, nq, k = 32, 70001, 1000, 64, 10
+    d, n, q0, nq = 32, 70001, 1000, 64
     X = synth.dense_embeddings(d=d, n=n, centres=50, seed=7)
     X[q0 + 5] = 0.0
     X[40000] = 0.0
     ctx = _lib.Context()
     h = C.c_void_p()
     _lib.check(ctx.lib.sdg_dense_upload(ctx.handle, X.data_ptr(), d, n, C.byref(h)))
-    got = dense_knn(ctx, h, q0, nq, code, k, 0)
+    got = dense_knn(ctx, h, q0, nq, code, k, mode)
     ctx.lib.sdg_dense_free(h)
     A = sp.csc_matrix(X.double().cpu().numpy().T)
     wi, wd, _ = OracleBackend().knn(A[:, q0:q0 + nq], A, k=k + 1, method=method)
