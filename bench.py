@@ -368,8 +368,9 @@ def run_c3(args):
             res["%s/%s" % (method, name)] = {"columns_per_s": B / (ms / 1000.0), "ms_per_block": ms,
                                              "candidates_per_query": st["pairs_exact"] / B,
                                              "overflow_queries": st["overflow_queries"],
-                                             "gemm_ms": gemm_ms / max(launches, 1),
-                                             "gemm_tflops": flops / (gemm_ms / max(launches, 1) / 1000.0) / 1e12}
+                                             "screen_kernel_ms_per_block": gemm_ms / args.steps,
+                                             "screen_launches_per_block": launches / args.steps,
+                                             "screen_tflops": flops / (gemm_ms / args.steps / 1000.0) / 1e12}
         res["%s/speedup_bf16_vs_fp32" % method] = (res["%s/bf16_tcgen05_fused_fp64_rerank" % method]["columns_per_s"] /
                                                    res["%s/plain_fp32" % method]["columns_per_s"])
     # correctness on a sample of query columns: the exact FP64 engine on the same data

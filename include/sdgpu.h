@@ -192,7 +192,9 @@ SDG_API int sdg_knn_resident(sdg_ctx* ctx, const sdg_matrix* X, const sdg_matrix
  * self-search sparseKNN(X, k, method) (include_self = FALSE,
  * drop_degenerate = TRUE) for cosine (dist) or euclidean.  mode 0: BF16
  * tensor-core screen with a rigorous bound and exact FP64 re-rank (the
- * reference's idx and distances); mode 1: the plain FP32 path (FP32 GEMM,
+ * reference's idx and distances), fused in one tcgen05 kernel (no slab in
+ * HBM) for k <= 32 and d <= 256, else as mode 2; mode 2: the same screen
+ * through a cuBLAS BF16 GEMM slab; mode 1: the plain FP32 path (FP32 GEMM,
  * top-k on FP32 values, no re-rank).  No counterpart in the reference, whose
  * dense inputs are coerced to dgCMatrix (R/sparseKNN.R:194-200); the FP64
  * values are those sparseKNN computes on the same data. */
