@@ -1,0 +1,91 @@
+"""Batched uneven problems (configuration 4's shape, at test size): many
+independent sparseKNNCross problems whose sizes are drawn log-uniformly,
+with the methods cycling binary / cosine / manhattan / js (js on
+column-normalised data) and k cycling 10 / 20 / 50, as in the configuration
+(512 problems, nq log-U[100, 50,000], nr log-U[1,000, 200,000], rows
+U[5,000, 30,000], density log-U[0.1 %, 10 %]).  Here nq, nr and the rows
+are scaled down so that the oracle finishes in seconds.
+
+Each problem's forward and reverse results must equal the oracle's
+(bit for bit for the pinned methods; js within 1e-12 relative with a
+tie-aware idx check), both run one after another and with every problem in
+flight at once on four host threads, each with its own context and stream
+(the library's work from different problems interleaving on the device)."""
+import concurrent.futures as cf
+import math
+
+import numpy as np
+import pytest
+
+from backends import GpuBackend, OracleBackend, make_x, normalise_cols
+from parity_cases import _knn_equal
+
+pytestmark = pytest.mark.gpu
+
+METHODS = ["binary", "cosine", "manhattan", "js"]
+KS = [10, 20, 50]
+
+
+def log_uniform(rng, lo, hi):
+    return int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+
+
+def problems(n=24, seed=404):
+    rng = np.random.default_rng(seed)
+    out = []
+    for t in range(n):
+        nq = log_uniform(rng, 20, 600)
+        nr = log_uniform(rng, 100, 3000)
+        rows = int(rng.integers(500, 3001))
+        dens = math.exp(rng.uniform(math.log(0.001), math.log(0.10)))
+        method, k = METHODS[t % 4], KS[t % 3]
+        X = make_x(rows, nq, dens, 10000 + 2 * t)
+        Y = make_x(rows, nr, dens, 10001 + 2 * t)
+        if method == "js":
+            X, Y = normalise_cols(X), normalise_cols(Y)
+            if X.shape[1] == 0 or Y.shape[1] == 0:
+                continue
+        out.append(dict(X=X, Y=Y, method=method, k=k, tag="%d:%s nq=%d nr=%d rows=%d dens=%.4f k=%d"
+                        % (t, method, X.shape[1], Y.shape[1], rows, dens, k)))
+    return out
+
+
+PROBLEMS = problems()
+
+
+@pytest.fixture(scope="module")
+def wanted():
+    orc = OracleBackend()
+    return [orc.knn_cross(p["X"], p["Y"], k=p["k"], method=p["method"]) for p in PROBLEMS]
+
+
+def check(p, got, want):
+    (fi, fd), (ri, rd), fl = got
+    (wfi, wfd), (wri, wrd), wfl = want
+    assert fl == wfl, p["tag"]
+    assert _knn_equal(p["method"], True, (fi, fd), (wfi, wfd)), p["tag"] + " forward"
+    assert _knn_equal(p["method"], True, (ri, rd), (wri, wrd)), p["tag"] + " reverse"
+
+
+@pytest.mark.parametrize("engine", [0, 2], ids=["auto", "screen"])
+def test_batched_uneven_cross_problems_one_by_one(gpu, wanted, engine):
+    gpu.set_engine(engine)
+    try:
+        for p, want in zip(PROBLEMS, wanted):
+            got = gpu.knn_cross(p["X"], p["Y"], k=p["k"], method=p["method"])
+            check(p, got, want)
+    finally:
+        gpu.set_engine(0)
+
+
+def test_batched_uneven_cross_problems_all_in_flight(wanted):
+    backends = [GpuBackend() for _ in range(4)]
+
+    def run(t):
+        p = PROBLEMS[t]
+        return backends[t % 4].knn_cross(p["X"], p["Y"], k=p["k"], method=p["method"])
+
+    with cf.ThreadPoolExecutor(4) as ex:
+        got = list(ex.map(run, range(len(PROBLEMS))))
+    for p, g, want in zip(PROBLEMS, got, wanted):
+        check(p, g, want)
