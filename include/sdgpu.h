@@ -262,7 +262,8 @@ SDG_API int sdg_ctx_set_stream(sdg_ctx* ctx, void* stream);
  * out[0] = pairs screened, out[1] = pairs re-ranked exactly, out[2] = queries
  * whose candidate buffer overflowed (finished by the exact path), out[3] =
  * kernels launched, out[4] = screening kernel time in microseconds (device
- * events), out[5] = total device time in microseconds. */
+ * events), out[5] = total device time in microseconds, out[6] = dense flops
+ * of the tensor-core screen's GEMMs. */
 SDG_API int sdg_last_stats(sdg_ctx* ctx, int64_t* out, int n);
 
 /* Device time of the kernel that bounds the kNN path (the pair-value slab of
@@ -274,8 +275,11 @@ SDG_API int sdg_kernel_time(sdg_ctx* ctx, double* ms, int64_t* launches);
 
 /* Selects the candidate-generation engine for subsequent calls on ctx:
  * 0 = automatic, 1 = exact FP64 slab for every pair, 2 = screened (FP32 /
- * integer screen, exact FP64 re-rank).  Results are identical; only speed
- * differs.  Used by tests to cross-check the two engines. */
+ * integer sparse screen, exact FP64 re-rank), 3 = tensor-core screen
+ * (cosine / euclidean: BF16 GEMM over dense copies of the screen values with
+ * a rigorous bound, exact FP64 re-rank; other methods, or values outside
+ * FP32's normal range, use 2).  Results are identical; only speed differs.
+ * Used by tests to cross-check the engines. */
 SDG_API int sdg_ctx_set_engine(sdg_ctx* ctx, int engine);
 
 #endif

@@ -166,7 +166,7 @@ class Context:
         check(self.lib.sdg_last_stats(self.handle, out.ctypes.data, 8))
         return {"pairs_screened": int(out[0]), "pairs_exact": int(out[1]),
                 "overflow_queries": int(out[2]), "kernels": int(out[3]),
-                "screen_us": int(out[4]), "device_us": int(out[5])}
+                "screen_us": int(out[4]), "device_us": int(out[5]), "tensor_flops": int(out[6])}
 
 
 _tls = threading.local()

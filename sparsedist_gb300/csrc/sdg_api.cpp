@@ -6,6 +6,7 @@
 // Reference behaviour restated here: R/sparseKNN.R:110-313 (sparseKNN),
 // R/sparseKNNCross.R:44-199 (sparseKNNCross), R/sparseSNN.R:120-250
 // (sparseSNN, edges = "knn") and the kernels' own checks in src/*.cpp.
+#include <cublas_v2.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -146,6 +147,7 @@ struct sdg_ctx {
   size_t tev_used = 0;
   double tev_folded_ms = 0.0;
   int64_t tev_launches = 0;
+  cublasHandle_t blas = nullptr;       // created on the first tensor-core screen
 };
 
 namespace {
@@ -203,9 +205,14 @@ struct sdg_matrix {
   bool have_moments = false;
   int js_status = 1;
   ScreenCache screen[4];        // screening data per method (sdg_screen.h), binary..manhattan
+  TensorCache tensor;           // dense BF16 screen values (tensor-core screen)
 
   ~sdg_matrix() {
-    if (ctx) cudaStreamSynchronize(ctx->stream);
+    if (ctx) {
+      for (auto& sc : screen) screen_cache_free(&sc, ctx->stream);
+      tensor_cache_free(&tensor, ctx->stream);
+      cudaStreamSynchronize(ctx->stream);
+    }
     for (DevBuf* b : {&p, &i, &x, &empty, &uval, &scale, &s1, &s2}) b->detach();
   }
 
@@ -391,12 +398,31 @@ void exact_engine(sdg_ctx* c, const KnnPlan& P, sdg_matrix* ref, sdg_matrix* qry
   CK(cudaGetLastError());
 }
 
-int pick_engine(sdg_ctx* c, const KnnPlan& P, int32_t nrow, int64_t nr, int64_t nq) {
+// 1: exact FP64 slab; 2: FP32 sparse screen; 3: BF16 tensor-core screen
+// (cosine / euclidean; falls back to 2 inside screen_knn when a matrix's
+// values do not admit the BF16 bound or its dense copy does not fit).
+int pick_engine(sdg_ctx* c, const KnnPlan& P, const sdg_matrix* ref, const sdg_matrix* X, int64_t nq) {
+  const int32_t nrow = ref->nrow;
+  const int64_t nr = ref->ncol;
   if (c->engine == 1) return 1;
   if (!screen_supported(P.method, P.k) || !screen_fits(nrow)) return 1;
   if (c->engine == 2) return 2;
+  if (c->engine == 3) return tensor_supported(P.method) ? 3 : 2;
   // Small problems: the exact slab is already latency-bound.
-  return (nr * nq <= (int64_t)1 << 22) ? 1 : 2;
+  if (nr * nq <= (int64_t)1 << 22) return 1;
+  // The tensor screen does 2 nrow nr nq dense flops where the FP32 screen
+  // visits nq / 16 * nnz(ref) stored entries: it wins from ~0.5 % density
+  // on, if the dense copies fit in half of the free device memory.
+  if (tensor_supported(P.method) && nrow > 0 && nr > 0) {
+    const double density = (double)ref->nnz / ((double)nrow * (double)nr);
+    size_t bytes = tensor_cache_bytes(nrow, nr);
+    if (X != ref) bytes += tensor_cache_bytes(nrow, X->ncol);
+    size_t fr = 0, tot = 0;
+    if (ref->tensor.method == P.method && ref->tensor.usable) bytes = 0;   // already resident
+    if (density >= 0.005 && cudaMemGetInfo(&fr, &tot) == cudaSuccess && bytes <= fr / 2) return 3;
+    cudaGetLastError();
+  }
+  return 2;
 }
 
 // sparseKNN core (R/sparseKNN.R:183-301) after argument checks.
@@ -449,8 +475,8 @@ void knn_device(sdg_ctx* c, sdg_matrix* X, sdg_matrix* Y, int method, int dist, 
     d_idx = hold_idx->as<int32_t>();
     d_val = hold_val->as<double>();
   }
-  const int eng = pick_engine(c, P, ref->nrow, ref->ncol, nq);
-  if (eng == 2) {
+  const int eng = pick_engine(c, P, ref, X, nq);
+  if (eng == 2 || eng == 3) {
     ScreenRun r;
     r.method = method; r.dist = dist; r.k = k; r.decreasing = P.decreasing;
     r.selfmode = selfmode; r.include_self = P.include_self;
@@ -458,13 +484,21 @@ void knn_device(sdg_ctx* c, sdg_matrix* X, sdg_matrix* Y, int method, int dist, 
     r.ref_mask = P.ref_mask; r.qry_blank = P.qry_blank;
     r.qry_empty = X->empty.as<uint8_t>();
     r.q_lo = q_lo; r.q_hi = q_hi; r.out_first = q_lo; r.out_ld = nq;
+    if (eng == 3) {
+      if (!c->blas && cublasCreate(&c->blas) != CUBLAS_STATUS_SUCCESS) {
+        c->blas = nullptr;
+        fail(SDG_E_CUDA, "cublasCreate failed");
+      }
+      r.tensor = true;
+      r.blas = c->blas;
+    }
     ScreenHooks h;
     h.check_cancel = [c]() { check_cancel(c); };
     h.time_begin = [c]() { sdg_time_begin(c); };
     h.time_end = [c]() { sdg_time_end(c); };
     h.exact_range = [&](int64_t q0, int64_t n) { exact_engine(c, P, ref, X, d_idx, d_val, q0, q0 + n); };
-    const int st = screen_knn(c->stream, r, ref->dev(), aux_of(ref), &ref->screen[method], X->dev(),
-                              aux_of(X), &X->screen[method], d_idx, d_val, c->stats, h);
+    const int st = screen_knn(c->stream, r, ref->dev(), aux_of(ref), &ref->screen[method], &ref->tensor,
+                              X->dev(), aux_of(X), &X->screen[method], &X->tensor, d_idx, d_val, c->stats, h);
     if (st) cuda_check((cudaError_t)st, "screen_knn");
   } else {
     exact_engine(c, P, ref, X, d_idx, d_val, q_lo, q_hi);
@@ -553,6 +587,7 @@ SDG_API int sdg_ctx_destroy(sdg_ctx* c) {
   for (auto& e : c->ev) if (e) cudaEventDestroy(e);
   for (auto& pr : c->tev) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
   cudaStreamDestroy(c->own_stream);
+  if (c->blas) cublasDestroy(c->blas);
   delete c;
   return SDG_OK;
 }
@@ -579,7 +614,7 @@ SDG_API int sdg_ctx_set_stream(sdg_ctx* c, void* stream) {
 }
 
 SDG_API int sdg_ctx_set_engine(sdg_ctx* c, int engine) {
-  if (!c || engine < 0 || engine > 2) { g_err = "invalid engine"; return SDG_E_ARG; }
+  if (!c || engine < 0 || engine > 3) { g_err = "invalid engine"; return SDG_E_ARG; }
   c->engine = engine;
   return SDG_OK;
 }

@@ -25,8 +25,11 @@
 // handed out part-major by an atomic counter, so the 152 SMs stream the same
 // reference part at the same time and it is read from HBM about once.
 #include <cub/device/device_radix_sort.cuh>
+#include <cublas_v2.h>
+#include <cuda_bf16.h>
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <vector>
 
@@ -411,7 +414,253 @@ __global__ void k_exact_candidates_prep(const int32_t* count, int64_t nq, int ca
   else { qidx[s] = -1; ridx[s] = -1; }
 }
 
+// ---------------------------------------------------------------------------
+// the tensor-core screen
+//
+// For cosine and euclidean the screen value of a pair is an inner product
+// over the rows, so a dense BF16 copy of the screen values of both matrices
+// (TensorCache) turns a block of screens into one GEMM on the tensor cores
+// (cuBLAS, BF16 in, FP32 accumulate and out), written as the slab
+// S[ql * ldS + c] in natural column order.  The bound: each BF16 factor has
+// relative error <= 2^-9 (+ 2^-24 from the FP32 value it rounds), so a
+// product errs by <= 0.0040 |x y|; the FP32 accumulation of at most
+// n = min(nnz_q, nnz_c) nonzero products (zero products add no error) is
+// allowed (n + 64) 2^-21 of sum |x y|; sum |x y| <= 1 for unit columns and
+// <= sqrt(Nq Nc) in general (Cauchy-Schwarz).  Values below FP32's smallest
+// normal are excluded at build time (TensorCache::usable), and a pair whose
+// key or bound is not finite is kept unconditionally.  The selection is split
+// across TSEG-reference segments (segment top-k of the pessimistic keys,
+// per-query merge to the exact k-th, segmented keep), one warp per
+// (query, segment), so that the slab streams at full bandwidth.
+// ---------------------------------------------------------------------------
+constexpr int TSEG = 32768;
+constexpr float BF16_REL = 0.0040f;
+constexpr float ACC_ULP = 4.76837158203125e-7f;   // 2^-21
+
+__global__ void k_tensor_fill(DevCsc M, const float* fval, __nv_bfloat16* dense, int64_t ld, int* bad) {
+  const int64_t j = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (j >= M.ncol) return;
+  __nv_bfloat16* col = dense + j * ld;
+  for (int64_t a = M.p[j] + lane; a < M.p[j + 1]; a += 32) {
+    const float f = fval[a];
+    const float af = fabsf(f);
+    if (f != 0.f && !(af >= FLT_MIN && af <= 3.0e38f)) atomicOr(bad, 1);
+    col[M.i[a]] = __float2bfloat16_rn(f);
+  }
+}
+
+struct TensorSelArgs {
+  int method, k;
+  const float* S;
+  int64_t ldS, nr;
+  const int32_t* rnnz; const float* rnorm;
+  const int32_t* qnnz; const float* qnorm;
+  const uint8_t* ref_mask;
+  const uint8_t* qry_blank;
+  const uint8_t* qry_force_exact;
+  int64_t q_begin, nq;
+  int selfmode, include_self;
+  int nseg;
+  float* segtop;             // [ql][seg][k]
+  float* cut;                // [ql]
+  int cap;
+  int32_t* cand;
+  int32_t* count;
+  int32_t* overflow;
+};
+
+// pessimistic / optimistic keys of pair (query q, reference c); -inf / -inf
+// when c is not eligible; +inf / +inf for the restored self pair.
+__device__ __forceinline__ void tensor_keys(const TensorSelArgs& A, int64_t q, int32_t nq_, float Nq, int64_t c,
+                                            float s, float& lo, float& hi) {
+  lo = hi = -INFINITY;
+  if (c >= A.nr || (A.ref_mask && A.ref_mask[c])) return;
+  if (A.selfmode && c == q) {
+    if (A.include_self) lo = hi = INFINITY;
+    return;
+  }
+  const int32_t nc_ = A.rnnz[c];
+  const float rel = BF16_REL + ((float)min(nq_, nc_) + 64.f) * ACC_ULP;
+  float key, err;
+  if (A.method == COSINE) {
+    key = s;
+    err = rel + 1e-12f;
+  } else {
+    const float Nc = A.rnorm[c], T = Nq + Nc;
+    key = 2.f * s - T;
+    err = 2.f * rel * 1.01f * sqrtf(Nq * Nc) + 9.5367431640625e-7f * T + 1e-30f;
+  }
+  if (!(fabsf(key) <= FLT_MAX) || !(err <= FLT_MAX)) { lo = -INFINITY; hi = INFINITY; return; }
+  lo = key - err;
+  hi = key + err;
+}
+
+__device__ __forceinline__ void warp_insert_desc(float* lst, int K, int& n, unsigned m, float v, int lane) {
+  while (m) {
+    const int src = __ffs(m) - 1;
+    m &= m - 1;
+    const float x = __shfl_sync(0xffffffffu, v, src);
+    if (n == K && !(x > lst[K - 1])) continue;
+    int a = 0, b = n;
+    while (a < b) { const int mid = (a + b) >> 1; if (lst[mid] >= x) a = mid + 1; else b = mid; }
+    const int last = (n < K) ? n : K - 1;
+    if (last > a) {
+      for (int cch = (last - 1) >> 5; cch >= (a >> 5); --cch) {
+        const int e = cch * 32 + lane;
+        const bool mv = (e >= a && e < last);
+        float t = 0.f;
+        if (mv) t = lst[e];
+        __syncwarp();
+        if (mv) lst[e + 1] = t;
+        __syncwarp();
+      }
+    }
+    if (lane == 0) lst[a] = x;
+    __syncwarp();
+    if (n < K) ++n;
+  }
+}
+
+__device__ __forceinline__ bool tensor_skip(const TensorSelArgs& A, int64_t q) {
+  return (A.qry_blank && A.qry_blank[q]) || (A.qry_force_exact && A.qry_force_exact[q]);
+}
+
+__global__ void k_tsel_segtop(TensorSelArgs A) {
+  extern __shared__ float lists[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t ql = (int64_t)blockIdx.x * SELECT_WARPS + warp;
+  const int seg = blockIdx.y;
+  if (ql >= A.nq) return;
+  const int64_t q = A.q_begin + ql;
+  const int K = A.k;
+  float* lst = lists + warp * K;
+  int n = 0;
+  if (!tensor_skip(A, q)) {
+    const int32_t nq_ = A.qnnz[q];
+    const float Nq = A.qnorm ? A.qnorm[q] : 0.f;
+    const float* Srow = A.S + ql * A.ldS;
+    const int64_t c_end = min(A.nr, (int64_t)(seg + 1) * TSEG);
+    for (int64_t p0 = (int64_t)seg * TSEG; p0 < c_end; p0 += 32) {
+      const int64_t c = p0 + lane;
+      float lo = -INFINITY, hi;
+      if (c < c_end) tensor_keys(A, q, nq_, Nq, c, Srow[c], lo, hi);
+      const unsigned m = __ballot_sync(0xffffffffu, lo > -INFINITY && (n < K || lo > lst[K - 1]));
+      if (m) warp_insert_desc(lst, K, n, m, lo, lane);
+    }
+  }
+  float* out = A.segtop + (ql * A.nseg + seg) * (int64_t)K;
+  for (int t = lane; t < K; t += 32) out[t] = t < n ? lst[t] : -INFINITY;
+}
+
+__global__ void k_tsel_thresh(TensorSelArgs A) {
+  extern __shared__ float lists[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t ql = (int64_t)blockIdx.x * SELECT_WARPS + warp;
+  if (ql >= A.nq) return;
+  const int64_t q = A.q_begin + ql;
+  const int K = A.k;
+  float* lst = lists + warp * K;
+  const float* in = A.segtop + ql * A.nseg * (int64_t)K;
+  const int64_t tot = (int64_t)A.nseg * K;
+  int n = 0;
+  for (int64_t p0 = 0; p0 < tot; p0 += 32) {
+    const float v = p0 + lane < tot ? in[p0 + lane] : -INFINITY;
+    const unsigned m = __ballot_sync(0xffffffffu, v > -INFINITY && (n < K || v > lst[K - 1]));
+    if (m) warp_insert_desc(lst, K, n, m, v, lane);
+  }
+  if (lane == 0) {
+    const float T = (n == K) ? lst[K - 1] : -INFINITY;
+    const float margin = (T == -INFINITY || T == INFINITY) ? 0.f : fabsf(T) * (8.f * U32) + 1e-30f;
+    A.cut[ql] = T - margin;
+    A.count[ql] = 0;
+    A.overflow[ql] = (A.qry_force_exact && A.qry_force_exact[q] && !(A.qry_blank && A.qry_blank[q])) ? 1 : 0;
+  }
+}
+
+__global__ void k_tsel_keep(TensorSelArgs A) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t ql = (int64_t)blockIdx.x * SELECT_WARPS + warp;
+  const int seg = blockIdx.y;
+  if (ql >= A.nq) return;
+  const int64_t q = A.q_begin + ql;
+  if (tensor_skip(A, q)) return;
+  const int32_t nq_ = A.qnnz[q];
+  const float Nq = A.qnorm ? A.qnorm[q] : 0.f;
+  const float cut = A.cut[ql];
+  const float* Srow = A.S + ql * A.ldS;
+  int32_t* out = A.cand + ql * (int64_t)A.cap;
+  const int64_t c_end = min(A.nr, (int64_t)(seg + 1) * TSEG);
+  for (int64_t p0 = (int64_t)seg * TSEG; p0 < c_end; p0 += 32) {
+    const int64_t c = p0 + lane;
+    float lo, hi = -INFINITY;
+    if (c < c_end) tensor_keys(A, q, nq_, Nq, c, Srow[c], lo, hi);
+    const bool keep = hi > -INFINITY && hi >= cut;
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (!m) continue;
+    int base = 0;
+    if (lane == 0) base = atomicAdd(A.count + ql, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0) + __popc(m & ((1u << lane) - 1u));
+    if (keep && base < A.cap) out[base] = (int32_t)c;
+  }
+}
+
+__global__ void k_tsel_overflow(int64_t nq, int cap, int32_t* count, int32_t* overflow) {
+  const int64_t ql = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (ql >= nq) return;
+  if (count[ql] > cap) { overflow[ql] = 1; count[ql] = 0; }
+}
+
 }  // namespace
+
+bool tensor_supported(int method) { return method == COSINE || method == EUCLIDEAN; }
+
+static int64_t tensor_ld(int32_t nrow) { return ((int64_t)nrow + 63) / 64 * 64; }
+
+size_t tensor_cache_bytes(int32_t nrow, int64_t ncol) {
+  return (size_t)tensor_ld(nrow) * (size_t)ncol * 2;
+}
+
+void tensor_cache_free(TensorCache* c, cudaStream_t s) {
+  if (c && c->dense) cudaFreeAsync(c->dense, s);
+  if (c) *c = TensorCache();
+}
+
+// Builds (or reuses) the dense BF16 copy of M's screen values for `method`
+// from its ScreenCache; an allocation failure leaves it unusable (the FP32
+// screen then runs) rather than failing the call.
+static int ensure_tensor(TensorCache* t, int method, const DevCsc& M, const ScreenCache* sc, cudaStream_t s) {
+  if (t->method == method) return 0;
+  tensor_cache_free(t, s);
+  t->method = method;
+  t->ld = tensor_ld(M.nrow);
+  const size_t bytes = tensor_cache_bytes(M.nrow, M.ncol) + 256;
+  cudaError_t e = cudaMallocAsync(&t->dense, bytes, s);
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    t->dense = nullptr;
+    t->usable = 0;
+    return 0;
+  }
+  SK(e);
+  int* bad = nullptr;
+  SK(cudaMallocAsync(&bad, sizeof(int), s));
+  SK(cudaMemsetAsync(bad, 0, sizeof(int), s));
+  SK(cudaMemsetAsync(t->dense, 0, bytes, s));
+  if (M.ncol > 0)
+    k_tensor_fill<<<blocks_for(M.ncol * 32, 256), 256, 0, s>>>(M, sc->fval, static_cast<__nv_bfloat16*>(t->dense),
+                                                               t->ld, bad);
+  int hbad = 0;
+  SK(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+  SK(cudaStreamSynchronize(s));
+  SK(cudaFreeAsync(bad, s));
+  t->usable = hbad ? 0 : 1;
+  if (!t->usable) {
+    SK(cudaFreeAsync(t->dense, s));
+    t->dense = nullptr;
+  }
+  return 0;
+}
 
 void launch_check_rows(const DevCsc& M, int* err, cudaStream_t s) {
   if (M.ncol > 0) k_check_rows<<<blocks_for(M.ncol, 128), 128, 0, s>>>(M, err);
@@ -476,10 +725,16 @@ static int ensure_cache(ScreenCache* c, int method, const DevCsc& M, const ColAu
 }
 
 int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColAux& ra,
-               ScreenCache* rc, const DevCsc& qry, const ColAux& qa, ScreenCache* qc,
-               int32_t* d_idx, double* d_val, int64_t* stats, const ScreenHooks& hooks) {
+               ScreenCache* rc, TensorCache* rt, const DevCsc& qry, const ColAux& qa, ScreenCache* qc,
+               TensorCache* qt, int32_t* d_idx, double* d_val, int64_t* stats, const ScreenHooks& hooks) {
   SK((cudaError_t)ensure_cache(rc, r.method, ref, ra, s));
   SK((cudaError_t)ensure_cache(qc, r.method, qry, qa, s));
+  bool use_t = r.tensor && r.blas && rt && qt && tensor_supported(r.method);
+  if (use_t) {
+    SK((cudaError_t)ensure_tensor(rt, r.method, ref, rc, s));
+    if (qt != rt) SK((cudaError_t)ensure_tensor(qt, r.method, qry, qc, s));
+    use_t = rt->usable && qt->usable && rt->ld == qt->ld;
+  }
   const int64_t nr = ref.ncol, nq = qry.ncol;
   const int32_t nrow = ref.nrow;
   const size_t tbytes = table_bytes(nrow);
@@ -494,11 +749,20 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
   const int64_t q_lo = r.q_lo, q_hi = (r.q_hi < 0) ? nq : r.q_hi;
   const int64_t out_ld = (r.out_ld < 0) ? nq : r.out_ld;
 
-  // queries per screen pass: the FP32 slab S is chunk x nr floats
+  // queries per screen pass: the FP32 slab S is chunk x ldS floats
   const int64_t sbudget = (int64_t)4 << 30;
+  const int64_t ldS = use_t ? (nr + 31) / 32 * 32 : nr;
   const int64_t chunk = std::max<int64_t>(
-      QT, std::min<int64_t>(std::max<int64_t>(q_hi - q_lo, 1), sbudget / (4 * std::max<int64_t>(nr, 1))));
-  const int cap = std::max(256, std::min(8192, 16 * r.k + 64));
+      QT, std::min<int64_t>(std::max<int64_t>(q_hi - q_lo, 1), sbudget / (4 * std::max<int64_t>(ldS, 1))));
+  // the BF16 bound is wider than the FP32 one: room for more candidates
+  const int cap = use_t ? std::max(512, std::min(16384, 64 * r.k + 256))
+                        : std::max(256, std::min(8192, 16 * r.k + 64));
+  const int nseg = (int)((nr + TSEG - 1) / TSEG);
+  float *segtop = nullptr, *cutv = nullptr;
+  if (use_t) {
+    SK(cudaMallocAsync(&segtop, sizeof(float) * (size_t)(chunk * nseg * r.k + 4), s));
+    SK(cudaMallocAsync(&cutv, sizeof(float) * (size_t)(chunk + 4), s));
+  }
 
   float* S = nullptr;
   int32_t *cand = nullptr, *count = nullptr, *over = nullptr, *qidx = nullptr, *ridx = nullptr;
@@ -507,7 +771,7 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
   double* rvals = nullptr;
   uint8_t* force = nullptr;
   const int64_t cslots = chunk * (int64_t)cap;
-  SK(cudaMallocAsync(&S, sizeof(float) * (size_t)(chunk * nr + 4), s));
+  SK(cudaMallocAsync(&S, sizeof(float) * (size_t)(chunk * ldS + 4), s));
   SK(cudaMallocAsync(&cand, sizeof(int32_t) * (size_t)cslots, s));
   SK(cudaMallocAsync(&count, sizeof(int32_t) * (size_t)chunk, s));
   SK(cudaMallocAsync(&over, sizeof(int32_t) * (size_t)chunk, s));
@@ -539,6 +803,40 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
   for (int64_t q0 = q_lo; q0 < q_hi; q0 += chunk) {
     hooks.check_cancel();
     const int64_t nb = std::min(chunk, q_hi - q0);
+    if (use_t) {
+      // S (nr x nb, column-major, leading dimension ldS) = R^T Q on the tensor cores
+      cublasHandle_t h = static_cast<cublasHandle_t>(r.blas);
+      const float one = 1.f, zero = 0.f;
+      const int64_t ld = rt->ld;
+      if (cublasSetStream(h, s) != CUBLAS_STATUS_SUCCESS) return (int)cudaErrorUnknown;
+      hooks.time_begin();
+      const cublasStatus_t bs = cublasGemmEx(
+          h, CUBLAS_OP_T, CUBLAS_OP_N, (int)nr, (int)nb, (int)ld, &one, rt->dense, CUDA_R_16BF, (int)ld,
+          static_cast<const __nv_bfloat16*>(qt->dense) + q0 * ld, CUDA_R_16BF, (int)ld, &zero, S, CUDA_R_32F,
+          (int)ldS, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
+      hooks.time_end();
+      if (bs != CUBLAS_STATUS_SUCCESS) return (int)cudaErrorUnknown;
+      TensorSelArgs T;
+      T.method = r.method; T.k = r.k; T.S = S; T.ldS = ldS; T.nr = nr;
+      T.rnnz = rc->nnz; T.rnorm = (r.method == EUCLIDEAN) ? rc->cnorm : nullptr;
+      T.qnnz = qc->nnz; T.qnorm = (r.method == EUCLIDEAN) ? qc->cnorm : nullptr;
+      T.ref_mask = r.ref_mask; T.qry_blank = r.qry_blank; T.qry_force_exact = force;
+      T.q_begin = q0; T.nq = nb; T.selfmode = r.selfmode; T.include_self = r.include_self;
+      T.nseg = nseg; T.segtop = segtop; T.cut = cutv;
+      T.cap = cap; T.cand = cand; T.count = count; T.overflow = over;
+      const size_t tsmem = sizeof(float) * (size_t)SELECT_WARPS * r.k;
+      if (tsmem > 48 * 1024) {
+        SK(cudaFuncSetAttribute(k_tsel_segtop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem));
+        SK(cudaFuncSetAttribute(k_tsel_thresh, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem));
+      }
+      const dim3 tgrid(blocks_for(nb, SELECT_WARPS), (unsigned)nseg);
+      k_tsel_segtop<<<tgrid, SELECT_WARPS * 32, tsmem, s>>>(T);
+      k_tsel_thresh<<<blocks_for(nb, SELECT_WARPS), SELECT_WARPS * 32, tsmem, s>>>(T);
+      k_tsel_keep<<<tgrid, SELECT_WARPS * 32, 0, s>>>(T);
+      k_tsel_overflow<<<blocks_for(nb, 256), 256, 0, s>>>(nb, cap, count, over);
+      SK(cudaGetLastError());
+      stats[6] += 2 * ld * nr * nb;
+    } else {
     // tiles: up to QT consecutive queries whose values fit the table
     std::vector<int32_t> tq, tn;
     int64_t j = 0;
@@ -595,6 +893,7 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
       SK(cudaFuncSetAttribute(k_screen_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssmem));
     k_screen_select<<<blocks_for(nb, SELECT_WARPS), SELECT_WARPS * 32, ssmem, s>>>(B);
     SK(cudaGetLastError());
+    }
 
     // exact FP64 values of the kept pairs, then the exact top-k
     if (rerank_warp_supported(r.method)) {
@@ -634,6 +933,8 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
   SK(cudaFreeAsync(over, s)); SK(cudaFreeAsync(qidx, s)); SK(cudaFreeAsync(ridx, s));
   SK(cudaFreeAsync(rvals, s)); SK(cudaFreeAsync(tile_q, s)); SK(cudaFreeAsync(tile_n, s));
   SK(cudaFreeAsync(work, s));
+  if (segtop) SK(cudaFreeAsync(segtop, s));
+  if (cutv) SK(cudaFreeAsync(cutv, s));
   // queries the screen could not bound: the exact slab engine, run by runs
   size_t a = 0;
   while (a < overflow_queries.size()) {

@@ -23,8 +23,25 @@ struct ScreenCache {
   int64_t nnz_total = 0;
 };
 
+// Dense BF16 copy of one matrix's screen values for the tensor-core screen
+// (cosine: the unit values; euclidean: the values), one column of ld rows
+// (nrow rounded up to 64, zero below nrow) per matrix column.  usable = 0
+// when a value is not finite or not normal in FP32 (the BF16 bound would not
+// hold): the FP32 screen is used instead.
+struct TensorCache {
+  int method = -1;
+  int usable = 0;
+  void* dense = nullptr;     // __nv_bfloat16[ncol * ld]
+  int64_t ld = 0;
+};
+
 struct ScreenRun {
   int method = 0, dist = 1, k = 1;
+  // the tensor-core screen (a BF16 GEMM through cuBLAS handle `blas`) instead
+  // of the FP32 sparse screen, when tensor_supported(method) and both
+  // matrices' TensorCache are usable
+  bool tensor = false;
+  void* blas = nullptr;
   bool decreasing = false, selfmode = false, include_self = false;
   double self_value = 0.0;                 // restored self value (include_self)
   const uint8_t* ref_mask = nullptr;       // excluded reference columns
@@ -44,14 +61,19 @@ struct ScreenHooks {
 
 bool screen_supported(int method, int k);
 bool screen_fits(int32_t nrow);
+bool tensor_supported(int method);
+// bytes of the TensorCache of an nrow x ncol matrix
+size_t tensor_cache_bytes(int32_t nrow, int64_t ncol);
 
 // Returns 0 or a cudaError_t value; exceptions thrown by the hooks propagate.
 // stats: see sdg_last_stats in include/sdgpu.h.
+// rt / qt: the TensorCaches of ref / qry (the same object for a self-search).
 int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColAux& ra,
-               ScreenCache* rc, const DevCsc& qry, const ColAux& qa, ScreenCache* qc,
-               int32_t* d_idx, double* d_val, int64_t* stats, const ScreenHooks& hooks);
+               ScreenCache* rc, TensorCache* rt, const DevCsc& qry, const ColAux& qa, ScreenCache* qc,
+               TensorCache* qt, int32_t* d_idx, double* d_val, int64_t* stats, const ScreenHooks& hooks);
 
 void screen_cache_free(ScreenCache* c, cudaStream_t s);
+void tensor_cache_free(TensorCache* c, cudaStream_t s);
 
 // Device check used at upload: rows in [0, nrow) and strictly ascending.
 void launch_check_rows(const DevCsc& M, int* err, cudaStream_t s);

@@ -10,8 +10,8 @@ from backends import METHODS, make_x, same_bits
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("method,engine", [("cosine", 1), ("cosine", 2), ("binary", 2),
-                                           ("euclidean", 2), ("manhattan", 1), ("js", 1)])
+@pytest.mark.parametrize("method,engine", [("cosine", 1), ("cosine", 2), ("cosine", 3), ("binary", 2),
+                                           ("euclidean", 2), ("euclidean", 3), ("manhattan", 1), ("js", 1)])
 def test_blocks_reassemble_the_full_search(gpu, method, engine):
     from sparsedist_gb300 import _lib
     X = make_x(400, 300, 0.08, 23)

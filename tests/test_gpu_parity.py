@@ -12,7 +12,7 @@ from parity_cases import KNOWN_ANSWERS, _knn_equal, check_golden_case
 pytestmark = pytest.mark.gpu
 
 CASES, ARR = load_golden()
-ENGINES = [1, 2]
+ENGINES = [1, 2, 3]
 
 
 @pytest.fixture(scope="module")
@@ -20,7 +20,7 @@ def orc():
     return OracleBackend()
 
 
-@pytest.fixture(scope="module", params=ENGINES, ids=["exact", "screen"])
+@pytest.fixture(scope="module", params=ENGINES, ids=["exact", "screen", "tensor"])
 def gpu_engine(request, gpu):
     gpu.set_engine(request.param)
     yield gpu
@@ -67,5 +67,8 @@ def test_gpu_engines_agree_bit_for_bit(gpu):
         a = gpu.knn(X, k=15, method=method)
         gpu.set_engine(2)
         b = gpu.knn(X, k=15, method=method)
+        gpu.set_engine(3)
+        c = gpu.knn(X, k=15, method=method)
         assert same_bits(a[0], b[0]) and same_bits(a[1], b[1]), method
+        assert same_bits(a[0], c[0]) and same_bits(a[1], c[1]), method
     gpu.set_engine(0)

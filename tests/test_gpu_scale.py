@@ -3,7 +3,8 @@
 Configuration-2-like data (30,000 rows, lognormal nnz per column, skewed row
 weights, log-count values) at reduced column counts: the screened engine must
 return exactly what the exact FP64 engine returns (idx and distances bit for
-bit), both must equal the oracle on a subset of query columns, and
+bit) with either screen (2: the FP32 sparse screen; 3: the BF16 tensor-core
+screen), both must equal the oracle on a subset of query columns, and
 size-independent properties hold (best-first ordering, no self, no masked)."""
 import numpy as np
 import pytest
@@ -21,13 +22,14 @@ def data():
     return sp.csc_matrix((x, i, p), shape=(30000, 6000))
 
 
+@pytest.mark.parametrize("engine", [2, 3])
 @pytest.mark.parametrize("method,dist", [("cosine", True), ("cosine", False), ("euclidean", True),
                                          ("manhattan", True), ("binary", True)])
-def test_screen_equals_exact_engine(gpu, data, method, dist):
+def test_screen_equals_exact_engine(gpu, data, method, dist, engine):
     Q = data[:, :512]
     gpu.set_engine(1)
     a = gpu.knn(Q, data, k=20, method=method, dist=dist)
-    gpu.set_engine(2)
+    gpu.set_engine(engine)
     b = gpu.knn(Q, data, k=20, method=method, dist=dist)
     st = gpu.ctx.stats()
     gpu.set_engine(0)
@@ -41,11 +43,12 @@ def test_screen_equals_exact_engine(gpu, data, method, dist):
         assert np.all(np.diff(d, axis=1) >= 0)
 
 
-def test_self_search_screen_vs_oracle(gpu, data):
+@pytest.mark.parametrize("engine", [2, 3])
+def test_self_search_screen_vs_oracle(gpu, data, engine):
     X = data[:, :1500]
     orc = OracleBackend()
     for method in ("cosine", "euclidean", "binary", "manhattan"):
-        gpu.set_engine(2)
+        gpu.set_engine(engine)
         got = gpu.knn(X, k=15, method=method)
         gpu.set_engine(0)
         want = orc.knn(X, k=15, method=method)
@@ -53,7 +56,8 @@ def test_self_search_screen_vs_oracle(gpu, data):
         assert not np.any(got[0] == np.arange(1, 1501)[:, None])
 
 
-def test_include_self_and_degenerate(gpu, data):
+@pytest.mark.parametrize("engine", [2, 3])
+def test_include_self_and_degenerate(gpu, data, engine):
     A = data[:, :800].tolil()
     for c in (3, 50, 51, 700):
         A[:, c] = 0
@@ -62,7 +66,7 @@ def test_include_self_and_degenerate(gpu, data):
     orc = OracleBackend()
     for method in ("cosine", "euclidean"):
         for inc in (True, False):
-            gpu.set_engine(2)
+            gpu.set_engine(engine)
             got = gpu.knn(X, k=10, method=method, include_self=inc)
             gpu.set_engine(0)
             want = orc.knn(X, k=10, method=method, include_self=inc)
