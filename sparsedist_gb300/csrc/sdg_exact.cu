@@ -294,6 +294,39 @@ __global__ void k_exact_pairs_sparse(int method, int dist, DevCsc ref, ColAux ra
                                     : pair_value(method, dist != 0, ref, ra, c, qry, qa, q);
 }
 
+// The value of a match-only pair from the ascending-row sum of matched
+// products (`sum`) and the matched-row count (`common`): Jaccard
+// (jacc_value, src/sparseDist.cpp:549-556), cosine (unit_cosine's NaN / clamp,
+// src/sparseDist.cpp:326-330) or pearson (arma::cor's formulation); A / i is
+// the reference column, B / j the query column.
+__device__ double match_finish(int method, bool dist, double sum, int64_t common, const DevCsc& A,
+                               const ColAux& aa, int32_t i, const DevCsc& B, const ColAux& ba, int32_t j) {
+  if (method == BINARY) {
+    const double ni = (double)(A.p[i + 1] - A.p[i]), nj = (double)(B.p[j + 1] - B.p[j]), c = (double)common;
+    const double denom = dsub(dadd(ni, nj), c);
+    const double sim = (denom > 0.0) ? (c / denom) : 1.0;
+    return dist ? dsub(1.0, sim) : sim;
+  }
+  if (method == COSINE) {
+    double c = sum;
+    if (!(c == c)) c = 0.0;
+    else if (c > 1.0) c = 1.0;
+    else if (c < -1.0) c = -1.0;
+    return dist ? dsub(1.0, c) : c;
+  }
+  // pearson
+  const double N = (double)A.nrow;
+  const double norm = (A.nrow > 1) ? dsub(N, 1.0) : 1.0;
+  const double cov = dsub(sum, dmul(aa.s[i], ba.s[j]) / N) / norm;
+  const double va = dsub(aa.ss[i], dmul(aa.s[i], aa.s[i]) / N) / norm;
+  const double vb = dsub(ba.ss[j], dmul(ba.s[j], ba.s[j]) / N) / norm;
+  double c = cov / dmul(sqrt(va), sqrt(vb));
+  if (!isfinite(c)) c = 0.0;
+  if (c > 1.0) c = 1.0;
+  if (c < -1.0) c = -1.0;
+  return dist ? dsub(1.0, c) : c;
+}
+
 // Match-only methods (binary, cosine, pearson): the value depends on the rows
 // both columns store, summed in ascending row order.  One warp per query row
 // of the candidate table: for each candidate, lanes take 32 consecutive
@@ -346,30 +379,7 @@ __device__ double warp_match_value(int method, bool dist, const DevCsc& A, const
     }
     l0 = __shfl_sync(0xffffffffu, lb, 31);
   }
-  if (method == BINARY) {
-    const double ni = (double)(ia1 - ia0), nj = (double)(jb1 - jb0), c = (double)common;
-    const double denom = dsub(dadd(ni, nj), c);
-    const double sim = (denom > 0.0) ? (c / denom) : 1.0;
-    return dist ? dsub(1.0, sim) : sim;
-  }
-  if (method == COSINE) {
-    double c = sum;
-    if (!(c == c)) c = 0.0;
-    else if (c > 1.0) c = 1.0;
-    else if (c < -1.0) c = -1.0;
-    return dist ? dsub(1.0, c) : c;
-  }
-  // pearson
-  const double N = (double)A.nrow;
-  const double norm = (A.nrow > 1) ? dsub(N, 1.0) : 1.0;
-  const double cov = dsub(sum, dmul(aa.s[i], ba.s[j]) / N) / norm;
-  const double va = dsub(aa.ss[i], dmul(aa.s[i], aa.s[i]) / N) / norm;
-  const double vb = dsub(ba.ss[j], dmul(ba.s[j], ba.s[j]) / N) / norm;
-  double c = cov / dmul(sqrt(va), sqrt(vb));
-  if (!isfinite(c)) c = 0.0;
-  if (c > 1.0) c = 1.0;
-  if (c < -1.0) c = -1.0;
-  return dist ? dsub(1.0, c) : c;
+  return match_finish(method, dist, sum, common, A, aa, i, B, ba, j);
 }
 
 __global__ void k_rerank_warp(int method, int dist, DevCsc ref, ColAux ra, DevCsc qry, ColAux qa,
@@ -386,6 +396,160 @@ __global__ void k_rerank_warp(int method, int dist, DevCsc ref, ColAux ra, DevCs
     if (restore_self && c == q) v = self_value;
     else v = warp_match_value(method, dist != 0, ref, ra, c, qry, qa, q, lane);
     if (lane == 0) out[ql * cap + t] = v;
+  }
+}
+
+// Query-centric re-rank of the match-only methods, one CTA per query row of
+// the candidate table.  The query column's rows go into a shared-memory
+// bitmap (bit r % 32 of word r / 32) with, for each word holding a row, the
+// index of its first entry, so a matched row r is entry
+// first[r / 32] + popc(word & below(r)) of the query; the query's values sit
+// in shared memory too (up to RQ_MAX_QV entries, else they are read from
+// global memory).
+//
+// One LANE per candidate: GB300's FP64 pipe spends the same time on an FP64
+// warp instruction whatever the number of active lanes, so the sequential sum
+// of a pair (one dadd per matched row, in ascending row order, as the
+// reference adds them) must not run one pair per warp.  A lane walks its
+// candidate column in row order (16-byte loads of 4 row indices once
+// aligned), testing each row against the bitmap and buffering the matches
+// (entry offsets) in shared memory; every RB matches the warp runs the
+// buffered dmul / dadd steps with all its lanes at once.  The candidates are
+// first sorted by column length (bitonic, in shared memory), so that the 32
+// lanes of a warp walk columns of similar length.  Each lane's sum is still
+// the reference's sequential sum bit for bit.
+constexpr int RQ_THREADS = 256;
+constexpr int32_t RQ_MAX_NROW = 1 << 18;
+constexpr int RQ_MAX_QV = 2048;
+constexpr int RB = 8;
+constexpr int RQ_MAX_CAND = 2048;     // candidates sorted in shared memory
+
+__global__ void k_rerank_q(int method, int dist, DevCsc ref, ColAux ra, DevCsc qry, ColAux qa,
+                           const int32_t* cand, const int32_t* count, int cap, int64_t q_begin,
+                           int restore_self, double self_value, double* out) {
+  extern __shared__ __align__(16) uint32_t rq_smem[];
+  const int W = (qry.nrow + 31) >> 5;
+  double* qvs = reinterpret_cast<double*>(rq_smem);                          // RQ_MAX_QV
+  uint64_t* order = reinterpret_cast<uint64_t*>(rq_smem + 2 * RQ_MAX_QV);    // RQ_MAX_CAND
+  int2* buf = reinterpret_cast<int2*>(order + RQ_MAX_CAND);                 // [RB][RQ_THREADS]
+  uint32_t* bits = reinterpret_cast<uint32_t*>(buf + RB * RQ_THREADS);
+  int32_t* first = reinterpret_cast<int32_t*>(bits + W);
+  const int64_t ql = blockIdx.x;
+  const int32_t q = (int32_t)(q_begin + ql);
+  const int n = min(count[ql], RQ_MAX_CAND);
+  if (n == 0) return;
+  for (int w = threadIdx.x; w < W; w += blockDim.x) bits[w] = 0u;
+  // sort keys: (column length, position in the list), longest first
+  int np2 = 1;
+  while (np2 < n) np2 <<= 1;
+  for (int t = threadIdx.x; t < np2; t += blockDim.x) {
+    uint64_t key = 0;                       // padding sorts last
+    if (t < n) {
+      const int32_t c = cand[ql * (int64_t)cap + t];
+      const int64_t len64 = ref.p[c + 1] - ref.p[c];
+      const uint32_t len = (uint32_t)(len64 < 0x7fffffff ? len64 : 0x7fffffff);
+      key = ((uint64_t)(len + 1u) << 32) | (uint32_t)t;
+    }
+    order[t] = key;
+  }
+  __syncthreads();
+  const int64_t q0 = qry.p[q], q1 = qry.p[q + 1];
+  const double* qsrc = ((method == COSINE) ? qa.uval : qry.x) + q0;
+  const bool qv_shared = (q1 - q0) <= RQ_MAX_QV;
+  for (int64_t e = q0 + threadIdx.x; e < q1; e += blockDim.x) {
+    const int32_t r = qry.i[e];
+    atomicOr(&bits[r >> 5], 1u << (r & 31));
+    if (e == q0 || (qry.i[e - 1] >> 5) != (r >> 5)) first[r >> 5] = (int32_t)(e - q0);
+    if (qv_shared && method != BINARY) qvs[e - q0] = qsrc[e - q0];
+  }
+  // bitonic sort of order[0 .. np2), descending
+  for (int k2 = 2; k2 <= np2; k2 <<= 1) {
+    for (int j = k2 >> 1; j > 0; j >>= 1) {
+      __syncthreads();
+      for (int t = threadIdx.x; t < np2; t += blockDim.x) {
+        const int u = t ^ j;
+        if (u > t) {
+          const uint64_t x = order[t], y = order[u];
+          const bool desc = (t & k2) == 0;
+          if (desc ? (x < y) : (x > y)) { order[t] = y; order[u] = x; }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  const double* qv = qv_shared ? qvs : qsrc;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const double* rv = (method == COSINE) ? ra.uval : ref.x;
+  const bool q_empty = (method == COSINE) && qa.scale[q] == 0.0;
+  int2* mybuf = buf + threadIdx.x;
+  for (int g = warp * 32; g < n; g += nw * 32) {
+    const int slot = g + lane;
+    const int t = (slot < n) ? (int)(uint32_t)order[slot] : -1;
+    int32_t c = -1;
+    double v = 0.0;
+    bool special = false;
+    int64_t a = 0, a_end = 0, c0 = 0;
+    if (t >= 0) {
+      c = cand[ql * (int64_t)cap + t];
+      if (restore_self && c == q) {
+        v = self_value;
+        special = true;
+      } else if (method == COSINE && (q_empty || ra.scale[c] == 0.0)) {
+        const double cv = (q_empty && ra.scale[c] == 0.0) ? 1.0 : 0.0;
+        v = dist ? dsub(1.0, cv) : cv;
+        special = true;
+      } else {
+        c0 = a = ref.p[c];
+        a_end = ref.p[c + 1];
+      }
+    }
+    bool active = (t >= 0) && !special && a < a_end;
+    double sum = 0.0;
+    int64_t common = 0;
+    int4 vb = make_int4(0, 0, 0, 0);        // row indices loaded ahead
+    int nv = 0, vi = 0;
+    while (__any_sync(0xffffffffu, active)) {
+      int fill = 0;
+      while (active && fill < RB) {
+        if (nv == 0) {
+          if ((a & 3) == 0 && a + 4 <= a_end) {
+            vb = __ldg(reinterpret_cast<const int4*>(ref.i + a));
+            nv = 4;
+          } else {
+            vb.x = __ldg(ref.i + a);
+            nv = 1;
+          }
+          vi = 0;
+        }
+        const int32_t r = (vi == 0) ? vb.x : (vi == 1) ? vb.y : (vi == 2) ? vb.z : vb.w;
+        ++vi;
+        --nv;
+        const uint32_t wd = bits[r >> 5];
+        const uint32_t bit = 1u << (r & 31);
+        if (wd & bit) {
+          if (method != BINARY)
+            mybuf[fill * RQ_THREADS] = make_int2((int)(a - c0), first[r >> 5] + __popc(wd & (bit - 1u)));
+          ++fill;
+        }
+        if (++a >= a_end) active = false;
+      }
+      __syncwarp();
+      common += fill;
+      if (method != BINARY) {
+        const int mx = __reduce_max_sync(0xffffffffu, fill);
+        for (int j = 0; j < mx; ++j) {
+          if (j < fill) {
+            const int2 be = mybuf[j * RQ_THREADS];
+            sum = dadd(sum, dmul(__ldg(rv + c0 + be.x), qv[be.y]));
+          }
+        }
+      }
+      __syncwarp();
+    }
+    if (t >= 0) {
+      if (!special) v = match_finish(method, dist != 0, sum, common, ref, ra, c, qry, qa, q);
+      out[ql * (int64_t)cap + t] = v;
+    }
   }
 }
 
@@ -441,10 +605,19 @@ void launch_rerank_warp(int method, int dist, const DevCsc& ref, const ColAux& r
                         const DevCsc& qry, const ColAux& qa, const int32_t* cand,
                         const int32_t* count, int cap, int64_t nq_local, int64_t q_begin,
                         int restore_self, double self_value, double* out, cudaStream_t s) {
-  if (nq_local > 0)
+  if (nq_local <= 0) return;
+  if (qry.nrow <= RQ_MAX_NROW && cap <= RQ_MAX_CAND) {
+    const size_t smem = (size_t)RQ_MAX_QV * 8 + (size_t)RQ_MAX_CAND * 8 + (size_t)RB * RQ_THREADS * 8 +
+                        (size_t)((qry.nrow + 31) / 32) * 8;
+    if (smem > 48 * 1024)
+      cudaFuncSetAttribute(k_rerank_q, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_rerank_q<<<(unsigned)nq_local, RQ_THREADS, smem, s>>>(method, dist, ref, ra, qry, qa, cand, count, cap,
+                                                           q_begin, restore_self, self_value, out);
+  } else {
     k_rerank_warp<<<blocks_for(nq_local, 8), 256, 0, s>>>(method, dist, ref, ra, qry, qa, cand,
                                                           count, cap, nq_local, q_begin,
                                                           restore_self, self_value, out);
+  }
 }
 
 void launch_exact_pairs_sparse(int method, int dist, const DevCsc& ref, const ColAux& ra,

@@ -9,7 +9,7 @@ are scaled down so that the oracle finishes in seconds.
 Each problem's forward and reverse results must equal the oracle's
 (bit for bit for the pinned methods; js within 1e-12 relative with a
 tie-aware idx check), both run one after another and with every problem in
-flight at once on four host threads, each with its own context and stream
+flight at once on four host threads, each owning one context and stream
 (the library's work from different problems interleaving on the device)."""
 import concurrent.futures as cf
 import math
@@ -79,13 +79,20 @@ def test_batched_uneven_cross_problems_one_by_one(gpu, wanted, engine):
 
 
 def test_batched_uneven_cross_problems_all_in_flight(wanted):
+    # a context belongs to one thread at a time: thread s owns context s and
+    # runs problems s, s + 4, s + 8, ...
     backends = [GpuBackend() for _ in range(4)]
 
-    def run(t):
-        p = PROBLEMS[t]
-        return backends[t % 4].knn_cross(p["X"], p["Y"], k=p["k"], method=p["method"])
+    def run_shard(sh):
+        out = []
+        for t in range(sh, len(PROBLEMS), 4):
+            p = PROBLEMS[t]
+            out.append((t, backends[sh].knn_cross(p["X"], p["Y"], k=p["k"], method=p["method"])))
+        return out
 
     with cf.ThreadPoolExecutor(4) as ex:
-        got = list(ex.map(run, range(len(PROBLEMS))))
-    for p, g, want in zip(PROBLEMS, got, wanted):
-        check(p, g, want)
+        shards = list(ex.map(run_shard, range(4)))
+    got = dict(item for shard in shards for item in shard)
+    assert sorted(got) == list(range(len(PROBLEMS)))
+    for t, (p, want) in enumerate(zip(PROBLEMS, wanted)):
+        check(p, got[t], want)
