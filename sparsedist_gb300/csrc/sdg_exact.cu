@@ -405,24 +405,25 @@ __global__ void k_rerank_warp(int method, int dist, DevCsc ref, ColAux ra, DevCs
 // index of its first entry, so a matched row r is entry
 // first[r / 32] + popc(word & below(r)) of the query; the query's values sit
 // in shared memory too (up to RQ_MAX_QV entries, else they are read from
-// global memory).
+// global memory).  The candidates are sorted by column length (bitonic, in
+// shared memory) and dealt to the warps in groups of 32.
 //
-// One LANE per candidate: GB300's FP64 pipe spends the same time on an FP64
-// warp instruction whatever the number of active lanes, so the sequential sum
-// of a pair (one dadd per matched row, in ascending row order, as the
-// reference adds them) must not run one pair per warp.  A lane walks its
-// candidate column in row order (16-byte loads of 4 row indices once
-// aligned), testing each row against the bitmap and buffering the matches
-// (entry offsets) in shared memory; every RB matches the warp runs the
-// buffered dmul / dadd steps with all its lanes at once.  The candidates are
-// first sorted by column length (bitonic, in shared memory), so that the 32
-// lanes of a warp walk columns of similar length.  Each lane's sum is still
-// the reference's sequential sum bit for bit.
+// GB300's FP64 pipe spends the same time on an FP64 warp instruction whatever
+// the number of active lanes, so the sequential sum of a pair (one dadd per
+// matched row, in ascending row order, as the reference adds them) runs one
+// pair per LANE.  A warp works on its 32 candidates in passes: (scan) for
+// each candidate in turn, the warp streams the column 32 entries a round
+// (coalesced, four rounds' loads in flight), tests the rows against the
+// bitmap and appends the matched (entry, query entry) pairs, in row order, to
+// that candidate's list of RM slots until it is full or the column ends;
+// (sum) lane j then runs candidate j's list: dmul, dadd, in order, all lanes
+// at once.  Each lane's sum is the reference's sequential sum bit for bit.
 constexpr int RQ_THREADS = 256;
+constexpr int RQ_WARPS = RQ_THREADS / 32;
 constexpr int32_t RQ_MAX_NROW = 1 << 18;
 constexpr int RQ_MAX_QV = 2048;
-constexpr int RB = 8;
 constexpr int RQ_MAX_CAND = 2048;     // candidates sorted in shared memory
+constexpr int RM = 32;                // list slots per candidate per pass
 
 __global__ void k_rerank_q(int method, int dist, DevCsc ref, ColAux ra, DevCsc qry, ColAux qa,
                            const int32_t* cand, const int32_t* count, int cap, int64_t q_begin,
@@ -431,8 +432,8 @@ __global__ void k_rerank_q(int method, int dist, DevCsc ref, ColAux ra, DevCsc q
   const int W = (qry.nrow + 31) >> 5;
   double* qvs = reinterpret_cast<double*>(rq_smem);                          // RQ_MAX_QV
   uint64_t* order = reinterpret_cast<uint64_t*>(rq_smem + 2 * RQ_MAX_QV);    // RQ_MAX_CAND
-  int2* buf = reinterpret_cast<int2*>(order + RQ_MAX_CAND);                 // [RB][RQ_THREADS]
-  uint32_t* bits = reinterpret_cast<uint32_t*>(buf + RB * RQ_THREADS);
+  int2* lists = reinterpret_cast<int2*>(order + RQ_MAX_CAND);               // [warp][32][RM]
+  uint32_t* bits = reinterpret_cast<uint32_t*>(lists + RQ_WARPS * 32 * RM);
   int32_t* first = reinterpret_cast<int32_t*>(bits + W);
   const int64_t ql = blockIdx.x;
   const int32_t q = (int32_t)(q_begin + ql);
@@ -462,8 +463,7 @@ __global__ void k_rerank_q(int method, int dist, DevCsc ref, ColAux ra, DevCsc q
     if (e == q0 || (qry.i[e - 1] >> 5) != (r >> 5)) first[r >> 5] = (int32_t)(e - q0);
     if (qv_shared && method != BINARY) qvs[e - q0] = qsrc[e - q0];
   }
-  // bitonic sort of order[0 .. np2), descending
-  for (int k2 = 2; k2 <= np2; k2 <<= 1) {
+  for (int k2 = 2; k2 <= np2; k2 <<= 1) {             // bitonic sort, descending
     for (int j = k2 >> 1; j > 0; j >>= 1) {
       __syncthreads();
       for (int t = threadIdx.x; t < np2; t += blockDim.x) {
@@ -478,11 +478,13 @@ __global__ void k_rerank_q(int method, int dist, DevCsc ref, ColAux ra, DevCsc q
   }
   __syncthreads();
   const double* qv = qv_shared ? qvs : qsrc;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
   const double* rv = (method == COSINE) ? ra.uval : ref.x;
   const bool q_empty = (method == COSINE) && qa.scale[q] == 0.0;
-  int2* mybuf = buf + threadIdx.x;
-  for (int g = warp * 32; g < n; g += nw * 32) {
+  int2* wl = lists + warp * 32 * RM;
+  for (int g = warp * 32; g < n; g += RQ_WARPS * 32) {
+    // lane j owns candidate g + j
     const int slot = g + lane;
     const int t = (slot < n) ? (int)(uint32_t)order[slot] : -1;
     int32_t c = -1;
@@ -506,40 +508,59 @@ __global__ void k_rerank_q(int method, int dist, DevCsc ref, ColAux ra, DevCsc q
     bool active = (t >= 0) && !special && a < a_end;
     double sum = 0.0;
     int64_t common = 0;
-    int4 vb = make_int4(0, 0, 0, 0);        // row indices loaded ahead
-    int nv = 0, vi = 0;
     while (__any_sync(0xffffffffu, active)) {
-      int fill = 0;
-      while (active && fill < RB) {
-        if (nv == 0) {
-          if ((a & 3) == 0 && a + 4 <= a_end) {
-            vb = __ldg(reinterpret_cast<const int4*>(ref.i + a));
-            nv = 4;
-          } else {
-            vb.x = __ldg(ref.i + a);
-            nv = 1;
+      int my_fill = 0;
+      // scan: each active candidate in turn, the whole warp on its column
+      for (int j = 0; j < 32; ++j) {
+        if (!__shfl_sync(0xffffffffu, active, j)) continue;
+        int64_t pos = __shfl_sync(0xffffffffu, a, j);
+        const int64_t end = __shfl_sync(0xffffffffu, a_end, j);
+        const int64_t base = __shfl_sync(0xffffffffu, c0, j);
+        int2* lj = wl + j * RM;
+        int fill = 0;
+        bool full = false;
+        while (pos < end && !full) {
+          int32_t r[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int64_t e = pos + 32 * u + lane;
+            r[u] = (e < end) ? __ldg(ref.i + e) : -1;
           }
-          vi = 0;
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            if (full || pos >= end) break;
+            bool hit = false;
+            int qe = 0;
+            if (r[u] >= 0) {
+              const uint32_t wd = bits[r[u] >> 5];
+              const uint32_t bit = 1u << (r[u] & 31);
+              if (wd & bit) { hit = true; qe = first[r[u] >> 5] + __popc(wd & (bit - 1u)); }
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, hit);
+            const int cnt = __popc(m);
+            if (method != BINARY) {
+              if (fill + cnt > RM) { full = true; break; }
+              if (hit) lj[fill + __popc(m & below)] = make_int2((int)(pos + lane - base), qe);
+            }
+            fill += cnt;
+            pos += 32;
+          }
         }
-        const int32_t r = (vi == 0) ? vb.x : (vi == 1) ? vb.y : (vi == 2) ? vb.z : vb.w;
-        ++vi;
-        --nv;
-        const uint32_t wd = bits[r >> 5];
-        const uint32_t bit = 1u << (r & 31);
-        if (wd & bit) {
-          if (method != BINARY)
-            mybuf[fill * RQ_THREADS] = make_int2((int)(a - c0), first[r >> 5] + __popc(wd & (bit - 1u)));
-          ++fill;
+        if (lane == j) {
+          a = pos < end ? pos : end;
+          active = pos < end;
+          my_fill = fill;
         }
-        if (++a >= a_end) active = false;
       }
       __syncwarp();
-      common += fill;
+      common += my_fill;
+      // sum: lane j runs candidate j's list in order
       if (method != BINARY) {
-        const int mx = __reduce_max_sync(0xffffffffu, fill);
-        for (int j = 0; j < mx; ++j) {
-          if (j < fill) {
-            const int2 be = mybuf[j * RQ_THREADS];
+        const int mx = __reduce_max_sync(0xffffffffu, my_fill);
+        const int2* ll = wl + lane * RM;
+        for (int s2 = 0; s2 < mx; ++s2) {
+          if (s2 < my_fill) {
+            const int2 be = ll[s2];
             sum = dadd(sum, dmul(__ldg(rv + c0 + be.x), qv[be.y]));
           }
         }
@@ -607,7 +628,7 @@ void launch_rerank_warp(int method, int dist, const DevCsc& ref, const ColAux& r
                         int restore_self, double self_value, double* out, cudaStream_t s) {
   if (nq_local <= 0) return;
   if (qry.nrow <= RQ_MAX_NROW && cap <= RQ_MAX_CAND) {
-    const size_t smem = (size_t)RQ_MAX_QV * 8 + (size_t)RQ_MAX_CAND * 8 + (size_t)RB * RQ_THREADS * 8 +
+    const size_t smem = (size_t)RQ_MAX_QV * 8 + (size_t)RQ_MAX_CAND * 8 + (size_t)RQ_WARPS * 32 * RM * 8 +
                         (size_t)((qry.nrow + 31) / 32) * 8;
     if (smem > 48 * 1024)
       cudaFuncSetAttribute(k_rerank_q, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
