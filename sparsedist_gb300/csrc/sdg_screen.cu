@@ -611,6 +611,141 @@ __global__ void k_tsel_overflow(int64_t nq, int cap, int32_t* count, int32_t* ov
   if (count[ql] > cap) { overflow[ql] = 1; count[ql] = 0; }
 }
 
+// ---------------------------------------------------------------------------
+// second screen of the tensor candidates: FP32 sparse dot products
+//
+// The BF16 bound keeps a few hundred candidates per query; the FP32 screen's
+// bound (key_and_bound) is ~100x tighter.  One CTA per query holds the query
+// column as a shared-memory bitmap (with each word's first entry, as in the
+// exact re-rank) and its FP32 screen values; a warp per candidate streams the
+// candidate column (coalesced, four rounds in flight), multiplies the matched
+// FP32 values and reduces across the warp.  The FP32 bound holds for any
+// summation order, so the reduction is a tree.  Then, per query, T2 = the
+// k-th largest pessimistic key and the list keeps the candidates whose
+// optimistic key reaches T2 - margin: the exact re-rank sees only those.
+// ---------------------------------------------------------------------------
+constexpr int RS_THREADS = 256;
+constexpr int RS_MAX_QV = 4096;
+constexpr int32_t RS_MAX_NROW = 1 << 18;
+
+struct RescreenArgs {
+  int method, k;
+  DevCsc ref, qry;
+  const float* rf;           // ScreenCache values (unit values / values)
+  const float* qf;
+  const int32_t* rnnz; const float* rnorm;
+  const int32_t* qnnz; const float* qnorm;
+  int64_t q_begin, nq;
+  int selfmode;
+  int cap;
+  int32_t* cand;
+  int32_t* count;
+  float* lo;                 // [ql * cap + t]
+  float* hi;
+};
+
+__global__ void k_rescreen(RescreenArgs A) {
+  extern __shared__ __align__(16) uint32_t rs_smem[];
+  const int W = (A.qry.nrow + 31) >> 5;
+  float* qvs = reinterpret_cast<float*>(rs_smem);             // RS_MAX_QV
+  uint32_t* bits = rs_smem + RS_MAX_QV;
+  int32_t* first = reinterpret_cast<int32_t*>(bits + W);
+  const int64_t ql = blockIdx.x;
+  const int64_t q = A.q_begin + ql;
+  const int n = A.count[ql];
+  if (n == 0) return;
+  for (int w = threadIdx.x; w < W; w += blockDim.x) bits[w] = 0u;
+  __syncthreads();
+  const int64_t q0 = A.qry.p[q], q1 = A.qry.p[q + 1];
+  const bool qv_shared = (q1 - q0) <= RS_MAX_QV;
+  for (int64_t e = q0 + threadIdx.x; e < q1; e += blockDim.x) {
+    const int32_t r = A.qry.i[e];
+    atomicOr(&bits[r >> 5], 1u << (r & 31));
+    if (e == q0 || (A.qry.i[e - 1] >> 5) != (r >> 5)) first[r >> 5] = (int32_t)(e - q0);
+    if (qv_shared) qvs[e - q0] = A.qf[e];
+  }
+  __syncthreads();
+  const float* qv = qv_shared ? qvs : A.qf + q0;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const int32_t nq_ = A.qnnz[q];
+  const float Nq = A.qnorm ? A.qnorm[q] : 0.f;
+  for (int t = warp; t < n; t += nw) {
+    const int32_t c = A.cand[ql * (int64_t)A.cap + t];
+    float lo, hi;
+    if (A.selfmode && c == q) {
+      lo = hi = INFINITY;                       // the restored self pair
+    } else {
+      float acc = 0.f;
+      const int64_t c0 = A.ref.p[c], c1 = A.ref.p[c + 1];
+      for (int64_t a0 = c0; a0 < c1; a0 += 128) {
+        int32_t r[4];
+        float f[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int64_t e = a0 + 32 * u + lane;
+          r[u] = (e < c1) ? __ldg(A.ref.i + e) : -1;
+          f[u] = (e < c1) ? __ldg(A.rf + e) : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          if (r[u] >= 0) {
+            const uint32_t wd = bits[r[u] >> 5];
+            const uint32_t bit = 1u << (r[u] & 31);
+            if (wd & bit) acc = fmaf(f[u], qv[first[r[u] >> 5] + __popc(wd & (bit - 1u))], acc);
+          }
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      float key, err;
+      key_and_bound(A.method, acc, nq_, Nq, A.rnnz[c], A.rnorm ? A.rnorm[c] : 0.f, key, err);
+      lo = key - err;
+      hi = key + err;
+      if (!(fabsf(key) <= FLT_MAX) || !(err <= FLT_MAX)) { lo = -INFINITY; hi = INFINITY; }
+    }
+    if (lane == 0) {
+      A.lo[ql * (int64_t)A.cap + t] = lo;
+      A.hi[ql * (int64_t)A.cap + t] = hi;
+    }
+  }
+}
+
+// per query: T2 = k-th largest pessimistic key; compact the list in place to
+// the candidates whose optimistic key reaches T2 - margin
+__global__ void k_rescreen_select(RescreenArgs A) {
+  extern __shared__ float lists[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t ql = (int64_t)blockIdx.x * SELECT_WARPS + warp;
+  if (ql >= A.nq) return;
+  const int n = A.count[ql];
+  if (n == 0) return;
+  const int K = A.k;
+  float* lst = lists + warp * K;
+  const float* lo = A.lo + ql * (int64_t)A.cap;
+  const float* hi = A.hi + ql * (int64_t)A.cap;
+  int m = 0;
+  for (int p0 = 0; p0 < n; p0 += 32) {
+    const float v = p0 + lane < n ? lo[p0 + lane] : -INFINITY;
+    const unsigned b = __ballot_sync(0xffffffffu, v > -INFINITY && (m < K || v > lst[K - 1]));
+    if (b) warp_insert_desc(lst, K, m, b, v, lane);
+  }
+  const float T = (m == K) ? lst[K - 1] : -INFINITY;
+  const float cut = T - ((T == -INFINITY || T == INFINITY) ? 0.f : fabsf(T) * (8.f * U32) + 1e-30f);
+  int32_t* cl = A.cand + ql * (int64_t)A.cap;
+  int w = 0;
+  for (int p0 = 0; p0 < n; p0 += 32) {
+    const int p = p0 + lane;
+    const bool keep = p < n && hi[p] >= cut;
+    const int32_t cv = p < n ? cl[p] : 0;
+    const unsigned b = __ballot_sync(0xffffffffu, keep);
+    __syncwarp();
+    if (keep) cl[w + __popc(b & ((1u << lane) - 1u))] = cv;
+    w += __popc(b);
+    __syncwarp();
+  }
+  if (lane == 0) A.count[ql] = w;
+}
+
 }  // namespace
 
 bool tensor_supported(int method) { return method == COSINE || method == EUCLIDEAN; }
@@ -758,10 +893,12 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
   const int cap = use_t ? std::max(512, std::min(16384, 64 * r.k + 256))
                         : std::max(256, std::min(8192, 16 * r.k + 64));
   const int nseg = (int)((nr + TSEG - 1) / TSEG);
-  float *segtop = nullptr, *cutv = nullptr;
+  float *segtop = nullptr, *cutv = nullptr, *rlo = nullptr, *rhi = nullptr;
   if (use_t) {
     SK(cudaMallocAsync(&segtop, sizeof(float) * (size_t)(chunk * nseg * r.k + 4), s));
     SK(cudaMallocAsync(&cutv, sizeof(float) * (size_t)(chunk + 4), s));
+    SK(cudaMallocAsync(&rlo, sizeof(float) * (size_t)(chunk * cap + 4), s));
+    SK(cudaMallocAsync(&rhi, sizeof(float) * (size_t)(chunk * cap + 4), s));
   }
 
   float* S = nullptr;
@@ -835,6 +972,23 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
       k_tsel_keep<<<tgrid, SELECT_WARPS * 32, 0, s>>>(T);
       k_tsel_overflow<<<blocks_for(nb, 256), 256, 0, s>>>(nb, cap, count, over);
       SK(cudaGetLastError());
+      if (nrow <= RS_MAX_NROW) {
+        RescreenArgs R;
+        R.method = r.method; R.k = r.k; R.ref = ref; R.qry = qry; R.rf = rc->fval; R.qf = qc->fval;
+        R.rnnz = rc->nnz; R.rnorm = (r.method == EUCLIDEAN) ? rc->cnorm : nullptr;
+        R.qnnz = qc->nnz; R.qnorm = (r.method == EUCLIDEAN) ? qc->cnorm : nullptr;
+        R.q_begin = q0; R.nq = nb; R.selfmode = r.selfmode; R.cap = cap; R.cand = cand; R.count = count;
+        R.lo = rlo; R.hi = rhi;
+        const size_t rsmem = (size_t)RS_MAX_QV * 4 + (size_t)((nrow + 31) / 32) * 8;
+        if (rsmem > 48 * 1024)
+          SK(cudaFuncSetAttribute(k_rescreen, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem));
+        k_rescreen<<<(unsigned)nb, RS_THREADS, rsmem, s>>>(R);
+        const size_t ssm = sizeof(float) * (size_t)SELECT_WARPS * r.k;
+        if (ssm > 48 * 1024)
+          SK(cudaFuncSetAttribute(k_rescreen_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm));
+        k_rescreen_select<<<blocks_for(nb, SELECT_WARPS), SELECT_WARPS * 32, ssm, s>>>(R);
+        SK(cudaGetLastError());
+      }
       stats[6] += 2 * ld * nr * nb;
     } else {
     // tiles: up to QT consecutive queries whose values fit the table
@@ -935,6 +1089,8 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
   SK(cudaFreeAsync(work, s));
   if (segtop) SK(cudaFreeAsync(segtop, s));
   if (cutv) SK(cudaFreeAsync(cutv, s));
+  if (rlo) SK(cudaFreeAsync(rlo, s));
+  if (rhi) SK(cudaFreeAsync(rhi, s));
   // queries the screen could not bound: the exact slab engine, run by runs
   size_t a = 0;
   while (a < overflow_queries.size()) {
