@@ -406,7 +406,7 @@ __global__ void k_rerank_warp(int method, int dist, DevCsc ref, ColAux ra, DevCs
 // first[r / 32] + popc(word & below(r)) of the query; the query's values sit
 // in shared memory too (up to RQ_MAX_QV entries, else they are read from
 // global memory).  The candidates are sorted by column length (bitonic, in
-// shared memory) and dealt to the warps in groups of 32.
+// shared memory) and dealt round-robin to the warps' lanes.
 //
 // GB300's FP64 pipe spends the same time on an FP64 warp instruction whatever
 // the number of active lanes, so the sequential sum of a pair (one dadd per
@@ -483,9 +483,10 @@ __global__ void k_rerank_q(int method, int dist, DevCsc ref, ColAux ra, DevCsc q
   const double* rv = (method == COSINE) ? ra.uval : ref.x;
   const bool q_empty = (method == COSINE) && qa.scale[q] == 0.0;
   int2* wl = lists + warp * 32 * RM;
-  for (int g = warp * 32; g < n; g += RQ_WARPS * 32) {
-    // lane j owns candidate g + j
-    const int slot = g + lane;
+  for (int g = 0; g < n; g += RQ_WARPS * 32) {
+    // lane j of warp w owns sorted candidate g + 8 j + w: the candidates are
+    // dealt round-robin, so every warp gets work even for short lists
+    const int slot = g + lane * RQ_WARPS + warp;
     const int t = (slot < n) ? (int)(uint32_t)order[slot] : -1;
     int32_t c = -1;
     double v = 0.0;
