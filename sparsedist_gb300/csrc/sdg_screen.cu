@@ -73,13 +73,17 @@ __global__ void k_check_rows(DevCsc M, int* err) {
 // fval: the value the screen multiplies (unit value for cosine, raw value for
 // euclidean / manhattan, 1 for binary); cnorm: sum of squares (euclidean) or
 // of magnitudes (manhattan), accumulated in FP64 then rounded; nnz per column.
+// One warp per column: the FP32 screen values (coalesced) and the column's
+// norm term (a warp sum in FP64, rounded to FP32: the screen bounds allow for
+// its rounding whatever the summation order).
 __global__ void k_screen_prep(DevCsc M, int method, const double* uval, float* fval, float* cnorm,
                               int32_t* nnz) {
-  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t j = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (j >= M.ncol) return;
   double acc = 0.0;
   const int64_t a0 = M.p[j], a1 = M.p[j + 1];
-  for (int64_t a = a0; a < a1; ++a) {
+  for (int64_t a = a0 + lane; a < a1; a += 32) {
     const double v = M.x[a];
     float f;
     if (method == COSINE) f = (float)uval[a];
@@ -89,8 +93,12 @@ __global__ void k_screen_prep(DevCsc M, int method, const double* uval, float* f
     if (method == EUCLIDEAN) acc += v * v;
     else if (method == MANHATTAN) acc += fabs(v);
   }
-  cnorm[j] = (float)acc;
-  nnz[j] = (int32_t)(a1 - a0);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) {
+    cnorm[j] = (float)acc;
+    nnz[j] = (int32_t)(a1 - a0);
+  }
 }
 
 __global__ void k_iota_neg_nnz(const int32_t* nnz, int64_t n, uint32_t* keys, int32_t* ids) {
@@ -496,6 +504,54 @@ __device__ __forceinline__ void tensor_keys(const TensorSelArgs& A, int64_t q, i
   hi = key + err;
 }
 
+// tensor_keys for references c0 .. c0 + 3 (c0 % 4 == 0), with 16-byte loads
+// of S, the reference sizes and norms and a 4-byte load of the mask when all
+// four are below nr
+__device__ __forceinline__ void tensor_keys4(const TensorSelArgs& A, int64_t q, int32_t nq_, float Nq,
+                                             const float* Srow, int64_t c0, float lo[4], float hi[4]) {
+  if (c0 + 3 < A.nr) {
+    const float4 s4 = *reinterpret_cast<const float4*>(Srow + c0);
+    const int4 n4 = *reinterpret_cast<const int4*>(A.rnnz + c0);
+    float4 r4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (A.rnorm) r4 = *reinterpret_cast<const float4*>(A.rnorm + c0);
+    uchar4 m4 = make_uchar4(0, 0, 0, 0);
+    if (A.ref_mask) m4 = *reinterpret_cast<const uchar4*>(A.ref_mask + c0);
+    const float sv[4] = {s4.x, s4.y, s4.z, s4.w};
+    const int32_t nv[4] = {n4.x, n4.y, n4.z, n4.w};
+    const float rn[4] = {r4.x, r4.y, r4.z, r4.w};
+    const uint8_t mv[4] = {m4.x, m4.y, m4.z, m4.w};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int64_t c = c0 + j;
+      lo[j] = hi[j] = -INFINITY;
+      if (mv[j]) continue;
+      if (A.selfmode && c == q) {
+        if (A.include_self) lo[j] = hi[j] = INFINITY;
+        continue;
+      }
+      const float rel = BF16_REL + ((float)min(nq_, nv[j]) + 64.f) * ACC_ULP;
+      float key, err;
+      if (A.method == COSINE) {
+        key = sv[j];
+        err = rel + 1e-12f;
+      } else {
+        const float T = Nq + rn[j];
+        key = 2.f * sv[j] - T;
+        err = 2.f * rel * 1.01f * sqrtf(Nq * rn[j]) + 9.5367431640625e-7f * T + 1e-30f;
+      }
+      if (!(fabsf(key) <= FLT_MAX) || !(err <= FLT_MAX)) { lo[j] = -INFINITY; hi[j] = INFINITY; continue; }
+      lo[j] = key - err;
+      hi[j] = key + err;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      lo[j] = hi[j] = -INFINITY;
+      if (c0 + j < A.nr) tensor_keys(A, q, nq_, Nq, c0 + j, Srow[c0 + j], lo[j], hi[j]);
+    }
+  }
+}
+
 __device__ __forceinline__ void warp_insert_desc(float* lst, int K, int& n, unsigned m, float v, int lane) {
   while (m) {
     const int src = __ffs(m) - 1;
@@ -541,12 +597,18 @@ __global__ void k_tsel_segtop(TensorSelArgs A) {
     const float Nq = A.qnorm ? A.qnorm[q] : 0.f;
     const float* Srow = A.S + ql * A.ldS;
     const int64_t c_end = min(A.nr, (int64_t)(seg + 1) * TSEG);
-    for (int64_t p0 = (int64_t)seg * TSEG; p0 < c_end; p0 += 32) {
-      const int64_t c = p0 + lane;
-      float lo = -INFINITY, hi;
-      if (c < c_end) tensor_keys(A, q, nq_, Nq, c, Srow[c], lo, hi);
-      const unsigned m = __ballot_sync(0xffffffffu, lo > -INFINITY && (n < K || lo > lst[K - 1]));
-      if (m) warp_insert_desc(lst, K, n, m, lo, lane);
+    float thr = -INFINITY;                       // lst[K - 1] once the list is full
+    for (int64_t p0 = (int64_t)seg * TSEG; p0 < c_end; p0 += 128) {
+      float lo[4], hi[4];
+      tensor_keys4(A, q, nq_, Nq, Srow, p0 + 4 * lane, lo, hi);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const unsigned m = __ballot_sync(0xffffffffu, lo[j] > -INFINITY && (n < K || lo[j] > thr));
+        if (m) {
+          warp_insert_desc(lst, K, n, m, lo[j], lane);
+          if (n == K) thr = lst[K - 1];
+        }
+      }
     }
   }
   float* out = A.segtop + (ql * A.nseg + seg) * (int64_t)K;
@@ -591,17 +653,30 @@ __global__ void k_tsel_keep(TensorSelArgs A) {
   const float* Srow = A.S + ql * A.ldS;
   int32_t* out = A.cand + ql * (int64_t)A.cap;
   const int64_t c_end = min(A.nr, (int64_t)(seg + 1) * TSEG);
-  for (int64_t p0 = (int64_t)seg * TSEG; p0 < c_end; p0 += 32) {
-    const int64_t c = p0 + lane;
-    float lo, hi = -INFINITY;
-    if (c < c_end) tensor_keys(A, q, nq_, Nq, c, Srow[c], lo, hi);
-    const bool keep = hi > -INFINITY && hi >= cut;
-    const unsigned m = __ballot_sync(0xffffffffu, keep);
-    if (!m) continue;
+  for (int64_t p0 = (int64_t)seg * TSEG; p0 < c_end; p0 += 128) {
+    float lo[4], hi[4];
+    tensor_keys4(A, q, nq_, Nq, Srow, p0 + 4 * lane, lo, hi);
+    int mine = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) mine += (hi[j] > -INFINITY && hi[j] >= cut);
+    int incl = mine;                              // warp inclusive scan of the lanes' counts
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    if (total == 0) continue;
     int base = 0;
-    if (lane == 0) base = atomicAdd(A.count + ql, __popc(m));
-    base = __shfl_sync(0xffffffffu, base, 0) + __popc(m & ((1u << lane) - 1u));
-    if (keep && base < A.cap) out[base] = (int32_t)c;
+    if (lane == 31) base = atomicAdd(A.count + ql, total);
+    base = __shfl_sync(0xffffffffu, base, 31) + incl - mine;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (hi[j] > -INFINITY && hi[j] >= cut) {
+        if (base < A.cap) out[base] = (int32_t)(p0 + 4 * lane + j);
+        ++base;
+      }
+    }
   }
 }
 
@@ -679,21 +754,27 @@ __global__ void k_rescreen(RescreenArgs A) {
       const int64_t c0 = A.ref.p[c], c1 = A.ref.p[c + 1];
       for (int64_t a0 = c0; a0 < c1; a0 += 128) {
         int32_t r[4];
-        float f[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
           const int64_t e = a0 + 32 * u + lane;
           r[u] = (e < c1) ? __ldg(A.ref.i + e) : -1;
-          f[u] = (e < c1) ? __ldg(A.rf + e) : 0.f;
         }
+        int qe[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
+          qe[u] = -1;
           if (r[u] >= 0) {
             const uint32_t wd = bits[r[u] >> 5];
             const uint32_t bit = 1u << (r[u] & 31);
-            if (wd & bit) acc = fmaf(f[u], qv[first[r[u] >> 5] + __popc(wd & (bit - 1u))], acc);
+            if (wd & bit) qe[u] = first[r[u] >> 5] + __popc(wd & (bit - 1u));
           }
         }
+        float f[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) f[u] = (qe[u] >= 0) ? __ldg(A.rf + a0 + 32 * u + lane) : 0.f;
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (qe[u] >= 0) acc = fmaf(f[u], qv[qe[u]], acc);
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -822,21 +903,24 @@ static int ensure_cache(ScreenCache* c, int method, const DevCsc& M, const ColAu
   int64_t h_nnz = 0;
   if (M.ncol > 0) SK(cudaMemcpyAsync(&h_nnz, M.p + M.ncol, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
   SK(cudaStreamSynchronize(s));
-  const size_t bytes = sizeof(float) * ((size_t)h_nnz + 4) + sizeof(float) * ((size_t)M.ncol + 4) +
-                       sizeof(int32_t) * ((size_t)M.ncol + 4) * 2 + 64;
+  // each array starts on a 256-byte boundary (16-byte vector loads of cnorm / nnz)
+  auto seg = [](size_t bytes) { return (bytes + 255) & ~(size_t)255; };
+  const size_t b_fval = seg(sizeof(float) * ((size_t)h_nnz + 4));
+  const size_t b_col = seg(sizeof(float) * ((size_t)M.ncol + 4));
+  const size_t bytes = b_fval + 3 * b_col;
   SK(cudaMallocAsync(&c->blob, bytes, s));
   char* b = static_cast<char*>(c->blob);
   c->fval = reinterpret_cast<float*>(b);
-  b += sizeof(float) * ((size_t)h_nnz + 4);
+  b += b_fval;
   c->cnorm = reinterpret_cast<float*>(b);
-  b += sizeof(float) * ((size_t)M.ncol + 4);
+  b += b_col;
   c->nnz = reinterpret_cast<int32_t*>(b);
-  b += sizeof(int32_t) * ((size_t)M.ncol + 4);
+  b += b_col;
   c->perm = reinterpret_cast<int32_t*>(b);
   c->nnz_total = h_nnz;
   if (M.ncol > 0) {
-    k_screen_prep<<<blocks_for(M.ncol, 128), 128, 0, s>>>(M, method, aux.uval, c->fval, c->cnorm,
-                                                           c->nnz);
+    k_screen_prep<<<blocks_for(M.ncol * 32, 256), 256, 0, s>>>(M, method, aux.uval, c->fval, c->cnorm,
+                                                                c->nnz);
     // descending-nnz order of the columns (radix sort on 32-bit keys)
     uint32_t *k_in = nullptr, *k_out = nullptr;
     int32_t* ids = nullptr;
