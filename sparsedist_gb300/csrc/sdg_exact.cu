@@ -414,10 +414,12 @@ __global__ void k_rerank_warp(int method, int dist, DevCsc ref, ColAux ra, DevCs
 // pair per LANE.  A warp works on its 32 candidates in passes: (scan) for
 // each candidate in turn, the warp streams the column 32 entries a round
 // (coalesced, four rounds' loads in flight), tests the rows against the
-// bitmap and appends the matched (entry, query entry) pairs, in row order, to
-// that candidate's list of RM slots until it is full or the column ends;
-// (sum) lane j then runs candidate j's list: dmul, dadd, in order, all lanes
-// at once.  Each lane's sum is the reference's sequential sum bit for bit.
+// bitmap, multiplies the matched values (dmul, the same product the
+// reference forms) and appends the products, in row order, to that
+// candidate's list of RM slots until it is full or the column ends; (sum)
+// lane j then adds candidate j's list in order, all lanes at once, operands
+// in shared memory.  Each lane's sum is the reference's sequential sum bit for
+// bit.
 constexpr int RQ_THREADS = 256;
 constexpr int RQ_WARPS = RQ_THREADS / 32;
 constexpr int32_t RQ_MAX_NROW = 1 << 18;
@@ -432,7 +434,7 @@ __global__ void k_rerank_q(int method, int dist, DevCsc ref, ColAux ra, DevCsc q
   const int W = (qry.nrow + 31) >> 5;
   double* qvs = reinterpret_cast<double*>(rq_smem);                          // RQ_MAX_QV
   uint64_t* order = reinterpret_cast<uint64_t*>(rq_smem + 2 * RQ_MAX_QV);    // RQ_MAX_CAND
-  int2* lists = reinterpret_cast<int2*>(order + RQ_MAX_CAND);               // [warp][32][RM]
+  double* lists = reinterpret_cast<double*>(order + RQ_MAX_CAND);           // [warp][32][RM]
   uint32_t* bits = reinterpret_cast<uint32_t*>(lists + RQ_WARPS * 32 * RM);
   int32_t* first = reinterpret_cast<int32_t*>(bits + W);
   const int64_t ql = blockIdx.x;
@@ -482,7 +484,7 @@ __global__ void k_rerank_q(int method, int dist, DevCsc ref, ColAux ra, DevCsc q
   const unsigned below = (1u << lane) - 1u;
   const double* rv = (method == COSINE) ? ra.uval : ref.x;
   const bool q_empty = (method == COSINE) && qa.scale[q] == 0.0;
-  int2* wl = lists + warp * 32 * RM;
+  double* wl = lists + warp * 32 * RM;
   for (int g = 0; g < n; g += RQ_WARPS * 32) {
     // lane j of warp w owns sorted candidate g + 8 j + w: the candidates are
     // dealt round-robin, so every warp gets work even for short lists
@@ -516,8 +518,7 @@ __global__ void k_rerank_q(int method, int dist, DevCsc ref, ColAux ra, DevCsc q
         if (!__shfl_sync(0xffffffffu, active, j)) continue;
         int64_t pos = __shfl_sync(0xffffffffu, a, j);
         const int64_t end = __shfl_sync(0xffffffffu, a_end, j);
-        const int64_t base = __shfl_sync(0xffffffffu, c0, j);
-        int2* lj = wl + j * RM;
+        double* lj = wl + j * RM;
         int fill = 0;
         bool full = false;
         while (pos < end && !full) {
@@ -527,21 +528,32 @@ __global__ void k_rerank_q(int method, int dist, DevCsc ref, ColAux ra, DevCsc q
             const int64_t e = pos + 32 * u + lane;
             r[u] = (e < end) ? __ldg(ref.i + e) : -1;
           }
+          int qe[4];
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
-            if (full || pos >= end) break;
-            bool hit = false;
-            int qe = 0;
+            qe[u] = -1;
             if (r[u] >= 0) {
               const uint32_t wd = bits[r[u] >> 5];
               const uint32_t bit = 1u << (r[u] & 31);
-              if (wd & bit) { hit = true; qe = first[r[u] >> 5] + __popc(wd & (bit - 1u)); }
+              if (wd & bit) qe[u] = first[r[u] >> 5] + __popc(wd & (bit - 1u));
             }
+          }
+          double pv[4];
+          if (method != BINARY) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u) pv[u] = (qe[u] >= 0) ? __ldg(rv + pos + 32 * u + lane) : 0.0;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) if (qe[u] >= 0) pv[u] = dmul(pv[u], qv[qe[u]]);
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            if (full || pos >= end) break;
+            const bool hit = qe[u] >= 0;
             const unsigned m = __ballot_sync(0xffffffffu, hit);
             const int cnt = __popc(m);
             if (method != BINARY) {
               if (fill + cnt > RM) { full = true; break; }
-              if (hit) lj[fill + __popc(m & below)] = make_int2((int)(pos + lane - base), qe);
+              if (hit) lj[fill + __popc(m & below)] = pv[u];
             }
             fill += cnt;
             pos += 32;
@@ -558,13 +570,9 @@ __global__ void k_rerank_q(int method, int dist, DevCsc ref, ColAux ra, DevCsc q
       // sum: lane j runs candidate j's list in order
       if (method != BINARY) {
         const int mx = __reduce_max_sync(0xffffffffu, my_fill);
-        const int2* ll = wl + lane * RM;
-        for (int s2 = 0; s2 < mx; ++s2) {
-          if (s2 < my_fill) {
-            const int2 be = ll[s2];
-            sum = dadd(sum, dmul(__ldg(rv + c0 + be.x), qv[be.y]));
-          }
-        }
+        const double* ll = wl + lane * RM;
+        for (int s2 = 0; s2 < mx; ++s2)
+          if (s2 < my_fill) sum = dadd(sum, ll[s2]);
       }
       __syncwarp();
     }
