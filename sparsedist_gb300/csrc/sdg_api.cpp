@@ -148,6 +148,10 @@ struct sdg_ctx {
   double tev_folded_ms = 0.0;
   int64_t tev_launches = 0;
   cublasHandle_t blas = nullptr;       // created on the first tensor-core screen
+  // false: choose the tensor-core screen only where the reference's dense
+  // copy already exists (serving workers share the reference and must not
+  // build it concurrently)
+  bool tensor_lazy = true;
 };
 
 namespace {
@@ -413,7 +417,8 @@ int pick_engine(sdg_ctx* c, const KnnPlan& P, const sdg_matrix* ref, const sdg_m
   // The tensor screen does 2 nrow nr nq dense flops where the FP32 screen
   // visits nq / 16 * nnz(ref) stored entries: it wins from ~0.5 % density
   // on, if the dense copies fit in half of the free device memory.
-  if (tensor_supported(P.method) && nrow > 0 && nr > 0) {
+  if (tensor_supported(P.method) && nrow > 0 && nr > 0 &&
+      (c->tensor_lazy || (ref->tensor.method == P.method && ref->tensor.usable))) {
     const double density = (double)ref->nnz / ((double)nrow * (double)nr);
     size_t bytes = tensor_cache_bytes(nrow, nr);
     if (X != ref) bytes += tensor_cache_bytes(nrow, X->ncol);
@@ -1227,11 +1232,41 @@ SDG_API int sdg_server_create(sdg_ctx* ctx, const sdg_matrix* ref, int workers, 
       knn_device(ctx, q.get(), S->ref, m, 1, 1, 0, 1, false, 0, nullptr, nullptr, &ke, &fl, &hi, &hv);
       CK(cudaStreamSynchronize(ctx->stream));
     }
+    // The tensor-core screen's dense copy of the reference (one method at a
+    // time) is built here too, for the first served method that can use it,
+    // when the automatic choice would take it; workers then never build it.
+    if (saved_engine == 0) {
+      for (int t = 0; t < nmethods; ++t) {
+        const int m = methods[t];
+        if (!tensor_supported(m) || !screen_fits(S->ref->nrow) || S->ref->ncol < 1) continue;
+        const double density = (double)S->ref->nnz / ((double)S->ref->nrow * (double)S->ref->ncol);
+        size_t fr = 0, tot = 0;
+        const size_t bytes = tensor_cache_bytes(S->ref->nrow, S->ref->ncol);
+        if (density < 0.005 || cudaMemGetInfo(&fr, &tot) != cudaSuccess || bytes > fr / 2) {
+          cudaGetLastError();
+          break;
+        }
+        sdg_csc one;
+        std::vector<int32_t> pi = {0, 0}, ii(1, 0);
+        std::vector<double> xx(1, 1.0);
+        one.nrow = S->ref->nrow; one.ncol = 1; one.p = pi.data(); one.i = ii.data(); one.x = xx.data();
+        auto q = upload(ctx, &one, "X");
+        DevBuf hi, hv;
+        int ke = 0, fl = 0;
+        ctx->engine = 3;
+        knn_device(ctx, q.get(), S->ref, m, 1, 1, 0, 0, false, 0, nullptr, nullptr, &ke, &fl, &hi, &hv);
+        CK(cudaStreamSynchronize(ctx->stream));
+        ctx->engine = saved_engine;
+        break;
+      }
+    }
     ctx->engine = saved_engine;
     for (int w = 0; w < workers; ++w) {
       sdg_ctx* c = nullptr;
       const int st = sdg_ctx_create(S->device, &c);
       if (st != SDG_OK) fail(st, std::string(g_err.data(), g_err.size()));
+      c->engine = saved_engine;
+      c->tensor_lazy = false;
       S->ctxs.push_back(c);
     }
     S->t_first = now_s();
