@@ -209,12 +209,12 @@ struct sdg_matrix {
   bool have_moments = false;
   int js_status = 1;
   ScreenCache screen[4];        // screening data per method (sdg_screen.h), binary..manhattan
-  TensorCache tensor;           // dense BF16 screen values (tensor-core screen)
+  TensorCache tensor[4];        // dense BF16 screen values per method (tensor-core screen)
 
   ~sdg_matrix() {
     if (ctx) {
       for (auto& sc : screen) screen_cache_free(&sc, ctx->stream);
-      tensor_cache_free(&tensor, ctx->stream);
+      for (auto& tc : tensor) tensor_cache_free(&tc, ctx->stream);
       cudaStreamSynchronize(ctx->stream);
     }
     for (DevBuf* b : {&p, &i, &x, &empty, &uval, &scale, &s1, &s2}) b->detach();
@@ -418,12 +418,12 @@ int pick_engine(sdg_ctx* c, const KnnPlan& P, const sdg_matrix* ref, const sdg_m
   // visits nq / 16 * nnz(ref) stored entries: it wins from ~0.5 % density
   // on, if the dense copies fit in half of the free device memory.
   if (tensor_supported(P.method) && nrow > 0 && nr > 0 &&
-      (c->tensor_lazy || (ref->tensor.method == P.method && ref->tensor.usable))) {
+      (c->tensor_lazy || (ref->tensor[P.method].method == P.method && ref->tensor[P.method].usable))) {
     const double density = (double)ref->nnz / ((double)nrow * (double)nr);
     size_t bytes = tensor_cache_bytes(nrow, nr);
     if (X != ref) bytes += tensor_cache_bytes(nrow, X->ncol);
     size_t fr = 0, tot = 0;
-    if (ref->tensor.method == P.method && ref->tensor.usable) bytes = 0;   // already resident
+    if (ref->tensor[P.method].method == P.method && ref->tensor[P.method].usable) bytes = 0;   // already resident
     if (density >= 0.005 && cudaMemGetInfo(&fr, &tot) == cudaSuccess && bytes <= fr / 2) return 3;
     cudaGetLastError();
   }
@@ -502,8 +502,8 @@ void knn_device(sdg_ctx* c, sdg_matrix* X, sdg_matrix* Y, int method, int dist, 
     h.time_begin = [c]() { sdg_time_begin(c); };
     h.time_end = [c]() { sdg_time_end(c); };
     h.exact_range = [&](int64_t q0, int64_t n) { exact_engine(c, P, ref, X, d_idx, d_val, q0, q0 + n); };
-    const int st = screen_knn(c->stream, r, ref->dev(), aux_of(ref), &ref->screen[method], &ref->tensor,
-                              X->dev(), aux_of(X), &X->screen[method], &X->tensor, d_idx, d_val, c->stats, h);
+    const int st = screen_knn(c->stream, r, ref->dev(), aux_of(ref), &ref->screen[method], &ref->tensor[method],
+                              X->dev(), aux_of(X), &X->screen[method], &X->tensor[method], d_idx, d_val, c->stats, h);
     if (st) cuda_check((cudaError_t)st, "screen_knn");
   } else {
     exact_engine(c, P, ref, X, d_idx, d_val, q_lo, q_hi);
@@ -1232,9 +1232,10 @@ SDG_API int sdg_server_create(sdg_ctx* ctx, const sdg_matrix* ref, int workers, 
       knn_device(ctx, q.get(), S->ref, m, 1, 1, 0, 1, false, 0, nullptr, nullptr, &ke, &fl, &hi, &hv);
       CK(cudaStreamSynchronize(ctx->stream));
     }
-    // The tensor-core screen's dense copy of the reference (one method at a
-    // time) is built here too, for the first served method that can use it,
-    // when the automatic choice would take it; workers then never build it.
+    // The tensor-core screen's dense copy of the reference is built here too,
+    // per served method that can use it while a copy fits in half the free
+    // device memory (the automatic choice's test) and leaves the admission
+    // budget free; workers never build one.
     if (saved_engine == 0) {
       for (int t = 0; t < nmethods; ++t) {
         const int m = methods[t];
@@ -1242,9 +1243,11 @@ SDG_API int sdg_server_create(sdg_ctx* ctx, const sdg_matrix* ref, int workers, 
         const double density = (double)S->ref->nnz / ((double)S->ref->nrow * (double)S->ref->ncol);
         size_t fr = 0, tot = 0;
         const size_t bytes = tensor_cache_bytes(S->ref->nrow, S->ref->ncol);
-        if (density < 0.005 || cudaMemGetInfo(&fr, &tot) != cudaSuccess || bytes > fr / 2) {
+        // the copy must leave the admission budget free for the requests
+        if (density < 0.005 || cudaMemGetInfo(&fr, &tot) != cudaSuccess || bytes > fr / 2 ||
+            (int64_t)(bytes + (size_t)mem_budget) > (int64_t)fr) {
           cudaGetLastError();
-          break;
+          continue;
         }
         sdg_csc one;
         std::vector<int32_t> pi = {0, 0}, ii(1, 0);
@@ -1257,7 +1260,6 @@ SDG_API int sdg_server_create(sdg_ctx* ctx, const sdg_matrix* ref, int workers, 
         knn_device(ctx, q.get(), S->ref, m, 1, 1, 0, 0, false, 0, nullptr, nullptr, &ke, &fl, &hi, &hv);
         CK(cudaStreamSynchronize(ctx->stream));
         ctx->engine = saved_engine;
-        break;
       }
     }
     ctx->engine = saved_engine;

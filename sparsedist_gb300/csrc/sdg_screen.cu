@@ -478,6 +478,40 @@ struct TensorSelArgs {
   int32_t* overflow;
 };
 
+// The BF16 bounds of one eligible pair from its GEMM value s (a key that is
+// not finite, or a bound that is not, keeps the pair unconditionally).
+// Binary: s estimates the matched-row count c (0 / 1 factors are exact in
+// BF16); with the accumulation allowance c lies in [c_lo, c_hi] and the
+// Jaccard key c / (nq + nc - c) increases with c.
+__device__ __forceinline__ void bf16_bounds(int method, float s, int32_t nq_, float Nq, int32_t nc_, float Nc,
+                                            float& lo, float& hi) {
+  const float nmin = (float)min(nq_, nc_);
+  const float rel = BF16_REL + (nmin + 64.f) * ACC_ULP;
+  float key, err;
+  if (method == BINARY) {
+    const float e = (nmin + 64.f) * ACC_ULP * 1.01f * fabsf(s) + 1e-6f;
+    const float clo = fmaxf(0.f, s - e), chi = fminf(nmin, s + e);
+    const float N = (float)nq_ + (float)nc_;
+    lo = (N - clo > 0.f) ? clo / (N - clo) : 1.f;
+    hi = (N - chi > 0.f) ? chi / (N - chi) : 1.f;
+    lo = lo * (1.f - 4.f * U32);
+    hi = hi * (1.f + 4.f * U32) + 1e-30f;
+    if (!(fabsf(s) <= FLT_MAX)) { lo = -INFINITY; hi = INFINITY; }
+    return;
+  }
+  if (method == COSINE) {
+    key = s;
+    err = rel + 1e-12f;
+  } else {
+    const float T = Nq + Nc;
+    key = 2.f * s - T;
+    err = 2.f * rel * 1.01f * sqrtf(Nq * Nc) + 9.5367431640625e-7f * T + 1e-30f;
+  }
+  if (!(fabsf(key) <= FLT_MAX) || !(err <= FLT_MAX)) { lo = -INFINITY; hi = INFINITY; return; }
+  lo = key - err;
+  hi = key + err;
+}
+
 // pessimistic / optimistic keys of pair (query q, reference c); -inf / -inf
 // when c is not eligible; +inf / +inf for the restored self pair.
 __device__ __forceinline__ void tensor_keys(const TensorSelArgs& A, int64_t q, int32_t nq_, float Nq, int64_t c,
@@ -488,20 +522,7 @@ __device__ __forceinline__ void tensor_keys(const TensorSelArgs& A, int64_t q, i
     if (A.include_self) lo = hi = INFINITY;
     return;
   }
-  const int32_t nc_ = A.rnnz[c];
-  const float rel = BF16_REL + ((float)min(nq_, nc_) + 64.f) * ACC_ULP;
-  float key, err;
-  if (A.method == COSINE) {
-    key = s;
-    err = rel + 1e-12f;
-  } else {
-    const float Nc = A.rnorm[c], T = Nq + Nc;
-    key = 2.f * s - T;
-    err = 2.f * rel * 1.01f * sqrtf(Nq * Nc) + 9.5367431640625e-7f * T + 1e-30f;
-  }
-  if (!(fabsf(key) <= FLT_MAX) || !(err <= FLT_MAX)) { lo = -INFINITY; hi = INFINITY; return; }
-  lo = key - err;
-  hi = key + err;
+  bf16_bounds(A.method, s, nq_, Nq, A.rnnz[c], A.rnorm ? A.rnorm[c] : 0.f, lo, hi);
 }
 
 // tensor_keys for references c0 .. c0 + 3 (c0 % 4 == 0), with 16-byte loads
@@ -529,19 +550,7 @@ __device__ __forceinline__ void tensor_keys4(const TensorSelArgs& A, int64_t q, 
         if (A.include_self) lo[j] = hi[j] = INFINITY;
         continue;
       }
-      const float rel = BF16_REL + ((float)min(nq_, nv[j]) + 64.f) * ACC_ULP;
-      float key, err;
-      if (A.method == COSINE) {
-        key = sv[j];
-        err = rel + 1e-12f;
-      } else {
-        const float T = Nq + rn[j];
-        key = 2.f * sv[j] - T;
-        err = 2.f * rel * 1.01f * sqrtf(Nq * rn[j]) + 9.5367431640625e-7f * T + 1e-30f;
-      }
-      if (!(fabsf(key) <= FLT_MAX) || !(err <= FLT_MAX)) { lo[j] = -INFINITY; hi[j] = INFINITY; continue; }
-      lo[j] = key - err;
-      hi[j] = key + err;
+      bf16_bounds(A.method, sv[j], nq_, Nq, nv[j], rn[j], lo[j], hi[j]);
     }
   } else {
 #pragma unroll
@@ -829,7 +838,7 @@ __global__ void k_rescreen_select(RescreenArgs A) {
 
 }  // namespace
 
-bool tensor_supported(int method) { return method == COSINE || method == EUCLIDEAN; }
+bool tensor_supported(int method) { return method == BINARY || method == COSINE || method == EUCLIDEAN; }
 
 static int64_t tensor_ld(int32_t nrow) { return ((int64_t)nrow + 63) / 64 * 64; }
 
