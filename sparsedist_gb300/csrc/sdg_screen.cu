@@ -445,16 +445,37 @@ constexpr int TSEG = 32768;
 constexpr float BF16_REL = 0.0040f;
 constexpr float ACC_ULP = 4.76837158203125e-7f;   // 2^-21
 
-__global__ void k_tensor_fill(DevCsc M, const float* fval, __nv_bfloat16* dense, int64_t ld, int* bad) {
+// One warp per column: scatter the BF16 values into the dense column and
+// compute ||v - b|| and ||b|| in FP64 (v: src, the exact values; b: the BF16
+// values the GEMM multiplies), rounded up to FP32.
+__global__ void k_tensor_fill(DevCsc M, const float* fval, const double* src, __nv_bfloat16* dense, int64_t ld,
+                              float* err_out, float* bn_out, int* bad) {
   const int64_t j = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (j >= M.ncol) return;
   __nv_bfloat16* col = dense + j * ld;
+  double se = 0.0, sb = 0.0;
   for (int64_t a = M.p[j] + lane; a < M.p[j + 1]; a += 32) {
     const float f = fval[a];
     const float af = fabsf(f);
     if (f != 0.f && !(af >= FLT_MIN && af <= 3.0e38f)) atomicOr(bad, 1);
-    col[M.i[a]] = __float2bfloat16_rn(f);
+    const __nv_bfloat16 bv = __float2bfloat16_rn(f);
+    col[M.i[a]] = bv;
+    const double b = (double)__bfloat162float(bv);
+    const double v = src ? src[a] : (double)f;
+    se += (v - b) * (v - b);
+    sb += b * b;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    se += __shfl_xor_sync(0xffffffffu, se, o);
+    sb += __shfl_xor_sync(0xffffffffu, sb, o);
+  }
+  if (lane == 0) {
+    // FP64 sums and sqrt are within a few units of 2^-52; the factor and the
+    // upward FP32 rounding cover them
+    err_out[j] = __double2float_ru(sqrt(se) * (1.0 + 1e-12));
+    bn_out[j] = __double2float_ru(sqrt(sb) * (1.0 + 1e-12));
   }
 }
 
@@ -464,6 +485,8 @@ struct TensorSelArgs {
   int64_t ldS, nr;
   const int32_t* rnnz; const float* rnorm;
   const int32_t* qnnz; const float* qnorm;
+  const float* rerr; const float* rbn;       // TensorCache norms (reference)
+  const float* qerr; const float* qbn;       // and query
   const uint8_t* ref_mask;
   const uint8_t* qry_blank;
   const uint8_t* qry_force_exact;
@@ -480,16 +503,22 @@ struct TensorSelArgs {
 
 // The BF16 bounds of one eligible pair from its GEMM value s (a key that is
 // not finite, or a bound that is not, keeps the pair unconditionally).
+// With v the exact values and b their BF16 copies (per column eq, er = ||v - b||
+// and bq, br = ||b||), Cauchy-Schwarz gives
+//   |sum v_q v_r - sum b_q b_r| <= eq ||v_r|| + bq er,
+// ||v_r|| = 1 for unit columns and sqrt(Nr) otherwise; the FP32 accumulation
+// of at most n = min(nnz_q, nnz_r) nonzero products is allowed
+// (n + 64) 2^-21 sum |b_q b_r| <= (n + 64) 2^-21 bq br.
 // Binary: s estimates the matched-row count c (0 / 1 factors are exact in
 // BF16); with the accumulation allowance c lies in [c_lo, c_hi] and the
 // Jaccard key c / (nq + nc - c) increases with c.
 __device__ __forceinline__ void bf16_bounds(int method, float s, int32_t nq_, float Nq, int32_t nc_, float Nc,
-                                            float& lo, float& hi) {
+                                            float eq, float bq, float er, float br, float& lo, float& hi) {
   const float nmin = (float)min(nq_, nc_);
-  const float rel = BF16_REL + (nmin + 64.f) * ACC_ULP;
+  const float acc = (nmin + 64.f) * ACC_ULP;
   float key, err;
   if (method == BINARY) {
-    const float e = (nmin + 64.f) * ACC_ULP * 1.01f * fabsf(s) + 1e-6f;
+    const float e = acc * 1.01f * fabsf(s) + 1e-6f;
     const float clo = fmaxf(0.f, s - e), chi = fminf(nmin, s + e);
     const float N = (float)nq_ + (float)nc_;
     lo = (N - clo > 0.f) ? clo / (N - clo) : 1.f;
@@ -501,11 +530,11 @@ __device__ __forceinline__ void bf16_bounds(int method, float s, int32_t nq_, fl
   }
   if (method == COSINE) {
     key = s;
-    err = rel + 1e-12f;
+    err = (1.000001f * eq + bq * er + acc * bq * br) * 1.01f + 1e-12f;
   } else {
     const float T = Nq + Nc;
     key = 2.f * s - T;
-    err = 2.f * rel * 1.01f * sqrtf(Nq * Nc) + 9.5367431640625e-7f * T + 1e-30f;
+    err = 2.f * (sqrtf(Nc) * 1.000001f * eq + bq * er + acc * bq * br) * 1.01f + 9.5367431640625e-7f * T + 1e-30f;
   }
   if (!(fabsf(key) <= FLT_MAX) || !(err <= FLT_MAX)) { lo = -INFINITY; hi = INFINITY; return; }
   lo = key - err;
@@ -522,7 +551,8 @@ __device__ __forceinline__ void tensor_keys(const TensorSelArgs& A, int64_t q, i
     if (A.include_self) lo = hi = INFINITY;
     return;
   }
-  bf16_bounds(A.method, s, nq_, Nq, A.rnnz[c], A.rnorm ? A.rnorm[c] : 0.f, lo, hi);
+  bf16_bounds(A.method, s, nq_, Nq, A.rnnz[c], A.rnorm ? A.rnorm[c] : 0.f, A.qerr[q], A.qbn[q], A.rerr[c], A.rbn[c],
+              lo, hi);
 }
 
 // tensor_keys for references c0 .. c0 + 3 (c0 % 4 == 0), with 16-byte loads
@@ -537,6 +567,11 @@ __device__ __forceinline__ void tensor_keys4(const TensorSelArgs& A, int64_t q, 
     if (A.rnorm) r4 = *reinterpret_cast<const float4*>(A.rnorm + c0);
     uchar4 m4 = make_uchar4(0, 0, 0, 0);
     if (A.ref_mask) m4 = *reinterpret_cast<const uchar4*>(A.ref_mask + c0);
+    const float4 e4 = *reinterpret_cast<const float4*>(A.rerr + c0);
+    const float4 b4 = *reinterpret_cast<const float4*>(A.rbn + c0);
+    const float ev[4] = {e4.x, e4.y, e4.z, e4.w};
+    const float bv[4] = {b4.x, b4.y, b4.z, b4.w};
+    const float eq = A.qerr[q], bq = A.qbn[q];
     const float sv[4] = {s4.x, s4.y, s4.z, s4.w};
     const int32_t nv[4] = {n4.x, n4.y, n4.z, n4.w};
     const float rn[4] = {r4.x, r4.y, r4.z, r4.w};
@@ -550,7 +585,7 @@ __device__ __forceinline__ void tensor_keys4(const TensorSelArgs& A, int64_t q, 
         if (A.include_self) lo[j] = hi[j] = INFINITY;
         continue;
       }
-      bf16_bounds(A.method, sv[j], nq_, Nq, nv[j], rn[j], lo[j], hi[j]);
+      bf16_bounds(A.method, sv[j], nq_, Nq, nv[j], rn[j], eq, bq, ev[j], bv[j], lo[j], hi[j]);
     }
   } else {
 #pragma unroll
@@ -848,13 +883,16 @@ size_t tensor_cache_bytes(int32_t nrow, int64_t ncol) {
 
 void tensor_cache_free(TensorCache* c, cudaStream_t s) {
   if (c && c->dense) cudaFreeAsync(c->dense, s);
+  if (c && c->err) cudaFreeAsync(c->err, s);
+  if (c && c->bn) cudaFreeAsync(c->bn, s);
   if (c) *c = TensorCache();
 }
 
 // Builds (or reuses) the dense BF16 copy of M's screen values for `method`
 // from its ScreenCache; an allocation failure leaves it unusable (the FP32
 // screen then runs) rather than failing the call.
-static int ensure_tensor(TensorCache* t, int method, const DevCsc& M, const ScreenCache* sc, cudaStream_t s) {
+static int ensure_tensor(TensorCache* t, int method, const DevCsc& M, const ColAux& aux, const ScreenCache* sc,
+                         cudaStream_t s) {
   if (t->method == method) return 0;
   tensor_cache_free(t, s);
   t->method = method;
@@ -868,13 +906,17 @@ static int ensure_tensor(TensorCache* t, int method, const DevCsc& M, const Scre
     return 0;
   }
   SK(e);
+  const size_t nbytes = sizeof(float) * ((size_t)M.ncol + 4);
+  SK(cudaMallocAsync(&t->err, nbytes, s));
+  SK(cudaMallocAsync(&t->bn, nbytes, s));
   int* bad = nullptr;
   SK(cudaMallocAsync(&bad, sizeof(int), s));
   SK(cudaMemsetAsync(bad, 0, sizeof(int), s));
   SK(cudaMemsetAsync(t->dense, 0, bytes, s));
   if (M.ncol > 0)
-    k_tensor_fill<<<blocks_for(M.ncol * 32, 256), 256, 0, s>>>(M, sc->fval, static_cast<__nv_bfloat16*>(t->dense),
-                                                               t->ld, bad);
+    k_tensor_fill<<<blocks_for(M.ncol * 32, 256), 256, 0, s>>>(
+        M, sc->fval, (method == COSINE) ? aux.uval : (method == EUCLIDEAN) ? M.x : nullptr,
+        static_cast<__nv_bfloat16*>(t->dense), t->ld, t->err, t->bn, bad);
   int hbad = 0;
   SK(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
   SK(cudaStreamSynchronize(s));
@@ -959,8 +1001,8 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
   SK((cudaError_t)ensure_cache(qc, r.method, qry, qa, s));
   bool use_t = r.tensor && r.blas && rt && qt && tensor_supported(r.method);
   if (use_t) {
-    SK((cudaError_t)ensure_tensor(rt, r.method, ref, rc, s));
-    if (qt != rt) SK((cudaError_t)ensure_tensor(qt, r.method, qry, qc, s));
+    SK((cudaError_t)ensure_tensor(rt, r.method, ref, ra, rc, s));
+    if (qt != rt) SK((cudaError_t)ensure_tensor(qt, r.method, qry, qa, qc, s));
     use_t = rt->usable && qt->usable && rt->ld == qt->ld;
   }
   const int64_t nr = ref.ncol, nq = qry.ncol;
@@ -1050,6 +1092,7 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
       T.method = r.method; T.k = r.k; T.S = S; T.ldS = ldS; T.nr = nr;
       T.rnnz = rc->nnz; T.rnorm = (r.method == EUCLIDEAN) ? rc->cnorm : nullptr;
       T.qnnz = qc->nnz; T.qnorm = (r.method == EUCLIDEAN) ? qc->cnorm : nullptr;
+      T.rerr = rt->err; T.rbn = rt->bn; T.qerr = qt->err; T.qbn = qt->bn;
       T.ref_mask = r.ref_mask; T.qry_blank = r.qry_blank; T.qry_force_exact = force;
       T.q_begin = q0; T.nq = nb; T.selfmode = r.selfmode; T.include_self = r.include_self;
       T.nseg = nseg; T.segtop = segtop; T.cut = cutv;

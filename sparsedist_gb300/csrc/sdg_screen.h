@@ -33,6 +33,11 @@ struct TensorCache {
   int usable = 0;
   void* dense = nullptr;     // __nv_bfloat16[ncol * ld]
   int64_t ld = 0;
+  // per column, rounded up to FP32: err = ||v - bf16(v)||_2 and bn = ||bf16(v)||_2,
+  // v the exact values the key is defined on (FP64 unit values for cosine,
+  // the values for euclidean)
+  float* err = nullptr;
+  float* bn = nullptr;
 };
 
 struct ScreenRun {
