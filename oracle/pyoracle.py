@@ -91,6 +91,12 @@ class Oracle:
         self._knn = getattr(self.lib, pre + "knn")
         self._cross = getattr(self.lib, pre + "knn_cross")
         self._graph = getattr(self.lib, pre + "snn_graph")
+        self._shared = getattr(self.lib, pre + ("snn_shared_c" if ref else "snn_shared"))
+        self._graph_shared = getattr(self.lib, pre + "snn_graph_shared")
+        self._shared.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int, C.c_double, C.c_void_p,
+                                 C.c_void_p, C.c_void_p, C.c_void_p]
+        self._graph_shared.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int, C.c_double,
+                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         for f in (self._topk, self._rows):
             f.argtypes = None
         self._topk.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.c_int, C.c_int,
@@ -178,6 +184,36 @@ class Oracle:
         return ((fi[:nq * f].reshape(f, nq).T.copy(), fd[:nq * f].reshape(f, nq).T.copy()),
                 (ri[:nr * r].reshape(r, nr).T.copy(), rd[:nr * r].reshape(r, nr).T.copy()),
                 flags.value)
+
+    def snn_shared(self, idx, include_self=True, prune=0.0):
+        """snnJaccardShared: (i, j, x) upper-triangle triplets, 1-based, in the
+        kernel's order."""
+        idx = np.asfortranarray(idx, dtype=np.int32)
+        n, k = idx.shape
+        m = C.c_int64(0)
+        self._check(self._shared(idx.ctypes.data, n, k, int(include_self), float(prune),
+                                 C.addressof(m), None, None, None))
+        ti = np.empty(max(m.value, 1), np.int32)
+        tj = np.empty(max(m.value, 1), np.int32)
+        tx = np.empty(max(m.value, 1), np.float64)
+        self._check(self._shared(idx.ctypes.data, n, k, int(include_self), float(prune),
+                                 C.addressof(m), ti.ctypes.data, tj.ctypes.data, tx.ctypes.data))
+        return ti[:m.value], tj[:m.value], tx[:m.value]
+
+    def snn_graph_shared(self, idx, include_self=True, prune=0.0):
+        """Returns (p, i, x) of the symmetric n x n dgCMatrix of edges = "shared"."""
+        idx = np.asfortranarray(idx, dtype=np.int32)
+        n, k = idx.shape
+        nnz = C.c_int64(0)
+        self._check(self._graph_shared(idx.ctypes.data, n, k, int(include_self), float(prune),
+                                       C.addressof(nnz), None, None, None))
+        p = np.empty(n + 1, np.int32)
+        i = np.empty(max(nnz.value, 1), np.int32)
+        x = np.empty(max(nnz.value, 1), np.float64)
+        self._check(self._graph_shared(idx.ctypes.data, n, k, int(include_self), float(prune),
+                                       C.addressof(nnz), p.ctypes.data, i.ctypes.data,
+                                       x.ctypes.data))
+        return p, i[:nnz.value], x[:nnz.value]
 
     def snn_graph(self, idx, include_self=True, prune=0.0, symmetrise=True):
         """Returns (p, i, x) of the n x n dgCMatrix."""

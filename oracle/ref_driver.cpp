@@ -33,6 +33,8 @@ void topKRowsAccum(const arma::mat& D, int k, bool decreasing, Rcpp::IntegerMatr
                    const Rcpp::IntegerVector& self_col, int ncores, int tile_rows);
 Rcpp::NumericMatrix snnJaccard(const Rcpp::IntegerMatrix& idx, bool include_self, int ncores,
                                bool verbose);
+Rcpp::List snnJaccardShared(const Rcpp::IntegerMatrix& idx, bool include_self, double prune,
+                            int ncores, bool verbose);
 
 namespace {
 
@@ -129,6 +131,27 @@ int ref_snn_jaccard(const int32_t* idx, int32_t n, int32_t k, int include_self, 
 
 const orc_backend g_ref_backend = {ref_slab, ref_topk_block, ref_topk_rows_accum, ref_snn_jaccard};
 
+int ref_snn_shared(const int32_t* idx, int32_t n, int32_t k, int include_self, double prune,
+                   int64_t* m_out, int32_t* ti, int32_t* tj, double* tx) {
+  try {
+    Rcpp::IntegerMatrix m = Rcpp::IntegerMatrix::view(const_cast<int32_t*>(idx), n, k);
+    Rcpp::List L = snnJaccardShared(m, include_self != 0, prune, g_threads, false);
+    Rcpp::IntegerVector I = L.get<Rcpp::IntegerVector>("i");
+    Rcpp::IntegerVector J = L.get<Rcpp::IntegerVector>("j");
+    Rcpp::NumericVector X = L.get<Rcpp::NumericVector>("x");
+    *m_out = (int64_t)I.size();
+    if (ti) {
+      std::memcpy(ti, I.begin(), sizeof(int32_t) * I.size());
+      std::memcpy(tj, J.begin(), sizeof(int32_t) * J.size());
+      std::memcpy(tx, X.begin(), sizeof(double) * X.size());
+    }
+    return ORC_OK;
+  } catch (const std::exception& e) {
+    g_msg = e.what();
+    return (g_msg.find("1-based") != std::string::npos) ? ORC_E_INDEX : ORC_E_ARG;
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -173,6 +196,18 @@ int ref_snn_graph(const int32_t* idx, int32_t n, int32_t k, int include_self, do
   g_msg.clear();
   return orc_snn_graph_with(&g_ref_backend, idx, n, k, include_self, prune, symmetrise, nnz_out,
                             out_p, out_i, out_x);
+}
+
+int ref_snn_shared_c(const int32_t* idx, int32_t n, int32_t k, int include_self, double prune,
+                     int64_t* m_out, int32_t* ti, int32_t* tj, double* tx) {
+  g_msg.clear();
+  return ref_snn_shared(idx, n, k, include_self, prune, m_out, ti, tj, tx);
+}
+int ref_snn_graph_shared(const int32_t* idx, int32_t n, int32_t k, int include_self, double prune,
+                         int64_t* nnz_out, int32_t* out_p, int32_t* out_i, double* out_x) {
+  g_msg.clear();
+  return orc_snn_graph_shared_with(ref_snn_shared, idx, n, k, include_self, prune, nnz_out, out_p,
+                                   out_i, out_x);
 }
 
 }  // extern "C"

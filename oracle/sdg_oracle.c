@@ -799,3 +799,142 @@ int orc_snn_graph(const int32_t* idx, int32_t n, int32_t k, int include_self,
   return orc_snn_graph_with(&g_self_backend, idx, n, k, include_self, prune, symmetrise,
                             nnz_out, out_p, out_i, out_x);
 }
+
+/* ------------------------------------------------------------------------- */
+/* sparseSNN(edges = "shared"): snnJaccardShared (src/snn.cpp:252-447) and    */
+/* its assembly (R/sparseSNN.R:202-219)                                       */
+/* ------------------------------------------------------------------------- */
+
+/* Neighbour sets as in snnJaccard (copy_indices :94-108, build_sets :119-141):
+ * NA dropped, self removed then added iff include_self, sorted, unique. */
+static int shared_sets(const int32_t* idx, int32_t n, int32_t k, int include_self,
+                       int32_t** sets_out, int32_t** size_out) {
+  if (n < 1 || k < 1) return fail(ORC_E_ARG, "'idx' must have at least one row and column.");
+  const int64_t N = n, S = (int64_t)k + 1;
+  for (int32_t t = 0; t < k; ++t)
+    for (int32_t i = 0; i < n; ++i) {
+      const int32_t v = idx[i + N * t];
+      if (v != NA_INT && (v < 1 || v > n))
+        return fail(ORC_E_INDEX,
+                    "'idx' entries must be NA or 1-based row indices in [1, nrow(idx)].");
+    }
+  int32_t* sets = malloc(sizeof(int32_t) * (size_t)(N * S));
+  int32_t* size = malloc(sizeof(int32_t) * (size_t)N);
+  if (!sets || !size) { free(sets); free(size); return fail(ORC_E_NOMEM, "out of memory"); }
+  for (int32_t i = 0; i < n; ++i) {
+    int32_t* s = sets + (int64_t)i * S;
+    int32_t c = 0;
+    if (include_self) s[c++] = i;
+    for (int32_t t = 0; t < k; ++t) {
+      const int32_t v = idx[i + N * t];
+      if (v == NA_INT) continue;
+      if (v - 1 != i) s[c++] = v - 1;
+    }
+    qsort(s, (size_t)c, sizeof(int32_t), cmp_int);
+    int32_t u = 0;
+    for (int32_t a = 0; a < c; ++a)
+      if (u == 0 || s[u - 1] != s[a]) s[u++] = s[a];
+    size[i] = u;
+  }
+  *sets_out = sets;
+  *size_out = size;
+  return ORC_OK;
+}
+
+int orc_snn_shared(const int32_t* idx, int32_t n, int32_t k, int include_self, double prune,
+                   int64_t* m_out, int32_t* ti, int32_t* tj, double* tx) {
+  int32_t *sets = NULL, *size = NULL;
+  int st = shared_sets(idx, n, k, include_self, &sets, &size);
+  if (st != ORC_OK) return st;
+  const int64_t N = n, S = (int64_t)k + 1;
+  /* inverted index R(m) = { i : m in N(i) } as CSR; filled in i order, so
+   * every R(m) is ascending (:319-339) */
+  int64_t* rp = calloc((size_t)N + 1, sizeof(int64_t));
+  int64_t tot = 0;
+  for (int32_t i = 0; i < n; ++i) tot += size[i];
+  int32_t* ri = malloc(sizeof(int32_t) * (size_t)(tot + 1));
+  int64_t* fill = malloc(sizeof(int64_t) * (size_t)(N + 1));
+  int32_t* acc = calloc((size_t)N, sizeof(int32_t));
+  int32_t* touched = malloc(sizeof(int32_t) * (size_t)N);
+  if (!rp || !ri || !fill || !acc || !touched) {
+    free(rp); free(ri); free(fill); free(acc); free(touched); free(sets); free(size);
+    return fail(ORC_E_NOMEM, "out of memory");
+  }
+  for (int32_t i = 0; i < n; ++i)
+    for (int32_t a = 0; a < size[i]; ++a) rp[sets[(int64_t)i * S + a] + 1] += 1;
+  for (int64_t m = 0; m < N; ++m) rp[m + 1] += rp[m];
+  for (int64_t m = 0; m < N; ++m) fill[m] = rp[m];
+  for (int32_t i = 0; i < n; ++i)
+    for (int32_t a = 0; a < size[i]; ++a) ri[fill[sets[(int64_t)i * S + a]]++] = i;
+  /* rows in order; per row the pairs (i, j > i) in first-touch order
+   * (accumulate_row :156-174), weights u / (ni + nj - u) (:179-181), kept
+   * when w > prune, 1-based */
+  int64_t m_count = 0;
+  for (int32_t i = 0; i < n; ++i) {
+    const int32_t* si = sets + (int64_t)i * S;
+    if (size[i] == 0) continue;
+    int64_t nt = 0;
+    for (int32_t a = 0; a < size[i]; ++a) {
+      const int32_t mm = si[a];
+      int64_t lo = rp[mm], hi = rp[mm + 1];
+      while (lo < hi) { const int64_t mid = (lo + hi) / 2; if (ri[mid] <= i) lo = mid + 1; else hi = mid; }
+      for (int64_t q = lo; q < rp[mm + 1]; ++q) {
+        const int32_t j = ri[q];
+        if (acc[j]++ == 0) touched[nt++] = j;
+      }
+    }
+    for (int64_t a = 0; a < nt; ++a) {
+      const int32_t j = touched[a];
+      const int64_t u = acc[j];
+      const double w = (double)u / (double)((int64_t)size[i] + size[j] - u);
+      if (w > prune) {
+        if (ti) { ti[m_count] = i + 1; tj[m_count] = j + 1; tx[m_count] = w; }
+        ++m_count;
+      }
+      acc[j] = 0;
+    }
+  }
+  *m_out = m_count;
+  free(rp); free(ri); free(fill); free(acc); free(touched); free(sets); free(size);
+  return ORC_OK;
+}
+
+/* sparseMatrix(i, j, x, symmetric = TRUE) of the upper-triangle triplets,
+ * then as(generalMatrix) / CsparseMatrix: every (i, j, w) stored at (i, j)
+ * and (j, i); no pair repeats and i != j, so there are no duplicates. */
+int orc_snn_graph_shared_with(orc_shared_fn f, const int32_t* idx, int32_t n, int32_t k,
+                              int include_self, double prune, int64_t* nnz_out, int32_t* out_p,
+                              int32_t* out_i, double* out_x) {
+  int64_t m = 0;
+  int st = f(idx, n, k, include_self, prune, &m, NULL, NULL, NULL);
+  if (st != ORC_OK) return st;
+  *nnz_out = 2 * m;
+  if (!out_p) return ORC_OK;
+  const int64_t N = n;
+  int32_t* ti = malloc(sizeof(int32_t) * (size_t)(m + 1));
+  int32_t* tj = malloc(sizeof(int32_t) * (size_t)(m + 1));
+  double* tx = malloc(sizeof(double) * (size_t)(m + 1));
+  trip* e = malloc(sizeof(trip) * (size_t)(2 * m + 1));
+  if (!ti || !tj || !tx || !e) { free(ti); free(tj); free(tx); free(e); return fail(ORC_E_NOMEM, "out of memory"); }
+  int64_t m2 = 0;
+  st = f(idx, n, k, include_self, prune, &m2, ti, tj, tx);
+  if (st != ORC_OK || m2 != m) { free(ti); free(tj); free(tx); free(e); return st != ORC_OK ? st : fail(ORC_E_ARG, "inconsistent edge count"); }
+  for (int64_t a = 0; a < m; ++a) {
+    const int64_t i = ti[a] - 1, j = tj[a] - 1;
+    e[2 * a].key = j * N + i; e[2 * a].ord = 0; e[2 * a].x = tx[a];          /* (i, j): column j */
+    e[2 * a + 1].key = i * N + j; e[2 * a + 1].ord = 0; e[2 * a + 1].x = tx[a];  /* (j, i): column i */
+  }
+  qsort(e, (size_t)(2 * m), sizeof(trip), cmp_trip);
+  for (int64_t c = 0; c <= N; ++c) out_p[c] = 0;
+  for (int64_t a = 0; a < 2 * m; ++a) out_p[e[a].key / N + 1] += 1;
+  for (int64_t c = 0; c < N; ++c) out_p[c + 1] += out_p[c];
+  for (int64_t a = 0; a < 2 * m; ++a) { out_i[a] = (int32_t)(e[a].key % N); out_x[a] = e[a].x; }
+  free(ti); free(tj); free(tx); free(e);
+  return ORC_OK;
+}
+
+int orc_snn_graph_shared(const int32_t* idx, int32_t n, int32_t k, int include_self, double prune,
+                         int64_t* nnz_out, int32_t* out_p, int32_t* out_i, double* out_x) {
+  return orc_snn_graph_shared_with(orc_snn_shared, idx, n, k, include_self, prune, nnz_out, out_p,
+                                   out_i, out_x);
+}

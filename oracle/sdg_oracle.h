@@ -87,6 +87,22 @@ int orc_snn_graph(const int32_t* idx, int32_t n, int32_t k, int include_self,
                   double prune, int symmetrise, int64_t* nnz_out,
                   int32_t* out_p, int32_t* out_i, double* out_x);
 
+/* snnJaccardShared: the 1-based upper-triangle triplets (i < j) of every pair
+ * sharing a neighbour with weight > prune, rows ascending, each row's pairs in
+ * first-touch order.  Two calls: with ti == NULL only *m_out is written. */
+int orc_snn_shared(const int32_t* idx, int32_t n, int32_t k, int include_self, double prune,
+                   int64_t* m_out, int32_t* ti, int32_t* tj, double* tx);
+typedef int (*orc_shared_fn)(const int32_t*, int32_t, int32_t, int, double, int64_t*, int32_t*,
+                             int32_t*, double*);
+
+/* sparseSNN(edges = "shared") assembly: the symmetric n x n dgCMatrix (both
+ * triangles, no diagonal).  Same two-call protocol as orc_snn_graph. */
+int orc_snn_graph_shared(const int32_t* idx, int32_t n, int32_t k, int include_self, double prune,
+                         int64_t* nnz_out, int32_t* out_p, int32_t* out_i, double* out_x);
+int orc_snn_graph_shared_with(orc_shared_fn f, const int32_t* idx, int32_t n, int32_t k,
+                              int include_self, double prune, int64_t* nnz_out, int32_t* out_p,
+                              int32_t* out_i, double* out_x);
+
 /* Plug-in points so the same orchestration can drive the reference's own
  * kernels (oracle/_ref) instead of this file's restatement. */
 typedef struct {
