@@ -168,6 +168,16 @@ SDG_API int sdg_snn_graph(sdg_ctx* ctx, const int32_t* idx, int32_t n, int32_t k
                           int include_self, double prune, int symmetrise, int64_t* nnz,
                           int32_t* p, int32_t* i, double* x);
 
+/* sparseSNN(idx, include_self, prune, edges = "shared") as the slots of the
+ * symmetric n x n dgCMatrix: every pair (i, j), i != j, whose neighbour sets
+ * intersect, weighted |N(i) n N(j)| / |N(i) u N(j)|, kept when the weight
+ * exceeds prune (no diagonal).  Same two-call protocol as sdg_snn_graph.
+ * Replaces snnJaccardShared (src/snn.cpp:252-447, R/RcppExports.R:16-18) plus the
+ * Matrix assembly of R/sparseSNN.R:202-219. */
+SDG_API int sdg_snn_graph_shared(sdg_ctx* ctx, const int32_t* idx, int32_t n, int32_t k,
+                                 int include_self, double prune, int64_t* nnz, int32_t* p,
+                                 int32_t* i, double* x);
+
 /* ---- device-resident inputs (serving / batching) ---------------------------- */
 
 /* A CSC matrix uploaded once and kept in device memory, with its per-column

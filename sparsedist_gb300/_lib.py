@@ -31,7 +31,8 @@ EXPORTED = ["sdg_version", "sdg_last_error", "sdg_ctx_create", "sdg_ctx_destroy"
             "sdg_last_stats", "sdg_ctx_set_engine", "sdg_kernel_time", "sdg_knn_block",
             "sdg_server_create", "sdg_server_submit", "sdg_server_wait", "sdg_server_result",
             "sdg_server_cancel", "sdg_server_stats", "sdg_server_destroy",
-            "sdg_matrix_upload_device", "sdg_dense_upload", "sdg_dense_free", "sdg_dense_knn_block"]
+            "sdg_matrix_upload_device", "sdg_dense_upload", "sdg_dense_free", "sdg_dense_knn_block",
+            "sdg_snn_graph_shared"]
 
 
 class SdgError(RuntimeError):
@@ -75,6 +76,8 @@ def load() -> C.CDLL:
             lib.sdg_topk_rows_accum.argtypes = [v, v, C.c_int64, C.c_int64, C.c_int, C.c_int, v, v,
                                                 C.c_int32, v]
             lib.sdg_snn_jaccard.argtypes = [v, v, C.c_int32, C.c_int32, C.c_int, v]
+            lib.sdg_snn_graph_shared.argtypes = [v, v, C.c_int32, C.c_int32, C.c_int, C.c_double,
+                                                 v, v, v, v]
             lib.sdg_snn_graph.argtypes = [v, v, C.c_int32, C.c_int32, C.c_int, C.c_double, C.c_int,
                                           v, v, v, v]
             lib.sdg_knn.argtypes = [v, v, v, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,

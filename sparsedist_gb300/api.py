@@ -331,20 +331,24 @@ def sparseSNN(idx, include_self=True, prune=0, symmetrise=None, edges=("knn", "s
             ncores > INT_MAX):
         raise ValueError("'ncores' must be a non-negative integer no larger than "
                          ".Machine$integer.max.")
-    if edges == "shared":
-        raise NotImplementedError("edges = \"shared\" is not provided by sparsedist_gb300")
     c = _ctx(ctx)
     nnz = np.zeros(1, np.int64)
-    _lib.check(c.lib.sdg_snn_graph(c.handle, M.ctypes.data, n, k, int(bool(include_self)),
-                                   float(prune), int(bool(symmetrise)), nnz.ctypes.data, None,
-                                   None, None))
+    if edges == "shared":
+        # snnJaccardShared + sparseMatrix(symmetric = TRUE) (R/sparseSNN.R:202-219)
+        def call(p_, i_, x_):
+            _lib.check(c.lib.sdg_snn_graph_shared(c.handle, M.ctypes.data, n, k, int(bool(include_self)),
+                                                  float(prune), nnz.ctypes.data, p_, i_, x_))
+    else:
+        def call(p_, i_, x_):
+            _lib.check(c.lib.sdg_snn_graph(c.handle, M.ctypes.data, n, k, int(bool(include_self)),
+                                           float(prune), int(bool(symmetrise)), nnz.ctypes.data,
+                                           p_, i_, x_))
+    call(None, None, None)
     m = int(nnz[0])
     p = np.empty(n + 1, np.int32)
     i = np.empty(max(m, 1), np.int32)
     x = np.empty(max(m, 1), np.float64)
-    _lib.check(c.lib.sdg_snn_graph(c.handle, M.ctypes.data, n, k, int(bool(include_self)),
-                                   float(prune), int(bool(symmetrise)), nnz.ctypes.data,
-                                   p.ctypes.data, i.ctypes.data, x.ctypes.data))
+    call(p.ctypes.data, i.ctypes.data, x.ctypes.data)
     _progress(verbose)
     g = sp.csc_matrix((x[:m], i[:m], p), shape=(n, n))
     g.rownames = rown

@@ -827,6 +827,50 @@ SDG_API int sdg_snn_graph(sdg_ctx* c, const int32_t* idx, int32_t n, int32_t k, 
   });
 }
 
+SDG_API int sdg_snn_graph_shared(sdg_ctx* c, const int32_t* idx, int32_t n, int32_t k, int include_self,
+                                 double prune, int64_t* nnz, int32_t* p, int32_t* i, double* x) {
+  return guarded([&] {
+    if (!c) fail(SDG_E_ARG, "ctx must not be NULL");
+    if (!nnz) fail(SDG_E_ARG, "nnz must not be NULL");
+    CK(cudaSetDevice(c->device));
+    if (!(prune >= 0.0 && prune <= 1.0))
+      fail(SDG_E_ARG, "'prune' must be a finite number between 0 and 1.");
+    if (n < 1 || k < 1) fail(SDG_E_ARG, "'idx' must have at least one row and column.");
+    cudaStream_t s = c->stream;
+    const int64_t total = (int64_t)n * k;
+    DevBuf di(sizeof(int32_t) * (size_t)total, s);
+    CK(cudaMemcpyAsync(di.p, idx, sizeof(int32_t) * (size_t)total, cudaMemcpyHostToDevice, s));
+    DevBuf err(sizeof(int), s);
+    CK(cudaMemsetAsync(err.p, 0, sizeof(int), s));
+    launch_snn_check(di.as<int32_t>(), n, k, err.as<int>(), s);
+    int herr = 0;
+    CK(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (herr)
+      fail(SDG_E_INDEX, "'idx' entries must be NA or 1-based row indices in [1, nrow(idx)].");
+    DevBuf sets(sizeof(int32_t) * (size_t)n * ((size_t)k + 1), s), sizes(sizeof(int32_t) * (size_t)n, s);
+    launch_snn_sets(di.as<int32_t>(), n, k, include_self, sets.as<int32_t>(), sizes.as<int32_t>(), s);
+    int32_t *dp = nullptr, *drow = nullptr;
+    double* dx = nullptr;
+    int64_t m = 0;
+    const int st = snn_shared_build(sets.as<int32_t>(), sizes.as<int32_t>(), n, k, prune, &m, &dp, &drow, &dx, s);
+    if (st) cuda_check((cudaError_t)st, "snn_shared_build");
+    DevBuf hp, hi, hx;
+    hp.p = dp; hp.s = s;
+    hi.p = drow; hi.s = s;
+    hx.p = dx; hx.s = s;
+    *nnz = m;
+    if (p) {
+      CK(cudaMemcpyAsync(p, dp, sizeof(int32_t) * ((size_t)n + 1), cudaMemcpyDeviceToHost, s));
+      if (m > 0) {
+        CK(cudaMemcpyAsync(i, drow, sizeof(int32_t) * (size_t)m, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(x, dx, sizeof(double) * (size_t)m, cudaMemcpyDeviceToHost, s));
+      }
+    }
+    CK(cudaStreamSynchronize(s));
+  });
+}
+
 SDG_API int sdg_knn(sdg_ctx* c, const sdg_csc* X, const sdg_csc* Y, int method, int dist, int k,
                     int include_self, int drop_degenerate, int block_size, int ncores,
                     int32_t* idx, double* dist_out, int* k_eff, int* flags) {

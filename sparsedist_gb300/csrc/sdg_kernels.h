@@ -108,6 +108,11 @@ void launch_snn_weights(const int32_t* idx, int32_t n, int32_t k, const int32_t*
 // Graph assembly: returns nnz through *nnz_host (synchronises the stream).
 // Buffers are allocated from the stream-ordered pool and returned; the caller
 // frees them with cudaFreeAsync.
+// sparseSNN(edges = "shared"): the symmetric graph of every pair sharing a
+// neighbour with weight > prune, from the device neighbour sets (sets: n x
+// (k + 1), sizes: n); outputs as snn_graph_build.
+int snn_shared_build(const int32_t* d_sets, const int32_t* d_sizes, int32_t n, int32_t k, double prune,
+                     int64_t* nnz_host, int32_t** d_p, int32_t** d_i, double** d_x, cudaStream_t s);
 int snn_graph_build(const int32_t* d_idx, const double* d_w, int32_t n, int32_t k,
                     double prune, int symmetrise, int64_t* nnz_host, int32_t** d_p,
                     int32_t** d_i, double** d_x, cudaStream_t s);

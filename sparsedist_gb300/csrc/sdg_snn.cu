@@ -7,6 +7,8 @@
 // reference.  The graph (R/sparseSNN.R:221-250) is assembled on the device:
 // kept triplets -> (column, row) keys -> radix sort -> unique -> CSC.
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_run_length_encode.cuh>
+#include <cub/device/device_scan.cuh>
 #include <cub/device/device_select.cuh>
 
 #include "sdg_kernels.h"
@@ -73,6 +75,86 @@ __global__ void k_snn_colptr(const uint64_t* keys, int64_t m, int32_t n, int32_t
 __global__ void k_snn_rows(const uint64_t* keys, int64_t m, int32_t n, int32_t* rows) {
   const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (a < m) rows[a] = (int32_t)(keys[a] % (uint64_t)n);
+}
+
+// ---- sparseSNN(edges = "shared"): snnJaccardShared (src/snn.cpp:252-447) ---
+//
+// The pairs (i, j), i < j, sharing a neighbour are the nonzeros of the upper
+// triangle of A A^T (A the n x n neighbourhood-membership matrix); their
+// overlap counts u are found by sorting instead of a per-row accumulator:
+// every (i, m in N(i), j in R(m), j > i) emits the key i n + j, a radix sort
+// brings equal keys together and a run-length encode counts them.  R(m) =
+// {i : m in N(i)} comes from a stable sort of the (m, i) pairs, so it is
+// ascending and j > i is a binary search.  Weights u / (|N(i)| + |N(j)| - u)
+// are the reference's integer counts and one IEEE division.
+
+// (m, i) for every member m of every set N(i), in (i, position) order
+__global__ void k_shared_pairs(const int32_t* sets, const int32_t* sizes, const int64_t* off, int32_t n,
+                               int32_t k, uint32_t* mkeys, int32_t* ivals) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int32_t* S = sets + i * (int64_t)(k + 1);
+  const int64_t o = off[i];
+  for (int32_t a = 0; a < sizes[i]; ++a) { mkeys[o + a] = (uint32_t)S[a]; ivals[o + a] = (int32_t)i; }
+}
+
+// rev_ptr[m] = first position of key m in the sorted member keys
+__global__ void k_shared_revptr(const uint32_t* keys, int64_t t, int32_t n, int64_t* rp) {
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (m > n) return;
+  int64_t lo = 0, hi = t;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (keys[mid] < (uint32_t)m) lo = mid + 1; else hi = mid;
+  }
+  rp[m] = lo;
+}
+
+// first position in R(m) holding a row > i
+__device__ __forceinline__ int64_t shared_after(const int32_t* rev, int64_t lo, int64_t hi, int32_t i) {
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (rev[mid] <= i) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+// per (i, member slot): how many j > i share that member
+__global__ void k_shared_count(const int32_t* mk_by_i, const int32_t* iv_by_i, int64_t t, const int64_t* rp,
+                               const int32_t* rev, int64_t* cnt) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= t) return;
+  const int32_t m = mk_by_i[e], i = iv_by_i[e];
+  cnt[e] = rp[m + 1] - shared_after(rev, rp[m], rp[m + 1], i);
+}
+
+__global__ void k_shared_emit(const int32_t* mk_by_i, const int32_t* iv_by_i, int64_t t, const int64_t* rp,
+                              const int32_t* rev, const int64_t* pos, int32_t n, uint64_t* keys) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= t) return;
+  const int32_t m = mk_by_i[e], i = iv_by_i[e];
+  const int64_t q0 = shared_after(rev, rp[m], rp[m + 1], i);
+  uint64_t* out = keys + pos[e];
+  for (int64_t q = q0; q < rp[m + 1]; ++q) out[q - q0] = (uint64_t)i * (uint64_t)n + (uint64_t)rev[q];
+}
+
+// one run = one pair (i, j) with its overlap count: weight, prune, and both
+// triangle entries as (column, row) keys
+__global__ void k_shared_weights(const uint64_t* ukeys, const int32_t* counts, const int64_t* nruns,
+                                 const int32_t* sizes, int32_t n, double prune, uint64_t* okeys,
+                                 double* ovals, unsigned long long* kept) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= *nruns) return;
+  const uint64_t key = ukeys[r];
+  const uint64_t i = key / (uint64_t)n, j = key % (uint64_t)n;
+  const int64_t u = counts[r];
+  const double w = (double)u / (double)((int64_t)sizes[i] + sizes[j] - u);
+  if (!(w > prune)) return;
+  const unsigned long long at = atomicAdd(kept, 2ull);
+  okeys[at] = j * (uint64_t)n + i;        // (row i, column j)
+  ovals[at] = w;
+  okeys[at + 1] = i * (uint64_t)n + j;    // (row j, column i)
+  ovals[at + 1] = w;
 }
 
 int key_bits(int32_t n) {
@@ -164,6 +246,132 @@ int snn_graph_build(const int32_t* d_idx, const double* d_w, int32_t n, int32_t 
   *d_p = p;
   *d_i = rows;
   *d_x = uvals;   // values already compacted in key order
+  return 0;
+}
+
+int snn_shared_build(const int32_t* d_sets, const int32_t* d_sizes, int32_t n, int32_t k, double prune,
+                     int64_t* nnz_host, int32_t** d_p, int32_t** d_i, double** d_x, cudaStream_t s) {
+  // set sizes -> offsets of the (m, i) member pairs
+  int64_t *off = nullptr, *rp = nullptr, *cnt = nullptr, *pos = nullptr, *nruns = nullptr;
+  void* tmp = nullptr;
+  size_t tb = 0, tb2 = 0;
+  SDG_TRY(cudaMallocAsync(&off, sizeof(int64_t) * ((size_t)n + 1), s));
+  {
+    // exclusive sum of the set sizes, widened to int64 (a strided copy into
+    // the low words of a zeroed int64 array; sizes are non-negative)
+    int64_t* sz64 = nullptr;
+    SDG_TRY(cudaMallocAsync(&sz64, sizeof(int64_t) * ((size_t)n + 1), s));
+    SDG_TRY(cudaMemsetAsync(sz64, 0, sizeof(int64_t) * ((size_t)n + 1), s));
+    SDG_TRY(cudaMemcpy2DAsync(sz64, sizeof(int64_t), d_sizes, sizeof(int32_t), sizeof(int32_t), (size_t)n,
+                              cudaMemcpyDeviceToDevice, s));
+    SDG_TRY(cub::DeviceScan::ExclusiveSum(nullptr, tb, sz64, off, (int)n + 1, s));
+    SDG_TRY(cudaMallocAsync(&tmp, tb + 16, s));
+    SDG_TRY(cub::DeviceScan::ExclusiveSum(tmp, tb, sz64, off, (int)n + 1, s));
+    SDG_TRY(cudaFreeAsync(tmp, s));
+    SDG_TRY(cudaFreeAsync(sz64, s));
+    tmp = nullptr;
+  }
+  int64_t t = 0;
+  SDG_TRY(cudaMemcpyAsync(&t, off + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  SDG_TRY(cudaStreamSynchronize(s));
+  uint32_t *mk = nullptr, *mk2 = nullptr;
+  int32_t *iv = nullptr, *rev = nullptr;
+  SDG_TRY(cudaMallocAsync(&mk, sizeof(uint32_t) * ((size_t)t + 1), s));
+  SDG_TRY(cudaMallocAsync(&mk2, sizeof(uint32_t) * ((size_t)t + 1), s));
+  SDG_TRY(cudaMallocAsync(&iv, sizeof(int32_t) * ((size_t)t + 1), s));
+  SDG_TRY(cudaMallocAsync(&rev, sizeof(int32_t) * ((size_t)t + 1), s));
+  SDG_TRY(cudaMallocAsync(&rp, sizeof(int64_t) * ((size_t)n + 1), s));
+  SDG_TRY(cudaMallocAsync(&cnt, sizeof(int64_t) * ((size_t)t + 1), s));
+  SDG_TRY(cudaMallocAsync(&pos, sizeof(int64_t) * ((size_t)t + 1), s));
+  k_shared_pairs<<<blocks_for(n, 128), 128, 0, s>>>(d_sets, d_sizes, off, n, k, mk, iv);
+  // R(m): a stable sort by m keeps each R(m) in ascending i
+  int mbits = 1;
+  while (mbits < 32 && ((uint64_t)n >> mbits) != 0) ++mbits;
+  SDG_TRY(cub::DeviceRadixSort::SortPairs(nullptr, tb, mk, mk2, iv, rev, (int)t, 0, mbits, s));
+  SDG_TRY(cudaMallocAsync(&tmp, tb + 16, s));
+  if (t > 0) SDG_TRY(cub::DeviceRadixSort::SortPairs(tmp, tb, mk, mk2, iv, rev, (int)t, 0, mbits, s));
+  SDG_TRY(cudaFreeAsync(tmp, s));
+  tmp = nullptr;
+  k_shared_revptr<<<blocks_for((int64_t)n + 1, 256), 256, 0, s>>>(mk2, t, n, rp);
+  // the members in (i, position) order again (mk / iv were sort inputs, unchanged)
+  if (t > 0) {
+    k_shared_count<<<blocks_for(t, 256), 256, 0, s>>>(reinterpret_cast<const int32_t*>(mk), iv, t, rp, rev, cnt);
+    SDG_TRY(cub::DeviceScan::ExclusiveSum(nullptr, tb, cnt, pos, (int)t, s));
+    SDG_TRY(cudaMallocAsync(&tmp, tb + 16, s));
+    SDG_TRY(cub::DeviceScan::ExclusiveSum(tmp, tb, cnt, pos, (int)t, s));
+    SDG_TRY(cudaFreeAsync(tmp, s));
+    tmp = nullptr;
+  }
+  int64_t E = 0;
+  if (t > 0) {
+    int64_t last_pos = 0, last_cnt = 0;
+    SDG_TRY(cudaMemcpyAsync(&last_pos, pos + (t - 1), sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    SDG_TRY(cudaMemcpyAsync(&last_cnt, cnt + (t - 1), sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    SDG_TRY(cudaStreamSynchronize(s));
+    E = last_pos + last_cnt;
+  }
+  if (E >= ((int64_t)1 << 31)) return (int)cudaErrorInvalidValue;   // beyond one CUB pass
+  uint64_t *keys = nullptr, *keys2 = nullptr, *okeys = nullptr, *okeys2 = nullptr;
+  int32_t* counts = nullptr;
+  double *ovals = nullptr, *ovals2 = nullptr;
+  unsigned long long* kept = nullptr;
+  SDG_TRY(cudaMallocAsync(&keys, sizeof(uint64_t) * ((size_t)E + 1), s));
+  SDG_TRY(cudaMallocAsync(&keys2, sizeof(uint64_t) * ((size_t)E + 1), s));
+  SDG_TRY(cudaMallocAsync(&counts, sizeof(int32_t) * ((size_t)E + 1), s));
+  SDG_TRY(cudaMallocAsync(&nruns, sizeof(int64_t), s));
+  SDG_TRY(cudaMallocAsync(&kept, sizeof(unsigned long long), s));
+  SDG_TRY(cudaMemsetAsync(nruns, 0, sizeof(int64_t), s));
+  SDG_TRY(cudaMemsetAsync(kept, 0, sizeof(unsigned long long), s));
+  if (E > 0) {
+    k_shared_emit<<<blocks_for(t, 256), 256, 0, s>>>(reinterpret_cast<const int32_t*>(mk), iv, t, rp, rev, pos, n,
+                                                     keys);
+    const int bits = key_bits(n);
+    SDG_TRY(cub::DeviceRadixSort::SortKeys(nullptr, tb, keys, keys2, (int)E, 0, bits, s));
+    SDG_TRY(cub::DeviceRunLengthEncode::Encode(nullptr, tb2, keys2, keys, counts, nruns, (int)E, s));
+    if (tb2 > tb) tb = tb2;
+    SDG_TRY(cudaMallocAsync(&tmp, tb + 16, s));
+    SDG_TRY(cub::DeviceRadixSort::SortKeys(tmp, tb, keys, keys2, (int)E, 0, bits, s));
+    SDG_TRY(cub::DeviceRunLengthEncode::Encode(tmp, tb, keys2, keys, counts, nruns, (int)E, s));
+    SDG_TRY(cudaFreeAsync(tmp, s));
+    tmp = nullptr;
+  }
+  int64_t runs = 0;
+  SDG_TRY(cudaMemcpyAsync(&runs, nruns, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  SDG_TRY(cudaStreamSynchronize(s));
+  SDG_TRY(cudaMallocAsync(&okeys, sizeof(uint64_t) * ((size_t)(2 * runs) + 1), s));
+  SDG_TRY(cudaMallocAsync(&okeys2, sizeof(uint64_t) * ((size_t)(2 * runs) + 1), s));
+  SDG_TRY(cudaMallocAsync(&ovals, sizeof(double) * ((size_t)(2 * runs) + 1), s));
+  SDG_TRY(cudaMallocAsync(&ovals2, sizeof(double) * ((size_t)(2 * runs) + 1), s));
+  if (runs > 0)
+    k_shared_weights<<<blocks_for(runs, 256), 256, 0, s>>>(keys, counts, nruns, d_sizes, n, prune, okeys, ovals,
+                                                          kept);
+  unsigned long long m_host = 0;
+  SDG_TRY(cudaMemcpyAsync(&m_host, kept, sizeof m_host, cudaMemcpyDeviceToHost, s));
+  SDG_TRY(cudaStreamSynchronize(s));
+  const int64_t m = (int64_t)m_host;
+  if (m > 0) {
+    const int bits = key_bits(n);
+    SDG_TRY(cub::DeviceRadixSort::SortPairs(nullptr, tb, okeys, okeys2, ovals, ovals2, (int)m, 0, bits, s));
+    SDG_TRY(cudaMallocAsync(&tmp, tb + 16, s));
+    SDG_TRY(cub::DeviceRadixSort::SortPairs(tmp, tb, okeys, okeys2, ovals, ovals2, (int)m, 0, bits, s));
+    SDG_TRY(cudaFreeAsync(tmp, s));
+    tmp = nullptr;
+  }
+  int32_t* p = nullptr;
+  int32_t* rows = nullptr;
+  SDG_TRY(cudaMallocAsync(&p, sizeof(int32_t) * ((size_t)n + 1), s));
+  SDG_TRY(cudaMallocAsync(&rows, sizeof(int32_t) * ((size_t)m + 1), s));
+  k_snn_colptr<<<blocks_for((int64_t)n + 1, 256), 256, 0, s>>>(okeys2, m, n, p);
+  if (m > 0) k_snn_rows<<<blocks_for(m, 256), 256, 0, s>>>(okeys2, m, n, rows);
+  SDG_TRY(cudaGetLastError());
+  for (void* q : {(void*)off, (void*)rp, (void*)cnt, (void*)pos, (void*)nruns, (void*)mk, (void*)mk2, (void*)iv,
+                  (void*)rev, (void*)keys, (void*)keys2, (void*)counts, (void*)kept, (void*)okeys,
+                  (void*)okeys2, (void*)ovals})
+    SDG_TRY(cudaFreeAsync(q, s));
+  *nnz_host = m;
+  *d_p = p;
+  *d_i = rows;
+  *d_x = ovals2;
   return 0;
 }
 
