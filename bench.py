@@ -65,7 +65,8 @@ def parse():
     ap.add_argument("--cpu-cols", type=int, default=256, help="query columns of the CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--config", default="c2", choices=["c2", "c1", "c3", "serve"],
+    ap.add_argument("--dist-cols", type=int, default=10000)
+    ap.add_argument("--config", default="c2", choices=["c2", "c1", "c3", "serve", "dist"],
                     help="c2: the default line (configuration 2); c1: the CPU-runnable "
                          "configuration 1; serve: configuration 5, the serving loop")
     ap.add_argument("--serve-ref-cols", type=int, default=1000000)
@@ -246,6 +247,73 @@ def run_c1(args):
     print(json.dumps({"metric": "kNN query columns/s, configuration 1 (e2e through the Python API)",
                       "config": {"workload": "2000x10000 CSC, 2% uniform, |N(0,1)|, k=15, self-search"},
                       "cores": os.cpu_count(), "results": out}))
+
+
+def run_dist(args):
+    """Full-matrix sparseDist(X, full = TRUE) on configuration 1's matrix
+    (2,000 x dist_cols CSC, 2 % uniform pattern, |N(0,1)| values), binary,
+    cosine and euclidean: the C-ABI call with host buffers (CSC in, the dense
+    n x n result out) per step, the pair kernel timed by CUDA events inside
+    it, bit-identical check against the oracle on a column sample, and the
+    oracle's single-matrix form on the host cores on a bounded sample."""
+    import scipy.sparse as sp
+    import torch
+    from sparsedist_gb300 import _lib, synth
+    from oracle import build as obuild
+    from oracle.pyoracle import Oracle
+    n = args.dist_cols
+    X = synth.uniform_csc(2000, n, 0.02, seed=1)
+    obuild.build_oracle()
+    threads = os.cpu_count() or 1
+    orc = Oracle(threads=threads)
+    ctx = _lib.Context()
+    held = _lib.HeldCSC(2000, n, X.indptr, X.indices, X.data)
+    D = np.empty((n, n), np.float64)
+    hbm_peak, _, peak_kind = measured_peaks()
+    out = {}
+    for method in ("binary", "cosine", "euclidean"):
+        code = METHOD_CODES[method]
+
+        def call():
+            _lib.check(ctx.lib.sdg_dist(ctx.handle, code, 1, held.ref, 1, 0, D.ctypes.data))
+
+        for _ in range(args.warmup):
+            call()
+        ctx.kernel_time()
+        with ClockSampler(0) as clk:
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                call()
+            e2e_s = (time.perf_counter() - t0) / args.steps
+        kms, kl = ctx.kernel_time()
+        pairs = n * (n - 1) / 2
+        sample = min(n, 400)
+        Xs = X[:, :sample]
+        want = orc.dist_single(method, Xs, True, False, True)
+        same = bool(np.array_equal(D.T[:sample, :sample].view(np.uint64), want.view(np.uint64)))
+        t0 = time.perf_counter()
+        cs = min(n, 3000)
+        orc.dist_single(method, X[:, :cs], True, False, True)
+        cpu_pairs_s = cs * (cs - 1) / 2 / (time.perf_counter() - t0)
+        kern_s = kms / 1000.0 / max(kl, 1)
+        alg = 8.0 * n * n / 2 + 12.0 * X.nnz      # lower triangle written + the CSC read
+        out[method] = {
+            "pairs_per_s_e2e": pairs / e2e_s, "ms_per_step_e2e": 1000 * e2e_s,
+            "pairs_per_s_kernel": pairs / kern_s, "kernel_ms": 1000 * kern_s,
+            "d2h_bytes_per_step": 8 * n * n, "h2d_bytes_per_step": int(4 * (n + 1) + 12 * X.nnz),
+            "roofline": {"bound": "hbm", "achieved": alg / kern_s / 1e9, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": alg / kern_s / 1e9 / hbm_peak,
+                         "peak_kind": peak_kind, "kernel": "k_self_slab",
+                         "alg_bytes_per_launch": alg},
+            "cpu_baseline": {"value": cpu_pairs_s, "unit": "pairs/s", "cores": threads, "kind": "port",
+                             "sample": "sparseDist(X[, 1:%d], full = TRUE)" % cs},
+            "identical_on_%d_columns" % sample: same, "clocks": clk.summary()}
+        torch.cuda.synchronize()
+    print(json.dumps({"metric": "full-matrix sparseDist column pairs/s",
+                      "config": {"workload": "sparseDist(X, full = TRUE, diag = FALSE), X 2000x%d CSC, "
+                                             "2%% uniform, |N(0,1)|" % n},
+                      "dtype": "f64", "data": "synthetic", "steps": args.steps, "warmup": args.warmup,
+                      "results": out}))
 
 
 def run_serve(args):
@@ -433,6 +501,9 @@ def main():
         return
     if args.config == "serve":
         run_serve(args)
+        return
+    if args.config == "dist":
+        run_dist(args)
         return
     if args.impl == "reference":
         run_reference(args)

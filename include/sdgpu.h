@@ -40,7 +40,8 @@ typedef enum {
   SDG_EUCLIDEAN = 2,
   SDG_MANHATTAN = 3,
   SDG_PEARSON = 4,
-  SDG_JS = 5          /* Jensen-Shannon distance sqrt(JSD) */
+  SDG_JS = 5,         /* Jensen-Shannon distance sqrt(JSD) */
+  SDG_COVARIANCE = 6  /* sample covariance (N - 1); a coefficient, kNN keeps the largest */
 } sdg_method;
 
 typedef enum {
@@ -94,12 +95,24 @@ SDG_API int sdg_ctx_reset_cancel(sdg_ctx* ctx);
 /* Distance / similarity slab between the columns of m and m2:
  * D is ncol(m) x ncol(m2), D(i, j) = method(column i of m, column j of m2).
  * Replaces fastJacc2 / fastCosine2 / fastEuclidean2 / fastManhattan2 /
- * fastCorr2 / fastJS2 (src/sparseDist.cpp:559, :967, :833, :734, :403, :1074;
- * .Call stubs R/RcppExports.R:29-67).  dist selects 1 - similarity for
- * binary / cosine / pearson and must be 1 for the other methods' kernels
- * (which ignore it, as the reference does). */
+ * fastCorr2 / fastJS2 / fastCov2 (src/sparseDist.cpp:559, :967, :833, :734,
+ * :403, :1074, :481; .Call stubs R/RcppExports.R:24-74).  dist selects
+ * 1 - similarity for binary / cosine / pearson and is ignored by the other
+ * methods' kernels, as the reference ignores it. */
 SDG_API int sdg_dist_cross(sdg_ctx* ctx, int method, int dist, const sdg_csc* m,
                            const sdg_csc* m2, double* D);
+
+/* Single-matrix form: D is the reference's dense ncol(m) x ncol(m) accumulator
+ * (column-major) before its dense-or-sparse return, i.e. the pair (i, j),
+ * i < j, at D(j, i) and, with full, also at D(i, j); the rest 0.  The
+ * diagonal: 0 / 1 (dist / similarity) for binary, cosine and pearson; the
+ * self pair for euclidean, manhattan and covariance with diag, else 0; 0 for
+ * js.  Replaces fastJacc / fastCosine / fastEuclidean / fastManhattan /
+ * fastCorr / fastJS / fastCov (src/sparseDist.cpp:620, :918, :786, :688,
+ * :339, :1021, :450; .Call stubs R/RcppExports.R:20-70), called by
+ * sparseDist(X) at R/sparseDist.R:162-171. */
+SDG_API int sdg_dist(sdg_ctx* ctx, int method, int dist, const sdg_csc* m, int full, int diag,
+                     double* D);
 
 /* Per-column top-k of a dense block D (nrow x ncol, column-major).
  * idx / dist are ncol x k.  self_row[b] is 0 or the 1-based row excluded for

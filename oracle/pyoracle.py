@@ -22,7 +22,7 @@ NA_INT = np.int32(-(2 ** 31))
 NA_REAL_BITS = np.uint64(0x7FF00000000007A2)
 
 METHODS = {"binary": 0, "jaccard": 0, "cosine": 1, "euclidean": 2, "manhattan": 3,
-           "pearson": 4, "js": 5}
+           "pearson": 4, "js": 5, "covariance": 6}
 
 
 class OracleError(RuntimeError):
@@ -85,6 +85,8 @@ class Oracle:
             self._err = self.lib.orc_last_error
             self.lib.orc_set_threads(int(threads))
         self._slab = getattr(self.lib, pre + ("slab_c" if ref else "slab"))
+        self._dist = getattr(self.lib, pre + ("dist_c" if ref else "dist"))
+        self._dist.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
         self._topk = getattr(self.lib, pre + ("topk_block_c" if ref else "topk_block"))
         self._rows = getattr(self.lib, pre + ("topk_rows_accum_c" if ref else "topk_rows_accum"))
         self._snn = getattr(self.lib, pre + ("snn_jaccard_c" if ref else "snn_jaccard"))
@@ -120,6 +122,16 @@ class Oracle:
         D = np.zeros((b.ncol, a.ncol), dtype=np.float64)     # column-major nc x nc2
         self._check(self._slab(METHODS[method], int(dist), C.byref(a.s), C.byref(b.s),
                                _ptr(D, C.c_double)))
+        return D.T
+
+    def dist_single(self, method, m, full=False, diag=False, dist=True):
+        """Single-matrix sparseDist(X): the dense n x n accumulator of the
+        reference's fastJacc / fastCosine / ... / fastCov (before the R-level
+        dense-or-sparse storage choice)."""
+        a = _Held(m)
+        D = np.zeros((a.ncol, a.ncol), dtype=np.float64)     # column-major n x n
+        self._check(self._dist(METHODS[method], int(dist), C.byref(a.s), int(bool(full)),
+                               int(bool(diag)), _ptr(D, C.c_double)))
         return D.T
 
     def topk_block(self, D, k, decreasing, self_row):

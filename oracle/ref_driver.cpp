@@ -26,6 +26,14 @@ arma::mat fastEuclidean2(const arma::sp_mat& m, const arma::sp_mat& m2, int ncor
 arma::mat fastManhattan2(const arma::sp_mat& m, const arma::sp_mat& m2, int ncores, bool verbose);
 SEXP fastCorr2(const arma::sp_mat& m, const arma::sp_mat& m2, int ncores, bool verbose, bool dist);
 arma::mat fastJS2(const arma::mat& m, const arma::mat& m2, int ncores, bool verbose);
+arma::sp_mat fastCov2(const arma::sp_mat& m, const arma::sp_mat& m2, int ncores, bool verbose);
+SEXP fastJacc(const arma::sp_mat& m, int ncores, bool verbose, bool full, bool diag, bool dist);
+SEXP fastCosine(const arma::sp_mat& m, int ncores, bool verbose, bool full, bool diag, bool dist);
+arma::mat fastEuclidean(const arma::sp_mat& m, int ncores, bool verbose, bool full, bool diag);
+arma::mat fastManhattan(const arma::sp_mat& m, int ncores, bool verbose, bool full, bool diag);
+SEXP fastCorr(const arma::sp_mat& m, int ncores, bool verbose, bool full, bool diag, bool dist);
+arma::mat fastJS(const arma::mat& m, int ncores, bool verbose, bool full, bool diag);
+arma::sp_mat fastCov(const arma::sp_mat& m, int ncores, bool verbose, bool full, bool diag);
 Rcpp::List topKBlock(const arma::mat& D, int k, bool decreasing,
                      const Rcpp::IntegerVector& self_row, int ncores);
 void topKRowsAccum(const arma::mat& D, int k, bool decreasing, Rcpp::IntegerMatrix best_idx,
@@ -72,6 +80,7 @@ int ref_slab(int method, int dist, const orc_csc* a, const orc_csc* b, double* D
         break;
       }
       case ORC_PEARSON: dense_out(fastCorr2(m, m2, g_threads, false, dist != 0), D); break;
+      case ORC_COVARIANCE: dense_out(Rcpp::wrap(fastCov2(m, m2, g_threads, false)), D); break;
       case ORC_JS: {
         // R/sparseKNN.R:194-196: js inputs are coerced with as.matrix.
         arma::mat d = fastJS2(m.dense(), m2.dense(), g_threads, false);
@@ -84,6 +93,29 @@ int ref_slab(int method, int dist, const orc_csc* a, const orc_csc* b, double* D
   } catch (const std::exception& e) {
     g_msg = e.what();
     return (g_msg.find("Mismatched") != std::string::npos) ? ORC_E_ROWS : ORC_E_NONFINITE;
+  }
+}
+
+// R/sparseDist.R:162-171: the single-matrix kernels
+int ref_dist(int method, int dist, const orc_csc* a, int full, int diag, double* D) {
+  try {
+    const arma::sp_mat m(a->nrow, a->ncol, a->p, a->i, a->x);
+    const bool f = full != 0, g = diag != 0, d = dist != 0;
+    auto put = [&](const arma::mat& r) { std::memcpy(D, r.mem.data(), sizeof(double) * r.n_elem); };
+    switch (method) {
+      case ORC_BINARY: dense_out(fastJacc(m, g_threads, false, f, g, d), D); break;
+      case ORC_COSINE: dense_out(fastCosine(m, g_threads, false, f, g, d), D); break;
+      case ORC_EUCLIDEAN: put(fastEuclidean(m, g_threads, false, f, g)); break;
+      case ORC_MANHATTAN: put(fastManhattan(m, g_threads, false, f, g)); break;
+      case ORC_PEARSON: dense_out(fastCorr(m, g_threads, false, f, g, d), D); break;
+      case ORC_COVARIANCE: dense_out(Rcpp::wrap(fastCov(m, g_threads, false, f, g)), D); break;
+      case ORC_JS: put(fastJS(m.dense(), g_threads, false, f, g)); break;
+      default: g_msg = "unknown method"; return ORC_E_ARG;
+    }
+    return ORC_OK;
+  } catch (const std::exception& e) {
+    g_msg = e.what();
+    return ORC_E_NONFINITE;
   }
 }
 
@@ -162,6 +194,10 @@ void ref_clear_error(void) { g_msg.clear(); }
 
 int ref_slab_c(int method, int dist, const orc_csc* m, const orc_csc* m2, double* D) {
   return ref_slab(method, dist, m, m2, D);
+}
+int ref_dist_c(int method, int dist, const orc_csc* m, int full, int diag, double* D) {
+  g_msg.clear();
+  return ref_dist(method, dist, m, full, diag, D);
 }
 int ref_topk_block_c(const double* D, int64_t nrow, int64_t ncol, int k, int decreasing,
                      const int32_t* self_row, int32_t* idx_out, double* dist_out) {

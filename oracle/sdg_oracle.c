@@ -209,6 +209,26 @@ static double pair_pearson(const orc_csc* A, const col_moments* ma, int32_t i,
 }
 
 /*
+ * covariance: fastCov2, src/sparseDist.cpp:480-510, i.e.
+ * as_scalar(arma::cov(li, vec(m2.col(j)))) with no clamp or non-finite fix:
+ * the cov of the single-pass form stated for pearson above (same sums, same
+ * order).  Parity with the real package: unpinned (tolerance only).
+ */
+static double pair_covariance(const orc_csc* A, const col_moments* ma, int32_t i,
+                              const orc_csc* B, const col_moments* mb, int32_t j) {
+  int64_t a = A->p[i], ae = A->p[i + 1], b = B->p[j], be = B->p[j + 1];
+  double sab = 0.0;
+  while (a < ae && b < be) {
+    if (A->i[a] == B->i[b]) { sab += A->x[a] * B->x[b]; ++a; ++b; }
+    else if (A->i[a] < B->i[b]) { ++a; }
+    else { ++b; }
+  }
+  const double N = (double)A->nrow;
+  const double norm = (A->nrow > 1) ? (N - 1.0) : 1.0;
+  return (sab - (ma[i].s * mb[j].s) / N) / norm;
+}
+
+/*
  * js: fastJS2, src/sparseDist.cpp:1099-1108, with xlogx :206-210.
  * Per dense row r the summand is ((xlogx(P)+xlogx(Q)) - xlogx(P+Q)) + (P+Q)*log(2)
  * (Armadillo's element-wise evaluation order of the expression at :1104), and
@@ -241,17 +261,22 @@ static double pair_js(const orc_csc* A, int32_t i, const orc_csc* B, int32_t j) 
   return (v > 0.0) ? sqrt(v) : 0.0;
 }
 
-static int check_js_input(const orc_csc* m) {
+static int check_js_input_named(const orc_csc* m, const char* fn) {
   const int64_t nnz = m->p[m->ncol];
   for (int64_t a = 0; a < nnz; ++a) {
     const double v = m->x[a];
-    if (!isfinite(v) || v < 0.0)
-      return fail(ORC_E_NONFINITE,
-                  "fastJS2 requires finite, non-negative input (columns should be "
-                  "normalised to sum to 1 for a true JS divergence).");
+    if (!isfinite(v) || v < 0.0) {
+      char buf[256];
+      snprintf(buf, sizeof buf,
+               "%s requires finite, non-negative input (columns should be "
+               "normalised to sum to 1 for a true JS divergence).", fn);
+      return fail(ORC_E_NONFINITE, buf);
+    }
   }
   return ORC_OK;
 }
+
+static int check_js_input(const orc_csc* m) { return check_js_input_named(m, "fastJS2"); }
 
 /* ------------------------------------------------------------------------- */
 /* fastXxx2 slab dispatch: R/sparseDist.R:172-182 -> src/sparseDist.cpp       */
@@ -282,13 +307,13 @@ int orc_slab(int method, int dist, const orc_csc* m, const orc_csc* m2, double* 
     st = unit_csc(m, ua, sa);
     if (st == ORC_OK) st = unit_csc(m2, ub, sb);
     if (st != ORC_OK) goto done;
-  } else if (method == ORC_PEARSON) {
+  } else if (method == ORC_PEARSON || method == ORC_COVARIANCE) {
     ma = malloc(sizeof(col_moments) * ((size_t)nc + 1));
     mb = malloc(sizeof(col_moments) * ((size_t)nc2 + 1));
     if (!ma || !mb) { st = fail(ORC_E_NOMEM, "out of memory"); goto done; }
     moments(m, ma);
     moments(m2, mb);
-  } else if (method < 0 || method > ORC_JS) {
+  } else if (method < 0 || method > ORC_COVARIANCE) {
     return fail(ORC_E_ARG, "unknown method");
   }
   /* parallel over the columns of m, as the reference's OpenMP loops are */
@@ -302,6 +327,7 @@ int orc_slab(int method, int dist, const orc_csc* m, const orc_csc* m2, double* 
         case ORC_EUCLIDEAN: v = pair_euclidean(m, (int32_t)i, m2, (int32_t)j); break;
         case ORC_MANHATTAN: v = pair_manhattan(m, (int32_t)i, m2, (int32_t)j); break;
         case ORC_PEARSON:   v = pair_pearson(m, ma, (int32_t)i, m2, mb, (int32_t)j, dist); break;
+        case ORC_COVARIANCE: v = pair_covariance(m, ma, (int32_t)i, m2, mb, (int32_t)j); break;
         default:            v = pair_js(m, (int32_t)i, m2, (int32_t)j); break;
       }
       D[j * nc + i] = v;
@@ -309,6 +335,69 @@ int orc_slab(int method, int dist, const orc_csc* m, const orc_csc* m2, double* 
   }
 done:
   free(ua); free(ub); free(sa); free(sb); free(ma); free(mb);
+  return st;
+}
+
+/* ------------------------------------------------------------------------- */
+/* single-matrix form: R/sparseDist.R:162-171 -> fastJacc (src/sparseDist.cpp: */
+/* 620-680), fastCosine (:918-960), fastEuclidean (:786-830), fastManhattan    */
+/* (:688-731), fastCorr (:339-398), fastCov (:450-478), fastJS (:1021-1071).   */
+/* Column i is visited against j = i (diag) or i + 1 .. n-1; the value of the  */
+/* pair (i, j) with i <= j goes to d(j, i) and, with full, to d(i, j) too.     */
+/* ------------------------------------------------------------------------- */
+
+int orc_dist(int method, int dist, const orc_csc* m, int full, int diag, double* D) {
+  if (method < 0 || method > ORC_COVARIANCE) return fail(ORC_E_ARG, "unknown method");
+  if (method == ORC_JS) {                       /* src/sparseDist.cpp:1024-1027 */
+    int st = check_js_input_named(m, "fastJS");
+    if (st != ORC_OK) return st;
+  }
+  const int64_t n = m->ncol;
+  double *ua = NULL, *sa = NULL;
+  col_moments* ma = NULL;
+  int st = ORC_OK;
+  memset(D, 0, sizeof(double) * (size_t)(n * n));
+  if (method == ORC_COSINE) {
+    ua = malloc(sizeof(double) * ((size_t)m->p[n] + 1));
+    sa = malloc(sizeof(double) * ((size_t)n + 1));
+    if (!ua || !sa) { st = fail(ORC_E_NOMEM, "out of memory"); goto done; }
+    st = unit_csc(m, ua, sa);
+    if (st != ORC_OK) goto done;
+  } else if (method == ORC_PEARSON || method == ORC_COVARIANCE) {
+    ma = malloc(sizeof(col_moments) * ((size_t)n + 1));
+    if (!ma) { st = fail(ORC_E_NOMEM, "out of memory"); goto done; }
+    moments(m, ma);
+  }
+#pragma omp parallel for num_threads(g_threads) schedule(dynamic)
+  for (int64_t i = 0; i < n; ++i) {
+    for (int64_t j = diag ? i : i + 1; j < n; ++j) {
+      double v;
+      switch (method) {
+        case ORC_BINARY:    v = pair_binary(m, (int32_t)i, m, (int32_t)j, dist); break;
+        case ORC_COSINE:    /* :937-939: the self pair is exact */
+          v = (i == j) ? (dist ? 0.0 : 1.0)
+                       : pair_cosine(m, ua, sa, (int32_t)i, m, ua, sa, (int32_t)j, dist);
+          break;
+        case ORC_EUCLIDEAN: v = pair_euclidean(m, (int32_t)i, m, (int32_t)j); break;
+        case ORC_MANHATTAN: v = pair_manhattan(m, (int32_t)i, m, (int32_t)j); break;
+        case ORC_PEARSON:   /* :358-363 */
+          v = (i == j) ? (dist ? 0.0 : 1.0)
+                       : pair_pearson(m, ma, (int32_t)i, m, ma, (int32_t)j, dist);
+          break;
+        case ORC_COVARIANCE: v = pair_covariance(m, ma, (int32_t)i, m, ma, (int32_t)j); break;
+        default:            /* :1045-1048: the self pair is skipped (stays 0) */
+          v = (i == j) ? 0.0 : pair_js(m, (int32_t)i, m, (int32_t)j);
+          break;
+      }
+      D[i * n + j] = v;
+      if (full) D[j * n + i] = v;
+    }
+  }
+  /* :393, :674, :957: the similarity forms carry a unit diagonal */
+  if (!dist && (method == ORC_BINARY || method == ORC_COSINE || method == ORC_PEARSON))
+    for (int64_t i = 0; i < n; ++i) D[i * n + i] = 1.0;
+done:
+  free(ua); free(sa); free(ma);
   return st;
 }
 
@@ -526,13 +615,14 @@ static int decreasing_for(int method, int dist) {
   /* R/sparseKNN.R:172-181 */
   switch (method) {
     case ORC_BINARY: case ORC_COSINE: case ORC_PEARSON: return !dist;
+    case ORC_COVARIANCE: return 1;               /* a coefficient: keep the largest */
     default: return 0;
   }
 }
 
 static int check_dist_form(int method, int dist) {
   /* R/sparseKNN.R:168-171 */
-  if (method < 0 || method > ORC_JS) return fail(ORC_E_ARG, "unknown method");
+  if (method < 0 || method > ORC_COVARIANCE) return fail(ORC_E_ARG, "unknown method");
   if ((method == ORC_EUCLIDEAN || method == ORC_MANHATTAN || method == ORC_JS) && !dist) {
     static const char* names[] = {"binary", "cosine", "euclidean", "manhattan", "pearson", "js"};
     char buf[256];
@@ -598,7 +688,8 @@ int orc_knn_with(const orc_backend* be, const orc_csc* X, const orc_csc* Y, int 
     if (st != ORC_OK) goto out;
     for (int64_t b = 0; b < nb; ++b)
       self_row[b] = (selfmode && !include_self) ? (int32_t)(from + b + 1) : 0;
-    if (selfmode && include_self) {                  /* R/sparseKNN.R:270-279 */
+    /* R/sparseKNN.R:270-279; covariance keeps its computed self value (the variance) */
+    if (selfmode && include_self && method != ORC_COVARIANCE) {
       const double sv = (method == ORC_BINARY || method == ORC_COSINE || method == ORC_PEARSON)
                             ? (dist ? 0.0 : 1.0) : 0.0;
       for (int64_t b = 0; b < nb; ++b) D[b * nref + (from + b)] = sv;

@@ -28,7 +28,7 @@ extern "C" {
 #endif
 
 enum { ORC_BINARY = 0, ORC_COSINE = 1, ORC_EUCLIDEAN = 2, ORC_MANHATTAN = 3,
-       ORC_PEARSON = 4, ORC_JS = 5 };
+       ORC_PEARSON = 4, ORC_JS = 5, ORC_COVARIANCE = 6 };
 
 /* Status codes; a message is available from orc_last_error(). */
 enum { ORC_OK = 0, ORC_E_ARG = -1, ORC_E_NONFINITE = -2, ORC_E_ROWS = -3,
@@ -53,6 +53,8 @@ double orc_na_real(void);           /* R's NA_real_ bit pattern */
 /* fastXxx2 slab: D is ncol(m) x ncol(m2), column-major, D(i, j) relates
  * column i of m to column j of m2. */
 int orc_slab(int method, int dist, const orc_csc* m, const orc_csc* m2, double* D);
+/* single-matrix sparseDist(X, full, diag): n x n column-major into D */
+int orc_dist(int method, int dist, const orc_csc* m, int full, int diag, double* D);
 
 /* topKBlock: idx_out / dist_out are ncol x k column-major, 1-based, NA padded. */
 int orc_topk_block(const double* D, int64_t nrow, int64_t ncol, int k, int decreasing,

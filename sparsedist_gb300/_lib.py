@@ -25,7 +25,7 @@ NA_INTEGER = np.int32(-(2 ** 31))
 NA_REAL_BITS = np.uint64(0x7FF00000000007A2)
 
 EXPORTED = ["sdg_version", "sdg_last_error", "sdg_ctx_create", "sdg_ctx_destroy", "sdg_ctx_cancel",
-            "sdg_ctx_reset_cancel", "sdg_dist_cross", "sdg_topk_block", "sdg_topk_rows_accum",
+            "sdg_ctx_reset_cancel", "sdg_dist_cross", "sdg_dist", "sdg_topk_block", "sdg_topk_rows_accum",
             "sdg_snn_jaccard", "sdg_knn", "sdg_knn_cross", "sdg_snn_graph", "sdg_matrix_upload",
             "sdg_matrix_free", "sdg_knn_resident", "sdg_knn_resident_device", "sdg_ctx_set_stream",
             "sdg_last_stats", "sdg_ctx_set_engine", "sdg_kernel_time", "sdg_knn_block",
@@ -72,6 +72,7 @@ def load() -> C.CDLL:
             lib.sdg_ctx_set_engine.argtypes = [v, C.c_int]
             lib.sdg_last_stats.argtypes = [v, v, C.c_int]
             lib.sdg_dist_cross.argtypes = [v, C.c_int, C.c_int, v, v, v]
+            lib.sdg_dist.argtypes = [v, C.c_int, C.c_int, v, C.c_int, C.c_int, v]
             lib.sdg_topk_block.argtypes = [v, v, C.c_int64, C.c_int64, C.c_int, C.c_int, v, v, v]
             lib.sdg_topk_rows_accum.argtypes = [v, v, C.c_int64, C.c_int64, C.c_int, C.c_int, v, v,
                                                 C.c_int32, v]

@@ -32,7 +32,8 @@ from ._lib import NA_INTEGER, NA_REAL_BITS, SdgError
 INT_MAX = 2 ** 31 - 1
 METHOD_CHOICES = ("binary", "jaccard", "cosine", "euclidean", "manhattan", "pearson", "js",
                   "covariance")
-METHOD_CODES = {"binary": 0, "cosine": 1, "euclidean": 2, "manhattan": 3, "pearson": 4, "js": 5}
+METHOD_CODES = {"binary": 0, "cosine": 1, "euclidean": 2, "manhattan": 3, "pearson": 4, "js": 5,
+                "covariance": 6}
 NA_REAL = np.array([NA_REAL_BITS], dtype=np.uint64).view(np.float64)[0]
 
 
@@ -183,8 +184,6 @@ def sparseKNN(X, Y=None, k=10, method="binary", dist=True, include_self=False,
     if method in ("euclidean", "manhattan", "js") and not dist:
         raise ValueError("'dist = FALSE' is only meaningful for methods \"binary\", \"cosine\" "
                          "and \"pearson\"; %s has no similarity form." % method)
-    if method == "covariance":
-        raise NotImplementedError("method \"covariance\" is not provided by sparsedist_gb300")
     nmX = _colnames(X)
     nq = _ncol(X)
     if nq is None or nq < 1:
@@ -234,8 +233,6 @@ def sparseKNNCross(X, Y=None, k=10, method=METHOD_CHOICES, dist=True, drop_degen
     if method in ("euclidean", "manhattan", "js") and not dist:
         raise ValueError("'dist = FALSE' is only meaningful for methods \"binary\", \"cosine\" "
                          "and \"pearson\"; %s has no similarity form." % method)
-    if method == "covariance":
-        raise NotImplementedError("method \"covariance\" is not provided by sparsedist_gb300")
     if X.shape[0] != Y.shape[0]:
         raise ValueError("'X' and 'Y' must have the same number of rows.")
     nq, nr = _ncol(X), _ncol(Y)
@@ -360,23 +357,38 @@ def sparseSNN(idx, include_self=True, prune=0, symmetrise=None, edges=("knn", "s
 # ---------------------------------------------------------------------------
 def sparseDist(X, Y=None, method="binary", ncores=1, verbose=True, full=False, diag=False,
                dist=True, *, ctx=None):
-    """Cross distances D[i, j] = method(column i of X, column j of Y) (dense)."""
+    """R/sparseDist.R:133-190.  With Y, the cross matrix D[i, j] = method(column
+    i of X, column j of Y); without, the matrix among the columns of X: its
+    lower triangle (full = False) or both (full = True), the diagonal as the
+    reference's single-matrix kernels leave it (`diag` only decides whether
+    the euclidean / manhattan / covariance self pairs are computed).
+
+    Storage follows the reference's (src/sparseDist.cpp, RESULT STORAGE):
+    distance-valued results are a dense ndarray; coefficient-valued ones
+    (covariance, and binary / cosine / pearson with dist = False) a
+    scipy.sparse.csc_matrix holding the non-zero entries."""
     if X is None:
         raise ValueError("'X' must be provided.")
     method = _match_arg(method, METHOD_CHOICES)
     if method == "jaccard":
         method = "binary"
-    if Y is None:
-        raise NotImplementedError("the single-matrix form of sparseDist() is not provided by "
-                                  "sparsedist_gb300 (only the two-matrix slab of the kNN path)")
-    if method == "covariance":
-        raise NotImplementedError("method \"covariance\" is not provided by sparsedist_gb300")
-    Xs, Ys = _held(_as_csparse(X)), _held(_as_csparse(Y))
     c = _ctx(ctx)
-    D = np.empty((Ys.ncol, Xs.ncol), np.float64)
-    _lib.check(c.lib.sdg_dist_cross(c.handle, METHOD_CODES[method], int(bool(dist)), Xs.ref,
-                                    Ys.ref, D.ctypes.data))
-    return D.T
+    Xs = _held(_as_csparse(X))
+    if Y is None:
+        n = Xs.ncol
+        D = np.empty((n, n), np.float64)
+        _lib.check(c.lib.sdg_dist(c.handle, METHOD_CODES[method], int(bool(dist)), Xs.ref,
+                                  int(bool(full)), int(bool(diag)), D.ctypes.data))
+    else:
+        Ys = _held(_as_csparse(Y))
+        D = np.empty((Ys.ncol, Xs.ncol), np.float64)
+        _lib.check(c.lib.sdg_dist_cross(c.handle, METHOD_CODES[method], int(bool(dist)), Xs.ref,
+                                        Ys.ref, D.ctypes.data))
+    D = D.T
+    if method == "covariance" or (method in ("binary", "cosine", "pearson") and not dist):
+        import scipy.sparse as sp
+        return sp.csc_matrix(D)
+    return D
 
 
 # ---------------------------------------------------------------------------

@@ -13,6 +13,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -82,12 +83,12 @@ const char* kMsgJS =
     "for a true JS divergence).";
 
 const char* method_name(int m) {
-  static const char* names[] = {"binary", "cosine", "euclidean", "manhattan", "pearson", "js"};
-  return (m >= 0 && m <= 5) ? names[m] : "?";
+  static const char* names[] = {"binary", "cosine", "euclidean", "manhattan", "pearson", "js", "covariance"};
+  return (m >= 0 && m <= 6) ? names[m] : "?";
 }
 
 void check_method(int method, int dist) {
-  if (method < 0 || method > 5) fail(SDG_E_ARG, "unknown method");
+  if (method < 0 || method > 6) fail(SDG_E_ARG, "unknown method");
   if ((method == EUCLIDEAN || method == MANHATTAN || method == JS) && !dist) {
     // R/sparseKNN.R:168-171
     fail(SDG_E_ARG, std::string("'dist = FALSE' is only meaningful for methods \"binary\", "
@@ -96,8 +97,9 @@ void check_method(int method, int dist) {
   }
 }
 
-// R/sparseKNN.R:172-181
+// R/sparseKNN.R:172-181 (covariance is a coefficient: always the largest)
 bool decreasing_for(int method, int dist) {
+  if (method == COVARIANCE) return true;
   return (method == BINARY || method == COSINE || method == PEARSON) ? !dist : false;
 }
 
@@ -315,9 +317,9 @@ void ensure_moments(sdg_matrix* m) {
   m->have_moments = true;
 }
 
-void ensure_js(sdg_matrix* m) {
+void ensure_js(sdg_matrix* m, const char* msg = kMsgJS) {
   if (m->js_status == 0) return;
-  if (m->js_status < 0) fail(SDG_E_NONFINITE, kMsgJS);
+  if (m->js_status < 0) fail(SDG_E_NONFINITE, msg);
   cudaStream_t s = m->ctx->stream;
   DevBuf err(sizeof(int), s);
   CK(cudaMemsetAsync(err.p, 0, sizeof(int), s));
@@ -326,14 +328,14 @@ void ensure_js(sdg_matrix* m) {
   CK(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   m->js_status = herr ? SDG_E_NONFINITE : 0;
-  if (herr) fail(SDG_E_NONFINITE, kMsgJS);
+  if (herr) fail(SDG_E_NONFINITE, msg);
 }
 
 // Method-specific preparation of the reference-side (m) and query-side (m2)
 // matrices, in the order the reference raises its errors.
 void prepare(int method, sdg_matrix* ref, sdg_matrix* qry) {
   if (method == COSINE) { ensure_cosine(ref); if (qry != ref) ensure_cosine(qry); }
-  else if (method == PEARSON) { ensure_moments(ref); if (qry != ref) ensure_moments(qry); }
+  else if (method == PEARSON || method == COVARIANCE) { ensure_moments(ref); if (qry != ref) ensure_moments(qry); }
   else if (method == JS) { ensure_js(ref); if (qry != ref) ensure_js(qry); }
 }
 
@@ -384,8 +386,9 @@ void exact_engine(sdg_ctx* c, const KnnPlan& P, sdg_matrix* ref, sdg_matrix* qry
     check_cancel(c);
     const int64_t nb = std::min(B, q_hi - q0);
     sdg_time_begin(c);
+    // R/sparseKNN.R:270-279; covariance keeps its computed self value (the variance)
     launch_exact_slab(P.method, P.dist, ref->dev(), ra, qry->dev(), qa, q0, nb, P.ref_mask,
-                      P.selfmode && P.include_self, self_value, D.as<double>(), s);
+                      P.selfmode && P.include_self && P.method != COVARIANCE, self_value, D.as<double>(), s);
     sdg_time_end(c);
     SelectArgs a;
     a.vals = D.as<double>();
@@ -647,7 +650,7 @@ SDG_API int sdg_dist_cross(sdg_ctx* c, int method, int dist, const sdg_csc* m, c
   return guarded([&] {
     if (!c) fail(SDG_E_ARG, "ctx must not be NULL");
     CK(cudaSetDevice(c->device));
-    if (method < 0 || method > 5) fail(SDG_E_ARG, "unknown method");
+    if (method < 0 || method > 6) fail(SDG_E_ARG, "unknown method");
     check_csc_host(m, "m");
     check_csc_host(m2, "m2");
     if (method == JS) {                              // src/sparseDist.cpp:1077-1081 first
@@ -675,6 +678,63 @@ SDG_API int sdg_dist_cross(sdg_ctx* c, int method, int dist, const sdg_csc* m, c
       CK(cudaGetLastError());
       CK(cudaMemcpyAsync(D + q0 * nc, Dd.p, sizeof(double) * (size_t)(nc * nb),
                          cudaMemcpyDeviceToHost, s));
+    }
+    CK(cudaStreamSynchronize(s));
+  });
+}
+
+SDG_API int sdg_dist(sdg_ctx* c, int method, int dist, const sdg_csc* m, int full, int diag,
+                     double* D) {
+  return guarded([&] {
+    if (!c) fail(SDG_E_ARG, "ctx must not be NULL");
+    CK(cudaSetDevice(c->device));
+    if (method < 0 || method > 6) fail(SDG_E_ARG, "unknown method");
+    check_csc_host(m, "m");
+    auto a = upload(c, m, "m");
+    if (method == JS)                                // src/sparseDist.cpp:1024-1027
+      ensure_js(a.get(), "fastJS requires finite, non-negative input (columns should be "
+                         "normalised to sum to 1 for a true JS divergence).");
+    prepare(method, a.get(), a.get());
+    cudaStream_t s = c->stream;
+    const int64_t n = a->ncol;
+    if (n == 0) return;
+    const size_t whole = sizeof(double) * (size_t)n * (size_t)n;
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    // device bytes the result may hold: half the free memory, or less where
+    // SDG_DIST_RESIDENT_BYTES says so (a tuning knob; it also reaches the
+    // streamed path on small inputs)
+    size_t cap = free_b / 2;
+    if (const char* e = std::getenv("SDG_DIST_RESIDENT_BYTES"))
+      cap = std::min<size_t>(cap, (size_t)std::strtoull(e, nullptr, 10));
+    if (whole <= cap) {
+      // resident: the lower triangle once, mirrored on the device with full
+      DevBuf Dd(whole, s);
+      sdg_time_begin(c);
+      launch_self_slab(method, dist, a->dev(), aux_of(a.get()), 0, n, 0, diag, Dd.as<double>(), s);
+      sdg_time_end(c);
+      CK(cudaGetLastError());
+      if (full) {
+        launch_mirror_lower(Dd.as<double>(), n, s);
+        CK(cudaGetLastError());
+      }
+      CK(cudaMemcpyAsync(D, Dd.p, whole, cudaMemcpyDeviceToHost, s));
+    } else {
+      // streamed in column blocks of about 1 GiB; with full both triangles
+      // are computed, as no earlier block stays on the device to mirror
+      const int64_t budget = std::min<int64_t>((int64_t)1 << 30, (int64_t)cap);
+      const int64_t B = std::max<int64_t>(1, std::min<int64_t>(n, budget / (n * 8)));
+      DevBuf Dd(sizeof(double) * (size_t)(n * B), s);
+      for (int64_t c0 = 0; c0 < n; c0 += B) {
+        const int64_t nb = std::min(B, n - c0);
+        sdg_time_begin(c);
+        launch_self_slab(method, dist, a->dev(), aux_of(a.get()), c0, nb, full, diag,
+                         Dd.as<double>(), s);
+        sdg_time_end(c);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(D + c0 * n, Dd.p, sizeof(double) * (size_t)(n * nb),
+                           cudaMemcpyDeviceToHost, s));
+      }
     }
     CK(cudaStreamSynchronize(s));
   });

@@ -225,6 +225,24 @@ __device__ __forceinline__ double xlogx(double x) {
   return isnan(r) ? 0.0 : r;
 }
 
+// covariance: fastCov2, src/sparseDist.cpp:480-510 -- arma::cov of the two
+// columns in the single-pass form used for pearson: (sum(ab) - sum(a) sum(b)
+// / N) / (N - 1), the matched products summed in ascending row order; no clamp
+__device__ double pair_covariance(const DevCsc& A, const ColAux& aa, int32_t i, const DevCsc& B,
+                                  const ColAux& ba, int32_t j) {
+  int64_t a = A.p[i], ae = A.p[i + 1], b = B.p[j], be = B.p[j + 1];
+  double sab = 0.0;
+  while (a < ae && b < be) {
+    const int32_t ra = __ldg(A.i + a), rb = __ldg(B.i + b);
+    if (ra == rb) { sab = dadd(sab, dmul(A.x[a], B.x[b])); ++a; ++b; }
+    else if (ra < rb) { ++a; }
+    else { ++b; }
+  }
+  const double N = (double)A.nrow;
+  const double norm = (A.nrow > 1) ? dsub(N, 1.0) : 1.0;
+  return dsub(sab, dmul(aa.s[i], ba.s[j]) / N) / norm;
+}
+
 __device__ double pair_js(const DevCsc& A, int32_t i, const DevCsc& B, int32_t j) {
   const double log2v = 0.69314718055994530942;   // log(2.0), correctly rounded
   int64_t a = A.p[i], ae = A.p[i + 1], b = B.p[j], be = B.p[j + 1];
@@ -254,6 +272,7 @@ __device__ __forceinline__ double pair_value(int method, bool dist, const DevCsc
     case EUCLIDEAN: return pair_euclidean(A, i, B, j);
     case MANHATTAN: return pair_manhattan(A, i, B, j);
     case PEARSON: return pair_pearson(A, aa, i, B, ba, j, dist);
+    case COVARIANCE: return pair_covariance(A, aa, i, B, ba, j);
     default: return pair_js(A, i, B, j);
   }
 }
@@ -270,6 +289,55 @@ __global__ void k_exact_slab(int method, int dist, DevCsc ref, ColAux ra, DevCsc
   else if (restore_self && i == q) v = self_value;
   else v = pair_value(method, dist != 0, ref, ra, (int32_t)i, qry, qa, (int32_t)q);
   D[b * (int64_t)ref.ncol + i] = v;
+}
+
+// Single-matrix form (src/sparseDist.cpp fastJacc :620-680, fastCosine
+// :918-960, fastEuclidean :786-830, fastManhattan :688-731, fastCorr
+// :339-398, fastCov :450-478, fastJS :1021-1071): entry (r, c) of the n x n
+// result holds the pair (min(r, c), max(r, c)) in the reference's i <= j
+// orientation.  The lower triangle (r > c) is always computed; the upper one
+// only with `upper` (else it is written 0: unwritten, or mirrored later).
+// The diagonal follows each kernel: a unit / zero self value for binary,
+// cosine and pearson; the computed self pair for euclidean, manhattan and
+// covariance only with `diag`; always 0 for js.
+__global__ void k_self_slab(int method, int dist, DevCsc m, ColAux a, int64_t c0, int upper,
+                            int diag, double* D) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t b = blockIdx.y;
+  if (r >= m.ncol) return;
+  const int64_t c = c0 + b;
+  double v = 0.0;
+  if (r == c) {
+    if (method == BINARY || method == COSINE || method == PEARSON) v = dist ? 0.0 : 1.0;
+    else if (diag && method != JS) v = pair_value(method, dist != 0, m, a, (int32_t)r, m, a, (int32_t)r);
+  } else if (r > c) {
+    v = pair_value(method, dist != 0, m, a, (int32_t)c, m, a, (int32_t)r);
+  } else if (upper) {
+    v = pair_value(method, dist != 0, m, a, (int32_t)r, m, a, (int32_t)c);
+  }
+  D[b * m.ncol + r] = v;
+}
+
+// D (n x n, column-major): copies the strict lower triangle onto the upper
+// one through a 32 x 32 shared-memory tile, so both the reads and the writes
+// are coalesced.  Block (tx, ty) with tx > ty owns the upper tile at rows
+// ty*32.., columns tx*32..; it reads the lower tile at rows tx*32..,
+// columns ty*32..  Diagonal tiles (tx == ty) mirror within themselves.
+__global__ void k_mirror_lower(double* D, int64_t n) {
+  __shared__ double t[32][33];
+  const int64_t tx = blockIdx.x, ty = blockIdx.y;
+  if (tx < ty) return;
+  const int64_t r0 = tx * 32, c0 = ty * 32;          // source tile (lower)
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int64_t r = r0 + threadIdx.x, c = c0 + k;
+    t[k][threadIdx.x] = (r < n && c < n) ? D[c * n + r] : 0.0;
+  }
+  __syncthreads();
+  // destination: row c0 + threadIdx.x, column r0 + k holds source (r0 + k, c0 + threadIdx.x)
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int64_t r = c0 + threadIdx.x, c = r0 + k;
+    if (r < n && c < n && r < c) D[c * n + r] = t[threadIdx.x][k];
+  }
 }
 
 __global__ void k_exact_pairs(int method, int dist, DevCsc ref, ColAux ra, DevCsc qry,
@@ -617,6 +685,24 @@ void launch_exact_slab(int method, int dist, const DevCsc& ref, const ColAux& ra
     k_exact_slab<<<grid, 128, 0, s>>>(method, dist, ref, ra, qry, qa, q0 + b0, ref_mask,
                                       restore_self, self_value, D + b0 * (int64_t)ref.ncol);
   }
+}
+
+void launch_self_slab(int method, int dist, const DevCsc& m, const ColAux& a, int64_t c0,
+                      int64_t nb, int upper, int diag, double* D, cudaStream_t s) {
+  if (m.ncol == 0 || nb == 0) return;
+  for (int64_t b0 = 0; b0 < nb; b0 += 65535) {            // gridDim.y limit
+    const int64_t cnt = (nb - b0 < 65535) ? nb - b0 : 65535;
+    dim3 grid(blocks_for(m.ncol, 128), (unsigned)cnt);
+    k_self_slab<<<grid, 128, 0, s>>>(method, dist, m, a, c0 + b0, upper, diag, D + b0 * (int64_t)m.ncol);
+  }
+}
+
+void launch_mirror_lower(double* D, int64_t n, cudaStream_t s) {
+  // the caller holds n x n doubles on the device, so n / 32 is far below the
+  // 65,535 limit of gridDim.y
+  if (n <= 1) return;
+  const unsigned T = (unsigned)((n + 31) / 32);
+  k_mirror_lower<<<dim3(T, T), dim3(32, 8), 0, s>>>(D, n);
 }
 
 void launch_exact_pairs(int method, int dist, const DevCsc& ref, const ColAux& ra,

@@ -40,6 +40,15 @@ void launch_exact_slab(int method, int dist, const DevCsc& ref, const ColAux& ra
                        const uint8_t* ref_mask, int restore_self, double self_value,
                        double* D, cudaStream_t s);
 
+// Single-matrix sparseDist: columns c0 .. c0 + nb - 1 of the n x n result
+// into D (nb columns of length n); the upper triangle is computed only with
+// `upper`, else written 0.
+void launch_self_slab(int method, int dist, const DevCsc& m, const ColAux& a, int64_t c0,
+                      int64_t nb, int upper, int diag, double* D, cudaStream_t s);
+// Copies the strict lower triangle of the device n x n matrix D onto its
+// upper triangle.
+void launch_mirror_lower(double* D, int64_t n, cudaStream_t s);
+
 // Exact values of listed pairs: out[t] = value(ref col ref_idx[t], query col
 // qry_idx[t]).
 void launch_exact_pairs(int method, int dist, const DevCsc& ref, const ColAux& ra,

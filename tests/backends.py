@@ -14,7 +14,7 @@ import scipy.sparse as sp
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 METHODS = {"binary": 0, "jaccard": 0, "cosine": 1, "euclidean": 2, "manhattan": 3,
-           "pearson": 4, "js": 5}
+           "pearson": 4, "js": 5, "covariance": 6}
 NA_INT = np.int32(-(2 ** 31))
 
 
@@ -76,6 +76,9 @@ class OracleBackend:
 
     def slab(self, method, m, m2, dist=True):
         return self.o.slab(method, m, m2, dist)
+
+    def dist_single(self, method, m, full=False, diag=False, dist=True):
+        return self.o.dist_single(method, m, full, diag, dist)
 
     def topk_block(self, D, k, decreasing, self_row):
         return self.o.topk_block(D, k, decreasing, self_row)
@@ -147,6 +150,13 @@ class GpuBackend:
         D = np.empty((b.ncol, a.ncol), np.float64)
         self.L.check(self.lib.sdg_dist_cross(self.h, METHODS[method], int(dist), a.ref, b.ref,
                                              D.ctypes.data))
+        return D.T
+
+    def dist_single(self, method, m, full=False, diag=False, dist=True):
+        a = self._held(m)
+        D = np.empty((a.ncol, a.ncol), np.float64)
+        self.L.check(self.lib.sdg_dist(self.h, METHODS[method], int(dist), a.ref, int(bool(full)),
+                                       int(bool(diag)), D.ctypes.data))
         return D.T
 
     def topk_block(self, D, k, decreasing, self_row):

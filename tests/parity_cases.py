@@ -55,7 +55,7 @@ def _knn_equal(method, dist_flag, got, want):
     wi, wd = want
     if method in PINNED:
         return same_bits(gi, wi) and same_bits(gd, wd)
-    dec = (method == "pearson" and not dist_flag)
+    dec = (method == "pearson" and not dist_flag) or method == "covariance"
     if same_bits(gi, wi) and _close(gd, wd):
         return True
     return _tie_aware_idx(gi, gd, wi, wd, dec) and gi.shape == wi.shape
@@ -139,6 +139,29 @@ def ka_pearson_self(b):
     assert dst[0, at] == 1.0
     idx, dst, _ = b.knn(X, k=2, method="pearson", dist=True, include_self=True)
     assert list(idx[:, 0]) == [1, 2] and list(dst[:, 0]) == [0.0, 0.0]
+
+
+def ka_covariance(b):
+    # test-sparseDist.R:169-179: the covariance slab is base R's cov();
+    # test-sparseKNN.R:208-226: the largest covariances are the neighbours
+    # whatever `dist` says; test-sparseKNN.R:278-290: the self value is the
+    # column variance (no restoration).
+    X = make_x(60, 10, 0.3, 1)
+    D = np.asarray(b.slab("covariance", X, X, True))
+    assert np.allclose(D, np.cov(X.toarray(), rowvar=False), rtol=1e-12, atol=1e-15)
+    off = D.copy()
+    np.fill_diagonal(off, -np.inf)
+    want = np.argsort(-off, axis=1, kind="stable")[:, :3] + 1
+    for d in (True, False):
+        idx, dst, _ = b.knn(X, k=3, method="covariance", dist=d)
+        assert np.array_equal(idx, want)
+        assert np.all(np.diff(dst, axis=1) <= 0)
+    X2 = make_x(60, 6, 0.3, 2)
+    idx, dst, _ = b.knn(X2, k=6, method="covariance", include_self=True)
+    var = X2.toarray().var(axis=0, ddof=1)
+    for i in range(6):
+        at = list(idx[i]).index(i + 1)
+        assert abs(dst[i, at] - var[i]) <= 1e-12 * var[i]
 
 
 def ka_js_self(b):
@@ -277,7 +300,7 @@ def ka_cross_is_two_knn(b):
         dens = float(rng.uniform(0.02, 0.25))
         k = int(rng.integers(1, 9))
         bs = int(rng.choice([1, 2, 3, 4, 5, 6, 7, 11, 16, 64]))
-        meth = ["binary", "cosine", "euclidean", "manhattan", "pearson", "js"][trial % 6]
+        meth = ["binary", "cosine", "euclidean", "manhattan", "pearson", "js", "covariance"][trial % 7]
         dst = bool(rng.integers(0, 2)) if meth in ("binary", "cosine", "pearson") else True
         X = make_x(nrw, ncx, dens, trial * 2)
         Y = make_x(nrw, ncy, dens, trial * 2 + 1)
@@ -322,7 +345,7 @@ def ka_rows_accum_validation(b):
         b.topk_rows_accum(D, 2, False, bi, bv, 0, [0, -1, 0, 0])
 
 
-KNOWN_ANSWERS = [ka_ties, ka_na_padding, ka_topk_validation, ka_pearson_self, ka_js_self,
+KNOWN_ANSWERS = [ka_ties, ka_na_padding, ka_topk_validation, ka_pearson_self, ka_covariance, ka_js_self,
                  ka_signed_cancel, ka_cross_degenerate, ka_k_clamp, ka_no_candidates,
                  ka_snn_knowns, ka_snn_awkward_knn_edges, ka_cosine_extremes, ka_js_disjoint,
                  ka_nonfinite, ka_cross_is_two_knn, ka_block_size_invariance,

@@ -37,7 +37,8 @@ def test_gpu_known_answers(gpu_engine, fn):
     fn(gpu_engine)
 
 
-@pytest.mark.parametrize("method", ["binary", "cosine", "euclidean", "manhattan", "pearson", "js"])
+@pytest.mark.parametrize("method", ["binary", "cosine", "euclidean", "manhattan", "pearson", "js",
+                                    "covariance"])
 def test_gpu_random_vs_oracle(gpu_engine, orc, method):
     rng = np.random.default_rng(11)
     for trial in range(5):
@@ -47,7 +48,7 @@ def test_gpu_random_vs_oracle(gpu_engine, orc, method):
         X, Y = make_x(n, nx, dens, 1000 + trial), make_x(n, ny, dens, 2000 + trial)
         if method == "js":
             X, Y = normalise_cols(X), normalise_cols(Y)
-        dists = (True, False) if method in ("binary", "cosine", "pearson") else (True,)
+        dists = (True, False) if method in ("binary", "cosine", "pearson", "covariance") else (True,)
         for d in dists:
             k = int(rng.integers(1, 25))
             for args in (dict(X=X, Y=None, include_self=False), dict(X=X, Y=None, include_self=True),

@@ -31,7 +31,8 @@ def test_oracle_known_answers(orc, fn):
     fn(orc)
 
 
-@pytest.mark.parametrize("method", ["binary", "cosine", "euclidean", "manhattan", "pearson", "js"])
+@pytest.mark.parametrize("method", ["binary", "cosine", "euclidean", "manhattan", "pearson", "js",
+                                    "covariance"])
 def test_oracle_bit_identical_to_reference_build(ref_oracle, method):
     orc = OracleBackend()
     rng = np.random.default_rng(7)
