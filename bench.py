@@ -66,7 +66,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--dist-cols", type=int, default=10000)
-    ap.add_argument("--config", default="c2", choices=["c2", "c1", "c3", "serve", "dist"],
+    ap.add_argument("--config", default="c2", choices=["c2", "c1", "c3", "serve", "dist", "snn"],
                     help="c2: the default line (configuration 2); c1: the CPU-runnable "
                          "configuration 1; serve: configuration 5, the serving loop")
     ap.add_argument("--serve-ref-cols", type=int, default=1000000)
@@ -316,6 +316,66 @@ def run_dist(args):
                       "results": out}))
 
 
+def run_snn(args):
+    """sparseSNN on configuration 2's kNN graph: the self-search
+    sparseKNN(X, k = 20, cosine) of the 30,000 x ncol log-count matrix (on
+    the GPU, in sdg_knn_block shares), then sparseSNN(prune = 1/15) with
+    edges = "knn" (symmetrise = TRUE) and edges = "shared" through the Python
+    API (idx in from the host, the dgCMatrix slots out), each checked bit for
+    bit against the oracle, which is also timed on all host cores."""
+    import torch
+    import sparsedist_gb300 as sdg
+    from sparsedist_gb300 import _lib
+    from oracle import build as obuild
+    from oracle.pyoracle import Oracle
+    p, i, x = make_workload(args, "cuda")
+    ctx = _lib.Context(0)
+    ref = _lib.Resident(ctx, args.nrow, args.ncol, p, i, x)
+    del p, i, x
+    torch.cuda.empty_cache()
+    n, k, B = args.ncol, args.k, 8192
+    idx = np.empty((n, k), np.int32)
+    t0 = time.perf_counter()
+    for q0 in range(0, n, B):
+        nb = min(B, n - q0)
+        bi = np.empty(nb * k, np.int32)
+        bv = np.empty(nb * k, np.float64)
+        ke, fl = np.zeros(1, np.int32), np.zeros(1, np.int32)
+        _lib.check(ctx.lib.sdg_knn_block(ctx.handle, ref.handle, None, q0, nb, METHOD_CODES[args.method], 1, k,
+                                         0, 1, bi.ctypes.data, bv.ctypes.data, 0, ke.ctypes.data,
+                                         fl.ctypes.data))
+        idx[q0:q0 + nb] = bi.reshape(int(ke[0]), nb).T
+    knn_s = time.perf_counter() - t0
+    ref.free()
+    obuild.build_oracle()
+    threads = os.cpu_count() or 1
+    orc = Oracle(threads=threads)
+    out = {"knn_graph_s": knn_s, "n": n, "k": k}
+    for edges in ("knn", "shared"):
+        for _ in range(args.warmup):
+            g = sdg.sparseSNN(idx, prune=1 / 15, edges=edges, verbose=False, ctx=ctx)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            g = sdg.sparseSNN(idx, prune=1 / 15, edges=edges, verbose=False, ctx=ctx)
+        gpu_s = (time.perf_counter() - t0) / args.steps
+        t0 = time.perf_counter()
+        if edges == "knn":
+            wp, wi, wx = orc.snn_graph(idx, True, 1 / 15, True)
+        else:
+            wp, wi, wx = orc.snn_graph_shared(idx, True, 1 / 15)
+        cpu_s = time.perf_counter() - t0
+        same = bool(np.array_equal(g.indptr, wp) and np.array_equal(g.indices, wi) and
+                    np.array_equal(g.data.view(np.uint64), np.asarray(wx).view(np.uint64)))
+        out[edges] = {"gpu_ms_e2e": 1000 * gpu_s, "nodes_per_s_e2e": n / gpu_s, "nnz": int(g.nnz),
+                      "cpu_baseline": {"value": n / cpu_s, "unit": "nodes/s", "cores": threads,
+                                       "kind": "port", "sample": "the whole graph"},
+                      "identical": same}
+    print(json.dumps({"metric": "sparseSNN nodes/s on configuration 2's kNN graph (e2e through the Python API)",
+                      "config": {"workload": "sparseSNN(sparseKNN(X, k=%d, %s), prune=1/15), X %dx%d "
+                                             "log-count CSC" % (k, args.method, args.nrow, n)},
+                      "steps": args.steps, "warmup": args.warmup, "results": out}))
+
+
 def run_serve(args):
     """Configuration 5: a resident 30,000 x serve_ref_cols log-count reference
     (configuration 2's generator), Poisson arrivals of query matrices with
@@ -504,6 +564,9 @@ def main():
         return
     if args.config == "dist":
         run_dist(args)
+        return
+    if args.config == "snn":
+        run_snn(args)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -710,13 +710,24 @@ SDG_API int sdg_dist(sdg_ctx* c, int method, int dist, const sdg_csc* m, int ful
     if (whole <= cap) {
       // resident: the lower triangle once, mirrored on the device with full
       DevBuf Dd(whole, s);
-      sdg_time_begin(c);
-      launch_self_slab(method, dist, a->dev(), aux_of(a.get()), 0, n, 0, diag, Dd.as<double>(), s);
-      sdg_time_end(c);
-      CK(cudaGetLastError());
-      if (full) {
-        launch_mirror_lower(Dd.as<double>(), n, s);
+      if (self_tri_supported(method, a->nrow)) {
+        // match-only methods: the upper triangle on the query-centric kernel
+        // (one pair per lane), then moved to the lower one
+        sdg_time_begin(c);
+        launch_self_tri(method, dist, a->dev(), aux_of(a.get()), diag, Dd.as<double>(), s);
+        sdg_time_end(c);
         CK(cudaGetLastError());
+        launch_mirror_upper(Dd.as<double>(), n, full ? 0 : 1, s);
+        CK(cudaGetLastError());
+      } else {
+        sdg_time_begin(c);
+        launch_self_slab(method, dist, a->dev(), aux_of(a.get()), 0, n, 0, diag, Dd.as<double>(), s);
+        sdg_time_end(c);
+        CK(cudaGetLastError());
+        if (full) {
+          launch_mirror_lower(Dd.as<double>(), n, s);
+          CK(cudaGetLastError());
+        }
       }
       CK(cudaMemcpyAsync(D, Dd.p, whole, cudaMemcpyDeviceToHost, s));
     } else {

@@ -340,6 +340,45 @@ __global__ void k_mirror_lower(double* D, int64_t n) {
   }
 }
 
+// D (n x n, column-major): copies the strict upper triangle onto the lower
+// one (tile transpose through shared memory, as k_mirror_lower), and with
+// `clear` zeroes the upper triangle once it has been read.  Block (tx, ty),
+// tx >= ty, reads the upper tile at rows ty*32.., columns tx*32.. and writes
+// the lower tile at rows tx*32.., columns ty*32..; each upper tile is read
+// by one block only, so the clearing races with nothing.
+__global__ void k_mirror_upper(double* D, int64_t n, int clear) {
+  __shared__ double t[32][33];
+  const int64_t tx = blockIdx.x, ty = blockIdx.y;
+  if (tx < ty) return;
+  const int64_t r0 = ty * 32, c0 = tx * 32;          // source tile (upper)
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int64_t r = r0 + threadIdx.x, c = c0 + k;
+    t[k][threadIdx.x] = (r < n && c < n) ? D[c * n + r] : 0.0;
+  }
+  __syncthreads();
+  // destination (c0 + threadIdx.x, r0 + k) holds source (r0 + k, c0 + threadIdx.x)
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int64_t r = c0 + threadIdx.x, c = r0 + k;
+    if (r < n && c < n && r > c) D[c * n + r] = t[threadIdx.x][k];
+  }
+  if (clear) {
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+      const int64_t r = r0 + threadIdx.x, c = c0 + k;
+      if (r < n && c < n && r < c) D[c * n + r] = 0.0;
+    }
+  }
+}
+
+// The diagonal of the single-matrix form (the rules of k_self_slab's r == c).
+__global__ void k_self_diag(int method, int dist, DevCsc m, ColAux a, int diag, double* D) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= m.ncol) return;
+  double v = 0.0;
+  if (method == BINARY || method == COSINE || method == PEARSON) v = dist ? 0.0 : 1.0;
+  else if (diag && method != JS) v = pair_value(method, dist != 0, m, a, (int32_t)r, m, a, (int32_t)r);
+  D[r * m.ncol + r] = v;
+}
+
 __global__ void k_exact_pairs(int method, int dist, DevCsc ref, ColAux ra, DevCsc qry,
                               ColAux qa, const int32_t* ref_idx, const int32_t* qry_idx,
                               int64_t npairs, double* out) {
@@ -382,9 +421,10 @@ __device__ double match_finish(int method, bool dist, double sum, int64_t common
     else if (c < -1.0) c = -1.0;
     return dist ? dsub(1.0, c) : c;
   }
-  // pearson
   const double N = (double)A.nrow;
   const double norm = (A.nrow > 1) ? dsub(N, 1.0) : 1.0;
+  if (method == COVARIANCE) return dsub(sum, dmul(aa.s[i], ba.s[j]) / N) / norm;
+  // pearson
   const double cov = dsub(sum, dmul(aa.s[i], ba.s[j]) / N) / norm;
   const double va = dsub(aa.ss[i], dmul(aa.s[i], aa.s[i]) / N) / norm;
   const double vb = dsub(ba.ss[j], dmul(ba.s[j], ba.s[j]) / N) / norm;
@@ -488,6 +528,12 @@ __global__ void k_rerank_warp(int method, int dist, DevCsc ref, ColAux ra, DevCs
 // lane j then adds candidate j's list in order, all lanes at once, operands
 // in shared memory.  Each lane's sum is the reference's sequential sum bit for
 // bit.
+//
+// kTri (the single-matrix sparseDist): no candidate table; CTA (x, y) takes
+// column q = x of m as the query and the reference columns c = y * 2048 ..
+// of m below it (c < q) as its candidates, in the reference's orientation
+// (first operand c, second q), and writes the strict upper triangle entry
+// out[q * ncol + c].
 constexpr int RQ_THREADS = 256;
 constexpr int RQ_WARPS = RQ_THREADS / 32;
 constexpr int32_t RQ_MAX_NROW = 1 << 18;
@@ -495,6 +541,7 @@ constexpr int RQ_MAX_QV = 2048;
 constexpr int RQ_MAX_CAND = 2048;     // candidates sorted in shared memory
 constexpr int RM = 32;                // list slots per candidate per pass
 
+template <bool kTri>
 __global__ void k_rerank_q(int method, int dist, DevCsc ref, ColAux ra, DevCsc qry, ColAux qa,
                            const int32_t* cand, const int32_t* count, int cap, int64_t q_begin,
                            int restore_self, double self_value, double* out) {
@@ -507,7 +554,8 @@ __global__ void k_rerank_q(int method, int dist, DevCsc ref, ColAux ra, DevCsc q
   int32_t* first = reinterpret_cast<int32_t*>(bits + W);
   const int64_t ql = blockIdx.x;
   const int32_t q = (int32_t)(q_begin + ql);
-  const int n = min(count[ql], RQ_MAX_CAND);
+  const int32_t cbase = kTri ? (int32_t)blockIdx.y * RQ_MAX_CAND : 0;
+  const int n = kTri ? max(0, min(q - cbase, RQ_MAX_CAND)) : min(count[ql], RQ_MAX_CAND);
   if (n == 0) return;
   for (int w = threadIdx.x; w < W; w += blockDim.x) bits[w] = 0u;
   // sort keys: (column length, position in the list), longest first
@@ -516,7 +564,7 @@ __global__ void k_rerank_q(int method, int dist, DevCsc ref, ColAux ra, DevCsc q
   for (int t = threadIdx.x; t < np2; t += blockDim.x) {
     uint64_t key = 0;                       // padding sorts last
     if (t < n) {
-      const int32_t c = cand[ql * (int64_t)cap + t];
+      const int32_t c = kTri ? cbase + t : cand[ql * (int64_t)cap + t];
       const int64_t len64 = ref.p[c + 1] - ref.p[c];
       const uint32_t len = (uint32_t)(len64 < 0x7fffffff ? len64 : 0x7fffffff);
       key = ((uint64_t)(len + 1u) << 32) | (uint32_t)t;
@@ -563,7 +611,7 @@ __global__ void k_rerank_q(int method, int dist, DevCsc ref, ColAux ra, DevCsc q
     bool special = false;
     int64_t a = 0, a_end = 0, c0 = 0;
     if (t >= 0) {
-      c = cand[ql * (int64_t)cap + t];
+      c = kTri ? cbase + t : cand[ql * (int64_t)cap + t];
       if (restore_self && c == q) {
         v = self_value;
         special = true;
@@ -646,7 +694,8 @@ __global__ void k_rerank_q(int method, int dist, DevCsc ref, ColAux ra, DevCsc q
     }
     if (t >= 0) {
       if (!special) v = match_finish(method, dist != 0, sum, common, ref, ra, c, qry, qa, q);
-      out[ql * (int64_t)cap + t] = v;
+      if (kTri) out[(int64_t)q * ref.ncol + c] = v;
+      else out[ql * (int64_t)cap + t] = v;
     }
   }
 }
@@ -697,6 +746,33 @@ void launch_self_slab(int method, int dist, const DevCsc& m, const ColAux& a, in
   }
 }
 
+bool self_tri_supported(int method, int32_t nrow) {
+  return (method == BINARY || method == COSINE || method == PEARSON || method == COVARIANCE) &&
+         nrow <= RQ_MAX_NROW;
+}
+
+void launch_self_tri(int method, int dist, const DevCsc& m, const ColAux& a, int diag, double* D,
+                     cudaStream_t s) {
+  const int64_t n = m.ncol;
+  if (n == 0) return;
+  if (n > 1) {
+    const size_t smem = (size_t)RQ_MAX_QV * 8 + (size_t)RQ_MAX_CAND * 8 + (size_t)RQ_WARPS * 32 * RM * 8 +
+                        (size_t)((m.nrow + 31) / 32) * 8;
+    if (smem > 48 * 1024)
+      cudaFuncSetAttribute(k_rerank_q<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const unsigned chunks = (unsigned)((n - 1 + RQ_MAX_CAND - 1) / RQ_MAX_CAND);
+    k_rerank_q<true><<<dim3((unsigned)n, chunks), RQ_THREADS, smem, s>>>(method, dist, m, a, m, a, nullptr,
+                                                                        nullptr, 0, 0, 0, 0.0, D);
+  }
+  k_self_diag<<<blocks_for(n, 256), 256, 0, s>>>(method, dist, m, a, diag, D);
+}
+
+void launch_mirror_upper(double* D, int64_t n, int clear, cudaStream_t s) {
+  if (n <= 1) return;
+  const unsigned T = (unsigned)((n + 31) / 32);
+  k_mirror_upper<<<dim3(T, T), dim3(32, 8), 0, s>>>(D, n, clear);
+}
+
 void launch_mirror_lower(double* D, int64_t n, cudaStream_t s) {
   // the caller holds n x n doubles on the device, so n / 32 is far below the
   // 65,535 limit of gridDim.y
@@ -726,8 +802,8 @@ void launch_rerank_warp(int method, int dist, const DevCsc& ref, const ColAux& r
     const size_t smem = (size_t)RQ_MAX_QV * 8 + (size_t)RQ_MAX_CAND * 8 + (size_t)RQ_WARPS * 32 * RM * 8 +
                         (size_t)((qry.nrow + 31) / 32) * 8;
     if (smem > 48 * 1024)
-      cudaFuncSetAttribute(k_rerank_q, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_rerank_q<<<(unsigned)nq_local, RQ_THREADS, smem, s>>>(method, dist, ref, ra, qry, qa, cand, count, cap,
+      cudaFuncSetAttribute(k_rerank_q<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_rerank_q<false><<<(unsigned)nq_local, RQ_THREADS, smem, s>>>(method, dist, ref, ra, qry, qa, cand, count, cap,
                                                            q_begin, restore_self, self_value, out);
   } else {
     k_rerank_warp<<<blocks_for(nq_local, 8), 256, 0, s>>>(method, dist, ref, ra, qry, qa, cand,

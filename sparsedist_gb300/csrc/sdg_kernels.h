@@ -48,6 +48,16 @@ void launch_self_slab(int method, int dist, const DevCsc& m, const ColAux& a, in
 // Copies the strict lower triangle of the device n x n matrix D onto its
 // upper triangle.
 void launch_mirror_lower(double* D, int64_t n, cudaStream_t s);
+// The match-only methods (binary, cosine, pearson, covariance; nrow <= 2^18)
+// of the single-matrix form on the query-centric re-rank kernel: the strict
+// upper triangle D(c, q) = value(column c, column q), c < q, and the
+// diagonal; the lower triangle is left for launch_mirror_upper.
+bool self_tri_supported(int method, int32_t nrow);
+void launch_self_tri(int method, int dist, const DevCsc& m, const ColAux& a, int diag, double* D,
+                     cudaStream_t s);
+// Copies the strict upper triangle of D onto the lower one; with clear, the
+// upper triangle is zeroed after it is read.
+void launch_mirror_upper(double* D, int64_t n, int clear, cudaStream_t s);
 
 // Exact values of listed pairs: out[t] = value(ref col ref_idx[t], query col
 // qry_idx[t]).
