@@ -66,6 +66,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--dist-cols", type=int, default=10000)
+    ap.add_argument("--dist-long", action="store_true", help="long columns (configuration 2's generator)")
     ap.add_argument("--config", default="c2", choices=["c2", "c1", "c3", "serve", "dist", "snn"],
                     help="c2: the default line (configuration 2); c1: the CPU-runnable "
                          "configuration 1; serve: configuration 5, the serving loop")
@@ -262,12 +263,20 @@ def run_dist(args):
     from oracle import build as obuild
     from oracle.pyoracle import Oracle
     n = args.dist_cols
-    X = synth.uniform_csc(2000, n, 0.02, seed=1)
+    if args.dist_long:
+        # long columns: configuration 2's generator (nnz/col lognormal mean 1,800)
+        p, i, x = synth.logcount_csc(nrow=30000, ncol=n, mean_nnz=1800, seed=2, device="cuda")
+        X = sp.csc_matrix((np.asarray(x), np.asarray(i), np.asarray(p)), shape=(30000, n))
+        shape = "30000x%d log-count CSC (nnz/col lognormal mean 1800)" % n
+    else:
+        X = synth.uniform_csc(2000, n, 0.02, seed=1)
+        shape = "2000x%d CSC, 2%% uniform, |N(0,1)|" % n
     obuild.build_oracle()
     threads = os.cpu_count() or 1
     orc = Oracle(threads=threads)
     ctx = _lib.Context()
-    held = _lib.HeldCSC(2000, n, X.indptr, X.indices, X.data)
+    ctx.set_engine(args.engine)
+    held = _lib.HeldCSC(X.shape[0], n, X.indptr, X.indices, X.data)
     D = np.empty((n, n), np.float64)
     hbm_peak, _, peak_kind = measured_peaks()
     out = {}
@@ -292,7 +301,7 @@ def run_dist(args):
         want = orc.dist_single(method, Xs, True, False, True)
         same = bool(np.array_equal(D.T[:sample, :sample].view(np.uint64), want.view(np.uint64)))
         t0 = time.perf_counter()
-        cs = min(n, 3000)
+        cs = min(n, 3000 if not args.dist_long else 600)
         orc.dist_single(method, X[:, :cs], True, False, True)
         cpu_pairs_s = cs * (cs - 1) / 2 / (time.perf_counter() - t0)
         kern_s = kms / 1000.0 / max(kl, 1)
@@ -310,8 +319,8 @@ def run_dist(args):
             "identical_on_%d_columns" % sample: same, "clocks": clk.summary()}
         torch.cuda.synchronize()
     print(json.dumps({"metric": "full-matrix sparseDist column pairs/s",
-                      "config": {"workload": "sparseDist(X, full = TRUE, diag = FALSE), X 2000x%d CSC, "
-                                             "2%% uniform, |N(0,1)|" % n},
+                      "config": {"workload": "sparseDist(X, full = TRUE, diag = FALSE), X " + shape,
+                                 "engine": args.engine},
                       "dtype": "f64", "data": "synthetic", "steps": args.steps, "warmup": args.warmup,
                       "results": out}))
 

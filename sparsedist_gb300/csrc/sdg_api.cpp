@@ -683,6 +683,10 @@ SDG_API int sdg_dist_cross(sdg_ctx* c, int method, int dist, const sdg_csc* m, c
   });
 }
 
+// mean stored entries per column from which the single-matrix form of the
+// match-only methods runs on the query-centric kernel
+constexpr double kSelfTriMinNnz = 256.0;
+
 SDG_API int sdg_dist(sdg_ctx* c, int method, int dist, const sdg_csc* m, int full, int diag,
                      double* D) {
   return guarded([&] {
@@ -710,9 +714,14 @@ SDG_API int sdg_dist(sdg_ctx* c, int method, int dist, const sdg_csc* m, int ful
     if (whole <= cap) {
       // resident: the lower triangle once, mirrored on the device with full
       DevBuf Dd(whole, s);
-      if (self_tri_supported(method, a->nrow)) {
-        // match-only methods: the upper triangle on the query-centric kernel
-        // (one pair per lane), then moved to the lower one
+      // match-only methods with long columns: the upper triangle on the
+      // query-centric kernel (one pair per lane), then moved to the lower
+      // one; short columns merge faster one pair per thread.  Engine 1 forces
+      // the per-thread kernel, 2 / 3 the query-centric one where supported.
+      const double mean_nnz = (double)a->nnz / (double)n;
+      const bool tri = self_tri_supported(method, a->nrow) &&
+                       (c->engine == 2 || c->engine == 3 || (c->engine == 0 && mean_nnz >= kSelfTriMinNnz));
+      if (tri) {
         sdg_time_begin(c);
         launch_self_tri(method, dist, a->dev(), aux_of(a.get()), diag, Dd.as<double>(), s);
         sdg_time_end(c);

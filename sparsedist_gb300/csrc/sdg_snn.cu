@@ -11,6 +11,11 @@
 #include <cub/device/device_scan.cuh>
 #include <cub/device/device_select.cuh>
 
+#include <algorithm>
+#include <cstdlib>
+#include <utility>
+#include <vector>
+
 #include "sdg_kernels.h"
 #include "sdg_snn_core.cuh"
 
@@ -128,14 +133,26 @@ __global__ void k_shared_count(const int32_t* mk_by_i, const int32_t* iv_by_i, i
   cnt[e] = rp[m + 1] - shared_after(rev, rp[m], rp[m + 1], i);
 }
 
-__global__ void k_shared_emit(const int32_t* mk_by_i, const int32_t* iv_by_i, int64_t t, const int64_t* rp,
-                              const int32_t* rev, const int64_t* pos, int32_t n, uint64_t* keys) {
-  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (e >= t) return;
+// the keys of members t0 .. t1 - 1 (whole rows), at pos[e] - base
+__global__ void k_shared_emit(const int32_t* mk_by_i, const int32_t* iv_by_i, int64_t t0, int64_t t1,
+                              const int64_t* rp, const int32_t* rev, const int64_t* pos, int64_t base,
+                              int32_t n, uint64_t* keys) {
+  const int64_t e = t0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= t1) return;
   const int32_t m = mk_by_i[e], i = iv_by_i[e];
   const int64_t q0 = shared_after(rev, rp[m], rp[m + 1], i);
-  uint64_t* out = keys + pos[e];
+  uint64_t* out = keys + (pos[e] - base);
   for (int64_t q = q0; q < rp[m + 1]; ++q) out[q - q0] = (uint64_t)i * (uint64_t)n + (uint64_t)rev[q];
+}
+
+// rowpos[i] = number of keys before row i's first member (members are in
+// row order; a row without members starts where the next one does)
+__global__ void k_shared_rowpos(const int64_t* off, const int64_t* pos, const int64_t* cnt, int64_t t,
+                                int32_t n, int64_t* rowpos) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i > n) return;
+  const int64_t o = off[i];
+  rowpos[i] = (o < t) ? pos[o] : (t > 0 ? pos[t - 1] + cnt[t - 1] : 0);
 }
 
 // one run = one pair (i, j) with its overlap count: weight, prune, and both
@@ -249,125 +266,187 @@ int snn_graph_build(const int32_t* d_idx, const double* d_w, int32_t n, int32_t 
   return 0;
 }
 
+// Device buffers of one build, released on every return path (stream
+// ordered); release() hands a buffer to the caller instead.
+struct AsyncBufs {
+  cudaStream_t s;
+  std::vector<void*> held;
+  explicit AsyncBufs(cudaStream_t st) : s(st) {}
+  ~AsyncBufs() { for (void* q : held) if (q) cudaFreeAsync(q, s); }
+  template <class T> cudaError_t alloc(T** out, size_t count) {
+    *out = nullptr;
+    const cudaError_t e = cudaMallocAsync((void**)out, sizeof(T) * (count ? count : 1), s);
+    if (e == cudaSuccess) held.push_back((void*)*out);
+    return e;
+  }
+  void drop(void* q) {
+    for (auto& h : held) if (h == q) { cudaFreeAsync(h, s); h = nullptr; }
+  }
+  void release(void* q) {
+    for (auto& h : held) if (h == q) h = nullptr;
+  }
+};
+
 int snn_shared_build(const int32_t* d_sets, const int32_t* d_sizes, int32_t n, int32_t k, double prune,
                      int64_t* nnz_host, int32_t** d_p, int32_t** d_i, double** d_x, cudaStream_t s) {
-  // set sizes -> offsets of the (m, i) member pairs
-  int64_t *off = nullptr, *rp = nullptr, *cnt = nullptr, *pos = nullptr, *nruns = nullptr;
-  void* tmp = nullptr;
+  AsyncBufs B(s);
   size_t tb = 0, tb2 = 0;
-  SDG_TRY(cudaMallocAsync(&off, sizeof(int64_t) * ((size_t)n + 1), s));
-  {
-    // exclusive sum of the set sizes, widened to int64 (a strided copy into
-    // the low words of a zeroed int64 array; sizes are non-negative)
-    int64_t* sz64 = nullptr;
-    SDG_TRY(cudaMallocAsync(&sz64, sizeof(int64_t) * ((size_t)n + 1), s));
-    SDG_TRY(cudaMemsetAsync(sz64, 0, sizeof(int64_t) * ((size_t)n + 1), s));
-    SDG_TRY(cudaMemcpy2DAsync(sz64, sizeof(int64_t), d_sizes, sizeof(int32_t), sizeof(int32_t), (size_t)n,
-                              cudaMemcpyDeviceToDevice, s));
-    SDG_TRY(cub::DeviceScan::ExclusiveSum(nullptr, tb, sz64, off, (int)n + 1, s));
-    SDG_TRY(cudaMallocAsync(&tmp, tb + 16, s));
-    SDG_TRY(cub::DeviceScan::ExclusiveSum(tmp, tb, sz64, off, (int)n + 1, s));
-    SDG_TRY(cudaFreeAsync(tmp, s));
-    SDG_TRY(cudaFreeAsync(sz64, s));
-    tmp = nullptr;
-  }
+  void* tmp = nullptr;
+  // set sizes -> offsets of the (m, i) member pairs
+  int64_t *off = nullptr, *sz64 = nullptr;
+  SDG_TRY(B.alloc(&off, (size_t)n + 1));
+  SDG_TRY(B.alloc(&sz64, (size_t)n + 1));
+  // exclusive sum of the set sizes, widened to int64 (a strided copy into the
+  // low words of a zeroed int64 array; sizes are non-negative)
+  SDG_TRY(cudaMemsetAsync(sz64, 0, sizeof(int64_t) * ((size_t)n + 1), s));
+  SDG_TRY(cudaMemcpy2DAsync(sz64, sizeof(int64_t), d_sizes, sizeof(int32_t), sizeof(int32_t), (size_t)n,
+                            cudaMemcpyDeviceToDevice, s));
+  SDG_TRY(cub::DeviceScan::ExclusiveSum(nullptr, tb, sz64, off, (int)n + 1, s));
+  SDG_TRY(B.alloc((char**)&tmp, tb + 16));
+  SDG_TRY(cub::DeviceScan::ExclusiveSum(tmp, tb, sz64, off, (int)n + 1, s));
+  B.drop(tmp);
+  B.drop(sz64);
   int64_t t = 0;
   SDG_TRY(cudaMemcpyAsync(&t, off + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
   SDG_TRY(cudaStreamSynchronize(s));
   uint32_t *mk = nullptr, *mk2 = nullptr;
   int32_t *iv = nullptr, *rev = nullptr;
-  SDG_TRY(cudaMallocAsync(&mk, sizeof(uint32_t) * ((size_t)t + 1), s));
-  SDG_TRY(cudaMallocAsync(&mk2, sizeof(uint32_t) * ((size_t)t + 1), s));
-  SDG_TRY(cudaMallocAsync(&iv, sizeof(int32_t) * ((size_t)t + 1), s));
-  SDG_TRY(cudaMallocAsync(&rev, sizeof(int32_t) * ((size_t)t + 1), s));
-  SDG_TRY(cudaMallocAsync(&rp, sizeof(int64_t) * ((size_t)n + 1), s));
-  SDG_TRY(cudaMallocAsync(&cnt, sizeof(int64_t) * ((size_t)t + 1), s));
-  SDG_TRY(cudaMallocAsync(&pos, sizeof(int64_t) * ((size_t)t + 1), s));
+  int64_t *rp = nullptr, *cnt = nullptr, *pos = nullptr;
+  SDG_TRY(B.alloc(&mk, (size_t)t + 1));
+  SDG_TRY(B.alloc(&mk2, (size_t)t + 1));
+  SDG_TRY(B.alloc(&iv, (size_t)t + 1));
+  SDG_TRY(B.alloc(&rev, (size_t)t + 1));
+  SDG_TRY(B.alloc(&rp, (size_t)n + 1));
+  SDG_TRY(B.alloc(&cnt, (size_t)t + 1));
+  SDG_TRY(B.alloc(&pos, (size_t)t + 1));
   k_shared_pairs<<<blocks_for(n, 128), 128, 0, s>>>(d_sets, d_sizes, off, n, k, mk, iv);
   // R(m): a stable sort by m keeps each R(m) in ascending i
   int mbits = 1;
   while (mbits < 32 && ((uint64_t)n >> mbits) != 0) ++mbits;
   SDG_TRY(cub::DeviceRadixSort::SortPairs(nullptr, tb, mk, mk2, iv, rev, (int)t, 0, mbits, s));
-  SDG_TRY(cudaMallocAsync(&tmp, tb + 16, s));
+  SDG_TRY(B.alloc((char**)&tmp, tb + 16));
   if (t > 0) SDG_TRY(cub::DeviceRadixSort::SortPairs(tmp, tb, mk, mk2, iv, rev, (int)t, 0, mbits, s));
-  SDG_TRY(cudaFreeAsync(tmp, s));
-  tmp = nullptr;
+  B.drop(tmp);
   k_shared_revptr<<<blocks_for((int64_t)n + 1, 256), 256, 0, s>>>(mk2, t, n, rp);
   // the members in (i, position) order again (mk / iv were sort inputs, unchanged)
   if (t > 0) {
     k_shared_count<<<blocks_for(t, 256), 256, 0, s>>>(reinterpret_cast<const int32_t*>(mk), iv, t, rp, rev, cnt);
     SDG_TRY(cub::DeviceScan::ExclusiveSum(nullptr, tb, cnt, pos, (int)t, s));
-    SDG_TRY(cudaMallocAsync(&tmp, tb + 16, s));
+    SDG_TRY(B.alloc((char**)&tmp, tb + 16));
     SDG_TRY(cub::DeviceScan::ExclusiveSum(tmp, tb, cnt, pos, (int)t, s));
-    SDG_TRY(cudaFreeAsync(tmp, s));
-    tmp = nullptr;
+    B.drop(tmp);
   }
-  int64_t E = 0;
-  if (t > 0) {
-    int64_t last_pos = 0, last_cnt = 0;
-    SDG_TRY(cudaMemcpyAsync(&last_pos, pos + (t - 1), sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-    SDG_TRY(cudaMemcpyAsync(&last_cnt, cnt + (t - 1), sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-    SDG_TRY(cudaStreamSynchronize(s));
-    E = last_pos + last_cnt;
+  // key count before each row's first member: chunks of whole rows, so that
+  // every pair (i, j), whose keys all come from row i's members, is counted
+  // within one chunk
+  int64_t* rowpos = nullptr;
+  SDG_TRY(B.alloc(&rowpos, (size_t)n + 1));
+  k_shared_rowpos<<<blocks_for((int64_t)n + 1, 256), 256, 0, s>>>(off, pos, cnt, t, n, rowpos);
+  std::vector<int64_t> h_rowpos((size_t)n + 1), h_off((size_t)n + 1);
+  SDG_TRY(cudaMemcpyAsync(h_rowpos.data(), rowpos, sizeof(int64_t) * ((size_t)n + 1), cudaMemcpyDeviceToHost, s));
+  SDG_TRY(cudaMemcpyAsync(h_off.data(), off, sizeof(int64_t) * ((size_t)n + 1), cudaMemcpyDeviceToHost, s));
+  SDG_TRY(cudaStreamSynchronize(s));
+  // one row emits at most (k + 1) n keys; a chunk holds at least one row.
+  // 2^28 keys (2 GiB of keys, about 7 GiB with the sort's buffers) unless
+  // SDG_SNN_CHUNK_KEYS asks for less
+  int64_t want = (int64_t)1 << 28;
+  if (const char* ev = std::getenv("SDG_SNN_CHUNK_KEYS")) {
+    const long long v = std::atoll(ev);
+    if (v > 0) want = std::min<int64_t>(want, (int64_t)v);
   }
-  if (E >= ((int64_t)1 << 31)) return (int)cudaErrorInvalidValue;   // beyond one CUB pass
-  uint64_t *keys = nullptr, *keys2 = nullptr, *okeys = nullptr, *okeys2 = nullptr;
+  const int64_t chunk_cap = std::max<int64_t>(want, (int64_t)(k + 1) * n);
+  std::vector<std::pair<int32_t, int32_t>> chunks;
+  int64_t max_chunk = 0;
+  for (int32_t i0 = 0; i0 < n;) {
+    int32_t i1 = i0 + 1;
+    while (i1 < n && h_rowpos[(size_t)i1 + 1] - h_rowpos[(size_t)i0] <= chunk_cap) ++i1;
+    const int64_t e = h_rowpos[(size_t)i1] - h_rowpos[(size_t)i0];
+    if (e > 0) {
+      chunks.emplace_back(i0, i1);
+      max_chunk = std::max(max_chunk, e);
+    }
+    i0 = i1;
+  }
+  if (max_chunk >= ((int64_t)1 << 31)) return (int)cudaErrorInvalidValue;
+  const int bits = key_bits(n);
+  uint64_t *keys = nullptr, *keys2 = nullptr, *okeys = nullptr;
   int32_t* counts = nullptr;
-  double *ovals = nullptr, *ovals2 = nullptr;
+  double* ovals = nullptr;
+  int64_t* nruns = nullptr;
   unsigned long long* kept = nullptr;
-  SDG_TRY(cudaMallocAsync(&keys, sizeof(uint64_t) * ((size_t)E + 1), s));
-  SDG_TRY(cudaMallocAsync(&keys2, sizeof(uint64_t) * ((size_t)E + 1), s));
-  SDG_TRY(cudaMallocAsync(&counts, sizeof(int32_t) * ((size_t)E + 1), s));
-  SDG_TRY(cudaMallocAsync(&nruns, sizeof(int64_t), s));
-  SDG_TRY(cudaMallocAsync(&kept, sizeof(unsigned long long), s));
-  SDG_TRY(cudaMemsetAsync(nruns, 0, sizeof(int64_t), s));
+  SDG_TRY(B.alloc(&keys, (size_t)max_chunk + 1));
+  SDG_TRY(B.alloc(&keys2, (size_t)max_chunk + 1));
+  SDG_TRY(B.alloc(&counts, (size_t)max_chunk + 1));
+  SDG_TRY(B.alloc(&nruns, 1));
+  SDG_TRY(B.alloc(&kept, 1));
   SDG_TRY(cudaMemsetAsync(kept, 0, sizeof(unsigned long long), s));
-  if (E > 0) {
-    k_shared_emit<<<blocks_for(t, 256), 256, 0, s>>>(reinterpret_cast<const int32_t*>(mk), iv, t, rp, rev, pos, n,
-                                                     keys);
-    const int bits = key_bits(n);
-    SDG_TRY(cub::DeviceRadixSort::SortKeys(nullptr, tb, keys, keys2, (int)E, 0, bits, s));
-    SDG_TRY(cub::DeviceRunLengthEncode::Encode(nullptr, tb2, keys2, keys, counts, nruns, (int)E, s));
+  if (max_chunk > 0) {
+    SDG_TRY(cub::DeviceRadixSort::SortKeys(nullptr, tb, keys, keys2, (int)max_chunk, 0, bits, s));
+    SDG_TRY(cub::DeviceRunLengthEncode::Encode(nullptr, tb2, keys2, keys, counts, nruns, (int)max_chunk, s));
     if (tb2 > tb) tb = tb2;
-    SDG_TRY(cudaMallocAsync(&tmp, tb + 16, s));
-    SDG_TRY(cub::DeviceRadixSort::SortKeys(tmp, tb, keys, keys2, (int)E, 0, bits, s));
-    SDG_TRY(cub::DeviceRunLengthEncode::Encode(tmp, tb, keys2, keys, counts, nruns, (int)E, s));
-    SDG_TRY(cudaFreeAsync(tmp, s));
-    tmp = nullptr;
+    SDG_TRY(B.alloc((char**)&tmp, tb + 16));
   }
-  int64_t runs = 0;
-  SDG_TRY(cudaMemcpyAsync(&runs, nruns, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-  SDG_TRY(cudaStreamSynchronize(s));
-  SDG_TRY(cudaMallocAsync(&okeys, sizeof(uint64_t) * ((size_t)(2 * runs) + 1), s));
-  SDG_TRY(cudaMallocAsync(&okeys2, sizeof(uint64_t) * ((size_t)(2 * runs) + 1), s));
-  SDG_TRY(cudaMallocAsync(&ovals, sizeof(double) * ((size_t)(2 * runs) + 1), s));
-  SDG_TRY(cudaMallocAsync(&ovals2, sizeof(double) * ((size_t)(2 * runs) + 1), s));
-  if (runs > 0)
-    k_shared_weights<<<blocks_for(runs, 256), 256, 0, s>>>(keys, counts, nruns, d_sizes, n, prune, okeys, ovals,
-                                                          kept);
-  unsigned long long m_host = 0;
-  SDG_TRY(cudaMemcpyAsync(&m_host, kept, sizeof m_host, cudaMemcpyDeviceToHost, s));
-  SDG_TRY(cudaStreamSynchronize(s));
-  const int64_t m = (int64_t)m_host;
+  int64_t out_cap = 0, kept_total = 0;
+  for (const auto& ch : chunks) {
+    const int64_t base = h_rowpos[(size_t)ch.first];
+    const int64_t e = h_rowpos[(size_t)ch.second] - base;
+    const int64_t t0 = h_off[(size_t)ch.first], t1 = h_off[(size_t)ch.second];
+    k_shared_emit<<<blocks_for(t1 - t0, 256), 256, 0, s>>>(reinterpret_cast<const int32_t*>(mk), iv, t0, t1, rp,
+                                                           rev, pos, base, n, keys);
+    size_t tbs = tb;
+    SDG_TRY(cub::DeviceRadixSort::SortKeys(tmp, tbs, keys, keys2, (int)e, 0, bits, s));
+    tbs = tb;
+    SDG_TRY(cub::DeviceRunLengthEncode::Encode(tmp, tbs, keys2, keys, counts, nruns, (int)e, s));
+    int64_t runs = 0;
+    SDG_TRY(cudaMemcpyAsync(&runs, nruns, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    SDG_TRY(cudaStreamSynchronize(s));
+    if (kept_total + 2 * runs > out_cap) {            // grow the kept (key, weight) lists
+      const int64_t cap = std::max<int64_t>(2 * out_cap, kept_total + 2 * runs);
+      uint64_t* nk = nullptr;
+      double* nv = nullptr;
+      SDG_TRY(B.alloc(&nk, (size_t)cap));
+      SDG_TRY(B.alloc(&nv, (size_t)cap));
+      if (kept_total > 0) {
+        SDG_TRY(cudaMemcpyAsync(nk, okeys, sizeof(uint64_t) * (size_t)kept_total, cudaMemcpyDeviceToDevice, s));
+        SDG_TRY(cudaMemcpyAsync(nv, ovals, sizeof(double) * (size_t)kept_total, cudaMemcpyDeviceToDevice, s));
+      }
+      if (okeys) B.drop(okeys);
+      if (ovals) B.drop(ovals);
+      okeys = nk;
+      ovals = nv;
+      out_cap = cap;
+    }
+    if (runs > 0)
+      k_shared_weights<<<blocks_for(runs, 256), 256, 0, s>>>(keys, counts, nruns, d_sizes, n, prune, okeys, ovals,
+                                                            kept);
+    unsigned long long m_host = 0;
+    SDG_TRY(cudaMemcpyAsync(&m_host, kept, sizeof m_host, cudaMemcpyDeviceToHost, s));
+    SDG_TRY(cudaStreamSynchronize(s));
+    kept_total = (int64_t)m_host;
+  }
+  const int64_t m = kept_total;
+  if (m >= ((int64_t)1 << 31)) return (int)cudaErrorInvalidValue;   // beyond a dgCMatrix
+  uint64_t* okeys2 = nullptr;
+  double* ovals2 = nullptr;
+  SDG_TRY(B.alloc(&okeys2, (size_t)m + 1));
+  SDG_TRY(B.alloc(&ovals2, (size_t)m + 1));
   if (m > 0) {
-    const int bits = key_bits(n);
-    SDG_TRY(cub::DeviceRadixSort::SortPairs(nullptr, tb, okeys, okeys2, ovals, ovals2, (int)m, 0, bits, s));
-    SDG_TRY(cudaMallocAsync(&tmp, tb + 16, s));
-    SDG_TRY(cub::DeviceRadixSort::SortPairs(tmp, tb, okeys, okeys2, ovals, ovals2, (int)m, 0, bits, s));
-    SDG_TRY(cudaFreeAsync(tmp, s));
-    tmp = nullptr;
+    size_t tbo = 0;
+    SDG_TRY(cub::DeviceRadixSort::SortPairs(nullptr, tbo, okeys, okeys2, ovals, ovals2, (int)m, 0, bits, s));
+    void* tmp2 = nullptr;
+    SDG_TRY(B.alloc((char**)&tmp2, tbo + 16));
+    SDG_TRY(cub::DeviceRadixSort::SortPairs(tmp2, tbo, okeys, okeys2, ovals, ovals2, (int)m, 0, bits, s));
   }
   int32_t* p = nullptr;
   int32_t* rows = nullptr;
-  SDG_TRY(cudaMallocAsync(&p, sizeof(int32_t) * ((size_t)n + 1), s));
-  SDG_TRY(cudaMallocAsync(&rows, sizeof(int32_t) * ((size_t)m + 1), s));
+  SDG_TRY(B.alloc(&p, (size_t)n + 1));
+  SDG_TRY(B.alloc(&rows, (size_t)m + 1));
   k_snn_colptr<<<blocks_for((int64_t)n + 1, 256), 256, 0, s>>>(okeys2, m, n, p);
   if (m > 0) k_snn_rows<<<blocks_for(m, 256), 256, 0, s>>>(okeys2, m, n, rows);
   SDG_TRY(cudaGetLastError());
-  for (void* q : {(void*)off, (void*)rp, (void*)cnt, (void*)pos, (void*)nruns, (void*)mk, (void*)mk2, (void*)iv,
-                  (void*)rev, (void*)keys, (void*)keys2, (void*)counts, (void*)kept, (void*)okeys,
-                  (void*)okeys2, (void*)ovals})
-    SDG_TRY(cudaFreeAsync(q, s));
+  B.release(p);
+  B.release(rows);
+  B.release(ovals2);
   *nnz_host = m;
   *d_p = p;
   *d_i = rows;

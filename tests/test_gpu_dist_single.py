@@ -28,27 +28,39 @@ def test_gpu_dist_known_answers(gpu, fn):
     fn(gpu)
 
 
-@pytest.mark.parametrize("resident", [None, "0", "4000"])
-def test_gpu_dist_random_vs_oracle(gpu, orc, resident, monkeypatch):
+@pytest.mark.parametrize("resident,engine", [(None, 0), (None, 1), (None, 2), ("0", 0), ("4000", 0)])
+def test_gpu_dist_random_vs_oracle(gpu, orc, resident, engine, monkeypatch):
+    # engine 1: the per-thread merge kernel; 2: the query-centric kernel for
+    # the match-only methods; 0: chosen by column length
     if resident is not None:
         monkeypatch.setenv("SDG_DIST_RESIDENT_BYTES", resident)
+    gpu.set_engine(engine)
     n = 0
-    for method, X, full, diag, dist in random_dist_cases(5 if resident is None else 6, 2):
-        got = gpu.dist_single(method, X, full, diag, dist)
-        want = orc.dist_single(method, X, full, diag, dist)
-        assert dist_equal(method, got, want), (method, X.shape, full, diag, dist, resident)
-        n += 1
+    try:
+        for method, X, full, diag, dist in random_dist_cases(5 if resident is None else 6, 2):
+            got = gpu.dist_single(method, X, full, diag, dist)
+            want = orc.dist_single(method, X, full, diag, dist)
+            assert dist_equal(method, got, want), (method, X.shape, full, diag, dist, resident, engine)
+            n += 1
+    finally:
+        gpu.set_engine(0)
     assert n > 60
 
 
-def test_gpu_dist_larger_than_one_tile_grid(gpu, orc):
-    # n not a multiple of 32 across several mirror tiles; 1,000 x 700 columns
-    X = make_x(1000, 700, 0.02, 3)
-    for method in ("binary", "euclidean", "covariance"):
-        for full in (False, True):
-            got = gpu.dist_single(method, X, full, True, True)
-            want = orc.dist_single(method, X, full, True, True)
-            assert dist_equal(method, got, want), (method, full)
+@pytest.mark.parametrize("engine", [1, 2])
+def test_gpu_dist_larger_than_one_tile_grid(gpu, orc, engine):
+    # n not a multiple of 32 across several mirror tiles and more than one
+    # 2,048-candidate chunk of the query-centric kernel; long columns too
+    gpu.set_engine(engine)
+    try:
+        for X in (make_x(1000, 2300, 0.02, 3), make_x(3000, 300, 0.3, 4)):
+            for method in ("binary", "cosine", "euclidean", "covariance"):
+                for full in (False, True):
+                    got = gpu.dist_single(method, X, full, True, True)
+                    want = orc.dist_single(method, X, full, True, True)
+                    assert dist_equal(method, got, want), (method, X.shape, full, engine)
+    finally:
+        gpu.set_engine(0)
 
 
 def test_sparse_dist_api_storage_and_values(orc):

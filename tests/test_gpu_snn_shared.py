@@ -70,3 +70,19 @@ def test_from_a_knn_result_through_the_api(oracle):
         d = (g - g.T)
         assert d.nnz == 0 or np.all(d.data == 0)
         assert np.all(g.diagonal() == 0)
+
+
+@pytest.mark.parametrize("chunk", ["1", "5000", "100000"])
+def test_expansion_in_row_chunks(ctx, oracle, monkeypatch, chunk):
+    """The (i, j) keys are expanded, sorted and counted in chunks of whole
+    rows when they exceed the chunk size (SDG_SNN_CHUNK_KEYS lowers it; a
+    chunk always holds at least one row): the graph must not change."""
+    monkeypatch.setenv("SDG_SNN_CHUNK_KEYS", chunk)
+    rng = np.random.default_rng(5)
+    n, k = 2500, 12
+    # a few hub columns shared by many rows make long R(m) lists
+    idx = np.where(rng.random((n, k)) < 0.3, rng.integers(1, 30, (n, k)),
+                   rng.integers(1, n + 1, (n, k))).astype(np.int32)
+    idx[rng.random((n, k)) < 0.05] = NA
+    for inc, pr in ((True, 0.0), (False, 1 / 15), (True, 0.3)):
+        assert same(gpu_graph(ctx, idx, inc, pr), oracle.snn_graph_shared(idx, inc, pr)), (chunk, inc, pr)
