@@ -175,8 +175,10 @@ SDG_API int sdg_knn_cross(sdg_ctx* ctx, const sdg_csc* X, const sdg_csc* Y, int 
 
 /* sparseSNN(idx, include_self, prune, symmetrise, edges = "knn") as the slots
  * of the n x n dgCMatrix.  Call once with p == NULL to learn *nnz, then with
- * p (n + 1), i and x (nnz each).  Replaces snnJaccard plus the Matrix
- * assembly of R/sparseSNN.R:221-250. */
+ * p (n + 1), i and x (nnz each).  The size query keeps its graph on the
+ * device and a fetch with the same arguments and idx contents copies it
+ * instead of building it again (any other call on ctx drops it).  Replaces
+ * snnJaccard plus the Matrix assembly of R/sparseSNN.R:221-250. */
 SDG_API int sdg_snn_graph(sdg_ctx* ctx, const int32_t* idx, int32_t n, int32_t k,
                           int include_self, double prune, int symmetrise, int64_t* nnz,
                           int32_t* p, int32_t* i, double* x);

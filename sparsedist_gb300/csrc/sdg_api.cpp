@@ -131,6 +131,23 @@ struct DevBuf {
   template <typename T> T* as() const { return static_cast<T*>(p); }
 };
 
+// The SNN graph a size query (p == NULL) built, kept on the device for the
+// call that fetches the slots, so that the two-call protocol computes the
+// graph once.  Matched on every argument and on a copy of idx's contents.
+struct GraphCache {
+  int kind = 0;                        // 1: edges = "knn", 2: edges = "shared"
+  int32_t n = 0, k = 0;
+  int include_self = 0, symmetrise = 0;
+  double prune = 0.0;
+  std::vector<int32_t> idx;
+  int64_t m = 0;
+  DevBuf p, i, x;
+  bool matches(int kind_, const int32_t* idx_, int32_t n_, int32_t k_, int inc, int sym, double prune_) const {
+    return kind == kind_ && n == n_ && k == k_ && include_self == inc && symmetrise == sym && prune == prune_ &&
+           std::memcmp(idx.data(), idx_, sizeof(int32_t) * (size_t)n_ * (size_t)k_) == 0;
+  }
+};
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -154,6 +171,7 @@ struct sdg_ctx {
   // copy already exists (serving workers share the reference and must not
   // build it concurrently)
   bool tensor_lazy = true;
+  std::unique_ptr<GraphCache> graph;   // see GraphCache
 };
 
 namespace {
@@ -592,6 +610,7 @@ SDG_API int sdg_ctx_create(int device, sdg_ctx** out) {
 SDG_API int sdg_ctx_destroy(sdg_ctx* c) {
   if (!c) return SDG_OK;
   cudaStreamSynchronize(c->stream);
+  c->graph.reset();
   for (auto& e : c->ev) if (e) cudaEventDestroy(e);
   for (auto& pr : c->tev) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
   cudaStreamDestroy(c->own_stream);
@@ -874,6 +893,61 @@ SDG_API int sdg_snn_jaccard(sdg_ctx* c, const int32_t* idx, int32_t n, int32_t k
   });
 }
 
+namespace {
+
+// Copies a graph's slots to the host (p, i, x non-NULL).
+void graph_to_host(sdg_ctx* c, int32_t n, int64_t m, const void* dp, const void* drow, const void* dx,
+                   int32_t* p, int32_t* i, double* x) {
+  CK(cudaMemcpyAsync(p, dp, sizeof(int32_t) * ((size_t)n + 1), cudaMemcpyDeviceToHost, c->stream));
+  if (m > 0) {
+    CK(cudaMemcpyAsync(i, drow, sizeof(int32_t) * (size_t)m, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(x, dx, sizeof(double) * (size_t)m, cudaMemcpyDeviceToHost, c->stream));
+  }
+  CK(cudaStreamSynchronize(c->stream));
+}
+
+// A fetch (p != NULL) that a size query with the same arguments prepared:
+// copies the kept graph and drops it.
+bool graph_from_cache(sdg_ctx* c, int kind, const int32_t* idx, int32_t n, int32_t k, int inc, int sym,
+                      double prune, int64_t* nnz, int32_t* p, int32_t* i, double* x) {
+  GraphCache* g = c->graph.get();
+  if (!p || !g || !idx || !g->matches(kind, idx, n, k, inc, sym, prune)) return false;
+  *nnz = g->m;
+  graph_to_host(c, n, g->m, g->p.p, g->i.p, g->x.p, p, i, x);
+  c->graph.reset();
+  return true;
+}
+
+// After a build: a size query keeps the graph for the fetch; a fetch copies it.
+void graph_finish(sdg_ctx* c, int kind, const int32_t* idx, int32_t n, int32_t k, int inc, int sym, double prune,
+                  int64_t m, DevBuf& hp, DevBuf& hi, DevBuf& hx, int64_t* nnz, int32_t* p, int32_t* i,
+                  double* x) {
+  *nnz = m;
+  if (p) {
+    graph_to_host(c, n, m, hp.p, hi.p, hx.p, p, i, x);
+    return;
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  auto g = std::make_unique<GraphCache>();
+  g->kind = kind;
+  g->n = n;
+  g->k = k;
+  g->include_self = inc;
+  g->symmetrise = sym;
+  g->prune = prune;
+  g->idx.assign(idx, idx + (size_t)n * (size_t)k);
+  g->m = m;
+  g->p = std::move(hp);
+  g->i = std::move(hi);
+  g->x = std::move(hx);
+  g->p.detach();                          // freed synchronously, whatever stream is current then
+  g->i.detach();
+  g->x.detach();
+  c->graph = std::move(g);
+}
+
+}  // namespace
+
 SDG_API int sdg_snn_graph(sdg_ctx* c, const int32_t* idx, int32_t n, int32_t k, int include_self,
                           double prune, int symmetrise, int64_t* nnz, int32_t* p, int32_t* i,
                           double* x) {
@@ -883,6 +957,8 @@ SDG_API int sdg_snn_graph(sdg_ctx* c, const int32_t* idx, int32_t n, int32_t k, 
     CK(cudaSetDevice(c->device));
     if (!(prune >= 0.0 && prune <= 1.0))
       fail(SDG_E_ARG, "'prune' must be a finite number between 0 and 1.");
+    if (graph_from_cache(c, 1, idx, n, k, include_self, symmetrise, prune, nnz, p, i, x)) return;
+    c->graph.reset();
     DevBuf di, dw;
     snn_weights_device(c, idx, n, k, include_self, &di, &dw);
     int32_t *dp = nullptr, *drow = nullptr;
@@ -895,15 +971,7 @@ SDG_API int sdg_snn_graph(sdg_ctx* c, const int32_t* idx, int32_t n, int32_t k, 
     hp.p = dp; hp.s = c->stream;
     hi.p = drow; hi.s = c->stream;
     hx.p = dx; hx.s = c->stream;
-    *nnz = m;
-    if (p) {
-      CK(cudaMemcpyAsync(p, dp, sizeof(int32_t) * ((size_t)n + 1), cudaMemcpyDeviceToHost, c->stream));
-      if (m > 0) {
-        CK(cudaMemcpyAsync(i, drow, sizeof(int32_t) * (size_t)m, cudaMemcpyDeviceToHost, c->stream));
-        CK(cudaMemcpyAsync(x, dx, sizeof(double) * (size_t)m, cudaMemcpyDeviceToHost, c->stream));
-      }
-    }
-    CK(cudaStreamSynchronize(c->stream));
+    graph_finish(c, 1, idx, n, k, include_self, symmetrise, prune, m, hp, hi, hx, nnz, p, i, x);
   });
 }
 
@@ -916,6 +984,8 @@ SDG_API int sdg_snn_graph_shared(sdg_ctx* c, const int32_t* idx, int32_t n, int3
     if (!(prune >= 0.0 && prune <= 1.0))
       fail(SDG_E_ARG, "'prune' must be a finite number between 0 and 1.");
     if (n < 1 || k < 1) fail(SDG_E_ARG, "'idx' must have at least one row and column.");
+    if (graph_from_cache(c, 2, idx, n, k, include_self, 1, prune, nnz, p, i, x)) return;
+    c->graph.reset();
     cudaStream_t s = c->stream;
     const int64_t total = (int64_t)n * k;
     DevBuf di(sizeof(int32_t) * (size_t)total, s);
@@ -939,15 +1009,7 @@ SDG_API int sdg_snn_graph_shared(sdg_ctx* c, const int32_t* idx, int32_t n, int3
     hp.p = dp; hp.s = s;
     hi.p = drow; hi.s = s;
     hx.p = dx; hx.s = s;
-    *nnz = m;
-    if (p) {
-      CK(cudaMemcpyAsync(p, dp, sizeof(int32_t) * ((size_t)n + 1), cudaMemcpyDeviceToHost, s));
-      if (m > 0) {
-        CK(cudaMemcpyAsync(i, drow, sizeof(int32_t) * (size_t)m, cudaMemcpyDeviceToHost, s));
-        CK(cudaMemcpyAsync(x, dx, sizeof(double) * (size_t)m, cudaMemcpyDeviceToHost, s));
-      }
-    }
-    CK(cudaStreamSynchronize(s));
+    graph_finish(c, 2, idx, n, k, include_self, 1, prune, m, hp, hi, hx, nnz, p, i, x);
   });
 }
 

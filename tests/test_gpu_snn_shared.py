@@ -86,3 +86,35 @@ def test_expansion_in_row_chunks(ctx, oracle, monkeypatch, chunk):
     idx[rng.random((n, k)) < 0.05] = NA
     for inc, pr in ((True, 0.0), (False, 1 / 15), (True, 0.3)):
         assert same(gpu_graph(ctx, idx, inc, pr), oracle.snn_graph_shared(idx, inc, pr)), (chunk, inc, pr)
+
+
+def test_two_call_protocol_reuses_only_an_identical_query(ctx, oracle):
+    """The size query's graph serves the fetch only when every argument and
+    the idx contents match; otherwise the fetch builds its own."""
+    from sparsedist_gb300 import _lib
+    rng = np.random.default_rng(8)
+    n, k = 400, 6
+    idx = np.asfortranarray(rng.integers(1, n + 1, (n, k)).astype(np.int32))
+    nnz = np.zeros(1, np.int64)
+    _lib.check(ctx.lib.sdg_snn_graph_shared(ctx.handle, idx.ctypes.data, n, k, 1, 0.0, nnz.ctypes.data,
+                                            None, None, None))
+    other = idx.copy(order="F")
+    other[0, 0] = other[0, 0] % n + 1                 # same pointer shape, other contents
+    want = oracle.snn_graph_shared(other, True, 0.0)
+    m = len(want[2])
+    p = np.empty(n + 1, np.int32)
+    i = np.empty(max(m, 1), np.int32)
+    x = np.empty(max(m, 1), np.float64)
+    _lib.check(ctx.lib.sdg_snn_graph_shared(ctx.handle, other.ctypes.data, n, k, 1, 0.0, nnz.ctypes.data,
+                                            p.ctypes.data, i.ctypes.data, x.ctypes.data))
+    assert int(nnz[0]) == m and same((p, i[:m], x[:m]), want)
+    # and the knn-edge graph after a shared size query with the same idx
+    _lib.check(ctx.lib.sdg_snn_graph_shared(ctx.handle, idx.ctypes.data, n, k, 1, 0.0, nnz.ctypes.data,
+                                            None, None, None))
+    wp, wi, wx = oracle.snn_graph(idx, True, 0.0, True)
+    p2 = np.empty(n + 1, np.int32)
+    i2 = np.empty(len(wx) + 1, np.int32)
+    x2 = np.empty(len(wx) + 1, np.float64)
+    _lib.check(ctx.lib.sdg_snn_graph(ctx.handle, idx.ctypes.data, n, k, 1, 0.0, 1, nnz.ctypes.data,
+                                     p2.ctypes.data, i2.ctypes.data, x2.ctypes.data))
+    assert int(nnz[0]) == len(wx) and same((p2, i2[:len(wx)], x2[:len(wx)]), (wp, wi, wx))
