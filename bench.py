@@ -194,7 +194,7 @@ def run_reference(args):
         t += dt
     v = cols * args.steps / t
     print(json.dumps({
-        "impl": "reference", "metric": "kNN query columns/s (sparseKNN cosine k=20, config 2)",
+        "impl": "reference", "metric": "kNN query columns/s (sparseKNN %s k=%d, config 2)" % (args.method, args.k),
         "value": v, "unit": "columns/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000 * t / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -718,7 +718,7 @@ def main():
     if rank == 0:
         st = ctx.stats()
         line = {
-            "metric": "kNN query columns/s (sparseKNN cosine k=20, config 2)",
+            "metric": "kNN query columns/s (sparseKNN %s k=%d, config 2)" % (args.method, args.k),
             "value": value, "unit": "columns/s", "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
