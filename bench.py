@@ -17,8 +17,8 @@ own block loop (R/sparseKNN.R:248-294).
   idx / dist results device -> host, inside the timed region.
 * roofline: the bounding kernel per launch, over its average CUDA-event
   duration.  With the tensor-core screen (the automatic choice here) that is
-  the BF16 GEMM: 2 * rows * references * queries flops against the measured
-  BF16 peak.  With the FP32 sparse screen (--engine 2) it is k_screen: the
+  the FP16 GEMM: 2 * rows * references * queries flops against the measured
+  BF16 peak (FP16 and BF16 run at the same dense tensor rate on GB300).  With the FP32 sparse screen (--engine 2) it is k_screen: the
   path's algorithmic bytes (12 bytes per stored entry touched per evaluated
   pair, plus 12 bytes per output slot) against the measured HBM bandwidth.
   sparse_alg_gbs reports the byte figure in both cases.
@@ -655,8 +655,9 @@ def main():
         # the tensor-core screen: its GEMM is the bounding kernel
         flops_launch = st_last["tensor_flops"] / launches_per_step
         roof = {"bound": "tensor", "achieved": flops_launch / (per_launch_ms / 1000.0) / 1e12,
-                "peak": bf16_peak, "unit": "TFLOP/s", "peak_kind": peak_kind + " (bf16, burst)",
-                "kernel": "cuBLAS BF16 GEMM of the tensor-core screen", "flops_per_launch": flops_launch}
+                "peak": bf16_peak, "unit": "TFLOP/s",
+                "peak_kind": peak_kind + " (bf16 burst; fp16 runs at the same tensor rate)",
+                "kernel": "cuBLAS FP16 GEMM of the tensor-core screen", "flops_per_launch": flops_launch}
     else:
         roof = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "peak_kind": peak_kind, "kernel": "k_screen", "alg_bytes_per_launch": alg / launches_per_step}

@@ -301,9 +301,9 @@ SDG_API int sdg_kernel_time(sdg_ctx* ctx, double* ms, int64_t* launches);
 /* Selects the candidate-generation engine for subsequent calls on ctx:
  * 0 = automatic, 1 = exact FP64 slab for every pair, 2 = screened (FP32 /
  * integer sparse screen, exact FP64 re-rank), 3 = tensor-core screen
- * (cosine / euclidean: BF16 GEMM over dense copies of the screen values with
- * a rigorous bound, exact FP64 re-rank; other methods, or values outside
- * FP32's normal range, use 2).  Results are identical; only speed differs.
+ * (binary / cosine / euclidean: FP16 GEMM over dense copies of the screen
+ * values with a rigorous bound, exact FP64 re-rank; other methods, or values
+ * beyond FP16's range, use 2).  Results are identical; only speed differs.
  * Used by tests to cross-check the engines. */
 SDG_API int sdg_ctx_set_engine(sdg_ctx* ctx, int engine);
 

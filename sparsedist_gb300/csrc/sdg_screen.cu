@@ -26,7 +26,7 @@
 // reference part at the same time and it is read from HBM about once.
 #include <cub/device/device_radix_sort.cuh>
 #include <cublas_v2.h>
-#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include <algorithm>
 #include <cfloat>
@@ -426,42 +426,46 @@ __global__ void k_exact_candidates_prep(const int32_t* count, int64_t nq, int ca
 // the tensor-core screen
 //
 // For cosine and euclidean the screen value of a pair is an inner product
-// over the rows, so a dense BF16 copy of the screen values of both matrices
+// over the rows, so a dense FP16 copy of the screen values of both matrices
 // (TensorCache) turns a block of screens into one GEMM on the tensor cores
-// (cuBLAS, BF16 in, FP32 accumulate and out), written as the slab
-// S[ql * ldS + c] in natural column order.  The bound: each BF16 factor has
-// relative error <= 2^-9 (+ 2^-24 from the FP32 value it rounds), so a
-// product errs by <= 0.0040 |x y|; the FP32 accumulation of at most
+// (cuBLAS, FP16 in, FP32 accumulate and out; FP16 runs at BF16's tensor rate
+// and rounds 4x finer, 2^-11), written as the slab S[ql * ldS + c] in natural
+// column order.  The bound (tc_bounds) is built from each column's exact
+// rounding error ||v - h|| (FP64, v the exact values, h the FP16 copy), so
+// it covers every way the copy differs: values below FP16's smallest normal
+// are written as 0, never as FP16 subnormals, and a value above FP16's range
+// makes the copy unusable (TensorCache::usable: the FP32 screen runs).  The
+// FP16 products are exact in FP32; the FP32 accumulation of at most
 // n = min(nnz_q, nnz_c) nonzero products (zero products add no error) is
-// allowed (n + 64) 2^-21 of sum |x y|; sum |x y| <= 1 for unit columns and
-// <= sqrt(Nq Nc) in general (Cauchy-Schwarz).  Values below FP32's smallest
-// normal are excluded at build time (TensorCache::usable), and a pair whose
-// key or bound is not finite is kept unconditionally.  The selection is split
+// allowed (n + 64) 2^-21 of sum |h_q h_c|.  A pair whose key or bound is not
+// finite is kept unconditionally.  The selection is split
 // across TSEG-reference segments (segment top-k of the pessimistic keys,
 // per-query merge to the exact k-th, segmented keep), one warp per
 // (query, segment), so that the slab streams at full bandwidth.
 // ---------------------------------------------------------------------------
 constexpr int TSEG = 32768;
-constexpr float BF16_REL = 0.0040f;
 constexpr float ACC_ULP = 4.76837158203125e-7f;   // 2^-21
 
-// One warp per column: scatter the BF16 values into the dense column and
-// compute ||v - b|| and ||b|| in FP64 (v: src, the exact values; b: the BF16
+constexpr float HALF_MAX = 65504.f;
+constexpr float HALF_MIN_NORMAL = 6.103515625e-05f;   // 2^-14
+
+// One warp per column: scatter the FP16 values into the dense column and
+// compute ||v - b|| and ||b|| in FP64 (v: src, the exact values; b: the FP16
 // values the GEMM multiplies), rounded up to FP32.
-__global__ void k_tensor_fill(DevCsc M, const float* fval, const double* src, __nv_bfloat16* dense, int64_t ld,
+__global__ void k_tensor_fill(DevCsc M, const float* fval, const double* src, __half* dense, int64_t ld,
                               float* err_out, float* bn_out, int* bad) {
   const int64_t j = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (j >= M.ncol) return;
-  __nv_bfloat16* col = dense + j * ld;
+  __half* col = dense + j * ld;
   double se = 0.0, sb = 0.0;
   for (int64_t a = M.p[j] + lane; a < M.p[j + 1]; a += 32) {
     const float f = fval[a];
     const float af = fabsf(f);
-    if (f != 0.f && !(af >= FLT_MIN && af <= 3.0e38f)) atomicOr(bad, 1);
-    const __nv_bfloat16 bv = __float2bfloat16_rn(f);
-    col[M.i[a]] = bv;
-    const double b = (double)__bfloat162float(bv);
+    if (!(af <= HALF_MAX)) atomicOr(bad, 1);          // beyond FP16, or not finite
+    const __half hv = __float2half_rn(af < HALF_MIN_NORMAL ? 0.f : f);
+    col[M.i[a]] = hv;
+    const double b = (double)__half2float(hv);
     const double v = src ? src[a] : (double)f;
     se += (v - b) * (v - b);
     sb += b * b;
@@ -501,18 +505,18 @@ struct TensorSelArgs {
   int32_t* overflow;
 };
 
-// The BF16 bounds of one eligible pair from its GEMM value s (a key that is
-// not finite, or a bound that is not, keeps the pair unconditionally).
-// With v the exact values and b their BF16 copies (per column eq, er = ||v - b||
+// The tensor-screen bounds of one eligible pair from its GEMM value s (a key
+// that is not finite, or a bound that is not, keeps the pair unconditionally).
+// With v the exact values and b their FP16 copies (per column eq, er = ||v - b||
 // and bq, br = ||b||), Cauchy-Schwarz gives
 //   |sum v_q v_r - sum b_q b_r| <= eq ||v_r|| + bq er,
 // ||v_r|| = 1 for unit columns and sqrt(Nr) otherwise; the FP32 accumulation
 // of at most n = min(nnz_q, nnz_r) nonzero products is allowed
 // (n + 64) 2^-21 sum |b_q b_r| <= (n + 64) 2^-21 bq br.
 // Binary: s estimates the matched-row count c (0 / 1 factors are exact in
-// BF16); with the accumulation allowance c lies in [c_lo, c_hi] and the
+// FP16); with the accumulation allowance c lies in [c_lo, c_hi] and the
 // Jaccard key c / (nq + nc - c) increases with c.
-__device__ __forceinline__ void bf16_bounds(int method, float s, int32_t nq_, float Nq, int32_t nc_, float Nc,
+__device__ __forceinline__ void tc_bounds(int method, float s, int32_t nq_, float Nq, int32_t nc_, float Nc,
                                             float eq, float bq, float er, float br, float& lo, float& hi) {
   const float nmin = (float)min(nq_, nc_);
   const float acc = (nmin + 64.f) * ACC_ULP;
@@ -551,7 +555,7 @@ __device__ __forceinline__ void tensor_keys(const TensorSelArgs& A, int64_t q, i
     if (A.include_self) lo = hi = INFINITY;
     return;
   }
-  bf16_bounds(A.method, s, nq_, Nq, A.rnnz[c], A.rnorm ? A.rnorm[c] : 0.f, A.qerr[q], A.qbn[q], A.rerr[c], A.rbn[c],
+  tc_bounds(A.method, s, nq_, Nq, A.rnnz[c], A.rnorm ? A.rnorm[c] : 0.f, A.qerr[q], A.qbn[q], A.rerr[c], A.rbn[c],
               lo, hi);
 }
 
@@ -585,7 +589,7 @@ __device__ __forceinline__ void tensor_keys4(const TensorSelArgs& A, int64_t q, 
         if (A.include_self) lo[j] = hi[j] = INFINITY;
         continue;
       }
-      bf16_bounds(A.method, sv[j], nq_, Nq, nv[j], rn[j], eq, bq, ev[j], bv[j], lo[j], hi[j]);
+      tc_bounds(A.method, sv[j], nq_, Nq, nv[j], rn[j], eq, bq, ev[j], bv[j], lo[j], hi[j]);
     }
   } else {
 #pragma unroll
@@ -733,7 +737,7 @@ __global__ void k_tsel_overflow(int64_t nq, int cap, int32_t* count, int32_t* ov
 // ---------------------------------------------------------------------------
 // second screen of the tensor candidates: FP32 sparse dot products
 //
-// The BF16 bound keeps a few hundred candidates per query; the FP32 screen's
+// The FP16 bound keeps a few hundred candidates per query; the FP32 screen's
 // bound (key_and_bound) is ~100x tighter.  One CTA per query holds the query
 // column as a shared-memory bitmap (with each word's first entry, as in the
 // exact re-rank) and its FP32 screen values; a warp per candidate streams the
@@ -888,7 +892,7 @@ void tensor_cache_free(TensorCache* c, cudaStream_t s) {
   if (c) *c = TensorCache();
 }
 
-// Builds (or reuses) the dense BF16 copy of M's screen values for `method`
+// Builds (or reuses) the dense FP16 copy of M's screen values for `method`
 // from its ScreenCache; an allocation failure leaves it unusable (the FP32
 // screen then runs) rather than failing the call.
 static int ensure_tensor(TensorCache* t, int method, const DevCsc& M, const ColAux& aux, const ScreenCache* sc,
@@ -916,7 +920,7 @@ static int ensure_tensor(TensorCache* t, int method, const DevCsc& M, const ColA
   if (M.ncol > 0)
     k_tensor_fill<<<blocks_for(M.ncol * 32, 256), 256, 0, s>>>(
         M, sc->fval, (method == COSINE) ? aux.uval : (method == EUCLIDEAN) ? M.x : nullptr,
-        static_cast<__nv_bfloat16*>(t->dense), t->ld, t->err, t->bn, bad);
+        static_cast<__half*>(t->dense), t->ld, t->err, t->bn, bad);
   int hbad = 0;
   SK(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
   SK(cudaStreamSynchronize(s));
@@ -1024,7 +1028,7 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
   const int64_t ldS = use_t ? (nr + 31) / 32 * 32 : nr;
   const int64_t chunk = std::max<int64_t>(
       QT, std::min<int64_t>(std::max<int64_t>(q_hi - q_lo, 1), sbudget / (4 * std::max<int64_t>(ldS, 1))));
-  // the BF16 bound is wider than the FP32 one: room for more candidates
+  // the FP16 bound is wider than the FP32 one: room for more candidates
   const int cap = use_t ? std::max(512, std::min(16384, 64 * r.k + 256))
                         : std::max(256, std::min(8192, 16 * r.k + 64));
   const int nseg = (int)((nr + TSEG - 1) / TSEG);
@@ -1083,8 +1087,8 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
       if (cublasSetStream(h, s) != CUBLAS_STATUS_SUCCESS) return (int)cudaErrorUnknown;
       hooks.time_begin();
       const cublasStatus_t bs = cublasGemmEx(
-          h, CUBLAS_OP_T, CUBLAS_OP_N, (int)nr, (int)nb, (int)ld, &one, rt->dense, CUDA_R_16BF, (int)ld,
-          static_cast<const __nv_bfloat16*>(qt->dense) + q0 * ld, CUDA_R_16BF, (int)ld, &zero, S, CUDA_R_32F,
+          h, CUBLAS_OP_T, CUBLAS_OP_N, (int)nr, (int)nb, (int)ld, &one, rt->dense, CUDA_R_16F, (int)ld,
+          static_cast<const __half*>(qt->dense) + q0 * ld, CUDA_R_16F, (int)ld, &zero, S, CUDA_R_32F,
           (int)ldS, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
       hooks.time_end();
       if (bs != CUBLAS_STATUS_SUCCESS) return (int)cudaErrorUnknown;

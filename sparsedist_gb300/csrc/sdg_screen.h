@@ -23,17 +23,17 @@ struct ScreenCache {
   int64_t nnz_total = 0;
 };
 
-// Dense BF16 copy of one matrix's screen values for the tensor-core screen
-// (cosine: the unit values; euclidean: the values), one column of ld rows
-// (nrow rounded up to 64, zero below nrow) per matrix column.  usable = 0
-// when a value is not finite or not normal in FP32 (the BF16 bound would not
-// hold): the FP32 screen is used instead.
+// Dense FP16 copy of one matrix's screen values for the tensor-core screen
+// (cosine: the unit values; euclidean: the values; binary: 1), one column of
+// ld rows (nrow rounded up to 64, zero below nrow) per matrix column; values
+// below FP16's smallest normal are stored as 0.  usable = 0 when a value is
+// not finite or beyond FP16's range: the FP32 screen is used instead.
 struct TensorCache {
   int method = -1;
   int usable = 0;
-  void* dense = nullptr;     // __nv_bfloat16[ncol * ld]
+  void* dense = nullptr;     // __half[ncol * ld]
   int64_t ld = 0;
-  // per column, rounded up to FP32: err = ||v - bf16(v)||_2 and bn = ||bf16(v)||_2,
+  // per column, rounded up to FP32: err = ||v - h(v)||_2 and bn = ||h(v)||_2,
   // v the exact values the key is defined on (FP64 unit values for cosine,
   // the values for euclidean)
   float* err = nullptr;
@@ -42,7 +42,7 @@ struct TensorCache {
 
 struct ScreenRun {
   int method = 0, dist = 1, k = 1;
-  // the tensor-core screen (a BF16 GEMM through cuBLAS handle `blas`) instead
+  // the tensor-core screen (an FP16 GEMM through cuBLAS handle `blas`) instead
   // of the FP32 sparse screen, when tensor_supported(method) and both
   // matrices' TensorCache are usable
   bool tensor = false;

@@ -3,7 +3,7 @@
 Configuration-2-like data (30,000 rows, lognormal nnz per column, skewed row
 weights, log-count values) at reduced column counts: the screened engine must
 return exactly what the exact FP64 engine returns (idx and distances bit for
-bit) with either screen (2: the FP32 sparse screen; 3: the BF16 tensor-core
+bit) with either screen (2: the FP32 sparse screen; 3: the FP16 tensor-core
 screen), both must equal the oracle on a subset of query columns, and
 size-independent properties hold (best-first ordering, no self, no masked)."""
 import numpy as np
