@@ -721,6 +721,8 @@ SDG_API int sdg_dist(sdg_ctx* c, int method, int dist, const sdg_csc* m, int ful
     cudaStream_t s = c->stream;
     const int64_t n = a->ncol;
     if (n == 0) return;
+    if ((uint64_t)n > ((uint64_t)1 << 30))                  // n^2 doubles would overflow size_t
+      fail(SDG_E_NOMEM, "the ncol x ncol result does not fit in memory");
     const size_t whole = sizeof(double) * (size_t)n * (size_t)n;
     size_t free_b = 0, total_b = 0;
     CK(cudaMemGetInfo(&free_b, &total_b));
@@ -953,7 +955,7 @@ SDG_API int sdg_snn_graph(sdg_ctx* c, const int32_t* idx, int32_t n, int32_t k, 
                           double* x) {
   return guarded([&] {
     if (!c) fail(SDG_E_ARG, "ctx must not be NULL");
-    if (!nnz) fail(SDG_E_ARG, "nnz must not be NULL");
+    if (!nnz || !idx) fail(SDG_E_ARG, "idx and nnz must not be NULL");
     CK(cudaSetDevice(c->device));
     if (!(prune >= 0.0 && prune <= 1.0))
       fail(SDG_E_ARG, "'prune' must be a finite number between 0 and 1.");
@@ -979,7 +981,7 @@ SDG_API int sdg_snn_graph_shared(sdg_ctx* c, const int32_t* idx, int32_t n, int3
                                  double prune, int64_t* nnz, int32_t* p, int32_t* i, double* x) {
   return guarded([&] {
     if (!c) fail(SDG_E_ARG, "ctx must not be NULL");
-    if (!nnz) fail(SDG_E_ARG, "nnz must not be NULL");
+    if (!nnz || !idx) fail(SDG_E_ARG, "idx and nnz must not be NULL");
     CK(cudaSetDevice(c->device));
     if (!(prune >= 0.0 && prune <= 1.0))
       fail(SDG_E_ARG, "'prune' must be a finite number between 0 and 1.");
