@@ -1,6 +1,7 @@
 """Generates tests/golden/golden.npz + golden.json: seeded inputs shaped like
 the reference's own test fixtures (make_X() = abs(rsparsematrix(60, 12, 0.3))
-and friends, tests/testthat/test-sparseKNN.R:7-12, test-sparseKNNCross.R:7-15)
+and friends, tests/testthat/test-sparseKNN.R:7-12, test-sparseKNNCross.R:7-15,
+test-sparseDist.R:6-19)
 together with the outputs of the reference's OWN kernels (src/sparseDist.cpp,
 src/topK.cpp, src/topKRows.cpp, src/snn.cpp compiled unmodified into
 oracle/_ref/ by oracle/build.py), driven by the oracle's restatement of the R
@@ -89,6 +90,9 @@ def main():
             case["flags"] = flags
         elif kind == "slab":
             arrays[cid + "_D"] = ref.slab(params["method"], X, Y, params["dist"])
+        elif kind == "dist":
+            arrays[cid + "_D"] = ref.dist_single(params["method"], X, params["full"], params["diag"],
+                                                 params["dist"])
         elif kind == "snn":
             idx = extra
             arrays[cid + "_knnidx"] = idx
@@ -143,6 +147,29 @@ def main():
         for prune, sym in ((0.0, True), (1 / 15, True), (0.2, False), (0.0, False)):
             add("snn", "snn include_self=%s prune=%.3f sym=%s" % (self_, prune, sym),
                 dict(include_self=self_, prune=prune, symmetrise=sym), X, extra=idx)
+    # covariance (fastCov2 through the sparseKNN / sparseKNNCross orchestration)
+    for tag, params, A, B in (
+            ("self k4", dict(k=4), X, None),
+            ("self include_self k3 (self value = variance)", dict(k=3, include_self=True), X, None),
+            ("block_size=3 k5", dict(k=5, block_size=3), X20, None),
+            ("signed k4", dict(k=4), Xs, None),
+            ("degenerate cols 2,5", dict(k=3), Xd, None),
+            ("cross X(60x12)->Y(60x5)", dict(k=3), X, X[:, :5])):
+        add("knn", "covariance " + tag, dict(params, method="covariance"), A, B)
+    add("cross", "covariance cross 300x80 / 300x50 bs16", dict(k=7, method="covariance", block_size=16),
+        Xb, Yb)
+    add("slab", "covariance slab", dict(method="covariance", dist=True), X, X20)
+    # single-matrix sparseDist(X): fastJacc / fastCosine / ... / fastCov with full / diag
+    for m, dists in (("binary", (True, False)), ("cosine", (True, False)), ("euclidean", (True,)),
+                     ("manhattan", (True,)), ("pearson", (True, False)), ("covariance", (True,)),
+                     ("js", (True,))):
+        mats = (("P", P),) if m == "js" else (("X", X), ("signed", Xs), ("degenerate", Xd))
+        for name, A in mats:
+            for full in (False, True):
+                for diag in (False, True):
+                    for d in dists:
+                        add("dist", "sparseDist(%s) %s full=%s diag=%s dist=%s" % (name, m, full, diag, d),
+                            dict(method=m, full=full, diag=diag, dist=d), A)
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **arrays)
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py",

@@ -84,6 +84,13 @@ def check_golden_case(backend, case, arr):
             assert same_bits(np.ascontiguousarray(D), np.ascontiguousarray(want)), case["tag"]
         else:
             assert _close(D, want), case["tag"]
+    elif kind == "dist":
+        D = backend.dist_single(p["method"], X, p["full"], p["diag"], p["dist"])
+        want = arr[cid + "_D"]
+        if p["method"] in PINNED:
+            assert same_bits(np.ascontiguousarray(D), np.ascontiguousarray(want)), case["tag"]
+        else:
+            assert _close(D, want), case["tag"]
     elif kind == "snn":
         idx = arr[cid + "_knnidx"]
         w = backend.snn_jaccard(idx, p["include_self"])
