@@ -1,7 +1,7 @@
 #!/usr/bin/env python
 """bench.py -- kNN query columns per second of sparseKNN on GB300.
 
-Workload (configuration 2, "plain sparse kNN at scale"): a 30,000 x 200,000
+Workload ("plain sparse kNN at scale"): a 30,000 x 200,000
 CSC float64 log-count matrix (per-column nnz ~ lognormal, mean 1,800, sdlog
 0.6; rows weighted by lognormal(0, 1.5) means; values log1p of NB(2) counts),
 generated seeded on the GPU (sparsedist_gb300/synth.py).  The reference
@@ -61,18 +61,21 @@ def parse():
     ap.add_argument("--ncol", type=int, default=200000)
     ap.add_argument("--nrow", type=int, default=30000)
     ap.add_argument("--mean-nnz", type=float, default=1800.0)
-    ap.add_argument("--engine", type=int, default=0, help="0 auto, 1 exact slab, 2 screened")
+    ap.add_argument("--engine", type=int, default=0, help="0 auto, 1 exact slab, 2 FP32 screen, 3 tensor-core screen")
     ap.add_argument("--cpu-cols", type=int, default=256, help="query columns of the CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--dist-cols", type=int, default=10000)
-    ap.add_argument("--dist-long", action="store_true", help="long columns (configuration 2's generator)")
-    ap.add_argument("--config", default="c2", choices=["c2", "c1", "c3", "serve", "dist", "snn"],
-                    help="c2: the default line (configuration 2); c1: the CPU-runnable "
-                         "configuration 1; serve: configuration 5, the serving loop")
+    ap.add_argument("--dist-long", action="store_true",
+                    help="long columns (the 30,000-row log-count generator)")
+    ap.add_argument("--config", default="logcount",
+                    choices=["logcount", "uniform", "dense", "serve", "dist", "snn"],
+                    help="logcount: the default line (30,000 x 200,000 log-count kNN); uniform: the "
+                         "CPU-runnable 2,000 x 10,000 case; dense: 256 x 2,000,000 embeddings; "
+                         "serve: the serving loop; dist: full-matrix sparseDist; snn: sparseSNN")
     ap.add_argument("--serve-ref-cols", type=int, default=1000000)
-    ap.add_argument("--c3-cols", type=int, default=2000000)
-    ap.add_argument("--c3-block", type=int, default=4096)
+    ap.add_argument("--dense-cols", type=int, default=2000000)
+    ap.add_argument("--dense-block", type=int, default=4096)
     ap.add_argument("--serve-requests", type=int, default=80)
     ap.add_argument("--serve-util", type=float, default=0.75)
     return ap.parse_args()
@@ -194,7 +197,7 @@ def run_reference(args):
         t += dt
     v = cols * args.steps / t
     print(json.dumps({
-        "impl": "reference", "metric": "kNN query columns/s (sparseKNN %s k=%d, config 2)" % (args.method, args.k),
+        "impl": "reference", "metric": "kNN query columns/s (sparseKNN %s k=%d, 30000x200000 log-count)" % (args.method, args.k),
         "value": v, "unit": "columns/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000 * t / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -205,15 +208,15 @@ def run_reference(args):
 
 
 def workload_config(args, block):
-    return {"workload": "config 2: sparseKNN(X[, block], X) on a resident %dx%d log-count CSC "
+    return {"workload": "sparseKNN(X[, block], X) on a resident %dx%d log-count CSC "
                         "(nnz/col lognormal mean %.0f), %s, k=%d" % (args.nrow, args.ncol,
                                                                     args.mean_nnz, args.method, args.k),
             "nrow": args.nrow, "ncol": args.ncol, "query_block": block, "method": args.method,
             "k": args.k, "l2": "inputs larger than L2: the 4.3 GB reference is streamed every step"}
 
 
-def run_c1(args):
-    """Configuration 1: 2,000 x 10,000 CSC, 2 % uniform pattern, |N(0,1)|
+def run_uniform(args):
+    """The CPU-runnable case: 2,000 x 10,000 CSC, 2 % uniform pattern, |N(0,1)|
     values; sparseKNN binary and cosine (k = 15, self-search), then
     sparseSNN(prune = 1/15, symmetrise = TRUE), through the Python API (host
     buffers in and out), against the CPU port on all host cores."""
@@ -245,13 +248,13 @@ def run_c1(args):
     g = sdg.sparseSNN(nn, prune=1 / 15, verbose=False)
     out["snn_ms"] = 1000 * (time.perf_counter() - t0)
     out["snn_nnz"] = int(g.nnz)
-    print(json.dumps({"metric": "kNN query columns/s, configuration 1 (e2e through the Python API)",
+    print(json.dumps({"metric": "kNN query columns/s, 2000x10000 uniform (e2e through the Python API)",
                       "config": {"workload": "2000x10000 CSC, 2% uniform, |N(0,1)|, k=15, self-search"},
                       "cores": os.cpu_count(), "results": out}))
 
 
 def run_dist(args):
-    """Full-matrix sparseDist(X, full = TRUE) on configuration 1's matrix
+    """Full-matrix sparseDist(X, full = TRUE) on the 2,000-row uniform matrix
     (2,000 x dist_cols CSC, 2 % uniform pattern, |N(0,1)| values), binary,
     cosine and euclidean: the C-ABI call with host buffers (CSC in, the dense
     n x n result out) per step, the pair kernel timed by CUDA events inside
@@ -264,7 +267,7 @@ def run_dist(args):
     from oracle.pyoracle import Oracle
     n = args.dist_cols
     if args.dist_long:
-        # long columns: configuration 2's generator (nnz/col lognormal mean 1,800)
+        # long columns: the log-count generator (nnz/col lognormal mean 1,800)
         p, i, x = synth.logcount_csc(nrow=30000, ncol=n, mean_nnz=1800, seed=2, device="cuda")
         X = sp.csc_matrix((np.asarray(x), np.asarray(i), np.asarray(p)), shape=(30000, n))
         shape = "30000x%d log-count CSC (nnz/col lognormal mean 1800)" % n
@@ -326,7 +329,7 @@ def run_dist(args):
 
 
 def run_snn(args):
-    """sparseSNN on configuration 2's kNN graph: the self-search
+    """sparseSNN on the log-count matrix's kNN graph: the self-search
     sparseKNN(X, k = 20, cosine) of the 30,000 x ncol log-count matrix (on
     the GPU, in sdg_knn_block shares), then sparseSNN(prune = 1/15) with
     edges = "knn" (symmetrise = TRUE) and edges = "shared" through the Python
@@ -379,15 +382,15 @@ def run_snn(args):
                       "cpu_baseline": {"value": n / cpu_s, "unit": "nodes/s", "cores": threads,
                                        "kind": "port", "sample": "the whole graph"},
                       "identical": same}
-    print(json.dumps({"metric": "sparseSNN nodes/s on configuration 2's kNN graph (e2e through the Python API)",
+    print(json.dumps({"metric": "sparseSNN nodes/s on the 30000x200000 log-count kNN graph (e2e through the Python API)",
                       "config": {"workload": "sparseSNN(sparseKNN(X, k=%d, %s), prune=1/15), X %dx%d "
                                              "log-count CSC" % (k, args.method, args.nrow, n)},
                       "steps": args.steps, "warmup": args.warmup, "results": out}))
 
 
 def run_serve(args):
-    """Configuration 5: a resident 30,000 x serve_ref_cols log-count reference
-    (configuration 2's generator), Poisson arrivals of query matrices with
+    """The serving loop: a resident 30,000 x serve_ref_cols log-count reference
+    (the log-count generator), Poisson arrivals of query matrices with
     1..4,096 columns (log-uniform), methods cycling cosine / binary /
     euclidean, k in {10, 20, 50}, admission under a 120 GB budget; reports
     p50 / p99 latency (submit to completion) and columns/s."""
@@ -454,7 +457,7 @@ def run_serve(args):
     st = srv.stats()
     # latencies of the Poisson requests only (drop the calibration requests)
     print(json.dumps({
-        "metric": "served kNN columns/s + p50/p99 latency, configuration 5",
+        "metric": "served kNN columns/s + p50/p99 latency, resident 30000x1000000 log-count",
         "value": float(sizes.sum()) / wall, "unit": "columns/s",
         "p50_latency_s": st["p50_s"], "p99_latency_s": st["p99_s"], "mean_latency_s": st["mean_s"],
         "requests": n, "columns": int(sizes.sum()), "batches": int(st["batches"] - srv_stats0["batches"]),
@@ -468,17 +471,17 @@ def run_serve(args):
     ref.free()
 
 
-def run_c3(args):
-    """Configuration 3: 256 x 2,000,000 FP32 embeddings (i.i.d. N(0,1) mixed
+def run_dense(args):
+    """Dense embeddings: 256 x 2,000,000 FP32 (i.i.d. N(0,1) mixed
     with 1,000 Gaussian clusters, sigma 0.3, plus 1 % near duplicates at 1e-6),
-    cosine and euclidean self-search, k = 20, in blocks of --c3-block (4,096) query columns:
+    cosine and euclidean self-search, k = 20, in blocks of --dense-block (4,096) query columns:
     the BF16 tensor-core screen + exact FP64 re-rank against the plain FP32
     path, with idx identity and distance error checked against the exact FP64
     engine on a sample of query columns."""
     import ctypes as C
     import torch
     from sparsedist_gb300 import _lib, synth
-    d, n, B, k = 256, args.c3_cols, args.c3_block, 20
+    d, n, B, k = 256, args.dense_cols, args.dense_block, 20
     X = synth.dense_embeddings(d=d, n=n, seed=5)
     ctx = _lib.Context()
     stream = torch.cuda.current_stream()
@@ -553,7 +556,7 @@ def run_c3(args):
             check["%s/%s" % (method, name)] = {"rows_with_identical_idx": same, "rows": qs,
                                                "max_abs_distance_error_vs_fp64": err}
     ctx.set_engine(0)
-    print(json.dumps({"metric": "dense kNN query columns/s, configuration 3 (k=20, %d-query blocks)" % B,
+    print(json.dumps({"metric": "dense kNN query columns/s, 256x2000000 embeddings (k=20, %d-query blocks)" % B,
                       "config": {"workload": "256x%d FP32 embeddings: N(0,1) + 1000 clusters (sigma 0.3) "
                                              "+ 1%% near duplicates (1e-6)" % n},
                       "results": res, "check_vs_fp64_engine": check}))
@@ -562,11 +565,11 @@ def run_c3(args):
 
 def main():
     args = parse()
-    if args.config == "c3":
-        run_c3(args)
+    if args.config == "dense":
+        run_dense(args)
         return
-    if args.config == "c1":
-        run_c1(args)
+    if args.config == "uniform":
+        run_uniform(args)
         return
     if args.config == "serve":
         run_serve(args)
@@ -719,7 +722,7 @@ def main():
     if rank == 0:
         st = ctx.stats()
         line = {
-            "metric": "kNN query columns/s (sparseKNN %s k=%d, config 2)" % (args.method, args.k),
+            "metric": "kNN query columns/s (sparseKNN %s k=%d, 30000x200000 log-count)" % (args.method, args.k),
             "value": value, "unit": "columns/s", "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",

@@ -1,4 +1,4 @@
-// sdg_dense.cu -- kNN over dense embedding columns (configuration 3).
+// sdg_dense.cu -- kNN over dense embedding columns (d <= 256 FP32 embeddings).
 //
 // Columns are dense (d values each).  A cosine / euclidean slab between
 // dense columns is a true contraction, so the screen runs on the tensor

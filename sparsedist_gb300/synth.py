@@ -1,13 +1,13 @@
 """Seeded synthetic inputs with the shapes and value distributions of the
-benchmark configurations (the reference's own bench reads 10x PBMC downloads,
+benchmark workloads (the reference's own bench reads 10x PBMC downloads,
 bench/R/03-datasets.R:56-71, which are not available offline; these stand in
 for them).
 
 * ``uniform_csc``: nrow x ncol CSC, a uniform random pattern of exactly
-  round(density * nrow * ncol) positions, |N(0,1)| values (configuration 1:
-  2,000 x 10,000 at 2%).
-* ``logcount_csc``: single-cell-like log counts (configuration 2: 30,000 x
-  200,000): per-column nnz ~ lognormal(log(mean_nnz) - sdlog^2/2, sdlog)
+  round(density * nrow * ncol) positions, |N(0,1)| values (the CPU-runnable
+  case: 2,000 x 10,000 at 2%).
+* ``logcount_csc``: single-cell-like log counts (the kNN-at-scale case:
+  30,000 x 200,000): per-column nnz ~ lognormal(log(mean_nnz) - sdlog^2/2, sdlog)
   clipped to [1, nrow]; rows drawn without replacement with probability
   proportional to row means mu_r ~ lognormal(0, row_sdlog) (exponential-race
   sampling); values log1p(NB(size 2, mean mu_r * s_c)) with column scales
@@ -33,7 +33,7 @@ def uniform_csc(nrow, ncol, density, seed=0):
 
 def dense_embeddings(d=256, n=2000000, centres=1000, sigma=0.3, cluster_frac=0.5, dup_frac=0.01,
                      eps=1e-6, seed=0, device="cuda"):
-    """Configuration 3's embeddings as a torch float32 tensor of shape (n, d)
+    """The dense-embedding workload as a torch float32 tensor of shape (n, d)
     (i.e. d x n column-major): a share of i.i.d. N(0,1) columns, the rest drawn
     around one of ``centres`` N(0,1) centres with N(0, sigma^2) noise, then
     ``dup_frac`` of the columns replaced by a copy of another column plus

@@ -18,7 +18,7 @@ import scipy.sparse as sp
 from backends import NA_INT, golden_matrix, make_x, same_bits
 
 PINNED = {"binary", "cosine", "euclidean", "manhattan"}
-REL_TOL = 1e-12            # plain-path distances: spec tolerance
+REL_TOL = 1e-12            # plain-path distances: the stated tolerance
 TESTTHAT_TOL = 1.5e-8      # testthat's expect_equal() default, where the R test uses it
 
 

@@ -1,7 +1,7 @@
-"""Batched uneven problems (configuration 4's shape, at test size): many
+"""Batched uneven problems (the shape of the 512-problem batch, at test size): many
 independent sparseKNNCross problems whose sizes are drawn log-uniformly,
 with the methods cycling binary / cosine / manhattan / js (js on
-column-normalised data) and k cycling 10 / 20 / 50, as in the configuration
+column-normalised data) and k cycling 10 / 20 / 50, as in the full batch
 (512 problems, nq log-U[100, 50,000], nr log-U[1,000, 200,000], rows
 U[5,000, 30,000], density log-U[0.1 %, 10 %]).  Here nq, nr and the rows
 are scaled down so that the oracle finishes in seconds.

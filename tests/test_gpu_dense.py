@@ -1,4 +1,4 @@
-"""Dense embedding columns (configuration 3's path): both BF16 screens (mode 0,
+"""Dense embedding columns (the 256 x 2,000,000 embedding path): both BF16 screens (mode 0,
 the fused tcgen05 kernel; mode 2, the cuBLAS slab) with the exact FP64 re-rank
 must return the oracle's sparseKNN result on the same data bit for bit (idx
 and distances), near-duplicate columns included; the plain FP32 path (mode 1)

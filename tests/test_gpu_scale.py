@@ -1,7 +1,7 @@
 """GPU parity at benchmark-like scale.
 
-Configuration-2-like data (30,000 rows, lognormal nnz per column, skewed row
-weights, log-count values) at reduced column counts: the screened engine must
+Data like the 30,000 x 200,000 log-count workload's (30,000 rows, lognormal
+nnz per column, skewed row weights, log-count values) at reduced column counts: the screened engine must
 return exactly what the exact FP64 engine returns (idx and distances bit for
 bit) with either screen (2: the FP32 sparse screen; 3: the FP16 tensor-core
 screen), both must equal the oracle on a subset of query columns, and
