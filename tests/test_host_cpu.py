@@ -87,6 +87,15 @@ def test_method_matching():
     assert _match_arg(METHOD_CHOICES, METHOD_CHOICES) == "binary"
     with pytest.raises(ValueError, match="should be one of"):
         _match_arg("nope", METHOD_CHOICES)
+    # match.arg's partial matching: "cov" is covariance, "co" is ambiguous
+    assert _match_arg("cov", METHOD_CHOICES) == "covariance"
+    with pytest.raises(ValueError, match="should be one of"):
+        _match_arg("co", METHOD_CHOICES)
+    # sparseDist validates the method before it needs a device
+    with pytest.raises(ValueError, match="should be one of"):
+        sdg.sparseDist(make_x(20, 4, 0.3, 1), method="nope", verbose=False)
+    with pytest.raises(ValueError, match="must be provided"):
+        sdg.sparseDist(None, verbose=False)
 
 
 def test_rows_and_columns_checked_first():
