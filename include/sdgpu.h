@@ -145,9 +145,11 @@ SDG_API int sdg_snn_jaccard(sdg_ctx* ctx, const int32_t* idx, int32_t n, int32_t
  * (NULL = the legacy default stream).  The neighbour sets live in a fixed
  * 32 MiB array compiled into the library (held by every GPU that loads it,
  * until exit): a call is rejected with SDG_E_UNSUPPORTED unless
- * n * (k + 2) + 1 <= 8,388,608.  Nothing is allocated.  The first call on a
- * device looks up the array's device address (make it before any stream
- * capture).  The call synchronises `stream` once, to read the index check.
+ * n * (k + 2) + 1 <= 8,388,608.  Nothing is allocated.  Every call looks up
+ * the array's device address in the current context (so a device reset or
+ * another context never leaves a stale address); the first call on a device
+ * loads the library's device code (make it before any stream capture).  The
+ * call synchronises `stream` once, to read the index check.
  * All calls share the array: calls whose work overlaps on the GPU race. */
 SDG_API int sdg_snn_jaccard_noalloc(const int32_t* idx, int32_t n, int32_t k, int include_self,
                                     double* w, void* stream);

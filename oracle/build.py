@@ -7,7 +7,9 @@
   (``src/sparseDist.cpp``, ``src/topK.cpp``, ``src/topKRows.cpp``,
   ``src/snn.cpp`` of gambalab/sparseDist) where they lie, against the
   project-written API shim in ``oracle/shim/``, into ``oracle/_ref/libsdref.so``.
-  It needs the reference checkout; where that is absent it does nothing.
+  It needs the reference checkout: ``$SDG_REFERENCE_ROOT`` if set, else a
+  ``reference`` directory beside this repository's root; where neither holds
+  the sources it does nothing.
 
 Run ``python oracle/build.py`` or call the functions.  Nothing under
 ``oracle/`` is part of the product.
@@ -24,7 +26,9 @@ REF_DIR = os.path.join(HERE, "_ref")
 ORACLE_SO = os.path.join(BUILD_DIR, "libsdgoracle.so")
 REF_SO = os.path.join(REF_DIR, "libsdref.so")
 REF_SOURCES = ("sparseDist.cpp", "topK.cpp", "topKRows.cpp", "snn.cpp")
-DEFAULT_REF_ROOT = "/root/reference"
+# the reference checkout when SDG_REFERENCE_ROOT is unset: a sibling of the
+# repository root
+SIBLING_REF_ROOT = os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 
 COMMON = ["-O2", "-fopenmp", "-ffp-contract=off", "-fPIC"]
 
@@ -50,7 +54,7 @@ def build_oracle(force: bool = False) -> str:
 
 
 def build_ref(ref_root: str | None = None, force: bool = False) -> str | None:
-    ref_root = ref_root or os.environ.get("SDG_REFERENCE_ROOT", DEFAULT_REF_ROOT)
+    ref_root = ref_root or os.environ.get("SDG_REFERENCE_ROOT") or SIBLING_REF_ROOT
     srcs = [os.path.join(ref_root, "src", s) for s in REF_SOURCES]
     if not all(os.path.exists(s) for s in srcs):
         return None

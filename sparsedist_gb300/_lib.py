@@ -275,6 +275,14 @@ class Server:
         e = ke.value
         return idx[:ncol * e].reshape(e, ncol).T.copy(), dst[:ncol * e].reshape(e, ncol).T.copy(), fl.value
 
+    def cancel(self, rid):
+        """True when the request was cancelled before it started (its result
+        then raises SDG_E_CANCELLED); False when it is already running."""
+        st = self.lib.sdg_server_cancel(self.handle, C.c_int64(rid))
+        if st < 0:
+            check(st)
+        return st == 0
+
     def stats(self):
         out = np.zeros(9, np.float64)
         check(self.lib.sdg_server_stats(self.handle, out.ctypes.data, 9))

@@ -1245,6 +1245,10 @@ struct sdg_server {
   int64_t budget = 0, in_use = 0;
   int max_slots = 1, active = 0;
   int64_t max_batch_cols = 8192;
+  // methods whose reference-side data sdg_server_create prepared (bit m for
+  // method m): the workers only read the shared reference, so submit refuses
+  // any other method rather than let two workers prepare it concurrently
+  uint32_t methods_ready = 0;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<Request*> pending, admitted;
@@ -1360,14 +1364,17 @@ void worker_main(sdg_server* S, sdg_ctx* c) {
       // the oldest admitted request decides the group; take every admitted
       // request of that group, oldest first, up to the batch column limit
       Request* head = S->admitted.front();
-      int64_t cols = 0;
+      int64_t cols = 0, nnz = 0;
       for (auto it = S->admitted.begin(); it != S->admitted.end();) {
         Request* r = *it;
         if (r->state == Request::CANCELLED) { it = S->admitted.erase(it); continue; }
         const bool same = r->method == head->method && r->dist == head->dist && r->drop == head->drop;
-        if (same && (batch.empty() || cols + r->ncol <= S->max_batch_cols)) {
+        // the packed query is a dgCMatrix: int32 column pointers
+        const int64_t rn = (int64_t)r->i.size();
+        if (same && (batch.empty() || (cols + r->ncol <= S->max_batch_cols && nnz + rn <= INT32_MAX))) {
           batch.push_back(r);
           cols += r->ncol;
+          nnz += rn;
           r->state = Request::RUNNING;
           r->t_start = now_s();
           it = S->admitted.erase(it);
@@ -1419,6 +1426,7 @@ SDG_API int sdg_server_create(sdg_ctx* ctx, const sdg_matrix* ref, int workers, 
       ctx->engine = screen_supported(m, 1) ? 2 : 1;
       knn_device(ctx, q.get(), S->ref, m, 1, 1, 0, 1, false, 0, nullptr, nullptr, &ke, &fl, &hi, &hv);
       CK(cudaStreamSynchronize(ctx->stream));
+      S->methods_ready |= 1u << m;
     }
     // The tensor-core screen's dense copy of the reference is built here too,
     // per served method that can use it while a copy fits in half the free
@@ -1472,6 +1480,9 @@ SDG_API int sdg_server_submit(sdg_server* S, const sdg_csc* Q, int method, int d
     if (!S || !id) fail(SDG_E_ARG, "NULL argument");
     if (k < 1) fail(SDG_E_ARG, kMsgK);
     check_method(method, dist);
+    if (!(S->methods_ready & (1u << method)))
+      fail(SDG_E_ARG, "method " + std::to_string(method) +
+                          " was not prepared by sdg_server_create (pass it in `methods`).");
     check_csc_host(Q, "X");
     if (Q->ncol < 1) fail(SDG_E_ARG, "'X' must have at least one column.");
     if (Q->nrow != S->ref->nrow) fail(SDG_E_ROWS, "'X' and 'Y' must have the same number of rows.");
@@ -1513,7 +1524,8 @@ SDG_API int sdg_server_result(sdg_server* S, int64_t id, int32_t* idx, double* d
     std::lock_guard<std::mutex> lock(S->mu);
     auto it = S->reqs.find(id);
     if (it == S->reqs.end()) { g_err = "unknown request"; return SDG_E_ARG; }
-    if (it->second->state != Request::DONE) { g_err = "request not finished"; return SDG_E_ARG; }
+    const auto st = it->second->state;
+    if (st != Request::DONE && st != Request::CANCELLED) { g_err = "request not finished"; return SDG_E_ARG; }
     r = std::move(it->second);
     S->reqs.erase(it);
   }
@@ -1533,6 +1545,8 @@ SDG_API int sdg_server_cancel(sdg_server* S, int64_t id) {
   Request* r = it->second.get();
   if (r->state == Request::PENDING || r->state == Request::ADMITTED) {
     if (r->state == Request::ADMITTED) { S->in_use -= r->mem; --S->active; }
+    // out of the queues now, so that sdg_server_result may release it
+    for (auto* q : {&S->pending, &S->admitted}) q->erase(std::remove(q->begin(), q->end(), r), q->end());
     r->state = Request::CANCELLED;
     r->status = SDG_E_CANCELLED;
     r->err = "Computation interrupted by the user.";

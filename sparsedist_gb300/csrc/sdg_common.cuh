@@ -46,7 +46,7 @@ __host__ __device__ inline double na_real() {
 // Order-preserving map of a finite double onto uint64 (ascending value ->
 // ascending key), flipped for "larger is better".  -0 maps like +0, so the
 // comparison agrees with IEEE equality, which is what the reference's
-// comparator (value, index) uses.
+// comparator (value, index) uses; the value itself is carried beside the key.
 __device__ __forceinline__ uint64_t order_key(double v, bool decreasing) {
   if (v == 0.0) v = 0.0;
   uint64_t b = (uint64_t)__double_as_longlong(v);
@@ -54,11 +54,6 @@ __device__ __forceinline__ uint64_t order_key(double v, bool decreasing) {
   return decreasing ? ~b : b;
 }
 
-__device__ __forceinline__ double key_value(uint64_t k, bool decreasing) {
-  if (decreasing) k = ~k;
-  k = (k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFULL) : ~k;
-  return __longlong_as_double((long long)k);
-}
 #endif
 
 }  // namespace sdg

@@ -17,8 +17,6 @@
 // it keeps the last call's contents, so each call clears the error flag
 // before use; two calls whose work overlaps on the GPU (different streams,
 // or the same array reached from two threads) race on it.
-#include <mutex>
-
 #include "../../include/sdgpu.h"
 #include "sdg_kernels.h"
 #include "sdg_snn_core.cuh"
@@ -31,11 +29,12 @@ constexpr int64_t kNoallocScratchInts = (int64_t)8 << 20;   // 32 MiB per device
 static __device__ __align__(256) int32_t g_noalloc_scratch[kNoallocScratchInts];
 
 // Host code may not use g_noalloc_scratch as an address: on the host the name
-// is a stand-in for the device symbol.  Its device address is looked up once
-// per device, with that device current, and cached here.
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mu;
-int32_t* g_scratch_dev[kMaxDevices] = {};
+// is a stand-in for the device symbol.  Its device address is looked up on
+// every call, in the calling thread's current context: an address cached
+// across calls would go stale when the module is loaded again at another
+// address (after cudaDeviceReset, or in another context of the same device).
+// The lookup allocates nothing; the first one on a device loads the module,
+// which is why the first call should come before any stream capture.
 
 inline unsigned blocks_for(int64_t n, int threads) {
   return (unsigned)((n + threads - 1) / threads);
@@ -87,22 +86,10 @@ SDG_API int sdg_snn_jaccard_noalloc(const int32_t* d_idx, int32_t n, int32_t k,
     return fail_with(SDG_E_UNSUPPORTED,
                      "sdg_snn_jaccard_noalloc: n * (k + 2) + 1 exceeds the fixed scratch of "
                      "8388608 integers; use sdg_snn_jaccard for this size.");
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+  void* sym = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&sym, g_noalloc_scratch);
   if (e != cudaSuccess) return cuda_fail(e);
-  if (dev < 0 || dev >= kMaxDevices) return fail_with(SDG_E_UNSUPPORTED, "device ordinal too large");
-  int32_t* scratch = nullptr;
-  {
-    // first call on this device: resolve the array's device address
-    std::lock_guard<std::mutex> lock(g_setup_mu);
-    if (!g_scratch_dev[dev]) {
-      void* p = nullptr;
-      e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-      if (e != cudaSuccess) return cuda_fail(e);
-      g_scratch_dev[dev] = static_cast<int32_t*>(p);
-    }
-    scratch = g_scratch_dev[dev];
-  }
+  int32_t* scratch = static_cast<int32_t*>(sym);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   int32_t* sets = scratch;
   int32_t* sizes = sets + (int64_t)n * (k + 1);

@@ -1062,12 +1062,10 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
   if (r.method == COSINE && r.qry_empty) force = const_cast<uint8_t*>(r.qry_empty);
 
   const size_t smem = tbytes + (size_t)vcap * 4 + 64;
-  static bool attr_set[2] = {false, false};
-  if (!attr_set[0]) {
-    SK(cudaFuncSetAttribute(k_screen<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax));
-    SK(cudaFuncSetAttribute(k_screen<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax));
-    attr_set[0] = true;
-  }
+  // a function attribute is per device: set on every call (cheap, thread-safe),
+  // never cached process-wide
+  SK(cudaFuncSetAttribute(k_screen<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax));
+  SK(cudaFuncSetAttribute(k_screen<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax));
   int nsm = 152;
   {
     int dev = 0;

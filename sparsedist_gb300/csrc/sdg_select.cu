@@ -2,7 +2,9 @@
 //
 // One warp owns one output row ("segment") and keeps its k best candidates in
 // shared memory as a list sorted best-first on the key (order_key(value),
-// index).  The comparator is a strict total order, so the result is the top-k
+// index), with each candidate's own value beside it: order_key maps -0 and +0
+// onto one key (IEEE equality, as the reference's comparator), and the value
+// written out is the candidate's, bit for bit, as topKBlock writes D's.  The comparator is a strict total order, so the result is the top-k
 // of the candidate set whatever order candidates arrive in: it equals the
 // bounded-heap results of topKBlock (src/topK.cpp:104-131) and of
 // topKRowsAccum's strictly-better replacement (src/topKRows.cpp:201-228).
@@ -18,8 +20,8 @@ __device__ __forceinline__ bool less_key(uint64_t ka, int32_t ia, uint64_t kb, i
 }
 
 // Warp-cooperative insertion of the lanes' candidates into the sorted list.
-__device__ __forceinline__ void insert_batch(bool valid, uint64_t key, int32_t gidx,
-                                             uint64_t* lk, int32_t* li, int& n, int K,
+__device__ __forceinline__ void insert_batch(bool valid, uint64_t key, int32_t gidx, double val,
+                                             uint64_t* lk, int32_t* li, double* lv, int& n, int K,
                                              int lane) {
   bool pass = valid;
   if (n == K) pass = pass && less_key(key, gidx, lk[K - 1], li[K - 1]);
@@ -29,6 +31,7 @@ __device__ __forceinline__ void insert_batch(bool valid, uint64_t key, int32_t g
     m &= m - 1;
     const uint64_t kk = __shfl_sync(FULL, key, src);
     const int32_t ii = __shfl_sync(FULL, gidx, src);
+    const double vv = __shfl_sync(FULL, val, src);
     if (n == K && !less_key(kk, ii, lk[K - 1], li[K - 1])) continue;
     int lo = 0, hi = n;
     while (lo < hi) {
@@ -42,13 +45,14 @@ __device__ __forceinline__ void insert_batch(bool valid, uint64_t key, int32_t g
         const bool mv = (e >= lo && e < last);
         uint64_t tk = 0;
         int32_t ti = 0;
-        if (mv) { tk = lk[e]; ti = li[e]; }
+        double tv = 0.0;
+        if (mv) { tk = lk[e]; ti = li[e]; tv = lv[e]; }
         __syncwarp();
-        if (mv) { lk[e + 1] = tk; li[e + 1] = ti; }
+        if (mv) { lk[e + 1] = tk; li[e + 1] = ti; lv[e + 1] = tv; }
         __syncwarp();
       }
     }
-    if (lane == 0) { lk[lo] = kk; li[lo] = ii; }
+    if (lane == 0) { lk[lo] = kk; li[lo] = ii; lv[lo] = vv; }
     __syncwarp();
     if (n < K) ++n;
   }
@@ -62,7 +66,8 @@ __global__ void k_select(SelectArgs a) {
   if (seg >= a.nseg) return;                         // uniform per warp
   const int K = a.k;
   uint64_t* lk = reinterpret_cast<uint64_t*>(smem) + (int64_t)warp * K;
-  int32_t* li = reinterpret_cast<int32_t*>(reinterpret_cast<uint64_t*>(smem) + (int64_t)warps * K) +
+  double* lv = reinterpret_cast<double*>(smem) + (int64_t)warps * K + (int64_t)warp * K;
+  int32_t* li = reinterpret_cast<int32_t*>(reinterpret_cast<uint64_t*>(smem) + 2 * (int64_t)warps * K) +
                 (int64_t)warp * K;
   const bool dec = a.decreasing != 0;
   const int64_t row = a.out_row0 + seg;
@@ -81,7 +86,7 @@ __global__ void k_select(SelectArgs a) {
         const unsigned bm = __ballot_sync(FULL, bad);
         const int lim = bm ? (__ffs(bm) - 1) : 32;
         const bool ok = (lane < lim) && (t < K);
-        insert_batch(ok, ok ? order_key(v, dec) : 0, ok ? gi - 1 : 0, lk, li, n, K, lane);
+        insert_batch(ok, ok ? order_key(v, dec) : 0, ok ? gi - 1 : 0, v, lk, li, lv, n, K, lane);
         if (bm) break;
       }
     }
@@ -95,19 +100,20 @@ __global__ void k_select(SelectArgs a) {
       bool ok = t < len;
       uint64_t key = 0;
       int32_t g = 0;
+      double v = 0.0;
       if (ok) {
-        const double v = base[t * a.elem_stride];
+        v = base[t * a.elem_stride];
         const int64_t gg = cidx ? (int64_t)cidx[t] : a.idx_base + t;
         ok = isfinite(v) && gg != skip && !(a.elem_mask && a.elem_mask[t]);
         key = order_key(v, dec);
         g = (int32_t)gg;
       }
-      insert_batch(ok, key, g, lk, li, n, K, lane);
+      insert_batch(ok, key, g, v, lk, li, lv, n, K, lane);
     }
   }
   for (int t = lane; t < K; t += 32) {
     const int64_t at = (int64_t)t * a.out_ld + row;
-    if (t < n) { a.out_idx[at] = li[t] + 1; a.out_val[at] = key_value(lk[t], dec); }
+    if (t < n) { a.out_idx[at] = li[t] + 1; a.out_val[at] = lv[t]; }
     else       { a.out_idx[at] = NA_INT;    a.out_val[at] = na_real(); }
   }
 }
@@ -117,8 +123,8 @@ __global__ void k_select(SelectArgs a) {
 void launch_select(const SelectArgs& a, cudaStream_t s) {
   if (a.nseg <= 0) return;
   int warps = 8;
-  while (warps > 1 && (size_t)warps * a.k * 12 > 48 * 1024) warps >>= 1;
-  const size_t smem = (size_t)warps * a.k * 12;
+  while (warps > 1 && (size_t)warps * a.k * 20 > 48 * 1024) warps >>= 1;
+  const size_t smem = (size_t)warps * a.k * 20;
   const int64_t blocks = (a.nseg + warps - 1) / warps;
   k_select<<<(unsigned)blocks, warps * 32, smem, s>>>(a);
 }

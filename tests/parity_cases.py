@@ -128,6 +128,22 @@ def ka_na_padding(b):
     assert dst[0, 1:].view(np.uint64).tolist() == [int(NA_REAL_BITS)] * 2
 
 
+def ka_signed_zero(b):
+    # src/topK.cpp:38-50, 140-148: -0 and +0 compare equal (the tie goes to the
+    # lower row) and each slot returns D's own value, sign of zero included
+    D = np.array([[-0.0, 1.0], [0.0, -0.0], [1.0, 0.0]])
+    for dec, want_i, want_v in ((False, [[1, 2, 3], [2, 3, 1]], [[-0.0, 0.0, 1.0], [-0.0, 0.0, 1.0]]),
+                                (True, [[3, 1, 2], [1, 2, 3]], [[1.0, -0.0, 0.0], [1.0, -0.0, 0.0]])):
+        idx, dst = b.topk_block(D, 3, dec, [0, 0])
+        assert idx.tolist() == want_i, dec
+        assert same_bits(dst, np.array(want_v)), dec
+    # the running per-row state keeps the sign too (topKRowsAccum)
+    bi = np.full((3, 2), NA_INT, np.int32, order="F")
+    bv = np.full((3, 2), np.nan, order="F")
+    bi, bv = b.topk_rows_accum(D, 2, False, bi, bv, 0, [0, 0, 0])
+    assert same_bits(bv, np.array([[-0.0, 1.0], [0.0, -0.0], [0.0, 1.0]])), bv
+
+
 def ka_topk_validation(b):
     # test-sparseKNN.R:196-206
     D = np.random.default_rng(0).random((3, 2))
@@ -352,7 +368,7 @@ def ka_rows_accum_validation(b):
         b.topk_rows_accum(D, 2, False, bi, bv, 0, [0, -1, 0, 0])
 
 
-KNOWN_ANSWERS = [ka_ties, ka_na_padding, ka_topk_validation, ka_pearson_self, ka_covariance, ka_js_self,
+KNOWN_ANSWERS = [ka_ties, ka_na_padding, ka_signed_zero, ka_topk_validation, ka_pearson_self, ka_covariance, ka_js_self,
                  ka_signed_cancel, ka_cross_degenerate, ka_k_clamp, ka_no_candidates,
                  ka_snn_knowns, ka_snn_awkward_knn_edges, ka_cosine_extremes, ka_js_disjoint,
                  ka_nonfinite, ka_cross_is_two_knn, ka_block_size_invariance,

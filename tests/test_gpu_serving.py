@@ -77,3 +77,72 @@ def test_each_result_is_the_same_alone_and_in_the_mix(reference, budget, slots):
         assert st["batches"] < len(reqs)                 # requests were packed together
     srv.close()
     res.free()
+
+
+def test_unprepared_method_is_refused(reference):
+    """The workers only read the shared reference: a method whose reference
+    data sdg_server_create did not prepare is refused at submit (from any
+    number of submitting threads), never prepared lazily by a worker."""
+    from sparsedist_gb300 import _lib
+    ctx = _lib.Context()
+    R = reference[:, :3000]
+    res = _lib.Resident(ctx, R.shape[0], R.shape[1], R.indptr, R.indices, R.data)
+    srv = _lib.Server(ctx, res, workers=2, max_slots=4, mem_budget=8 << 30, methods=[METHODS["cosine"]])
+    Q = R[:, :5]
+
+    def submit(method):
+        try:
+            srv.submit(Q.shape[0], Q.shape[1], Q.indptr, Q.indices, Q.data, METHODS[method], True, 5)
+            return None
+        except _lib.SdgError as e:
+            return e.code, str(e)
+
+    with cf.ThreadPoolExecutor(2) as ex:
+        got = list(ex.map(submit, ["binary", "euclidean", "manhattan", "binary"]))
+    for g in got:
+        assert g is not None and g[0] == -1 and "not prepared" in g[1]
+    rid = srv.submit(Q.shape[0], Q.shape[1], Q.indptr, Q.indices, Q.data, METHODS["cosine"], True, 5)
+    assert srv.wait(rid, 600000)
+    srv.result(rid)
+    srv.close()
+    res.free()
+
+
+def test_cancel_pending_and_admitted_requests(reference):
+    """One worker, two slots: the first (large) request runs, the second is
+    admitted behind it and the rest wait for a slot.  A cancel that returns
+    True must make the request finish with SDG_E_CANCELLED and release it (a
+    second result call finds no such request); one that returns False must
+    deliver the ordinary result.  Every other request still completes."""
+    from sparsedist_gb300 import _lib
+    ctx = _lib.Context()
+    R = reference
+    res = _lib.Resident(ctx, R.shape[0], R.shape[1], R.indptr, R.indices, R.data)
+    srv = _lib.Server(ctx, res, workers=1, max_slots=2, mem_budget=64 << 30,
+                      methods=[METHODS["cosine"], METHODS["binary"]])
+    big = R[:, :2000]
+    small = [R[:, 10 * t:10 * t + 7] for t in range(6)]
+    first = srv.submit(big.shape[0], big.shape[1], big.indptr, big.indices, big.data, METHODS["cosine"],
+                       True, 10)
+    ids = [srv.submit(Q.shape[0], Q.shape[1], Q.indptr, Q.indices, Q.data, METHODS["binary"], True, 10)
+           for Q in small]
+    cancelled = {rid: srv.cancel(rid) for rid in ids[::2]}
+    assert any(cancelled.values())          # the waiting requests cannot all have started
+    for rid, Q in zip(ids, small):
+        assert srv.wait(rid, 600000)
+        if cancelled.get(rid):
+            with pytest.raises(_lib.SdgError) as e:
+                srv.result(rid)
+            assert e.value.code == -9
+            srv._held[rid] = (Q.shape[1], 10)
+            with pytest.raises(_lib.SdgError) as e:
+                srv.result(rid)                 # released by the first result call
+            assert e.value.code == -1
+        else:
+            gi, gd, _ = srv.result(rid)
+            wi, wd = alone(ctx, res, Q, "binary", 10)
+            assert same_bits(gi, wi) and same_bits(gd, wd)
+    assert srv.wait(first, 600000)
+    srv.result(first)
+    srv.close()
+    res.free()
