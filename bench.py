@@ -1,35 +1,38 @@
 #!/usr/bin/env python
-"""bench.py -- kNN query columns per second of sparseKNN on GB300.
+"""bench.py -- kNN query columns per second on GB300.
 
-Workload ("plain sparse kNN at scale"): a 30,000 x 200,000
-CSC float64 log-count matrix (per-column nnz ~ lognormal, mean 1,800, sdlog
-0.6; rows weighted by lognormal(0, 1.5) means; values log1p of NB(2) counts),
-generated seeded on the GPU (sparsedist_gb300/synth.py).  The reference
-matrix stays resident in HBM.  One step = one block of B query columns of
-that matrix searched against all 200,000 reference columns, cosine, k = 20,
-i.e. one block of sparseKNN(X[, block], X) -- the unit of the reference's
-own block loop (R/sparseKNN.R:248-294).
+Default line (--config dense): the precision path.  A resident 256 x
+2,000,000 FP32 embedding matrix (i.i.d. N(0,1) columns mixed with 1,000
+Gaussian clusters, sigma 0.3, and 1 % near duplicates at 1e-6; seeded,
+generated on the GPU by sparsedist_gb300/synth.py).  One step = one block of
+4,096 columns of that matrix searched as query vectors against all 2,000,000
+columns, cosine, k = 20: sparseKNN(X[, block], X) with the reference's idx
+and FP64 distances (R/sparseKNN.R:183-301 on the dgCMatrix of the same data).
 
-* value: query columns / s with inputs resident in HBM (CUDA events on the
-  library's stream, which is torch's current stream).
-* e2e:   the same through the C ABI with host buffers: per step the query
-  block's CSC arrays are copied host -> device from pinned memory and the
-  idx / dist results device -> host, inside the timed region.
-* roofline: the bounding kernel per launch, over its average CUDA-event
-  duration.  With the tensor-core screen (the automatic choice here) that is
-  the FP16 GEMM: 2 * rows * references * queries flops against the measured
-  BF16 peak (FP16 and BF16 run at the same dense tensor rate on GB300).  With the FP32 sparse screen (--engine 2) it is k_screen: the
-  path's algorithmic bytes (12 bytes per stored entry touched per evaluated
-  pair, plus 12 bytes per output slot) against the measured HBM bandwidth.
-  sparse_alg_gbs reports the byte figure in both cases.
-* cpu_baseline: the reference's algorithm on this machine's host cores (the
-  oracle port, OpenMP over all cores) on one block of 256 query columns
-  against the full reference.
+* value: columns / s of the BF16-screened path (the fused tcgen05 screen
+  k_dense_tc + exact FP64 re-rank), inputs resident in HBM, CUDA events on
+  the library's stream (torch's current stream).
+* plain_fp32 / vs_plain_fp32: the same blocks through the plain GPU FP32
+  path (FP32 SGEMM, top-k on the FP32 values, no re-rank) and the ratio.
+* e2e: the same blocks submitted as host FP32 vectors to the serving loop
+  (sdg_server_create_dense / submit / wait / result), host idx / dist back,
+  two requests in flight; p50 / p99 request latency beside it.
+* roofline: k_dense_tc per launch, 2 * 256 * 2,000,000 * 4,096 BF16 flops
+  over its average CUDA-event duration, against the measured BF16 burst.
+* cpu_baseline + parity: the oracle (the reference's algorithm, OpenMP over
+  all host cores) on the first 128 columns of one block against the whole
+  reference; the GPU's result for the same columns is compared with it (idx
+  and distances bit for bit for the screened path; agreement and the
+  largest distance error for the plain FP32 path).
 
---impl reference times that CPU implementation alone, on the same workload.
-Multi-GPU (torchrun): each rank searches its own query blocks against its
-own replica of the reference (query-column sharding, no collective on the
-data path); value = all ranks' columns / max-over-ranks time.
+--config logcount: sparse kNN at scale (30,000 x 200,000 log-count CSC,
+cosine k = 20, 4,096-query blocks of sparseKNN(X[, block], X)), with the
+same keys and a bit-for-bit parity check of a 256-column oracle sample.
+--impl reference times the oracle alone on bounded samples of the chosen
+workload.  Multi-GPU (torchrun): each rank searches its own query blocks
+against its own replica of the reference (query-column sharding, no
+collective on the data path); value = all ranks' columns / max-over-ranks
+time.
 """
 from __future__ import annotations
 
@@ -68,14 +71,19 @@ def parse():
     ap.add_argument("--dist-cols", type=int, default=10000)
     ap.add_argument("--dist-long", action="store_true",
                     help="long columns (the 30,000-row log-count generator)")
-    ap.add_argument("--config", default="logcount",
-                    choices=["logcount", "uniform", "dense", "serve", "dist", "snn"],
-                    help="logcount: the default line (30,000 x 200,000 log-count kNN); uniform: the "
-                         "CPU-runnable 2,000 x 10,000 case; dense: 256 x 2,000,000 embeddings; "
-                         "serve: the serving loop; dist: full-matrix sparseDist; snn: sparseSNN")
+    ap.add_argument("--config", default="dense",
+                    choices=["dense", "logcount", "uniform", "serve", "dist", "snn"],
+                    help="dense: the default line (256 x 2,000,000 embeddings, BF16-screened vs plain "
+                         "FP32, served e2e); logcount: 30,000 x 200,000 log-count sparse kNN; uniform: "
+                         "the CPU-runnable 2,000 x 10,000 case; serve: the sparse serving loop; dist: "
+                         "full-matrix sparseDist; snn: sparseSNN")
     ap.add_argument("--serve-ref-cols", type=int, default=1000000)
     ap.add_argument("--dense-cols", type=int, default=2000000)
     ap.add_argument("--dense-block", type=int, default=4096)
+    ap.add_argument("--dense-cpu-cols", type=int, default=128,
+                    help="query columns of the dense CPU-baseline / parity sample")
+    ap.add_argument("--ref-cols", type=int, default=16,
+                    help="query columns per step of the dense --impl reference arm")
     ap.add_argument("--serve-requests", type=int, default=80)
     ap.add_argument("--serve-util", type=float, default=0.75)
     return ap.parse_args()
@@ -164,7 +172,7 @@ def bytes_alg(p, c0, c1, nnz_ref, ncol_ref, k, method):
     return s * (ncol_ref * nnz_q + nq * nnz_ref) + nq * k * 12
 
 
-def cpu_baseline(p, i, x, nrow, ncol, method, k, cols, threads):
+def cpu_baseline(p, i, x, nrow, ncol, method, k, cols, threads, keep=False):
     import scipy.sparse as sp
     from oracle import build as obuild
     from oracle.pyoracle import Oracle
@@ -174,8 +182,10 @@ def cpu_baseline(p, i, x, nrow, ncol, method, k, cols, threads):
     qp, qi, qx = block_arrays(p, i, x, 0, cols)
     Q = sp.csc_matrix((qx, qi, qp), shape=(nrow, cols))
     t0 = time.perf_counter()
-    orc.knn(Q, ref, k=k, method=method, block_size=256)
+    idx, dst, _ = orc.knn(Q, ref, k=k, method=method, block_size=256)
     dt = time.perf_counter() - t0
+    if keep:
+        return cols / dt, dt, (idx, dst)
     return cols / dt, dt
 
 
@@ -471,102 +481,253 @@ def run_serve(args):
     ref.free()
 
 
-def run_dense(args):
-    """Dense embeddings: 256 x 2,000,000 FP32 (i.i.d. N(0,1) mixed
-    with 1,000 Gaussian clusters, sigma 0.3, plus 1 % near duplicates at 1e-6),
-    cosine and euclidean self-search, k = 20, in blocks of --dense-block (4,096) query columns:
-    the BF16 tensor-core screen + exact FP64 re-rank against the plain FP32
-    path, with idx identity and distance error checked against the exact FP64
-    engine on a sample of query columns."""
+def dense_csc(X):
+    """(n, d) float32 embeddings (torch, any device) -> host CSC arrays of the
+    d x n dgCMatrix the reference would receive: every value stored (exact
+    zeros dropped, as Matrix does)."""
+    import scipy.sparse as sp
+    A = np.ascontiguousarray(X.double().cpu().numpy())
+    n, d = A.shape
+    M = sp.csc_matrix((A.ravel(), np.tile(np.arange(d, dtype=np.int32), n),
+                       np.arange(0, (n + 1) * d, d, dtype=np.int64)), shape=(d, n))
+    M.eliminate_zeros()
+    return M
+
+
+def dense_block_starts(args, n, B, rank, count):
+    nblocks = n // B
+    return [((rank * count + s) * 7919 % nblocks) * B for s in range(count)]
+
+
+def dense_workload_config(args, B):
+    return {"workload": "sparseKNN(X[, block], X) on resident 256x%d FP32 embeddings (N(0,1) + 1000 "
+                        "Gaussian clusters sigma 0.3 + 1%% near duplicates at 1e-6), %s, k=%d, "
+                        "BF16 tcgen05 screen + exact FP64 re-rank" % (args.dense_cols, args.method, args.k),
+            "d": 256, "ncol": args.dense_cols, "query_block": B, "method": args.method, "k": args.k,
+            "l2": "inputs larger than L2: the 1 GB BF16 reference copy is streamed every step"}
+
+
+def dense_oracle_sample(Xcsc, X, q0, cols, k, method, threads):
+    """The oracle's sparseKNN(X[, q0 + 0..cols-1], X) and its wall time."""
+    from oracle import build as obuild
+    from oracle.pyoracle import Oracle
+    obuild.build_oracle()
+    orc = Oracle(threads=threads)
+    Q = Xcsc[:, q0:q0 + cols]
+    t0 = time.perf_counter()
+    idx, dst, _ = orc.knn(Q, Xcsc, k=k, method=method, block_size=256)
+    return idx, dst, time.perf_counter() - t0
+
+
+def run_dense_reference(args):
+    """--impl reference on the dense workload: the reference's algorithm (the
+    oracle port, OpenMP over all host cores) on a bounded sample of each step's
+    query block against all reference columns."""
+    import torch
+    from sparsedist_gb300 import synth
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    d, n, B, k = 256, args.dense_cols, args.dense_block, args.k
+    X = synth.dense_embeddings(d=d, n=n, seed=5, device="cuda" if torch.cuda.is_available() else "cpu")
+    Xcsc = dense_csc(X)
+    threads = os.cpu_count() or 1
+    cols = args.ref_cols
+    starts = dense_block_starts(args, n, B, 0, args.warmup + args.steps)
+    for s in range(args.warmup):
+        dense_oracle_sample(Xcsc, X, starts[s], cols, k, args.method, threads)
+    t = 0.0
+    for s in range(args.steps):
+        t += dense_oracle_sample(Xcsc, X, starts[args.warmup + s], cols, k, args.method, threads)[2]
+    v = cols * args.steps / t
+    print(json.dumps({
+        "impl": "reference", "metric": dense_metric(args), "value": v, "unit": "columns/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": dense_workload_config(args, cols),
+        "cpu_baseline": {"value": v, "unit": "columns/s", "cores": threads, "kind": "port",
+                         "sample": "%d query columns x %d reference columns per step" % (cols, n)},
+        "e2e": {"value": v, "unit": "columns/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+
+
+def dense_metric(args):
+    return ("kNN query columns/s, served BF16-screened vs plain GPU FP32 at exact top-k "
+            "(%s k=%d, 256x%d embeddings)" % (args.method, args.k, args.dense_cols))
+
+
+def run_dense_main(args):
+    """The default line: dense embeddings, 256 x 2,000,000 FP32, cosine k = 20.
+    One step = one block of 4,096 query columns (columns of X, passed as
+    device-resident FP32 query vectors) searched against all 2,000,000
+    columns: sparseKNN(X[, block], X) through sdg_dense_knn_query, mode 0 (the
+    fused BF16 tcgen05 screen + exact FP64 re-rank).  The same blocks through
+    mode 1 (plain FP32 SGEMM + top-k on FP32 values) give the plain GPU
+    figure; e2e submits the same blocks as host vectors to the serving loop
+    (sdg_server_create_dense, two workers, two requests in flight) and reads
+    the results back.  The oracle computes the CPU-baseline sample, and the
+    same columns' GPU results are compared with it bit for bit."""
     import ctypes as C
     import torch
+    import torch.distributed as dist
     from sparsedist_gb300 import _lib, synth
-    d, n, B, k = 256, args.dense_cols, args.dense_block, 20
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    d, n, B, k = 256, args.dense_cols, args.dense_block, args.k
+    code = METHOD_CODES[args.method]
+    K, W = args.steps, args.warmup
     X = synth.dense_embeddings(d=d, n=n, seed=5)
-    ctx = _lib.Context()
+    ctx = _lib.Context(local)
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream.cuda_stream)
     h = C.c_void_p()
     _lib.check(ctx.lib.sdg_dense_upload(ctx.handle, X.data_ptr(), d, n, C.byref(h)))
+    starts = dense_block_starts(args, n, B, rank, W + K)
     d_idx = torch.empty(B * k, dtype=torch.int32, device="cuda")
     d_val = torch.empty(B * k, dtype=torch.float64, device="cuda")
     ke, fl = np.zeros(1, np.int32), np.zeros(1, np.int32)
-    res = {}
-    for method, code in (("cosine", 1), ("euclidean", 2)):
-        for mode, name in ((0, "bf16_tcgen05_fused_fp64_rerank"), (2, "bf16_cublas_slab_fp64_rerank"),
-                           (1, "plain_fp32")):
-            def step(s):
-                _lib.check(ctx.lib.sdg_dense_knn_block(ctx.handle, h, (s * B) % (n - B), B, code, k,
-                                                       mode, d_idx.data_ptr(), d_val.data_ptr(), 1,
-                                                       ke.ctypes.data, fl.ctypes.data))
-            for s in range(args.warmup):
-                step(s)
-            torch.cuda.synchronize()
-            ctx.kernel_time()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            for s in range(args.steps):
-                step(args.warmup + s)
-            e1.record(stream)
-            torch.cuda.synchronize()
-            ms = e0.elapsed_time(e1) / args.steps
-            gemm_ms, launches = ctx.kernel_time()
-            st = ctx.stats()                              # the last block's counters
-            flops = 2.0 * d * B * n
-            res["%s/%s" % (method, name)] = {"columns_per_s": B / (ms / 1000.0), "ms_per_block": ms,
-                                             "candidates_per_query": st["pairs_exact"] / B,
-                                             "overflow_queries": st["overflow_queries"],
-                                             "screen_kernel_ms_per_block": gemm_ms / args.steps,
-                                             "screen_launches_per_block": launches / args.steps,
-                                             "screen_tflops": flops / (gemm_ms / args.steps / 1000.0) / 1e12}
-        res["%s/speedup_bf16_vs_fp32" % method] = (res["%s/bf16_tcgen05_fused_fp64_rerank" % method]["columns_per_s"] /
-                                                   res["%s/plain_fp32" % method]["columns_per_s"])
-    # correctness on a sample of query columns: the exact FP64 engine on the same data
-    qs = 16
-    A = X.double()                                        # (n, d)
-    p = torch.arange(0, (n + 1) * d, d, dtype=torch.int32, device="cuda")
-    rows = torch.arange(d, dtype=torch.int32, device="cuda").repeat(n)
-    full = _lib.Resident.from_device(ctx, d, n, p, rows, A.reshape(-1))
-    qp = torch.arange(0, (qs + 1) * d, d, dtype=torch.int32, device="cuda")
-    qsamp = _lib.Resident.from_device(ctx, d, qs, qp, rows[:qs * d], A[:qs].reshape(-1))
-    ctx.set_engine(1)
-    check = {}
-    for method, code in (("cosine", 1), ("euclidean", 2)):
-        wi = np.empty(qs * (k + 1), np.int32)
-        wd = np.empty(qs * (k + 1), np.float64)
-        _lib.check(ctx.lib.sdg_knn_resident(ctx.handle, qsamp.handle, full.handle, code, 1, k + 1, 0, 1,
-                                            wi.ctypes.data, wd.ctypes.data, ke.ctypes.data,
-                                            fl.ctypes.data))
-        wi = wi.reshape(k + 1, qs).T
-        wd = wd.reshape(k + 1, qs).T
-        for mode, name in ((0, "bf16_tcgen05_fused_fp64_rerank"), (2, "bf16_cublas_slab_fp64_rerank"),
-                           (1, "plain_fp32")):
-            gi = np.empty(qs * k, np.int32)
-            gd = np.empty(qs * k, np.float64)
-            _lib.check(ctx.lib.sdg_dense_knn_block(ctx.handle, h, 0, qs, code, k, mode, gi.ctypes.data,
-                                                   gd.ctypes.data, 0, ke.ctypes.data, fl.ctypes.data))
-            gi = gi.reshape(k, qs).T
-            gd = gd.reshape(k, qs).T
-            same, err = 0, 0.0
-            for q in range(qs):
-                keep = wi[q] != q + 1                     # the cross form includes the query itself
-                ri, rd = wi[q][keep][:k], wd[q][keep][:k]
-                same += int(np.array_equal(gi[q], ri))
-                err = max(err, float(np.max(np.abs(gd[q] - rd))))
-            check["%s/%s" % (method, name)] = {"rows_with_identical_idx": same, "rows": qs,
-                                               "max_abs_distance_error_vs_fp64": err}
-    ctx.set_engine(0)
-    print(json.dumps({"metric": "dense kNN query columns/s, 256x2000000 embeddings (k=20, %d-query blocks)" % B,
-                      "config": {"workload": "256x%d FP32 embeddings: N(0,1) + 1000 clusters (sigma 0.3) "
-                                             "+ 1%% near duplicates (1e-6)" % n},
-                      "results": res, "check_vs_fp64_engine": check}))
+
+    def step(q0, mode):
+        _lib.check(ctx.lib.sdg_dense_knn_query(ctx.handle, h, X[q0:q0 + B].data_ptr(), d, B, code, k, mode,
+                                               d_idx.data_ptr(), d_val.data_ptr(), 1, ke.ctypes.data,
+                                               fl.ctypes.data))
+
+    def timed(mode, sample_clocks):
+        for s in range(W):
+            step(starts[s], mode)
+        torch.cuda.synchronize()
+        ctx.kernel_time()                       # reset the bounding-kernel timer
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        clk = ClockSampler(local) if sample_clocks else None
+        if clk:
+            clk.__enter__()
+        e0.record(stream)
+        for s in range(K):
+            step(starts[W + s], mode)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if clk:
+            clk.__exit__()
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        t = torch.tensor([e0.elapsed_time(e1)], dtype=torch.float64, device="cuda")
+        if world > 1:
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        kms, kl = ctx.kernel_time()
+        return float(t.item()), kms, kl, ctx.stats(), (clk.summary() if clk else None)
+
+    ms, kms, klaunch, st, clocks = timed(0, True)
+    value = world * B * K / (ms / 1000.0)
+    launches = int(st["kernels"]) * K
+    ms1, _, _, _, _ = timed(1, False)
+    plain = world * B * K / (ms1 / 1000.0)
+
+    # roofline of the fused screen k_dense_tc: 2 * 256 * n * B BF16 flops per launch
+    hbm_peak, bf16_peak, peak_kind = measured_peaks()
+    flops = 2.0 * d * n * B
+    per_launch_ms = kms / max(klaunch, 1)
+    achieved = flops / (per_launch_ms / 1000.0) / 1e12 if klaunch else None
+    roof = {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
+            "frac": (achieved / bf16_peak) if achieved else None,
+            "peak_kind": peak_kind + " (cuBLAS bf16 burst)", "kernel": "k_dense_tc (fused BF16 tcgen05 screen)",
+            "flops_per_launch": flops, "kernel_ms_per_launch": per_launch_ms,
+            "launches_per_step": klaunch / max(K, 1), "traffic": DENSE_TRAFFIC}
+
+    # e2e: the serving loop with host query vectors, two requests in flight
+    e2e = None
+    if not args.no_e2e:
+        hq = [np.ascontiguousarray(X[q0:q0 + B].cpu().numpy()) for q0 in starts]
+
+        def serve(blocks):
+            srv = _lib.Server(ctx, h, workers=2, max_slots=4, mem_budget=64 << 30, dense=True)
+            ids, t0 = [], time.perf_counter()
+            for j, q in enumerate(blocks):
+                if j >= 2:
+                    srv.wait(ids[j - 2])
+                    srv.result(ids[j - 2])
+                ids.append(srv.submit_dense(q, code, k))
+            for rid in ids[-2:]:
+                srv.wait(rid)
+                srv.result(rid)
+            dt = time.perf_counter() - t0
+            stt = srv.stats()
+            srv.close()
+            return dt, stt
+
+        serve(hq[:W])
+        if world > 1:
+            dist.barrier()
+        dt, sst = serve(hq[W:])
+        et = torch.tensor([dt], dtype=torch.float64, device="cuda")
+        if world > 1:
+            dist.all_reduce(et, op=dist.ReduceOp.MAX)
+        e2e = {"value": world * B * K / float(et.item()), "unit": "columns/s",
+               "h2d_bytes_per_step": B * d * 4, "d2h_bytes_per_step": B * k * 12,
+               "path": "sdg_server_submit_dense / wait / result (host FP32 queries in, host idx/dist out)",
+               "p50_latency_s": sst["p50_s"], "p99_latency_s": sst["p99_s"], "requests": K,
+               "in_flight": 2, "batches": int(sst["batches"])}
+
+    cpu, parity = None, None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        Xcsc = dense_csc(X)
+        q0 = starts[W]
+        cols = args.dense_cpu_cols
+        oi, od, dt = dense_oracle_sample(Xcsc, X, q0, cols, k, args.method, threads)
+        cpu = {"value": cols / dt, "unit": "columns/s", "cores": threads, "kind": "port",
+               "sample": "%d query columns x %d reference columns, %.1f s" % (cols, n, dt)}
+        got = {}
+        for mode in (0, 1):
+            gi = np.empty(cols * k, np.int32)
+            gd = np.empty(cols * k, np.float64)
+            _lib.check(ctx.lib.sdg_dense_knn_query(ctx.handle, h, X[q0:q0 + cols].data_ptr(), d, cols, code, k,
+                                                   mode, gi.ctypes.data, gd.ctypes.data, 0, ke.ctypes.data,
+                                                   fl.ctypes.data))
+            got[mode] = (gi.reshape(k, cols).T, gd.reshape(k, cols).T)
+        parity = {"cols": cols, "vs": "oracle (the reference's algorithm, FP64)",
+                  "bf16_screened": {"idx_identical": bool(np.array_equal(got[0][0], oi)),
+                                    "dist_bit_identical": bool(np.array_equal(got[0][1].view(np.uint64),
+                                                                              od.view(np.uint64))),
+                                    "max_abs_dist_err": float(np.max(np.abs(got[0][1] - od)))},
+                  "plain_fp32": {"idx_agree_frac": float(np.mean(got[1][0] == oi)),
+                                 "rows_identical": int(np.sum(np.all(got[1][0] == oi, axis=1))),
+                                 "max_abs_dist_err": float(np.max(np.abs(got[1][1] - od)))}}
+    if rank == 0:
+        line = {
+            "metric": dense_metric(args), "value": value, "unit": "columns/s", "n_gpus": world, "steps": K,
+            "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16 screen, f64 re-rank", "data": "synthetic",
+            "config": dense_workload_config(args, B) | {"parallelism": "query-column shards x%d" % world},
+            "plain_fp32": {"value": plain, "unit": "columns/s", "ms_per_step": ms1 / K,
+                           "path": "sdg_dense_knn_query mode 1 (FP32 SGEMM, top-k on FP32 values)"},
+            "vs_plain_fp32": value / plain,
+            "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "parity": parity,
+            "clocks": clocks, "stats_last_call": st}
+        print(json.dumps(line))
     ctx.lib.sdg_dense_free(h)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_dense_tc launch (ncu, see
+# profiles/); None until captured
+DENSE_TRAFFIC = None
 
 
 def main():
     args = parse()
     if args.config == "dense":
-        run_dense(args)
+        if args.impl == "reference":
+            run_dense_reference(args)
+        else:
+            run_dense_main(args)
         return
     if args.config == "uniform":
         run_uniform(args)
@@ -583,6 +744,14 @@ def main():
     if args.impl == "reference":
         run_reference(args)
         return
+    run_logcount(args)
+
+
+def run_logcount(args):
+    """--config logcount: sparse kNN at scale (the 30,000 x 200,000 log-count
+    matrix, cosine k = 20, 4,096-query blocks), the tensor-core screen of the
+    sparse path; the CPU-baseline sample's oracle result is compared with the
+    GPU's result on the same columns bit for bit."""
     import torch
     import torch.distributed as dist
 
@@ -711,13 +880,26 @@ def main():
         e2e = {"value": world * B * K / float(et.item()), "unit": "columns/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": B * k * 12}
 
-    cpu = None
+    cpu, parity = None, None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        v, dt = cpu_baseline(p, i, x, args.nrow, args.ncol, args.method, k, args.cpu_cols, threads)
+        v, dt, (oi, od) = cpu_baseline(p, i, x, args.nrow, args.ncol, args.method, k, args.cpu_cols, threads,
+                                       keep=True)
         cpu = {"value": v, "unit": "columns/s", "cores": threads, "kind": "port",
                "sample": "%d query columns x %d reference columns (one reference block), %.1f s"
                          % (args.cpu_cols, args.ncol, dt)}
+        # the same columns through the library (the bench step's call, host outputs)
+        cols = args.cpu_cols
+        q = _lib.Resident(ctx, args.nrow, cols, *block_arrays(p, i, x, 0, cols))
+        gi = np.empty(cols * k, np.int32)
+        gd = np.empty(cols * k, np.float64)
+        _lib.check(lib.sdg_knn_resident(ctx.handle, q.handle, ref.handle, method, 1, k, 0, 1, gi.ctypes.data,
+                                        gd.ctypes.data, keff.ctypes.data, flags.ctypes.data))
+        q.free()
+        gi, gd = gi.reshape(k, cols).T, gd.reshape(k, cols).T
+        parity = {"cols": cols, "vs": "oracle (the reference's algorithm, FP64)",
+                  "identical": bool(np.array_equal(gi, oi) and np.array_equal(gd.view(np.uint64),
+                                                                               od.view(np.uint64)))}
 
     if rank == 0:
         st = ctx.stats()
@@ -732,6 +914,7 @@ def main():
             "gpu_launches": int(stats_launches) * K,
             "roofline": roof,
             "cpu_baseline": cpu,
+            "parity": parity,
             "clocks": clk.summary(),
             "stats_last_call": st,
         }

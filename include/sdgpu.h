@@ -220,7 +220,7 @@ SDG_API int sdg_knn_resident(sdg_ctx* ctx, const sdg_matrix* X, const sdg_matrix
  * drop_degenerate = TRUE) for cosine (dist) or euclidean.  mode 0: BF16
  * tensor-core screen with a rigorous bound and exact FP64 re-rank (the
  * reference's idx and distances), fused in one tcgen05 kernel (no slab in
- * HBM) for k <= 32 and d <= 256, else as mode 2; mode 2: the same screen
+ * HBM) for k <= 64 and d <= 256, else as mode 2; mode 2: the same screen
  * through a cuBLAS BF16 GEMM slab; mode 1: the plain FP32 path (FP32 GEMM,
  * top-k on FP32 values, no re-rank).  No counterpart in the reference, whose
  * dense inputs are coerced to dgCMatrix (R/sparseKNN.R:194-200); the FP64
@@ -229,6 +229,17 @@ typedef struct sdg_dense sdg_dense;
 SDG_API int sdg_dense_upload(sdg_ctx* ctx, const float* X, int32_t d, int64_t n, sdg_dense** out);
 SDG_API int sdg_dense_free(sdg_dense* D);
 SDG_API int sdg_dense_knn_block(sdg_ctx* ctx, const sdg_dense* D, int64_t q0, int64_t nq,
+                                int method, int k, int mode, int32_t* idx, double* dist_out,
+                                int device_out, int* k_eff, int* flags);
+
+/* sparseKNN(Q, D, k, method) for new query embeddings: Q is d x nq FP32
+ * (column-major, host or device pointer), searched against the resident D
+ * (drop_degenerate = TRUE; no self-exclusion, as in the reference's
+ * two-matrix form, R/sparseKNN.R:183-301 with Y given).  Same modes, outputs
+ * and clamp as sdg_dense_knn_block; idx are 1-based columns of D.  The
+ * queries' FP64 / unit / BF16 forms are built on the context's stream from
+ * its memory pool and released when the call returns. */
+SDG_API int sdg_dense_knn_query(sdg_ctx* ctx, const sdg_dense* D, const float* Q, int32_t d, int64_t nq,
                                 int method, int k, int mode, int32_t* idx, double* dist_out,
                                 int device_out, int* k_eff, int* flags);
 
@@ -248,6 +259,18 @@ SDG_API int sdg_server_create(sdg_ctx* ctx, const sdg_matrix* ref, int workers, 
                               sdg_server** out);
 SDG_API int sdg_server_submit(sdg_server* server, const sdg_csc* Q, int method, int dist, int k,
                               int drop_degenerate, int64_t* request_id);
+/* A server over a resident dense reference (sdg_dense_upload): requests are
+ * d x nq FP32 query columns (column-major, host memory, copied at submit),
+ * method cosine or euclidean, any k; admitted requests of one method are
+ * packed column-wise into one fused BF16 tensor-core search with the exact
+ * FP64 re-rank (sdg_dense_knn_query at the batch's largest k), so a
+ * request's result is sparseKNN(Q, ref, k, method) exactly, alone or in any
+ * mix.  sdg_server_wait / result / cancel / stats / destroy as above.  No
+ * counterpart in the reference. */
+SDG_API int sdg_server_create_dense(sdg_ctx* ctx, const sdg_dense* ref, int workers, int max_slots,
+                                    int64_t mem_budget, sdg_server** out);
+SDG_API int sdg_server_submit_dense(sdg_server* server, const float* Q, int32_t d, int32_t nq,
+                                    int method, int k, int64_t* request_id);
 /* 0 when the request finished, 1 on timeout (timeout_ms < 0 waits forever). */
 SDG_API int sdg_server_wait(sdg_server* server, int64_t request_id, int timeout_ms);
 /* Copies a finished request's ncol(Q) x k_eff result and releases it. */

@@ -32,6 +32,7 @@ EXPORTED = ["sdg_version", "sdg_last_error", "sdg_ctx_create", "sdg_ctx_destroy"
             "sdg_server_create", "sdg_server_submit", "sdg_server_wait", "sdg_server_result",
             "sdg_server_cancel", "sdg_server_stats", "sdg_server_destroy",
             "sdg_matrix_upload_device", "sdg_dense_upload", "sdg_dense_free", "sdg_dense_knn_block",
+            "sdg_dense_knn_query", "sdg_server_create_dense", "sdg_server_submit_dense",
             "sdg_snn_graph_shared"]
 
 
@@ -95,10 +96,14 @@ def load() -> C.CDLL:
             lib.sdg_dense_free.argtypes = [v]
             lib.sdg_dense_knn_block.argtypes = [v, v, C.c_int64, C.c_int64, C.c_int, C.c_int, C.c_int,
                                                 v, v, C.c_int, v, v]
+            lib.sdg_dense_knn_query.argtypes = [v, v, v, C.c_int32, C.c_int64, C.c_int, C.c_int, C.c_int,
+                                                v, v, C.c_int, v, v]
             lib.sdg_matrix_upload_device.argtypes = [v, C.c_int32, C.c_int32, v, v, v, C.POINTER(v)]
             lib.sdg_server_create.argtypes = [v, v, C.c_int, C.c_int, C.c_int64, v, C.c_int,
                                               C.POINTER(v)]
             lib.sdg_server_submit.argtypes = [v, v, C.c_int, C.c_int, C.c_int, C.c_int, v]
+            lib.sdg_server_create_dense.argtypes = [v, v, C.c_int, C.c_int, C.c_int64, C.POINTER(v)]
+            lib.sdg_server_submit_dense.argtypes = [v, v, C.c_int32, C.c_int32, C.c_int, C.c_int, v]
             lib.sdg_server_wait.argtypes = [v, C.c_int64, C.c_int]
             lib.sdg_server_result.argtypes = [v, C.c_int64, v, v, v, v]
             lib.sdg_server_cancel.argtypes = [v, C.c_int64]
@@ -240,16 +245,35 @@ class Resident:
 class Server:
     """sdg_server: continuous-batching kNN service against a resident reference."""
 
-    def __init__(self, ctx: Context, ref: Resident, workers=2, max_slots=64,
-                 mem_budget=120 << 30, methods=(1,)):
+    def __init__(self, ctx: Context, ref, workers=2, max_slots=64,
+                 mem_budget=120 << 30, methods=(1,), dense=False):
+        """ref: a Resident (sparse reference) or, with dense=True, the handle
+        of an sdg_dense (sdg_dense_upload)."""
         self.ctx, self.ref = ctx, ref
-        m = np.ascontiguousarray(methods, dtype=np.int32)
         h = C.c_void_p()
-        check(ctx.lib.sdg_server_create(ctx.handle, ref.handle, int(workers), int(max_slots),
-                                        int(mem_budget), m.ctypes.data, len(m), C.byref(h)))
+        if dense:
+            check(ctx.lib.sdg_server_create_dense(ctx.handle, ref, int(workers), int(max_slots),
+                                                  int(mem_budget), C.byref(h)))
+        else:
+            m = np.ascontiguousarray(methods, dtype=np.int32)
+            check(ctx.lib.sdg_server_create(ctx.handle, ref.handle, int(workers), int(max_slots),
+                                            int(mem_budget), m.ctypes.data, len(m), C.byref(h)))
         self.handle = h
         self.lib = ctx.lib
         self._held = {}
+
+    def submit_dense(self, Q, method=1, k=10):
+        """Q: d x nq FP32 query columns (host memory, column-major: a
+        C-contiguous (nq, d) array is read as its transpose)."""
+        Q = np.asarray(Q)
+        if Q.dtype != np.float32 or not Q.flags.c_contiguous:
+            raise ValueError("Q must be a C-contiguous float32 (nq, d) array")
+        nq, d = Q.shape
+        rid = C.c_int64()
+        check(self.lib.sdg_server_submit_dense(self.handle, Q.ctypes.data, int(d), int(nq), int(method),
+                                               int(k), C.byref(rid)))
+        self._held[rid.value] = (nq, k)
+        return rid.value
 
     def submit(self, nrow, ncol, p, i, x, method=1, dist=True, k=10, drop_degenerate=True):
         held = HeldCSC(nrow, ncol, p, i, x)

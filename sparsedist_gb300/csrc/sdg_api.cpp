@@ -1228,6 +1228,7 @@ struct Request {
   int32_t nrow = 0, ncol = 0;
   std::vector<int32_t> p, i;
   std::vector<double> x;
+  std::vector<float> q;           // dense queries: nrow x ncol FP32, column-major
   std::vector<int32_t> idx;
   std::vector<double> val;
   int k_eff = 0, flags = 0, status = SDG_OK;
@@ -1241,6 +1242,7 @@ struct Request {
 
 struct sdg_server {
   sdg_matrix* ref = nullptr;
+  const sdg_dense* dref = nullptr;        // a dense reference instead (sdg_server_create_dense)
   int device = 0;
   int64_t budget = 0, in_use = 0;
   int max_slots = 1, active = 0;
@@ -1268,6 +1270,7 @@ namespace {
 // the FP32 screen slab (capped by the engine's per-pass slab), the candidate
 // table and exact values, and the result buffers.
 int64_t request_mem(const sdg_server* S, int64_t ncol, int64_t nnz, int k) {
+  if (S->dref) return dense_query_bytes(S->dref, ncol, k);
   const int64_t nr = S->ref->ncol;
   const int64_t slab_cols = std::min<int64_t>(ncol, std::max<int64_t>(16, ((int64_t)4 << 30) / (4 * std::max<int64_t>(nr, 1))));
   const int64_t cap = std::max(256, std::min(8192, 16 * k + 64));
@@ -1288,7 +1291,57 @@ void admit_locked(sdg_server* S) {
   }
 }
 
+// Copies the packed result (ncol_total x k_eff, column-major) into each
+// request's own ncol x min(k, k_eff) matrix.
+void split_results(std::vector<Request*>& batch, int64_t ncol_total, int k_eff, const std::vector<int32_t>& idx,
+                   const std::vector<double>& val) {
+  int64_t col0 = 0;
+  for (Request* r : batch) {
+    const int ke = std::min(r->k, k_eff);
+    r->k_eff = ke;
+    r->flags = (r->k > ke) ? SDG_WARN_CLAMP_FWD : 0;
+    r->idx.resize((size_t)r->ncol * ke);
+    r->val.resize((size_t)r->ncol * ke);
+    for (int t = 0; t < ke; ++t)
+      for (int32_t j = 0; j < r->ncol; ++j) {
+        r->idx[(size_t)t * r->ncol + j] = idx[(size_t)t * ncol_total + col0 + j];
+        r->val[(size_t)t * r->ncol + j] = val[(size_t)t * ncol_total + col0 + j];
+      }
+    col0 += r->ncol;
+  }
+}
+
+void finish_batch(sdg_server* S, std::vector<Request*>& batch, int st);
+
+// A batch against a dense reference: the requests' query columns packed into
+// one d x ncol FP32 matrix, one fused tensor-core search at the largest k.
+void run_dense_batch(sdg_server* S, sdg_ctx* c, std::vector<Request*>& batch) {
+  const int32_t d = dense_rows(S->dref);
+  std::vector<float> q;
+  int64_t ncol = 0;
+  int kmax = 1;
+  for (Request* r : batch) {
+    q.insert(q.end(), r->q.begin(), r->q.end());
+    ncol += r->ncol;
+    kmax = std::max(kmax, r->k);
+  }
+  const int st = guarded([&] {
+    std::vector<int32_t> idx((size_t)ncol * kmax);
+    std::vector<double> val((size_t)ncol * kmax);
+    int k_eff = 0, flags = 0;
+    const int rc = dense_query(c, S->dref, q.data(), d, ncol, batch.front()->method, kmax, 0, idx.data(),
+                               val.data(), 0, &k_eff, &flags);
+    if (rc != SDG_OK) throw Fail{rc};
+    split_results(batch, ncol, k_eff, idx, val);
+  });
+  finish_batch(S, batch, st);
+}
+
 void run_batch(sdg_server* S, sdg_ctx* c, std::vector<Request*>& batch) {
+  if (S->dref) {
+    run_dense_batch(S, c, batch);
+    return;
+  }
   // pack the requests' columns into one dgCMatrix
   sdg_csc Q;
   std::vector<int32_t> p(1, 0), i;
@@ -1317,22 +1370,12 @@ void run_batch(sdg_server* S, sdg_ctx* c, std::vector<Request*>& batch) {
     CK(cudaMemcpyAsync(val.data(), hv.p, sizeof(double) * val.size(), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     // k_eff here is min(kmax, available); each request keeps min(k, available)
-    const int avail_k = k_eff;
-    int64_t col0 = 0;
-    for (Request* r : batch) {
-      const int ke = std::min(r->k, avail_k);
-      r->k_eff = ke;
-      r->flags = (r->k > ke) ? SDG_WARN_CLAMP_FWD : 0;
-      r->idx.resize((size_t)r->ncol * ke);
-      r->val.resize((size_t)r->ncol * ke);
-      for (int t = 0; t < ke; ++t)
-        for (int32_t j = 0; j < r->ncol; ++j) {
-          r->idx[(size_t)t * r->ncol + j] = idx[(size_t)t * Q.ncol + col0 + j];
-          r->val[(size_t)t * r->ncol + j] = val[(size_t)t * Q.ncol + col0 + j];
-        }
-      col0 += r->ncol;
-    }
+    split_results(batch, Q.ncol, k_eff, idx, val);
   });
+  finish_batch(S, batch, st);
+}
+
+void finish_batch(sdg_server* S, std::vector<Request*>& batch, int st) {
   const std::string err = st == SDG_OK ? std::string() : std::string(g_err.data(), g_err.size());
   const double t = now_s();
   std::lock_guard<std::mutex> lock(S->mu);
@@ -1474,10 +1517,63 @@ SDG_API int sdg_server_create(sdg_ctx* ctx, const sdg_matrix* ref, int workers, 
   });
 }
 
+SDG_API int sdg_server_create_dense(sdg_ctx* ctx, const sdg_dense* ref, int workers, int max_slots,
+                                    int64_t mem_budget, sdg_server** out) {
+  return guarded([&] {
+    if (!ctx || !ref || !out || workers < 1 || max_slots < 1 || mem_budget <= 0)
+      fail(SDG_E_ARG, "invalid server arguments");
+    CK(cudaSetDevice(ctx->device));
+    auto S = std::make_unique<sdg_server>();
+    S->dref = ref;
+    S->device = ctx->device;
+    S->budget = mem_budget;
+    S->max_slots = max_slots;
+    // a dense reference holds every form both methods read (sdg_dense_upload)
+    S->methods_ready = (1u << COSINE) | (1u << EUCLIDEAN);
+    for (int w = 0; w < workers; ++w) {
+      sdg_ctx* c = nullptr;
+      const int st = sdg_ctx_create(S->device, &c);
+      if (st != SDG_OK) fail(st, std::string(g_err.data(), g_err.size()));
+      S->ctxs.push_back(c);
+    }
+    S->t_first = now_s();
+    sdg_server* raw = S.get();
+    for (sdg_ctx* c : S->ctxs) S->workers.emplace_back(worker_main, raw, c);
+    *out = S.release();
+  });
+}
+
+SDG_API int sdg_server_submit_dense(sdg_server* S, const float* Q, int32_t d, int32_t nq, int method, int k,
+                                    int64_t* id) {
+  return guarded([&] {
+    if (!S || !id || !Q) fail(SDG_E_ARG, "NULL argument");
+    if (!S->dref) fail(SDG_E_ARG, "the server's reference is sparse: submit a dgCMatrix (sdg_server_submit)");
+    if (k < 1) fail(SDG_E_ARG, kMsgK);
+    check_method(method, 1);
+    if (!(S->methods_ready & (1u << method))) fail(SDG_E_UNSUPPORTED, "dense kNN supports cosine and euclidean");
+    if (nq < 1) fail(SDG_E_ARG, "'X' must have at least one column.");
+    if (d != dense_rows(S->dref)) fail(SDG_E_ROWS, "'X' and 'Y' must have the same number of rows.");
+    auto r = std::make_unique<Request>();
+    r->method = method; r->dist = 1; r->k = k; r->drop = 1;
+    r->nrow = d; r->ncol = nq;
+    r->q.assign(Q, Q + (size_t)d * (size_t)nq);
+    r->mem = request_mem(S, nq, 0, k);
+    r->t_submit = now_s();
+    std::lock_guard<std::mutex> lock(S->mu);
+    r->id = S->next_id++;
+    *id = r->id;
+    S->pending.push_back(r.get());
+    S->reqs.emplace(r->id, std::move(r));
+    admit_locked(S);
+    S->cv_work.notify_all();
+  });
+}
+
 SDG_API int sdg_server_submit(sdg_server* S, const sdg_csc* Q, int method, int dist, int k,
                               int drop_degenerate, int64_t* id) {
   return guarded([&] {
     if (!S || !id) fail(SDG_E_ARG, "NULL argument");
+    if (S->dref) fail(SDG_E_ARG, "the server's reference is dense: submit FP32 columns (sdg_server_submit_dense)");
     if (k < 1) fail(SDG_E_ARG, kMsgK);
     check_method(method, dist);
     if (!(S->methods_ready & (1u << method)))

@@ -82,8 +82,11 @@ struct DenseSelArgs {
   int64_t ldS;                   // multiple of 4 (float4 rows)
   int64_t n, q0, nq;
   int32_t d;
+  int self;                      // queries are columns of the reference: skip r == q
   const float* norm2;            // padded to ldS entries
   const uint8_t* empty;          // padded to ldS entries (padding = 1)
+  const float* qnorm2;           // query sums of squares
+  const uint8_t* qempty;         // degenerate queries
   int nseg;
   float* segtop;                 // [ql][seg][k], best first, -inf padded
   float* cut;                    // [ql]: T - margin
@@ -136,7 +139,7 @@ __device__ __forceinline__ void dense_keys4(const DenseSelArgs& A, int64_t q, fl
   for (int j = 0; j < 4; ++j) {
     const int64_t r = r0 + j;
     lo[j] = hi[j] = -INFINITY;
-    if (r < A.n && r != q && !ev[j]) {
+    if (r < A.n && !(A.self && r == q) && !ev[j]) {
       float key, err;
       dense_key(A.method, A.mode, A.d, sv[j], Nq, nv[j], key, err);
       lo[j] = key - err;
@@ -156,8 +159,8 @@ __global__ void k_dense_segtop(DenseSelArgs A) {
   const int K = A.k;
   float* lst = lists + warp * K;
   int n = 0;
-  if (!A.empty[q]) {
-    const float Nq = A.norm2[q];
+  if (!A.qempty[q]) {
+    const float Nq = A.qnorm2[q];
     const float* Srow = A.S + ql * A.ldS;
     const int64_t r_end = min(A.n, (int64_t)(seg + 1) * DSEG);
     float thr = -INFINITY;                       // lst[K - 1] once the list is full
@@ -207,8 +210,8 @@ __global__ void k_dense_keep(DenseSelArgs A) {
   const int seg = blockIdx.y;
   if (ql >= A.nq) return;
   const int64_t q = A.q0 + ql;
-  if (A.empty[q]) return;
-  const float Nq = A.norm2[q];
+  if (A.qempty[q]) return;
+  const float Nq = A.qnorm2[q];
   const float cut = A.cut[ql];
   const float* Srow = A.S + ql * A.ldS;
   int32_t* out = A.cand + ql * (int64_t)A.cap;
@@ -252,7 +255,8 @@ __global__ void k_dense_overflow(int64_t nq, int cap, int32_t* count, int32_t* o
 // Exact FP64 value of each kept pair, in the reference's arithmetic; in the
 // plain mode the FP32 value of the slab instead.
 __global__ void k_dense_values(int method, int mode, int32_t d, const double* x64, const double* u64,
-                               const float* S, int64_t ldS, const float* norm2, const int32_t* cand,
+                               const double* qx64, const double* qu64, const float* S, int64_t ldS,
+                               const float* norm2, const float* qnorm2, const int32_t* cand,
                                const int32_t* count, int cap, int64_t q0, int64_t nq, double* out) {
   const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= nq * cap) return;
@@ -262,13 +266,13 @@ __global__ void k_dense_values(int method, int mode, int32_t d, const double* x6
   if (mode == 1) {
     const float sv = S[ql * ldS + r];
     out[s] = (method == COSINE) ? (double)(1.f - fminf(1.f, fmaxf(-1.f, sv)))
-                                : (double)sqrtf(fmaxf(0.f, norm2[q] + norm2[r] - 2.f * sv));
+                                : (double)sqrtf(fmaxf(0.f, qnorm2[q] + norm2[r] - 2.f * sv));
     return;
   }
   if (method == COSINE) {
     // unit_dot / unit_cosine (src/sparseDist.cpp:287-331), reference column first
     const double* a = u64 + r * d;
-    const double* b = u64 + q * d;
+    const double* b = qu64 + q * d;
     double acc = 0.0;
     for (int32_t k = 0; k < d; ++k) acc = __dadd_rn(acc, __dmul_rn(a[k], b[k]));
     double c = acc;
@@ -279,7 +283,7 @@ __global__ void k_dense_values(int method, int mode, int32_t d, const double* x6
   } else {
     // fastEuclidean2's pair loop with every row stored (src/sparseDist.cpp:855-871)
     const double* a = x64 + r * d;
-    const double* b = x64 + q * d;
+    const double* b = qx64 + q * d;
     double num = 0.0;
     for (int32_t k = 0; k < d; ++k) {
       const double diff = __dsub_rn(a[k], b[k]);
@@ -291,19 +295,20 @@ __global__ void k_dense_values(int method, int mode, int32_t d, const double* x6
 
 // exact FP64 values of one query against every reference (overflow fallback)
 __global__ void k_dense_exact_row(int method, int32_t d, const double* x64, const double* u64,
-                                  const uint8_t* empty, int64_t n, int64_t q, double* out) {
+                                  const double* qx64, const double* qu64, const uint8_t* empty, int64_t n,
+                                  int64_t q, int self, double* out) {
   const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= n) return;
-  if (r == q || empty[r]) { out[r] = na_real(); return; }
+  if ((self && r == q) || empty[r]) { out[r] = na_real(); return; }
   double acc = 0.0;
   if (method == COSINE) {
-    for (int32_t k = 0; k < d; ++k) acc = __dadd_rn(acc, __dmul_rn(u64[r * d + k], u64[q * d + k]));
+    for (int32_t k = 0; k < d; ++k) acc = __dadd_rn(acc, __dmul_rn(u64[r * d + k], qu64[q * d + k]));
     double c = acc;
     if (!(c == c)) c = 0.0; else if (c > 1.0) c = 1.0; else if (c < -1.0) c = -1.0;
     out[r] = __dsub_rn(1.0, c);
   } else {
     for (int32_t k = 0; k < d; ++k) {
-      const double diff = __dsub_rn(x64[r * d + k], x64[q * d + k]);
+      const double diff = __dsub_rn(x64[r * d + k], qx64[q * d + k]);
       acc = __dadd_rn(acc, __dmul_rn(diff, diff));
     }
     out[r] = sqrt(acc);
@@ -323,90 +328,104 @@ int cuda_fail(cudaError_t e) {
 
 using namespace sdg;
 
-extern "C" {
+namespace {
 
-SDG_API int sdg_dense_upload(sdg_ctx* ctx, const float* X, int32_t d, int64_t n, sdg_dense** out) {
-  if (!ctx || !X || !out || d < 1 || n < 1) return fail_with(SDG_E_ARG, "invalid dense upload arguments");
+// Builds the resident form of d x n FP32 columns X (host or device memory):
+// FP64 values and unit columns (unit_csc on each dense column), their FP32
+// and BF16 copies (rows padded to a multiple of 64 with zeros), sums of
+// squares and degenerate flags.  `async` takes the buffers from the stream's
+// pool (a per-request query matrix) instead of cudaMalloc (a resident
+// reference); `blas` creates the cuBLAS handle of the slab and plain modes.
+int dense_build(sdg_ctx* ctx, const float* X, int32_t d, int64_t n, bool async, bool blas, sdg_dense** out) {
   cudaStream_t s = ctx_stream(ctx);
   DK(cudaSetDevice(ctx_device(ctx)));
   auto D = new sdg_dense();
   D->device = ctx_device(ctx);
   D->d = d;
   D->n = n;
+  D->async = async;
+  D->stream = s;
+  auto alloc = [&](auto** p, size_t bytes) {
+    return async ? cudaMallocAsync((void**)p, bytes, s) : cudaMalloc((void**)p, bytes);
+  };
   const size_t tot = (size_t)d * (size_t)n;
   int* err = nullptr;
-  DK(cudaMalloc(&D->x64, tot * 8)); DK(cudaMalloc(&D->u64, tot * 8));
-  DK(cudaMalloc(&D->x32, tot * 4)); DK(cudaMalloc(&D->u32, tot * 4));
-  DK(cudaMalloc(&D->xb, tot * 2)); DK(cudaMalloc(&D->ub, tot * 2));
   const int64_t npad = (n + 127) / 128 * 128;       // float4 / uchar4 reads past n stay in bounds
   D->npad = npad;
   D->dpad = (d + 63) / 64 * 64;
-  DK(cudaMalloc(&D->norm2, npad * 4)); DK(cudaMalloc(&D->scale, n * 8));
-  DK(cudaMalloc(&D->empty, npad)); DK(cudaMalloc(&D->pview, (n + 1) * 8));
-  DK(cudaMemsetAsync(D->norm2, 0, npad * 4, s));
-  DK(cudaMemsetAsync(D->empty, 1, npad, s));
-  DK(cudaMalloc(&err, sizeof(int)));
-  DK(cudaMemsetAsync(err, 0, sizeof(int), s));
-  DK(cudaMemcpyAsync(D->x32, X, tot * 4, cudaMemcpyDefault, s));
-  k_dense_prep<<<blocks_for(n + 1, 128), 128, 0, s>>>(d, n, D->x32, D->x64, D->norm2, D->empty,
-                                                      D->pview, err);
-  DevCsc M;
-  M.nrow = d; M.ncol = (int32_t)n; M.p = D->pview; M.i = nullptr; M.x = D->x64;
-  launch_unit_csc(M, D->u64, D->scale, err, s);
-  k_dense_cast<<<152 * 16, 256, 0, s>>>((int64_t)tot, D->u64, D->x32, D->u32, D->ub, D->xb);
+  cudaError_t e = cudaSuccess;
+  auto chk = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
+  chk(alloc(&D->x64, tot * 8)); chk(alloc(&D->u64, tot * 8));
+  chk(alloc(&D->x32, tot * 4)); chk(alloc(&D->u32, tot * 4));
+  chk(alloc(&D->xb, tot * 2)); chk(alloc(&D->ub, tot * 2));
+  chk(alloc(&D->norm2, npad * 4)); chk(alloc(&D->scale, n * 8));
+  chk(alloc(&D->empty, npad)); chk(alloc(&D->pview, (n + 1) * 8));
+  chk(alloc(&err, sizeof(int)));
+  if (D->dpad != d) {
+    const size_t ptot = (size_t)D->dpad * (size_t)n;
+    chk(alloc(&D->ubp, ptot * 2)); chk(alloc(&D->xbp, ptot * 2));
+  }
+  if (e != cudaSuccess) { sdg_dense_free(D); return cuda_fail(e); }
+  chk(cudaMemsetAsync(D->norm2, 0, npad * 4, s));
+  chk(cudaMemsetAsync(D->empty, 1, npad, s));
+  chk(cudaMemsetAsync(err, 0, sizeof(int), s));
+  chk(cudaMemcpyAsync(D->x32, X, tot * 4, cudaMemcpyDefault, s));
+  if (e == cudaSuccess) {
+    k_dense_prep<<<blocks_for(n + 1, 128), 128, 0, s>>>(d, n, D->x32, D->x64, D->norm2, D->empty,
+                                                        D->pview, err);
+    DevCsc M;
+    M.nrow = d; M.ncol = (int32_t)n; M.p = D->pview; M.i = nullptr; M.x = D->x64;
+    launch_unit_csc(M, D->u64, D->scale, err, s);
+    k_dense_cast<<<152 * 16, 256, 0, s>>>((int64_t)tot, D->u64, D->x32, D->u32, D->ub, D->xb);
+  }
   if (D->dpad == d) {
     D->ubp = D->ub;
     D->xbp = D->xb;
-  } else {                                          // rows d..dpad-1 of the padded copies are zero
-    const size_t ptot = (size_t)D->dpad * (size_t)n;
-    DK(cudaMalloc(&D->ubp, ptot * 2)); DK(cudaMalloc(&D->xbp, ptot * 2));
-    DK(cudaMemset2DAsync(D->ubp, (size_t)D->dpad * 2, 0, (size_t)D->dpad * 2, (size_t)n, s));
-    DK(cudaMemset2DAsync(D->xbp, (size_t)D->dpad * 2, 0, (size_t)D->dpad * 2, (size_t)n, s));
-    DK(cudaMemcpy2DAsync(D->ubp, (size_t)D->dpad * 2, D->ub, (size_t)d * 2, (size_t)d * 2, (size_t)n,
-                         cudaMemcpyDeviceToDevice, s));
-    DK(cudaMemcpy2DAsync(D->xbp, (size_t)D->dpad * 2, D->xb, (size_t)d * 2, (size_t)d * 2, (size_t)n,
-                         cudaMemcpyDeviceToDevice, s));
+  } else if (e == cudaSuccess) {                    // rows d..dpad-1 of the padded copies are zero
+    chk(cudaMemset2DAsync(D->ubp, (size_t)D->dpad * 2, 0, (size_t)D->dpad * 2, (size_t)n, s));
+    chk(cudaMemset2DAsync(D->xbp, (size_t)D->dpad * 2, 0, (size_t)D->dpad * 2, (size_t)n, s));
+    chk(cudaMemcpy2DAsync(D->ubp, (size_t)D->dpad * 2, D->ub, (size_t)d * 2, (size_t)d * 2, (size_t)n,
+                          cudaMemcpyDeviceToDevice, s));
+    chk(cudaMemcpy2DAsync(D->xbp, (size_t)D->dpad * 2, D->xb, (size_t)d * 2, (size_t)d * 2, (size_t)n,
+                          cudaMemcpyDeviceToDevice, s));
   }
+  chk(cudaGetLastError());
   int herr = 0;
   std::vector<uint8_t> he((size_t)n);
-  DK(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
-  DK(cudaMemcpyAsync(he.data(), D->empty, (size_t)n, cudaMemcpyDeviceToHost, s));
-  DK(cudaStreamSynchronize(s));
-  cudaFree(err);
+  chk(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  chk(cudaMemcpyAsync(he.data(), D->empty, (size_t)n, cudaMemcpyDeviceToHost, s));
+  if (async) chk(cudaFreeAsync(err, s));
+  chk(cudaStreamSynchronize(s));
+  if (!async) cudaFree(err);
+  if (e != cudaSuccess) { sdg_dense_free(D); return cuda_fail(e); }
   for (uint8_t v : he) D->n_empty += v;
   if (herr) { sdg_dense_free(D); return fail_with(SDG_E_NONFINITE, "Cosine requires finite input (found NA, NaN or Inf)."); }
-  DB(cublasCreate(&D->blas));
+  if (blas && cublasCreate(&D->blas) != CUBLAS_STATUS_SUCCESS) {
+    sdg_dense_free(D);
+    return fail_with(SDG_E_CUDA, "cublasCreate failed");
+  }
   *out = D;
   return SDG_OK;
 }
 
-SDG_API int sdg_dense_free(sdg_dense* D) {
-  if (!D) return SDG_OK;
-  cudaSetDevice(D->device);
-  cudaDeviceSynchronize();
-  if (D->ubp && D->ubp != D->ub) cudaFree(D->ubp);
-  if (D->xbp && D->xbp != D->xb) cudaFree(D->xbp);
-  for (void* p : {(void*)D->x64, (void*)D->u64, (void*)D->x32, (void*)D->u32, (void*)D->xb,
-                  (void*)D->ub, (void*)D->norm2, (void*)D->scale, (void*)D->empty, (void*)D->pview})
-    if (p) cudaFree(p);
-  if (D->blas) cublasDestroy(D->blas);
-  delete D;
-  return SDG_OK;
-}
-
-SDG_API int sdg_dense_knn_block(sdg_ctx* ctx, const sdg_dense* D, int64_t q0, int64_t nq,
-                                int method, int k, int mode, int32_t* idx, double* dist_out,
-                                int device_out, int* k_eff, int* flags) {
-  if (!ctx || !D || !idx || !dist_out || !k_eff || !flags) return fail_with(SDG_E_ARG, "NULL argument");
+// Rows q0 .. q0+nq-1 (query columns of Q) of sparseKNN(Q, R, k, method) with
+// drop_degenerate = TRUE: the self-search with include_self = FALSE when self
+// (Q is R), else the two-matrix search.  See sdg_dense_knn_block for modes.
+int dense_search(sdg_ctx* ctx, const sdg_dense* Q, int64_t q0, int64_t nq, const sdg_dense* D, bool self,
+                 int method, int k, int mode, int32_t* idx, double* dist_out, int device_out, int* k_eff,
+                 int* flags) {
+  if (!ctx || !Q || !D || !idx || !dist_out || !k_eff || !flags) return fail_with(SDG_E_ARG, "NULL argument");
   if (method != COSINE && method != EUCLIDEAN) return fail_with(SDG_E_UNSUPPORTED, "dense kNN supports cosine and euclidean");
   if (mode < 0 || mode > 2)
     return fail_with(SDG_E_ARG, "mode must be 0 (BF16 screen), 1 (plain FP32) or 2 (BF16 slab screen)");
   if (k < 1) return fail_with(SDG_E_ARG, "'k' must be a positive integer no larger than .Machine$integer.max.");
-  if (q0 < 0 || nq < 1 || q0 + nq > D->n) return fail_with(SDG_E_ARG, "invalid query column range");
+  if (q0 < 0 || nq < 1 || q0 + nq > Q->n) return fail_with(SDG_E_ARG, "invalid query column range");
+  if (Q->d != D->d) return fail_with(SDG_E_ROWS, "'X' and 'Y' must have the same number of rows.");
+  if (mode != 0 && !D->blas) return fail_with(SDG_E_ARG, "modes 1 and 2 need the reference's cuBLAS handle");
   DK(cudaSetDevice(D->device));
   cudaStream_t s = ctx_stream(ctx);
   *flags = 0;
-  const int64_t avail = D->n - D->n_empty - 1;        // self-search, include_self = FALSE
+  const int64_t avail = D->n - D->n_empty - (self ? 1 : 0);   // include_self = FALSE
   if (avail < 1) return fail_with(SDG_E_NOCAND, "No candidate neighbours available.");
   if (k > avail) { k = (int)avail; *flags |= SDG_WARN_CLAMP_FWD; }
   if (k > kMaxK) return fail_with(SDG_E_UNSUPPORTED, "k above 1024 is not supported by this build.");
@@ -438,7 +457,12 @@ SDG_API int sdg_dense_knn_block(sdg_ctx* ctx, const sdg_dense* D, int64_t q0, in
     DK(cudaMallocAsync(&o_idx, sizeof(int32_t) * (size_t)(nq * k), s));
     DK(cudaMallocAsync(&o_val, sizeof(double) * (size_t)(nq * k), s));
   }
-  DB(cublasSetStream(D->blas, s));
+  // the slab and plain modes share the reference's cuBLAS handle: one caller at a time
+  std::unique_lock<std::mutex> blas_lock(const_cast<sdg_dense*>(D)->blas_mu, std::defer_lock);
+  if (!fused) {
+    blas_lock.lock();
+    DB(cublasSetStream(D->blas, s));
+  }
   const float one = 1.f, zero = 0.f;
   std::vector<int64_t> overflow;
   ctx_stats_reset(ctx);
@@ -446,26 +470,32 @@ SDG_API int sdg_dense_knn_block(sdg_ctx* ctx, const sdg_dense* D, int64_t q0, in
   for (int64_t c0 = q0; c0 < q0 + nq; c0 += chunk) {
     const int64_t nb = std::min(chunk, q0 + nq - c0);
     if (fused) {
-      const int st = tc_screen(ctx, D, method, k, c0, nb, cand, count, over, cap, s);
+      const int st = tc_screen(ctx, Q, D, self, method, k, c0, nb, cand, count, over, cap, s);
       if (st != SDG_OK) return st;
+      ctx_stats_add(ctx, 6, 2 * (int64_t)D->dpad * n * nb);
     } else {
     // S (n x nb, column-major, leading dimension ldS) = R^T Q:
     // S[ql * ldS + r] = <col r, col c0 + ql>
     sdg_time_begin(ctx);
     if (smode == 0) {
       const __nv_bfloat16* M = (method == COSINE) ? D->ub : D->xb;
+      const __nv_bfloat16* QM = (method == COSINE) ? Q->ub : Q->xb;
       DB(cublasGemmEx(D->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)n, (int)nb, D->d, &one, M,
-                      CUDA_R_16BF, D->d, M + (size_t)c0 * D->d, CUDA_R_16BF, D->d, &zero, S,
+                      CUDA_R_16BF, D->d, QM + (size_t)c0 * D->d, CUDA_R_16BF, D->d, &zero, S,
                       CUDA_R_32F, (int)ldS, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT));
     } else {
       const float* M = (method == COSINE) ? D->u32 : D->x32;
+      const float* QM = (method == COSINE) ? Q->u32 : Q->x32;
       DB(cublasSgemm(D->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)n, (int)nb, D->d, &one, M, D->d,
-                     M + (size_t)c0 * D->d, D->d, &zero, S, (int)ldS));
+                     QM + (size_t)c0 * D->d, D->d, &zero, S, (int)ldS));
     }
     sdg_time_end(ctx);
+    ctx_stats_add(ctx, 6, 2 * (int64_t)D->d * n * nb);
     DenseSelArgs A;
     A.method = method; A.k = k; A.mode = smode; A.S = S; A.ldS = ldS; A.n = n; A.q0 = c0; A.nq = nb;
-    A.d = D->d; A.norm2 = D->norm2; A.empty = D->empty; A.nseg = nseg; A.segtop = segtop; A.cut = cut;
+    A.d = D->d; A.self = self ? 1 : 0; A.norm2 = D->norm2; A.empty = D->empty;
+    A.qnorm2 = Q->norm2; A.qempty = Q->empty;
+    A.nseg = nseg; A.segtop = segtop; A.cut = cut;
     A.cap = cap; A.cand = cand; A.count = count; A.overflow = over;
     const size_t smem = sizeof(float) * (size_t)DSEL_WARPS * k;     // <= 32 KB (k <= 1024)
     const dim3 grid(blocks_for(nb, DSEL_WARPS), (unsigned)nseg);
@@ -474,12 +504,13 @@ SDG_API int sdg_dense_knn_block(sdg_ctx* ctx, const sdg_dense* D, int64_t q0, in
     k_dense_keep<<<grid, DSEL_WARPS * 32, 0, s>>>(A);
     k_dense_overflow<<<blocks_for(nb, 256), 256, 0, s>>>(nb, cap, count, over);
     }
-    k_dense_values<<<blocks_for(nb * cap, 128), 128, 0, s>>>(method, smode, D->d, D->x64, D->u64, S, ldS,
-                                                              D->norm2, cand, count, cap, c0, nb, vals);
+    k_dense_values<<<blocks_for(nb * cap, 128), 128, 0, s>>>(method, smode, D->d, D->x64, D->u64, Q->x64, Q->u64,
+                                                              S, ldS, D->norm2, Q->norm2, cand, count, cap, c0,
+                                                              nb, vals);
     SelectArgs sa;
     sa.vals = vals; sa.seg_stride = cap; sa.elem_stride = 1; sa.nseg = nb;
     sa.cand = cand; sa.cand_count = count; sa.cand_ld = cap;
-    sa.seg_blank = D->empty + q0;          // rows are relative to q0
+    sa.seg_blank = Q->empty + q0;          // rows are relative to q0
     sa.out_idx = o_idx; sa.out_val = o_val; sa.out_ld = nq; sa.out_row0 = c0 - q0;
     sa.k = k; sa.decreasing = 0;
     launch_select(sa, s);
@@ -496,11 +527,11 @@ SDG_API int sdg_dense_knn_block(sdg_ctx* ctx, const sdg_dense* D, int64_t q0, in
   if (!overflow.empty()) {
     DK(cudaMallocAsync(&row, sizeof(double) * (size_t)n, s));
     for (int64_t q : overflow) {
-      k_dense_exact_row<<<blocks_for(n, 256), 256, 0, s>>>(method, D->d, D->x64, D->u64, D->empty,
-                                                            n, q, row);
+      k_dense_exact_row<<<blocks_for(n, 256), 256, 0, s>>>(method, D->d, D->x64, D->u64, Q->x64, Q->u64,
+                                                            D->empty, n, q, self ? 1 : 0, row);
       SelectArgs sa;
       sa.vals = row; sa.seg_stride = 0; sa.elem_stride = 1; sa.len = n; sa.nseg = 1;
-      sa.seg_blank = D->empty + q0;
+      sa.seg_blank = Q->empty + q0;
       sa.out_idx = o_idx; sa.out_val = o_val; sa.out_ld = nq; sa.out_row0 = q - q0;
       sa.k = k; sa.decreasing = 0;
       launch_select(sa, s);
@@ -520,7 +551,75 @@ SDG_API int sdg_dense_knn_block(sdg_ctx* ctx, const sdg_dense* D, int64_t q0, in
   if (!device_out) { DK(cudaFreeAsync(o_idx, s)); DK(cudaFreeAsync(o_val, s)); }
   DK(cudaStreamSynchronize(s));
   ctx_add_overflow(ctx, (int64_t)overflow.size());
+  ctx_stats_add(ctx, 3, fused ? 4 : 7);
   return SDG_OK;
+}
+
+}  // namespace
+
+namespace sdg {
+int32_t dense_rows(const sdg_dense* D) { return D->d; }
+int64_t dense_cols(const sdg_dense* D) { return D->n; }
+int64_t dense_query_bytes(const sdg_dense* D, int64_t nq, int k) {
+  const int64_t cap = std::max(512, std::min(16384, 64 * k + 256));
+  // the query's forms (FP64 x2, FP32 x2, BF16 x2 + padded), candidates and
+  // exact values, results, and the fused screen's per-(query, range) lists
+  // (at most 152 ranges for a single query tile, ~9 for full tiles)
+  const int64_t ranges = std::max<int64_t>(9, 152 / std::max<int64_t>(1, (nq + 255) / 256));
+  return nq * (36 * (int64_t)D->dpad + cap * 12 + (int64_t)k * 12 + ranges * (768 * 8 + (int64_t)k * 4 + 4)) +
+         ((int64_t)1 << 20);
+}
+int dense_query(sdg_ctx* ctx, const sdg_dense* D, const float* Q, int32_t d, int64_t nq, int method, int k,
+                int mode, int32_t* idx, double* dist_out, int device_out, int* k_eff, int* flags) {
+  if (!ctx || !D || !Q) return fail_with(SDG_E_ARG, "NULL argument");
+  if (d != D->d) return fail_with(SDG_E_ROWS, "'X' and 'Y' must have the same number of rows.");
+  if (nq < 1) return fail_with(SDG_E_ARG, "'X' must have at least one column.");
+  sdg_dense* QD = nullptr;
+  int st = dense_build(ctx, Q, d, nq, true, false, &QD);
+  if (st != SDG_OK) return st;
+  st = dense_search(ctx, QD, 0, nq, D, false, method, k, mode, idx, dist_out, device_out, k_eff, flags);
+  sdg_dense_free(QD);
+  return st;
+}
+}  // namespace sdg
+
+extern "C" {
+
+SDG_API int sdg_dense_upload(sdg_ctx* ctx, const float* X, int32_t d, int64_t n, sdg_dense** out) {
+  if (!ctx || !X || !out || d < 1 || n < 1) return fail_with(SDG_E_ARG, "invalid dense upload arguments");
+  return dense_build(ctx, X, d, n, false, true, out);
+}
+
+SDG_API int sdg_dense_free(sdg_dense* D) {
+  if (!D) return SDG_OK;
+  cudaSetDevice(D->device);
+  void* bufs[] = {(void*)D->x64, (void*)D->u64, (void*)D->x32, (void*)D->u32, (void*)D->xb, (void*)D->ub,
+                  (void*)D->norm2, (void*)D->scale, (void*)D->empty, (void*)D->pview,
+                  (void*)(D->ubp != D->ub ? D->ubp : nullptr), (void*)(D->xbp != D->xb ? D->xbp : nullptr)};
+  if (D->async) {
+    // a per-request matrix: stream-ordered frees after the work queued on its stream
+    for (void* p : bufs)
+      if (p) cudaFreeAsync(p, D->stream);
+  } else {
+    cudaDeviceSynchronize();
+    for (void* p : bufs)
+      if (p) cudaFree(p);
+  }
+  if (D->blas) cublasDestroy(D->blas);
+  delete D;
+  return SDG_OK;
+}
+
+SDG_API int sdg_dense_knn_block(sdg_ctx* ctx, const sdg_dense* D, int64_t q0, int64_t nq,
+                                int method, int k, int mode, int32_t* idx, double* dist_out,
+                                int device_out, int* k_eff, int* flags) {
+  return dense_search(ctx, D, q0, nq, D, true, method, k, mode, idx, dist_out, device_out, k_eff, flags);
+}
+
+SDG_API int sdg_dense_knn_query(sdg_ctx* ctx, const sdg_dense* D, const float* Q, int32_t d, int64_t nq,
+                                int method, int k, int mode, int32_t* idx, double* dist_out,
+                                int device_out, int* k_eff, int* flags) {
+  return dense_query(ctx, D, Q, d, nq, method, k, mode, idx, dist_out, device_out, k_eff, flags);
 }
 
 }  // extern "C"

@@ -4,6 +4,7 @@
 #pragma once
 
 #include <cstdint>
+#include <mutex>
 #include <cublas_v2.h>
 #include <cuda_bf16.h>
 
@@ -28,7 +29,10 @@ struct sdg_dense {
   uint8_t* empty = nullptr;       // padded to npad with 1
   int64_t* pview = nullptr;       // column offsets j * d, for the CSC kernels
   int64_t n_empty = 0;
-  cublasHandle_t blas = nullptr;
+  cublasHandle_t blas = nullptr;  // slab (mode 2) and plain (mode 1) GEMMs; resident references only
+  std::mutex blas_mu;             // one caller at a time on `blas` (it is bound to a stream)
+  bool async = false;             // buffers from the stream-ordered pool of `stream`
+  cudaStream_t stream = nullptr;
 };
 
 namespace sdg {
@@ -57,12 +61,14 @@ __device__ __forceinline__ float dense_cut(float T) {
 }
 
 // Fused tensor-core screen (sdg_dense_tc.cu).  Supported for cosine and
-// euclidean with k <= 32 and dpad <= 256.  Fills, for the nq queries q0.., the
+// euclidean with k <= 64 and dpad <= 256.  Fills, for the nq queries q0.., the
 // candidate lists cand[ql * cap + t] (t < count[ql]) with every reference
 // whose optimistic key reaches the query's cut, or sets over[ql] (count 0)
 // when a list does not fit; degenerate queries get count 0.
+// Queries are columns q0.. of Q, references the columns of D (self: Q is D
+// and each query's own column is skipped).
 bool tc_screen_supported(const sdg_dense* D, int method, int k);
-int tc_screen(sdg_ctx* ctx, const sdg_dense* D, int method, int k, int64_t q0, int64_t nq,
-              int32_t* cand, int32_t* count, int32_t* over, int cap, cudaStream_t s);
+int tc_screen(sdg_ctx* ctx, const sdg_dense* Q, const sdg_dense* D, bool self, int method, int k, int64_t q0,
+              int64_t nq, int32_t* cand, int32_t* count, int32_t* over, int cap, cudaStream_t s);
 
 }  // namespace sdg

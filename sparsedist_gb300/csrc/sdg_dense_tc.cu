@@ -48,7 +48,7 @@ constexpr int BN = 128;                 // references per tile (UMMA N)
 constexpr int BK = 64;                  // rows of a K chunk: 64 BF16 = one 128-byte swizzle row
 constexpr int QT = 2;                   // query tiles per CTA
 constexpr int STAGES = 4;               // reference chunk ring
-constexpr int KT = 32;                  // largest k of the fused screen
+constexpr int KT = 64;                  // largest k of the fused screen
 constexpr int THREADS = 320;
 constexpr uint32_t TILE_BYTES = BN * BK * 2;   // 16 KB (a 128 x 64 BF16 tile)
 constexpr uint32_t TMEM_COLS = 512;
@@ -59,12 +59,15 @@ constexpr uint64_t WAIT_NS = 1000000000ull;    // 1 s per wait
 
 struct TcArgs {
   int method, k, dch, nqg, nrr, tiles_per_range, ecap;
+  int self;                   // queries are columns of the reference (skip r == q)
   int32_t d;
   int64_t n, q0, nq, ntiles;
   float a;                    // x = a * s - w[r] (1 cosine, 2 euclidean)
   float one_minus_c;          // euclidean hot-test coefficient
   const float* w;             // [npad]: +inf for degenerate / padding references
-  const float* norm2;         // [npad]
+  const float* norm2;         // [npad] reference sums of squares
+  const float* qnorm2;        // query sums of squares
+  const uint8_t* qempty;      // degenerate queries (no list)
   float* lists;               // [nq][nrr][k]
   int32_t* ecount;            // [nq][nrr]
   int32_t* eidx;              // [nq][nrr][ecap]
@@ -184,7 +187,8 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
 
 // ---- the fused screen ------------------------------------------------------
 template <int KL>
-__global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__ CUtensorMap tmap, TcArgs P) {
+__global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__ CUtensorMap qmap,
+                                                       const __grid_constant__ CUtensorMap rmap, TcArgs P) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint8_t* sA = base;                                    // QT * dch tiles
@@ -229,11 +233,12 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
   if (warp == 0) {
     // ---- TMA producer ----
     if (lane == 0 && ntile > 0) {
-      asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmap) : "memory");
+      asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&qmap) : "memory");
+      asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&rmap) : "memory");
       mbar_expect_tx(a_full, (uint32_t)(QT * dch) * TILE_BYTES);
       for (int qt = 0; qt < QT; ++qt)
         for (int c = 0; c < dch; ++c)
-          tma_load_2d(sA + (size_t)(qt * MAX_DCH + c) * TILE_BYTES, &tmap, a_full, c * BK,
+          tma_load_2d(sA + (size_t)(qt * MAX_DCH + c) * TILE_BYTES, &qmap, a_full, c * BK,
                       (int)(qbase + qt * BM));
       int it = 0;
       bool ok = true;
@@ -243,7 +248,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
           const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
           if (!mbar_wait(emptyb + s, ph ^ 1u, abort_flag, P.status)) { ok = false; break; }
           mbar_expect_tx(full + s, TILE_BYTES);
-          tma_load_2d(sB + (size_t)s * TILE_BYTES, &tmap, full + s, c * BK, (int)((t0 + j) * BN));
+          tma_load_2d(sB + (size_t)s * TILE_BYTES, &rmap, full + s, c * BK, (int)((t0 + j) * BN));
         }
       }
       // every issued copy lands before the CTA can exit
@@ -303,8 +308,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
     bool active = q < P.q0 + P.nq;
     float Nq = 0.f;
     if (active) {
-      active = P.w[q] != INFINITY;          // a degenerate query has no list
-      Nq = P.norm2[q];
+      active = !P.qempty[q];                 // a degenerate query has no list
+      Nq = P.qnorm2[q];
     }
     const int32_t d = P.d;
     const float rel = 0.0040f + (float)d * 2.384185791015625e-7f;
@@ -361,7 +366,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
           const int jj = __ffs(mask) - 1;
           mask &= mask - 1;
           const int64_t r = r0 + jj;
-          if (r == q) continue;
+          if (P.self && r == q) continue;
           float s = 0.f;
 #pragma unroll
           for (int t = 0; t < 32; ++t) s = (t == jj) ? __uint_as_float(v[t]) : s;
@@ -421,7 +426,7 @@ __device__ __forceinline__ void warp_insert_desc_tc(float* lst, int K, int& n, u
     int a = 0, b = n;
     while (a < b) { const int mid = (a + b) >> 1; if (lst[mid] >= x) a = mid + 1; else b = mid; }
     const int last = (n < K) ? n : K - 1;
-    if (lane == 0) {                               // K <= 32: a serial shift is short
+    if (lane == 0) {                               // K <= 64: a serial shift is short
       for (int e = last; e > a; --e) lst[e] = lst[e - 1];
       lst[a] = x;
     }
@@ -503,27 +508,32 @@ int fail(int code, const char* msg) { set_error(msg); return code; }
 
 }  // namespace
 
-bool tc_screen_supported(const sdg_dense* D, int method, int k) {
-  return (method == COSINE || method == EUCLIDEAN) && k >= 1 && k <= KT && D->dpad <= MAX_DCH * BK &&
-         D->n < (int64_t)1 << 30 && encode_fn() != nullptr;
+bool tc_screen_supported(const sdg_dense* R, int method, int k) {
+  return (method == COSINE || method == EUCLIDEAN) && k >= 1 && k <= KT && R->dpad <= MAX_DCH * BK &&
+         R->n < (int64_t)1 << 30 && encode_fn() != nullptr;
 }
 
-int tc_screen(sdg_ctx* ctx, const sdg_dense* D, int method, int k, int64_t q0, int64_t nq, int32_t* cand,
-              int32_t* count, int32_t* over, int cap, cudaStream_t s) {
+int tc_screen(sdg_ctx* ctx, const sdg_dense* Q, const sdg_dense* D, bool self, int method, int k, int64_t q0,
+              int64_t nq, int32_t* cand, int32_t* count, int32_t* over, int cap, cudaStream_t s) {
   EncodeTiledFn enc = encode_fn();
   if (!enc) return fail(SDG_E_CUDA, "cuTensorMapEncodeTiled is unavailable");
+  if (Q->dpad != D->dpad || Q->n >= (int64_t)1 << 30) return fail(SDG_E_ARG, "query and reference shapes differ");
   const int64_t n = D->n;
   const int dch = D->dpad / BK;
-  const __nv_bfloat16* M = (method == COSINE) ? D->ubp : D->xbp;
-  CUtensorMap tmap;
-  const cuuint64_t gdim[2] = {(cuuint64_t)D->dpad, (cuuint64_t)n};
-  const cuuint64_t gstride[1] = {(cuuint64_t)D->dpad * 2};
-  const cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)BN};
-  const cuuint32_t estr[2] = {1, 1};
-  if (enc(&tmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)M, gdim, gstride, box, estr,
-          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-    return fail(SDG_E_CUDA, "cuTensorMapEncodeTiled failed");
+  // one map per operand: 64-row x 128-column boxes of the K-major BF16 copy
+  // (rows padded to dpad with zeros; columns beyond the matrix read as zero)
+  auto encode = [&](const sdg_dense* M, CUtensorMap* map) {
+    const __nv_bfloat16* base = (method == COSINE) ? M->ubp : M->xbp;
+    const cuuint64_t gdim[2] = {(cuuint64_t)M->dpad, (cuuint64_t)M->n};
+    const cuuint64_t gstride[1] = {(cuuint64_t)M->dpad * 2};
+    const cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)BN};
+    const cuuint32_t estr[2] = {1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)base, gdim, gstride, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  };
+  CUtensorMap qmap, rmap;
+  if (!encode(Q, &qmap) || !encode(D, &rmap)) return fail(SDG_E_CUDA, "cuTensorMapEncodeTiled failed");
 
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, D->device);
@@ -555,18 +565,21 @@ int tc_screen(sdg_ctx* ctx, const sdg_dense* D, int method, int k, int64_t q0, i
     k_tc_weights<<<(unsigned)((D->npad + 255) / 256), 256, 0, s>>>(method, n, D->npad, omc, D->norm2, D->empty, w);
     TcArgs P;
     P.method = method; P.k = k; P.dch = dch; P.nqg = nqg; P.nrr = nrr; P.tiles_per_range = tpr; P.ecap = ecap;
+    P.self = self ? 1 : 0;
     P.d = D->d; P.n = n; P.q0 = q0; P.nq = nq; P.ntiles = ntiles;
     P.a = (method == COSINE) ? 1.f : 2.f; P.one_minus_c = omc;
-    P.w = w; P.norm2 = D->norm2; P.lists = lists; P.ecount = ecount; P.eidx = eidx; P.ehi = ehi;
+    P.w = w; P.norm2 = D->norm2; P.qnorm2 = Q->norm2; P.qempty = Q->empty;
+    P.lists = lists; P.ecount = ecount; P.eidx = eidx; P.ehi = ehi;
     P.status = status;
-    // the list length: the smallest of 16 / 24 / 32 that holds k
-    auto kern = (k <= 16) ? k_dense_tc<16> : (k <= 24) ? k_dense_tc<24> : k_dense_tc<32>;
+    // the list length: the smallest of 16 / 24 / 32 / 48 / 64 that holds k
+    auto kern = (k <= 16) ? k_dense_tc<16> : (k <= 24) ? k_dense_tc<24> : (k <= 32) ? k_dense_tc<32>
+              : (k <= 48) ? k_dense_tc<48> : k_dense_tc<64>;
     chk(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
     sdg_time_begin(ctx);
-    if (e == cudaSuccess) kern<<<(unsigned)(nqg * nrr), THREADS, SMEM_BYTES, s>>>(tmap, P);
+    if (e == cudaSuccess) kern<<<(unsigned)(nqg * nrr), THREADS, SMEM_BYTES, s>>>(qmap, rmap, P);
     sdg_time_end(ctx);
     chk(cudaGetLastError());
-    k_tc_merge<<<(unsigned)((nq + MW - 1) / MW), MW * 32, 0, s>>>(q0, nq, nrr, k, ecap, D->empty, lists, ecount,
+    k_tc_merge<<<(unsigned)((nq + MW - 1) / MW), MW * 32, 0, s>>>(q0, nq, nrr, k, ecap, Q->empty, lists, ecount,
                                                                   eidx, ehi, cap, cand, count, over);
     chk(cudaGetLastError());
   }

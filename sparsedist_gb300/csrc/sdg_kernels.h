@@ -8,6 +8,7 @@
 #include "sdg_common.cuh"
 
 struct sdg_ctx;
+struct sdg_dense;
 // Bracket one launch of the bounding kernel (sdg_kernel_time).
 void sdg_time_begin(sdg_ctx* c);
 void sdg_time_end(sdg_ctx* c);
@@ -135,5 +136,15 @@ int snn_shared_build(const int32_t* d_sets, const int32_t* d_sizes, int32_t n, i
 int snn_graph_build(const int32_t* d_idx, const double* d_w, int32_t n, int32_t k,
                     double prune, int symmetrise, int64_t* nnz_host, int32_t** d_p,
                     int32_t** d_i, double** d_x, cudaStream_t s);
+
+// ---- sdg_dense.cu: resident dense embeddings (host-side view) ---------------------
+// sparseKNN(Q, D, k, method) of nq new query columns Q (d x nq FP32, host or
+// device) against the resident D; the body of sdg_dense_knn_query.
+int dense_query(sdg_ctx* ctx, const sdg_dense* D, const float* Q, int32_t d, int64_t nq, int method, int k,
+                int mode, int32_t* idx, double* dist_out, int device_out, int* k_eff, int* flags);
+int32_t dense_rows(const sdg_dense* D);
+int64_t dense_cols(const sdg_dense* D);
+// device memory one dense_query of nq columns at k takes from the pool
+int64_t dense_query_bytes(const sdg_dense* D, int64_t nq, int k);
 
 }  // namespace sdg

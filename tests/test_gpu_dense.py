@@ -79,3 +79,131 @@ def test_bf16_screen_many_segments_and_zero_columns(method, code, mode, k):
         assert same_bits(got[1][t], wd[t][keep][:k]), t
         assert 40001 not in got[0][t]
     torch.cuda.synchronize()
+
+
+def dense_query(ctx, D, Q, method, k, mode):
+    """sdg_dense_knn_query: Q is a C-contiguous float32 (nq, d) array."""
+    from sparsedist_gb300 import _lib
+    nq, d = Q.shape
+    idx = np.empty(nq * k, np.int32)
+    dst = np.empty(nq * k, np.float64)
+    ke, fl = np.zeros(1, np.int32), np.zeros(1, np.int32)
+    _lib.check(ctx.lib.sdg_dense_knn_query(ctx.handle, D, Q.ctypes.data, d, nq, method, k, mode,
+                                           idx.ctypes.data, dst.ctypes.data, 0, ke.ctypes.data,
+                                           fl.ctypes.data))
+    e = int(ke[0])
+    return idx[:nq * e].reshape(e, nq).T.copy(), dst[:nq * e].reshape(e, nq).T.copy()
+
+
+def as_csc(X):
+    """(n, d) embeddings -> the d x n dgCMatrix the reference would receive
+    (every value stored, exact zeros dropped as Matrix does)."""
+    A = np.ascontiguousarray(X.double().cpu().numpy())
+    n, d = A.shape
+    M = sp.csc_matrix((A.ravel(), np.tile(np.arange(d, dtype=np.int32), n),
+                       np.arange(0, (n + 1) * d, d, dtype=np.int64)), shape=(d, n))
+    M.eliminate_zeros()
+    return M
+
+
+@pytest.mark.parametrize("mode", [0, 2])
+@pytest.mark.parametrize("method,code", [("cosine", 1), ("euclidean", 2)])
+def test_d256_block_equals_oracle(method, code, mode):
+    """The target configuration's kernel shape: d = 256 (four 64-row K chunks),
+    200,000 references from the embedding generator (Gaussian clusters and
+    1 % near duplicates at 1e-6), a 64-query block from the middle of the
+    matrix, k = 20; idx and distances bit for bit against the oracle's
+    two-matrix search with k + 1 neighbours minus each query's own column."""
+    import ctypes as C
+    import torch
+    from sparsedist_gb300 import _lib, synth
+    d, n, q0, nq, k = 256, 200000, 123456, 64, 20
+    X = synth.dense_embeddings(d=d, n=n, seed=5)
+    ctx = _lib.Context()
+    h = C.c_void_p()
+    _lib.check(ctx.lib.sdg_dense_upload(ctx.handle, X.data_ptr(), d, n, C.byref(h)))
+    got = dense_knn(ctx, h, q0, nq, code, k, mode)
+    ctx.lib.sdg_dense_free(h)
+    A = as_csc(X)
+    wi, wd, _ = OracleBackend().knn(A[:, q0:q0 + nq], A, k=k + 1, method=method)
+    for t in range(nq):
+        keep = wi[t] != q0 + t + 1
+        assert same_bits(got[0][t], wi[t][keep][:k]), t
+        assert same_bits(got[1][t], wd[t][keep][:k]), t
+    torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("k", [20, 50, 64])
+@pytest.mark.parametrize("mode", [0, 2])
+@pytest.mark.parametrize("method,code", [("cosine", 1), ("euclidean", 2)])
+def test_query_entry_equals_oracle(method, code, mode, k):
+    """sdg_dense_knn_query: new query embeddings (host memory, drawn from the
+    same generator with another seed, plus exact copies of two reference
+    columns and one all-zero query) against a resident 20,001-column
+    reference; the oracle's two-matrix sparseKNN(Q, X) bit for bit.  k = 50
+    and 64 use the fused kernel's 64-long lists."""
+    import ctypes as C
+    import torch
+    from sparsedist_gb300 import _lib, synth
+    d, n, nq = 96, 20001, 300
+    X = synth.dense_embeddings(d=d, n=n, centres=40, seed=8)
+    Q = synth.dense_embeddings(d=d, n=nq, centres=40, seed=9)
+    Q[7] = X[4242]
+    Q[8] = X[20000]
+    Q[9] = 0.0
+    ctx = _lib.Context()
+    h = C.c_void_p()
+    _lib.check(ctx.lib.sdg_dense_upload(ctx.handle, X.data_ptr(), d, n, C.byref(h)))
+    Qh = np.ascontiguousarray(Q.cpu().numpy())
+    got = dense_query(ctx, h, Qh, code, k, mode)
+    ctx.lib.sdg_dense_free(h)
+    want = OracleBackend().knn(as_csc(Q), as_csc(X), k=k, method=method)
+    assert same_bits(got[0], want[0]) and same_bits(got[1], want[1])
+    assert got[0][7][0] == 4243 and got[0][8][0] == 20001
+    assert np.all(got[0][9] == np.iinfo(np.int32).min)
+    torch.cuda.synchronize()
+
+
+def test_dense_server_each_result_alone_and_in_the_mix():
+    """The serving loop over a resident dense reference: 30 requests of 1 to
+    700 query columns, cosine and euclidean, k in {10, 20, 50}, submitted
+    from 6 threads under a budget that admits several at once; each result is
+    bit-identical to the same query alone through sdg_dense_knn_query, and a
+    sample of requests to the oracle."""
+    import concurrent.futures as cf
+    import ctypes as C
+    import torch
+    from sparsedist_gb300 import _lib, synth
+    d, n = 128, 30000
+    X = synth.dense_embeddings(d=d, n=n, centres=60, seed=12)
+    Qall = np.ascontiguousarray(synth.dense_embeddings(d=d, n=6000, centres=60, seed=13).cpu().numpy())
+    ctx = _lib.Context()
+    h = C.c_void_p()
+    _lib.check(ctx.lib.sdg_dense_upload(ctx.handle, X.data_ptr(), d, n, C.byref(h)))
+    rng = np.random.default_rng(3)
+    reqs, c0 = [], 0
+    for r in range(30):
+        m = int(np.exp(rng.uniform(0, np.log(700))))
+        reqs.append((Qall[c0:c0 + m], ["cosine", "euclidean"][r % 2], int(rng.choice([10, 20, 50]))))
+        c0 = (c0 + m) % 5000
+    codes = {"cosine": 1, "euclidean": 2}
+    want = [dense_query(ctx, h, Q, codes[m], k, 0) for Q, m, k in reqs]
+    srv = _lib.Server(ctx, h, workers=2, max_slots=16, mem_budget=8 << 30, dense=True)
+    with cf.ThreadPoolExecutor(6) as ex:
+        ids = list(ex.map(lambda t: srv.submit_dense(t[0], codes[t[1]], t[2]), reqs))
+    for rid, (Q, m, k), (wi, wd) in zip(ids, reqs, want):
+        assert srv.wait(rid, 600000)
+        gi, gd, _ = srv.result(rid)
+        assert same_bits(gi, wi) and same_bits(gd, wd), (m, k, Q.shape)
+    orc = OracleBackend()
+    for Q, m, k in reqs[:4]:
+        oi, od, _ = orc.knn(sp.csc_matrix(Q.astype(np.float64).T), as_csc(X), k=k, method=m)
+        gi, gd = dense_query(ctx, h, Q, codes[m], k, 0)
+        assert same_bits(gi, oi) and same_bits(gd, od)
+    st = srv.stats()
+    assert st["completed"] == len(reqs) and st["batches"] < len(reqs)
+    with pytest.raises(_lib.SdgError):
+        srv.submit_dense(Qall[:3], 0, 10)                 # binary: not a dense method
+    srv.close()
+    ctx.lib.sdg_dense_free(h)
+    torch.cuda.synchronize()
