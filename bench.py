@@ -824,12 +824,12 @@ def run_logcount(args):
     hbm_peak, bf16_peak, peak_kind = measured_peaks()
     st_last = ctx.stats()
     if st_last.get("tensor_flops", 0) > 0 and klaunch:
-        # the tensor-core screen: its GEMM is the bounding kernel
+        # the tensor-core screen: the fused tcgen05 kernel is the bounding kernel
         flops_launch = st_last["tensor_flops"] / launches_per_step
         roof = {"bound": "tensor", "achieved": flops_launch / (per_launch_ms / 1000.0) / 1e12,
                 "peak": bf16_peak, "unit": "TFLOP/s",
                 "peak_kind": peak_kind + " (bf16 burst; fp16 runs at the same tensor rate)",
-                "kernel": "cuBLAS FP16 GEMM of the tensor-core screen", "flops_per_launch": flops_launch}
+                "kernel": "k_sparse_tc (fused FP16 tcgen05 screen)", "flops_per_launch": flops_launch}
     else:
         roof = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "peak_kind": peak_kind, "kernel": "k_screen", "alg_bytes_per_launch": alg / launches_per_step}

@@ -34,6 +34,7 @@ UNITS = [
     ("sdg_noalloc.cu", []),
     ("sdg_dense.cu", []),
     ("sdg_dense_tc.cu", []),
+    ("sdg_sparse_tc.cu", []),
     ("sdg_api.cpp", []),
 ]
 

@@ -6,7 +6,6 @@
 // Reference behaviour restated here: R/sparseKNN.R:110-313 (sparseKNN),
 // R/sparseKNNCross.R:44-199 (sparseKNNCross), R/sparseSNN.R:120-250
 // (sparseSNN, edges = "knn") and the kernels' own checks in src/*.cpp.
-#include <cublas_v2.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -166,7 +165,6 @@ struct sdg_ctx {
   size_t tev_used = 0;
   double tev_folded_ms = 0.0;
   int64_t tev_launches = 0;
-  cublasHandle_t blas = nullptr;       // created on the first tensor-core screen
   // false: choose the tensor-core screen only where the reference's dense
   // copy already exists (serving workers share the reference and must not
   // build it concurrently)
@@ -432,13 +430,13 @@ int pick_engine(sdg_ctx* c, const KnnPlan& P, const sdg_matrix* ref, const sdg_m
   if (c->engine == 1) return 1;
   if (!screen_supported(P.method, P.k) || !screen_fits(nrow)) return 1;
   if (c->engine == 2) return 2;
-  if (c->engine == 3) return tensor_supported(P.method) ? 3 : 2;
+  if (c->engine == 3) return (tensor_supported(P.method) && stc_supported(P.k)) ? 3 : 2;
   // Small problems: the exact slab is already latency-bound.
   if (nr * nq <= (int64_t)1 << 22) return 1;
   // The tensor screen does 2 nrow nr nq dense flops where the FP32 screen
   // visits nq / 16 * nnz(ref) stored entries: it wins from ~0.5 % density
   // on, if the dense copies fit in half of the free device memory.
-  if (tensor_supported(P.method) && nrow > 0 && nr > 0 &&
+  if (tensor_supported(P.method) && stc_supported(P.k) && nrow > 0 && nr > 0 &&
       (c->tensor_lazy || (ref->tensor[P.method].method == P.method && ref->tensor[P.method].usable))) {
     const double density = (double)ref->nnz / ((double)nrow * (double)nr);
     size_t bytes = tensor_cache_bytes(nrow, nr);
@@ -511,12 +509,7 @@ void knn_device(sdg_ctx* c, sdg_matrix* X, sdg_matrix* Y, int method, int dist, 
     r.qry_empty = X->empty.as<uint8_t>();
     r.q_lo = q_lo; r.q_hi = q_hi; r.out_first = q_lo; r.out_ld = nq;
     if (eng == 3) {
-      if (!c->blas && cublasCreate(&c->blas) != CUBLAS_STATUS_SUCCESS) {
-        c->blas = nullptr;
-        fail(SDG_E_CUDA, "cublasCreate failed");
-      }
       r.tensor = true;
-      r.blas = c->blas;
     }
     ScreenHooks h;
     h.check_cancel = [c]() { check_cancel(c); };
@@ -614,7 +607,6 @@ SDG_API int sdg_ctx_destroy(sdg_ctx* c) {
   for (auto& e : c->ev) if (e) cudaEventDestroy(e);
   for (auto& pr : c->tev) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
   cudaStreamDestroy(c->own_stream);
-  if (c->blas) cublasDestroy(c->blas);
   delete c;
   return SDG_OK;
 }

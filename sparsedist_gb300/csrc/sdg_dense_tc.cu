@@ -39,6 +39,7 @@
 
 #include "../../include/sdgpu.h"
 #include "sdg_dense.h"
+#include "sdg_tc_ptx.cuh"
 
 namespace sdg {
 namespace {
@@ -55,7 +56,6 @@ constexpr uint32_t TMEM_COLS = 512;
 constexpr int MAX_DCH = 4;              // dpad <= 256
 // 1 KB alignment slack, A tiles, B ring, barriers
 constexpr size_t SMEM_BYTES = 1024 + (size_t)(QT * MAX_DCH + STAGES) * TILE_BYTES + 256;
-constexpr uint64_t WAIT_NS = 1000000000ull;    // 1 s per wait
 
 struct TcArgs {
   int method, k, dch, nqg, nrr, tiles_per_range, ecap;
@@ -75,114 +75,11 @@ struct TcArgs {
   int* status;
 };
 
-// ---- PTX wrappers ----------------------------------------------------------
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ uint64_t gtimer() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Bounded wait for the phase of the given parity; false when it ran out or the
-// CTA aborted (then *abort is set).
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
-                                          int* status) {
-  if (mbar_try_wait(bar, parity)) return true;
-  const uint64_t t0 = gtimer();
-  for (uint32_t spin = 1;; ++spin) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if ((spin & 255u) == 0) {
-      if (*abort_flag) return false;
-      if (gtimer() - t0 > WAIT_NS) {
-        *abort_flag = 1;
-        atomicExch(status, 1);
-        return false;
-      }
-    }
-  }
-}
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
-      ::"r"(smem_u32(dst)), "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
-      : "memory");
-}
-__device__ __forceinline__ void fence_before() {
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void fence_after() {
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-}
-// Shared-memory matrix descriptor of a K-major SWIZZLE_128B tile: rows of 128
-// bytes, 8-row (1024-byte) swizzle atoms stacked at SBO = 1024; LBO is unused
-// for swizzled K-major operands; version 1 (bits 46-47); layout 2 = 128B
-// swizzle (bits 61-63).  The tile base is 1024-byte aligned, so the base
-// offset (bits 49-51) is 0; a K step of 16 BF16 advances the start by 32 B.
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
-  uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
-  d |= (uint64_t)1 << 16;                  // LBO = 16 B (ignored)
-  d |= (uint64_t)(1024 >> 4) << 32;        // SBO
-  d |= (uint64_t)1 << 46;
-  d |= (uint64_t)2 << 61;
-  return d;
-}
-// Instruction descriptor, kind::f16: D F32 (bits 4-5 = 1), A and B BF16
-// (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits
-// 17-22, M >> 4 at bits 24-28.
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                           ((uint32_t)(BM >> 4) << 24);
+using namespace tc;
+constexpr uint32_t IDESC = idesc_f16(BM, BN, true);
 
 __device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accum) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-      ::"r"(d_tmem), "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accum)
-      : "memory");
-}
-__device__ __forceinline__ void umma_commit(uint64_t* bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-               ::"r"(smem_u32(bar))
-               : "memory");
-}
-// 32 consecutive accumulator columns of this thread's lane; the wait carries
-// the registers as operands so that no use is scheduled before it
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
-#define SDG_R8(o) "=r"(v[o]), "=r"(v[o + 1]), "=r"(v[o + 2]), "=r"(v[o + 3]), "=r"(v[o + 4]), "=r"(v[o + 5]), \
-                  "=r"(v[o + 6]), "=r"(v[o + 7])
-#define SDG_P8(o) "+r"(v[o]), "+r"(v[o + 1]), "+r"(v[o + 2]), "+r"(v[o + 3]), "+r"(v[o + 4]), "+r"(v[o + 5]), \
-                  "+r"(v[o + 6]), "+r"(v[o + 7])
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-      : SDG_R8(0), SDG_R8(8), SDG_R8(16), SDG_R8(24)
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" : SDG_P8(0), SDG_P8(8), SDG_P8(16), SDG_P8(24) :: "memory");
-#undef SDG_R8
-#undef SDG_P8
+  umma_f16(d_tmem, adesc, bdesc, IDESC, accum);
 }
 
 // ---- the fused screen ------------------------------------------------------

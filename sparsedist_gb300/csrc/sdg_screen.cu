@@ -25,7 +25,6 @@
 // handed out part-major by an atomic counter, so the 152 SMs stream the same
 // reference part at the same time and it is read from HBM about once.
 #include <cub/device/device_radix_sort.cuh>
-#include <cublas_v2.h>
 #include <cuda_fp16.h>
 
 #include <algorithm>
@@ -35,6 +34,7 @@
 
 #include "sdg_kernels.h"
 #include "sdg_screen.h"
+#include "sdg_tc_bounds.cuh"
 
 namespace sdg {
 namespace {
@@ -426,26 +426,20 @@ __global__ void k_exact_candidates_prep(const int32_t* count, int64_t nq, int ca
 // the tensor-core screen
 //
 // For cosine and euclidean the screen value of a pair is an inner product
-// over the rows, so a dense FP16 copy of the screen values of both matrices
-// (TensorCache) turns a block of screens into one GEMM on the tensor cores
-// (cuBLAS, FP16 in, FP32 accumulate and out; FP16 runs at BF16's tensor rate
-// and rounds 4x finer, 2^-11), written as the slab S[ql * ldS + c] in natural
-// column order.  The bound (tc_bounds) is built from each column's exact
-// rounding error ||v - h|| (FP64, v the exact values, h the FP16 copy), so
-// it covers every way the copy differs: values below FP16's smallest normal
-// are written as 0, never as FP16 subnormals, and a value above FP16's range
-// makes the copy unusable (TensorCache::usable: the FP32 screen runs).  The
-// FP16 products are exact in FP32; the FP32 accumulation of at most
-// n = min(nnz_q, nnz_c) nonzero products (zero products add no error) is
-// allowed (n + 64) 2^-21 of sum |h_q h_c|.  A pair whose key or bound is not
-// finite is kept unconditionally.  The selection is split
-// across TSEG-reference segments (segment top-k of the pessimistic keys,
-// per-query merge to the exact k-th, segmented keep), one warp per
-// (query, segment), so that the slab streams at full bandwidth.
+// over the rows (binary: of the 0 / 1 patterns, the matched-row count), so a
+// dense FP16 copy of the screen values of both matrices (TensorCache) turns a
+// block of screens into one GEMM on the tensor cores: the fused tcgen05
+// kernel of sdg_sparse_tc.cu (FP16 in, FP32 accumulate; FP16 runs at BF16's
+// tensor rate and rounds 4x finer, 2^-11) with the selection in its
+// epilogue.  The bound (tcb::tc_bounds, sdg_tc_bounds.cuh) is built from each
+// column's exact rounding error ||v - h|| (FP64, v the exact values, h the
+// FP16 copy), so it covers every way the copy differs: values below FP16's
+// smallest normal are written as 0, never as FP16 subnormals, and a value
+// above FP16's range makes the copy unusable (TensorCache::usable: the FP32
+// screen runs).  The FP16 products are exact in FP32; the FP32 accumulation
+// of at most n = min(nnz_q, nnz_c) nonzero products (zero products add no
+// error) is allowed (n + 64) 2^-21 of sum |h_q h_c|.
 // ---------------------------------------------------------------------------
-constexpr int TSEG = 32768;
-constexpr float ACC_ULP = 4.76837158203125e-7f;   // 2^-21
-
 constexpr float HALF_MAX = 65504.f;
 constexpr float HALF_MIN_NORMAL = 6.103515625e-05f;   // 2^-14
 
@@ -483,123 +477,8 @@ __global__ void k_tensor_fill(DevCsc M, const float* fval, const double* src, __
   }
 }
 
-struct TensorSelArgs {
-  int method, k;
-  const float* S;
-  int64_t ldS, nr;
-  const int32_t* rnnz; const float* rnorm;
-  const int32_t* qnnz; const float* qnorm;
-  const float* rerr; const float* rbn;       // TensorCache norms (reference)
-  const float* qerr; const float* qbn;       // and query
-  const uint8_t* ref_mask;
-  const uint8_t* qry_blank;
-  const uint8_t* qry_force_exact;
-  int64_t q_begin, nq;
-  int selfmode, include_self;
-  int nseg;
-  float* segtop;             // [ql][seg][k]
-  float* cut;                // [ql]
-  int cap;
-  int32_t* cand;
-  int32_t* count;
-  int32_t* overflow;
-};
-
-// The tensor-screen bounds of one eligible pair from its GEMM value s (a key
-// that is not finite, or a bound that is not, keeps the pair unconditionally).
-// With v the exact values and b their FP16 copies (per column eq, er = ||v - b||
-// and bq, br = ||b||), Cauchy-Schwarz gives
-//   |sum v_q v_r - sum b_q b_r| <= eq ||v_r|| + bq er,
-// ||v_r|| = 1 for unit columns and sqrt(Nr) otherwise; the FP32 accumulation
-// of at most n = min(nnz_q, nnz_r) nonzero products is allowed
-// (n + 64) 2^-21 sum |b_q b_r| <= (n + 64) 2^-21 bq br.
-// Binary: s estimates the matched-row count c (0 / 1 factors are exact in
-// FP16); with the accumulation allowance c lies in [c_lo, c_hi] and the
-// Jaccard key c / (nq + nc - c) increases with c.
-__device__ __forceinline__ void tc_bounds(int method, float s, int32_t nq_, float Nq, int32_t nc_, float Nc,
-                                            float eq, float bq, float er, float br, float& lo, float& hi) {
-  const float nmin = (float)min(nq_, nc_);
-  const float acc = (nmin + 64.f) * ACC_ULP;
-  float key, err;
-  if (method == BINARY) {
-    const float e = acc * 1.01f * fabsf(s) + 1e-6f;
-    const float clo = fmaxf(0.f, s - e), chi = fminf(nmin, s + e);
-    const float N = (float)nq_ + (float)nc_;
-    lo = (N - clo > 0.f) ? clo / (N - clo) : 1.f;
-    hi = (N - chi > 0.f) ? chi / (N - chi) : 1.f;
-    lo = lo * (1.f - 4.f * U32);
-    hi = hi * (1.f + 4.f * U32) + 1e-30f;
-    if (!(fabsf(s) <= FLT_MAX)) { lo = -INFINITY; hi = INFINITY; }
-    return;
-  }
-  if (method == COSINE) {
-    key = s;
-    err = (1.000001f * eq + bq * er + acc * bq * br) * 1.01f + 1e-12f;
-  } else {
-    const float T = Nq + Nc;
-    key = 2.f * s - T;
-    err = 2.f * (sqrtf(Nc) * 1.000001f * eq + bq * er + acc * bq * br) * 1.01f + 9.5367431640625e-7f * T + 1e-30f;
-  }
-  if (!(fabsf(key) <= FLT_MAX) || !(err <= FLT_MAX)) { lo = -INFINITY; hi = INFINITY; return; }
-  lo = key - err;
-  hi = key + err;
-}
-
-// pessimistic / optimistic keys of pair (query q, reference c); -inf / -inf
-// when c is not eligible; +inf / +inf for the restored self pair.
-__device__ __forceinline__ void tensor_keys(const TensorSelArgs& A, int64_t q, int32_t nq_, float Nq, int64_t c,
-                                            float s, float& lo, float& hi) {
-  lo = hi = -INFINITY;
-  if (c >= A.nr || (A.ref_mask && A.ref_mask[c])) return;
-  if (A.selfmode && c == q) {
-    if (A.include_self) lo = hi = INFINITY;
-    return;
-  }
-  tc_bounds(A.method, s, nq_, Nq, A.rnnz[c], A.rnorm ? A.rnorm[c] : 0.f, A.qerr[q], A.qbn[q], A.rerr[c], A.rbn[c],
-              lo, hi);
-}
-
-// tensor_keys for references c0 .. c0 + 3 (c0 % 4 == 0), with 16-byte loads
-// of S, the reference sizes and norms and a 4-byte load of the mask when all
-// four are below nr
-__device__ __forceinline__ void tensor_keys4(const TensorSelArgs& A, int64_t q, int32_t nq_, float Nq,
-                                             const float* Srow, int64_t c0, float lo[4], float hi[4]) {
-  if (c0 + 3 < A.nr) {
-    const float4 s4 = *reinterpret_cast<const float4*>(Srow + c0);
-    const int4 n4 = *reinterpret_cast<const int4*>(A.rnnz + c0);
-    float4 r4 = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (A.rnorm) r4 = *reinterpret_cast<const float4*>(A.rnorm + c0);
-    uchar4 m4 = make_uchar4(0, 0, 0, 0);
-    if (A.ref_mask) m4 = *reinterpret_cast<const uchar4*>(A.ref_mask + c0);
-    const float4 e4 = *reinterpret_cast<const float4*>(A.rerr + c0);
-    const float4 b4 = *reinterpret_cast<const float4*>(A.rbn + c0);
-    const float ev[4] = {e4.x, e4.y, e4.z, e4.w};
-    const float bv[4] = {b4.x, b4.y, b4.z, b4.w};
-    const float eq = A.qerr[q], bq = A.qbn[q];
-    const float sv[4] = {s4.x, s4.y, s4.z, s4.w};
-    const int32_t nv[4] = {n4.x, n4.y, n4.z, n4.w};
-    const float rn[4] = {r4.x, r4.y, r4.z, r4.w};
-    const uint8_t mv[4] = {m4.x, m4.y, m4.z, m4.w};
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int64_t c = c0 + j;
-      lo[j] = hi[j] = -INFINITY;
-      if (mv[j]) continue;
-      if (A.selfmode && c == q) {
-        if (A.include_self) lo[j] = hi[j] = INFINITY;
-        continue;
-      }
-      tc_bounds(A.method, sv[j], nq_, Nq, nv[j], rn[j], eq, bq, ev[j], bv[j], lo[j], hi[j]);
-    }
-  } else {
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      lo[j] = hi[j] = -INFINITY;
-      if (c0 + j < A.nr) tensor_keys(A, q, nq_, Nq, c0 + j, Srow[c0 + j], lo[j], hi[j]);
-    }
-  }
-}
-
+// Warp-cooperative insertion of the lanes flagged in m (value v on each lane)
+// into lst[0..n), kept sorted descending and at most K long.
 __device__ __forceinline__ void warp_insert_desc(float* lst, int K, int& n, unsigned m, float v, int lane) {
   while (m) {
     const int src = __ffs(m) - 1;
@@ -624,114 +503,6 @@ __device__ __forceinline__ void warp_insert_desc(float* lst, int K, int& n, unsi
     __syncwarp();
     if (n < K) ++n;
   }
-}
-
-__device__ __forceinline__ bool tensor_skip(const TensorSelArgs& A, int64_t q) {
-  return (A.qry_blank && A.qry_blank[q]) || (A.qry_force_exact && A.qry_force_exact[q]);
-}
-
-__global__ void k_tsel_segtop(TensorSelArgs A) {
-  extern __shared__ float lists[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t ql = (int64_t)blockIdx.x * SELECT_WARPS + warp;
-  const int seg = blockIdx.y;
-  if (ql >= A.nq) return;
-  const int64_t q = A.q_begin + ql;
-  const int K = A.k;
-  float* lst = lists + warp * K;
-  int n = 0;
-  if (!tensor_skip(A, q)) {
-    const int32_t nq_ = A.qnnz[q];
-    const float Nq = A.qnorm ? A.qnorm[q] : 0.f;
-    const float* Srow = A.S + ql * A.ldS;
-    const int64_t c_end = min(A.nr, (int64_t)(seg + 1) * TSEG);
-    float thr = -INFINITY;                       // lst[K - 1] once the list is full
-    for (int64_t p0 = (int64_t)seg * TSEG; p0 < c_end; p0 += 128) {
-      float lo[4], hi[4];
-      tensor_keys4(A, q, nq_, Nq, Srow, p0 + 4 * lane, lo, hi);
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const unsigned m = __ballot_sync(0xffffffffu, lo[j] > -INFINITY && (n < K || lo[j] > thr));
-        if (m) {
-          warp_insert_desc(lst, K, n, m, lo[j], lane);
-          if (n == K) thr = lst[K - 1];
-        }
-      }
-    }
-  }
-  float* out = A.segtop + (ql * A.nseg + seg) * (int64_t)K;
-  for (int t = lane; t < K; t += 32) out[t] = t < n ? lst[t] : -INFINITY;
-}
-
-__global__ void k_tsel_thresh(TensorSelArgs A) {
-  extern __shared__ float lists[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t ql = (int64_t)blockIdx.x * SELECT_WARPS + warp;
-  if (ql >= A.nq) return;
-  const int64_t q = A.q_begin + ql;
-  const int K = A.k;
-  float* lst = lists + warp * K;
-  const float* in = A.segtop + ql * A.nseg * (int64_t)K;
-  const int64_t tot = (int64_t)A.nseg * K;
-  int n = 0;
-  for (int64_t p0 = 0; p0 < tot; p0 += 32) {
-    const float v = p0 + lane < tot ? in[p0 + lane] : -INFINITY;
-    const unsigned m = __ballot_sync(0xffffffffu, v > -INFINITY && (n < K || v > lst[K - 1]));
-    if (m) warp_insert_desc(lst, K, n, m, v, lane);
-  }
-  if (lane == 0) {
-    const float T = (n == K) ? lst[K - 1] : -INFINITY;
-    const float margin = (T == -INFINITY || T == INFINITY) ? 0.f : fabsf(T) * (8.f * U32) + 1e-30f;
-    A.cut[ql] = T - margin;
-    A.count[ql] = 0;
-    A.overflow[ql] = (A.qry_force_exact && A.qry_force_exact[q] && !(A.qry_blank && A.qry_blank[q])) ? 1 : 0;
-  }
-}
-
-__global__ void k_tsel_keep(TensorSelArgs A) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t ql = (int64_t)blockIdx.x * SELECT_WARPS + warp;
-  const int seg = blockIdx.y;
-  if (ql >= A.nq) return;
-  const int64_t q = A.q_begin + ql;
-  if (tensor_skip(A, q)) return;
-  const int32_t nq_ = A.qnnz[q];
-  const float Nq = A.qnorm ? A.qnorm[q] : 0.f;
-  const float cut = A.cut[ql];
-  const float* Srow = A.S + ql * A.ldS;
-  int32_t* out = A.cand + ql * (int64_t)A.cap;
-  const int64_t c_end = min(A.nr, (int64_t)(seg + 1) * TSEG);
-  for (int64_t p0 = (int64_t)seg * TSEG; p0 < c_end; p0 += 128) {
-    float lo[4], hi[4];
-    tensor_keys4(A, q, nq_, Nq, Srow, p0 + 4 * lane, lo, hi);
-    int mine = 0;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) mine += (hi[j] > -INFINITY && hi[j] >= cut);
-    int incl = mine;                              // warp inclusive scan of the lanes' counts
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int t = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += t;
-    }
-    const int total = __shfl_sync(0xffffffffu, incl, 31);
-    if (total == 0) continue;
-    int base = 0;
-    if (lane == 31) base = atomicAdd(A.count + ql, total);
-    base = __shfl_sync(0xffffffffu, base, 31) + incl - mine;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      if (hi[j] > -INFINITY && hi[j] >= cut) {
-        if (base < A.cap) out[base] = (int32_t)(p0 + 4 * lane + j);
-        ++base;
-      }
-    }
-  }
-}
-
-__global__ void k_tsel_overflow(int64_t nq, int cap, int32_t* count, int32_t* overflow) {
-  const int64_t ql = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (ql >= nq) return;
-  if (count[ql] > cap) { overflow[ql] = 1; count[ql] = 0; }
 }
 
 // ---------------------------------------------------------------------------
@@ -1003,7 +774,7 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
                TensorCache* qt, int32_t* d_idx, double* d_val, int64_t* stats, const ScreenHooks& hooks) {
   SK((cudaError_t)ensure_cache(rc, r.method, ref, ra, s));
   SK((cudaError_t)ensure_cache(qc, r.method, qry, qa, s));
-  bool use_t = r.tensor && r.blas && rt && qt && tensor_supported(r.method);
+  bool use_t = r.tensor && rt && qt && tensor_supported(r.method) && stc_supported(r.k);
   if (use_t) {
     SK((cudaError_t)ensure_tensor(rt, r.method, ref, ra, rc, s));
     if (qt != rt) SK((cudaError_t)ensure_tensor(qt, r.method, qry, qa, qc, s));
@@ -1023,19 +794,19 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
   const int64_t q_lo = r.q_lo, q_hi = (r.q_hi < 0) ? nq : r.q_hi;
   const int64_t out_ld = (r.out_ld < 0) ? nq : r.out_ld;
 
-  // queries per screen pass: the FP32 slab S is chunk x ldS floats
+  // queries per screen pass: the FP32 sparse screen's slab S is chunk x nr
+  // floats; the fused tensor screen writes no slab and takes 4,096 queries
+  // (16 query groups of 256, about one CTA per SM at ~10 reference ranges)
   const int64_t sbudget = (int64_t)4 << 30;
-  const int64_t ldS = use_t ? (nr + 31) / 32 * 32 : nr;
-  const int64_t chunk = std::max<int64_t>(
-      QT, std::min<int64_t>(std::max<int64_t>(q_hi - q_lo, 1), sbudget / (4 * std::max<int64_t>(ldS, 1))));
+  const int64_t ldS = nr;
+  const int64_t chunk = use_t ? std::min<int64_t>(std::max<int64_t>(q_hi - q_lo, 1), 4096)
+                              : std::max<int64_t>(QT, std::min<int64_t>(std::max<int64_t>(q_hi - q_lo, 1),
+                                                                         sbudget / (4 * std::max<int64_t>(ldS, 1))));
   // the FP16 bound is wider than the FP32 one: room for more candidates
   const int cap = use_t ? std::max(512, std::min(16384, 64 * r.k + 256))
                         : std::max(256, std::min(8192, 16 * r.k + 64));
-  const int nseg = (int)((nr + TSEG - 1) / TSEG);
-  float *segtop = nullptr, *cutv = nullptr, *rlo = nullptr, *rhi = nullptr;
+  float *rlo = nullptr, *rhi = nullptr;
   if (use_t) {
-    SK(cudaMallocAsync(&segtop, sizeof(float) * (size_t)(chunk * nseg * r.k + 4), s));
-    SK(cudaMallocAsync(&cutv, sizeof(float) * (size_t)(chunk + 4), s));
     SK(cudaMallocAsync(&rlo, sizeof(float) * (size_t)(chunk * cap + 4), s));
     SK(cudaMallocAsync(&rhi, sizeof(float) * (size_t)(chunk * cap + 4), s));
   }
@@ -1047,7 +818,7 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
   double* rvals = nullptr;
   uint8_t* force = nullptr;
   const int64_t cslots = chunk * (int64_t)cap;
-  SK(cudaMallocAsync(&S, sizeof(float) * (size_t)(chunk * ldS + 4), s));
+  if (!use_t) SK(cudaMallocAsync(&S, sizeof(float) * (size_t)(chunk * ldS + 4), s));
   SK(cudaMallocAsync(&cand, sizeof(int32_t) * (size_t)cslots, s));
   SK(cudaMallocAsync(&count, sizeof(int32_t) * (size_t)chunk, s));
   SK(cudaMallocAsync(&over, sizeof(int32_t) * (size_t)chunk, s));
@@ -1078,38 +849,19 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
     hooks.check_cancel();
     const int64_t nb = std::min(chunk, q_hi - q0);
     if (use_t) {
-      // S (nr x nb, column-major, leading dimension ldS) = R^T Q on the tensor cores
-      cublasHandle_t h = static_cast<cublasHandle_t>(r.blas);
-      const float one = 1.f, zero = 0.f;
-      const int64_t ld = rt->ld;
-      if (cublasSetStream(h, s) != CUBLAS_STATUS_SUCCESS) return (int)cudaErrorUnknown;
-      hooks.time_begin();
-      const cublasStatus_t bs = cublasGemmEx(
-          h, CUBLAS_OP_T, CUBLAS_OP_N, (int)nr, (int)nb, (int)ld, &one, rt->dense, CUDA_R_16F, (int)ld,
-          static_cast<const __half*>(qt->dense) + q0 * ld, CUDA_R_16F, (int)ld, &zero, S, CUDA_R_32F,
-          (int)ldS, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
-      hooks.time_end();
-      if (bs != CUBLAS_STATUS_SUCCESS) return (int)cudaErrorUnknown;
-      TensorSelArgs T;
-      T.method = r.method; T.k = r.k; T.S = S; T.ldS = ldS; T.nr = nr;
+      // the fused tcgen05 screen: FP16 GEMM tiles of the block against every
+      // reference with the FP16-bound selection in the epilogue
+      StcRun T;
+      T.method = r.method; T.k = r.k; T.selfmode = r.selfmode; T.include_self = r.include_self;
+      T.ld = rt->ld; T.nr = nr; T.q0 = q0; T.nq = nb;
+      T.rdense = static_cast<const __half*>(rt->dense); T.qdense = static_cast<const __half*>(qt->dense);
       T.rnnz = rc->nnz; T.rnorm = (r.method == EUCLIDEAN) ? rc->cnorm : nullptr;
+      T.rerr = rt->err; T.rbn = rt->bn; T.ref_mask = r.ref_mask;
       T.qnnz = qc->nnz; T.qnorm = (r.method == EUCLIDEAN) ? qc->cnorm : nullptr;
-      T.rerr = rt->err; T.rbn = rt->bn; T.qerr = qt->err; T.qbn = qt->bn;
-      T.ref_mask = r.ref_mask; T.qry_blank = r.qry_blank; T.qry_force_exact = force;
-      T.q_begin = q0; T.nq = nb; T.selfmode = r.selfmode; T.include_self = r.include_self;
-      T.nseg = nseg; T.segtop = segtop; T.cut = cutv;
-      T.cap = cap; T.cand = cand; T.count = count; T.overflow = over;
-      const size_t tsmem = sizeof(float) * (size_t)SELECT_WARPS * r.k;
-      if (tsmem > 48 * 1024) {
-        SK(cudaFuncSetAttribute(k_tsel_segtop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem));
-        SK(cudaFuncSetAttribute(k_tsel_thresh, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem));
-      }
-      const dim3 tgrid(blocks_for(nb, SELECT_WARPS), (unsigned)nseg);
-      k_tsel_segtop<<<tgrid, SELECT_WARPS * 32, tsmem, s>>>(T);
-      k_tsel_thresh<<<blocks_for(nb, SELECT_WARPS), SELECT_WARPS * 32, tsmem, s>>>(T);
-      k_tsel_keep<<<tgrid, SELECT_WARPS * 32, 0, s>>>(T);
-      k_tsel_overflow<<<blocks_for(nb, 256), 256, 0, s>>>(nb, cap, count, over);
-      SK(cudaGetLastError());
+      T.qerr = qt->err; T.qbn = qt->bn;
+      T.qry_blank = r.qry_blank; T.qry_force = force;
+      const int64_t ld = rt->ld;
+      SK((cudaError_t)stc_screen(T, s, cand, count, over, cap, hooks.time_begin, hooks.time_end));
       if (nrow <= RS_MAX_NROW) {
         RescreenArgs R;
         R.method = r.method; R.k = r.k; R.ref = ref; R.qry = qry; R.rf = rc->fval; R.qf = qc->fval;
@@ -1221,12 +973,11 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
   overflow_queries.erase(std::unique(overflow_queries.begin(), overflow_queries.end()),
                          overflow_queries.end());
   stats[2] += (int64_t)overflow_queries.size();
-  SK(cudaFreeAsync(S, s)); SK(cudaFreeAsync(cand, s)); SK(cudaFreeAsync(count, s));
+  if (S) SK(cudaFreeAsync(S, s));
+  SK(cudaFreeAsync(cand, s)); SK(cudaFreeAsync(count, s));
   SK(cudaFreeAsync(over, s)); SK(cudaFreeAsync(qidx, s)); SK(cudaFreeAsync(ridx, s));
   SK(cudaFreeAsync(rvals, s)); SK(cudaFreeAsync(tile_q, s)); SK(cudaFreeAsync(tile_n, s));
   SK(cudaFreeAsync(work, s));
-  if (segtop) SK(cudaFreeAsync(segtop, s));
-  if (cutv) SK(cudaFreeAsync(cutv, s));
   if (rlo) SK(cudaFreeAsync(rlo, s));
   if (rhi) SK(cudaFreeAsync(rhi, s));
   // queries the screen could not bound: the exact slab engine, run by runs

@@ -5,6 +5,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda_fp16.h>
 #include <functional>
 
 #include "sdg_common.cuh"
@@ -42,11 +43,10 @@ struct TensorCache {
 
 struct ScreenRun {
   int method = 0, dist = 1, k = 1;
-  // the tensor-core screen (an FP16 GEMM through cuBLAS handle `blas`) instead
-  // of the FP32 sparse screen, when tensor_supported(method) and both
-  // matrices' TensorCache are usable
+  // the tensor-core screen (the fused tcgen05 FP16 screen, sdg_sparse_tc.cu)
+  // instead of the FP32 sparse screen, when tensor_supported(method),
+  // stc_supported(k) and both matrices' TensorCache are usable
   bool tensor = false;
-  void* blas = nullptr;
   bool decreasing = false, selfmode = false, include_self = false;
   double self_value = 0.0;                 // restored self value (include_self)
   const uint8_t* ref_mask = nullptr;       // excluded reference columns
@@ -63,6 +63,30 @@ struct ScreenHooks {
   std::function<void()> time_begin, time_end;        // bracket the screen kernel
   std::function<void(int64_t, int64_t)> exact_range;  // finish queries [q0, q0+n) exactly
 };
+
+// The fused tcgen05 screen of the tensor engine (sdg_sparse_tc.cu): the FP16
+// GEMM of the query block against every reference column with the
+// selection of the slab path in its epilogue.  Fills cand / count / over (as
+// the slab selection does) for queries q0 .. q0 + nq - 1 of the query matrix.
+struct StcRun {
+  int method = 0, k = 1;
+  int selfmode = 0, include_self = 0;
+  int64_t ld = 0;                          // rows of the dense copies (multiple of 64)
+  int64_t nr = 0, q0 = 0, nq = 0;
+  const __half* rdense = nullptr;          // TensorCache of the reference
+  const __half* qdense = nullptr;          // TensorCache of the query matrix
+  const int32_t* rnnz = nullptr; const float* rnorm = nullptr;
+  const float* rerr = nullptr; const float* rbn = nullptr;
+  const uint8_t* ref_mask = nullptr;
+  const int32_t* qnnz = nullptr; const float* qnorm = nullptr;
+  const float* qerr = nullptr; const float* qbn = nullptr;
+  const uint8_t* qry_blank = nullptr;      // global query index
+  const uint8_t* qry_force = nullptr;
+};
+bool stc_supported(int k);
+// 0 or a cudaError_t value (the message is set)
+int stc_screen(const StcRun& r, cudaStream_t s, int32_t* cand, int32_t* count, int32_t* over, int cap,
+               const std::function<void()>& time_begin, const std::function<void()>& time_end);
 
 bool screen_supported(int method, int k);
 bool screen_fits(int32_t nrow);

@@ -71,3 +71,22 @@ def test_include_self_and_degenerate(gpu, data, engine):
             gpu.set_engine(0)
             want = orc.knn(X, k=10, method=method, include_self=inc)
             assert same_bits(got[0], want[0]) and same_bits(got[1], want[1]), (method, inc)
+
+
+@pytest.mark.parametrize("method,k", [("cosine", 5), ("cosine", 40), ("cosine", 64), ("euclidean", 40),
+                                      ("binary", 40), ("euclidean", 64)])
+def test_fused_tensor_screen_list_lengths_and_passes(gpu, data, method, k):
+    """The fused tcgen05 screen's three list lengths (16, 32 and 64 running
+    keys per thread) and a query range of 4,600 columns starting at column
+    100: two passes of at most 4,096 queries, the last query group ragged,
+    against 6,000 references (the last 256-column reference tile ragged).
+    Engine 3 must return the exact engine's idx and distances bit for bit."""
+    Q = data[:, 100:4700]
+    gpu.set_engine(1)
+    a = gpu.knn(Q, data, k=k, method=method)
+    gpu.set_engine(3)
+    b = gpu.knn(Q, data, k=k, method=method)
+    st = gpu.ctx.stats()
+    gpu.set_engine(0)
+    assert same_bits(a[0], b[0]) and same_bits(a[1], b[1])
+    assert st["tensor_flops"] > 0                  # the tensor screen ran
