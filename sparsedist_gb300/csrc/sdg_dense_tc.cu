@@ -3,7 +3,7 @@
 // The BF16 screen of the dense path without a slab in HBM: each CTA owns 256
 // query columns (two 128-row UMMA A tiles, resident in shared memory) and a
 // range of reference columns, streamed by TMA in 128-column x 64-row K chunks
-// (SWIZZLE_128B, four-stage ring).  One thread issues tcgen05.mma
+// (SWIZZLE_128B, five-stage ring).  One thread issues tcgen05.mma
 // (M = 128 queries, N = 128 references, K = 16, BF16 in, FP32 accumulate) into
 // TMEM: two query tiles x two accumulator buffers = 4 x 128 = 512 columns, so
 // the MMAs of reference tile j + 1 run while eight epilogue warps read tile j
@@ -48,14 +48,16 @@ constexpr int BM = 128;                 // queries per UMMA tile (TMEM lanes)
 constexpr int BN = 128;                 // references per tile (UMMA N)
 constexpr int BK = 64;                  // rows of a K chunk: 64 BF16 = one 128-byte swizzle row
 constexpr int QT = 2;                   // query tiles per CTA
-constexpr int STAGES = 4;               // reference chunk ring
+constexpr int STAGES = 5;               // reference chunk ring
+constexpr int NB = 8;                   // buffered passing references per epilogue thread
+constexpr int EPI_THREADS = 256;
 constexpr int KT = 64;                  // largest k of the fused screen
 constexpr int THREADS = 320;
 constexpr uint32_t TILE_BYTES = BN * BK * 2;   // 16 KB (a 128 x 64 BF16 tile)
 constexpr uint32_t TMEM_COLS = 512;
 constexpr int MAX_DCH = 4;              // dpad <= 256
 // 1 KB alignment slack, A tiles, B ring, barriers
-constexpr size_t SMEM_BYTES = 1024 + (size_t)(QT * MAX_DCH + STAGES) * TILE_BYTES + 256;
+constexpr size_t SMEM_BYTES = 1024 + (size_t)(QT * MAX_DCH + STAGES) * TILE_BYTES + (size_t)NB * EPI_THREADS * 8 + 256;
 
 struct TcArgs {
   int method, k, dch, nqg, nrr, tiles_per_range, ecap;
@@ -90,7 +92,11 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
   uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint8_t* sA = base;                                    // QT * dch tiles
   uint8_t* sB = base + (size_t)QT * MAX_DCH * TILE_BYTES;  // STAGES tiles
-  uint64_t* bars = (uint64_t*)(sB + (size_t)STAGES * TILE_BYTES);
+  // per epilogue thread NB (reference, GEMM value) slots, slot-major so that a
+  // warp's accesses to one slot are conflict-free
+  int32_t* buf_r = (int32_t*)(sB + (size_t)STAGES * TILE_BYTES);
+  float* buf_s = (float*)(buf_r + NB * EPI_THREADS);
+  uint64_t* bars = (uint64_t*)(buf_s + NB * EPI_THREADS);
   uint64_t* full = bars;
   uint64_t* emptyb = bars + STAGES;
   uint64_t* acc_full = bars + 2 * STAGES;
@@ -149,16 +155,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
         }
       }
       // every issued copy lands before the CTA can exit
-      for (int x = max(0, it - STAGES); x < it; ++x) {
-        const int s = x % STAGES;
-        const uint32_t ph = (uint32_t)(x / STAGES) & 1u;
-        uint64_t tw = gtimer();
-        while (!mbar_try_wait(full + s, ph) && gtimer() - tw < WAIT_NS) {}
-      }
-      {
-        uint64_t tw = gtimer();
-        while (!mbar_try_wait(a_full, 0) && gtimer() - tw < WAIT_NS) {}
-      }
+      for (int x = max(0, it - STAGES); x < it; ++x) mbar_drain(full + x % STAGES, (uint32_t)(x / STAGES) & 1u);
+      mbar_drain(a_full, 0);
     }
     __syncwarp();
   } else if (warp == 1) {
@@ -192,8 +190,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
       }
       // all issued MMAs complete before TMEM is freed
       umma_commit(mma_done);
-      uint64_t tw = gtimer();
-      while (!mbar_try_wait(mma_done, 0) && gtimer() - tw < WAIT_NS) {}
+      mbar_drain(mma_done, 0);
     }
     __syncwarp();
   } else {
@@ -210,6 +207,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
     }
     const int32_t d = P.d;
     const float rel = 0.0040f + (float)d * 2.384185791015625e-7f;
+    const bool cosine = P.method == COSINE;
     // this thread's top k pessimistic keys, sorted descending, in registers:
     // KL - k leading +inf sentinels, so that lst[KL - 1] is the k-th best
     float lst[KL];
@@ -224,6 +222,134 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
     int32_t* my_idx = P.eidx + slot * P.ecap;
     float* my_hi = P.ehi + slot * P.ecap;
     const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+
+    // The exact key bounds of one reference r with GEMM value s (the slow
+    // path): append it if its optimistic key reaches the running cut, insert
+    // its pessimistic key into the running top k and tighten the hot test.
+    // Degenerate and padding references carry w = +inf and are skipped (their
+    // GEMM value is exactly 0, so w is read only then).
+    auto process = [&](int64_t r, float s) {
+      if (P.self && r == q) return;
+      if (s == 0.f && P.w[r] == INFINITY) return;
+      const float Nr = cosine ? 0.f : P.norm2[r];
+      float key, err;
+      dense_key(P.method, 0, d, s, Nq, Nr, key, err);
+      const float lo = key - err, hi = key + err;
+      if (hi >= dense_cut(T)) {
+        if (cnt < P.ecap) { my_idx[cnt] = (int32_t)r; my_hi[cnt] = hi; }
+        ++cnt;
+      }
+      if (lo > T) {
+        // sorted insert: the new lst[i] is the median of lst[i - 1], lo, lst[i]
+#pragma unroll
+        for (int i = KL - 1; i > 0; --i) lst[i] = fmaxf(lst[i], fminf(lst[i - 1], lo));
+        lst[0] = fmaxf(lst[0], lo);
+        T = lst[KL - 1];
+        const float cut = dense_cut(T);
+        // hi >= cut implies x >= e_thr (the hot-test bound in the file
+        // header), with 2^-12 slack for the FP32 roundings of x and e_thr
+        e_thr = cosine ? cut - rel - (2.44140625e-4f * (fabsf(cut) + 1.f) + 1e-30f)
+                       : cut + P.one_minus_c * Nq - (2.44140625e-4f * (fabsf(cut) + Nq) + 1e-30f);
+        e_thr = fmaxf(-FLT_MAX, e_thr);
+      }
+    };
+    // Passing references wait in this thread's NB shared-memory slots and are
+    // processed by the whole warp at once when some lane's slots run out (and
+    // at the end), so that the slow path runs with most lanes active instead
+    // of one lane at a time; a deferred reference is judged against the cut
+    // current when it is processed, which only tightens the test.
+    const int et = threadIdx.x - 64;                  // epilogue thread 0 .. 255
+    int nbuf = 0;
+    auto flush = [&]() {
+      const int nmax = __reduce_max_sync(0xffffffffu, nbuf);
+      for (int i = 0; i < nmax; ++i)
+        if (i < nbuf) process(buf_r[i * EPI_THREADS + et], buf_s[i * EPI_THREADS + et]);
+      nbuf = 0;
+      __syncwarp();
+    };
+    // The hot test of one 32-reference chunk: x = s (cosine) or x = 2 s - w[r]
+    // (euclidean), the maximum as a tree; the mask of the references with
+    // x >= e_thr (0 for an inactive lane), built as a tree of ORs.  Trees keep
+    // the dependent chains five instructions deep.
+    auto hot_mask = [&](const uint32_t (&v)[32], int64_t r0) -> uint32_t {
+      if (!active) return 0u;
+      float x[32];
+      if (cosine) {
+#pragma unroll
+        for (int t = 0; t < 32; ++t) x[t] = __uint_as_float(v[t]);
+      } else {
+        const float4* w4 = reinterpret_cast<const float4*>(P.w + r0);
+#pragma unroll
+        for (int j4 = 0; j4 < 8; ++j4) {
+          const float4 ww = __ldg(w4 + j4);
+          x[4 * j4 + 0] = fmaf(P.a, __uint_as_float(v[4 * j4 + 0]), -ww.x);
+          x[4 * j4 + 1] = fmaf(P.a, __uint_as_float(v[4 * j4 + 1]), -ww.y);
+          x[4 * j4 + 2] = fmaf(P.a, __uint_as_float(v[4 * j4 + 2]), -ww.z);
+          x[4 * j4 + 3] = fmaf(P.a, __uint_as_float(v[4 * j4 + 3]), -ww.w);
+        }
+      }
+      float m[16];
+#pragma unroll
+      for (int t = 0; t < 16; ++t) m[t] = fmaxf(x[2 * t], x[2 * t + 1]);
+#pragma unroll
+      for (int w = 8; w > 0; w >>= 1)
+#pragma unroll
+        for (int t = 0; t < w; ++t) m[t] = fmaxf(m[t], m[t + w]);
+      if (!(m[0] >= e_thr)) return 0u;
+      uint32_t b[16];
+#pragma unroll
+      for (int t = 0; t < 16; ++t)
+        b[t] = (x[2 * t] >= e_thr ? 1u << (2 * t) : 0u) | (x[2 * t + 1] >= e_thr ? 2u << (2 * t) : 0u);
+#pragma unroll
+      for (int w = 8; w > 0; w >>= 1)
+#pragma unroll
+        for (int t = 0; t < w; ++t) b[t] |= b[t + w];
+      return b[0];
+    };
+    // v[jj] as a five-level tree of selects on the bits of jj
+    auto pick = [](const uint32_t (&v)[32], int jj) -> float {
+      uint32_t a[16];
+#pragma unroll
+      for (int t = 0; t < 16; ++t) a[t] = (jj & 1) ? v[2 * t + 1] : v[2 * t];
+#pragma unroll
+      for (int lvl = 1, w = 8; w > 0; ++lvl, w >>= 1)
+#pragma unroll
+        for (int t = 0; t < w; ++t) a[t] = ((jj >> lvl) & 1) ? a[2 * t + 1] : a[2 * t];
+      return __uint_as_float(a[0]);
+    };
+    // The passing references of one chunk into this lane's slots (lanes
+    // converged): the warp flushes first if some lane's slots would overflow;
+    // a lane with more than NB of them (only while its list is filling) takes
+    // the slow path at once.
+    auto take = [&](const uint32_t (&v)[32], uint32_t mask, int64_t r0) {
+      const int nnew = __popc(mask);
+      if (__any_sync(0xffffffffu, nbuf + nnew > NB)) flush();
+      if (nnew > NB) {
+        while (mask) {
+          const int jj = __ffs(mask) - 1;
+          mask &= mask - 1;
+          process(r0 + jj, pick(v, jj));
+        }
+      } else {
+        while (mask) {
+          const int jj = __ffs(mask) - 1;
+          mask &= mask - 1;
+          buf_r[nbuf * EPI_THREADS + et] = (int32_t)(r0 + jj);
+          buf_s[nbuf * EPI_THREADS + et] = pick(v, jj);
+          ++nbuf;
+        }
+      }
+      __syncwarp();
+    };
+    // two chunks at once: their hot tests are independent, so they overlap
+    auto chunk2 = [&](const uint32_t (&va)[32], int64_t ra, const uint32_t (&vb)[32], int64_t rb) {
+      const uint32_t ma = hot_mask(va, ra), mb = hot_mask(vb, rb);
+      if (__any_sync(0xffffffffu, (ma | mb) != 0u)) {
+        take(va, ma, ra);
+        take(vb, mb, rb);
+      }
+    };
+
     for (int j = 0; j < ntile; ++j) {
       const int buf = j & 1;
       const uint32_t aph = (uint32_t)(j >> 1) & 1u;
@@ -231,70 +357,35 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
       if (!__all_sync(0xffffffffu, ok)) break;     // the warp leaves together (tcgen05.ld is .aligned)
       fence_after();
       const int64_t rtile = (t0 + j) * BN;
+      const uint32_t tb = tmem + lane_base + (uint32_t)((buf * QT + qt) * BN);
+      static_assert(BN % 64 == 0, "pairs of 32-column chunks");
+      if constexpr (KL <= 32) {
+        // chunks in pairs (the TMEM loads take a few tens of cycles; the
+        // pair's hot tests overlap)
 #pragma unroll 1
-      for (int hh = 0; hh < BN / 32; ++hh) {
-        uint32_t v[32];
-        const uint32_t ta = tmem + lane_base + (uint32_t)((buf * QT + qt) * BN + hh * 32);
-        tmem_ld32(ta, v);
-        if (!active) continue;
-        const int64_t r0 = rtile + hh * 32;
-        const float4* w4 = reinterpret_cast<const float4*>(P.w + r0);
-        // hot test: the largest x of the 32 against the threshold
-        float mx = -INFINITY;
-#pragma unroll
-        for (int j4 = 0; j4 < 8; ++j4) {
-          const float4 ww = __ldg(w4 + j4);
-          mx = fmaxf(mx, fmaf(P.a, __uint_as_float(v[4 * j4 + 0]), -ww.x));
-          mx = fmaxf(mx, fmaf(P.a, __uint_as_float(v[4 * j4 + 1]), -ww.y));
-          mx = fmaxf(mx, fmaf(P.a, __uint_as_float(v[4 * j4 + 2]), -ww.z));
-          mx = fmaxf(mx, fmaf(P.a, __uint_as_float(v[4 * j4 + 3]), -ww.w));
+        for (int hh = 0; hh < BN / 32; hh += 2) {
+          uint32_t va[32], vb[32];
+          tmem_ld32_issue(tb + hh * 32, va);
+          tmem_ld32_issue(tb + hh * 32 + 32, vb);
+          tmem_ld_wait(va);
+          tmem_ld_wait(vb);
+          chunk2(va, rtile + hh * 32, vb, rtile + hh * 32 + 32);
         }
-        if (!(mx >= e_thr)) continue;
-        uint32_t mask = 0;
-#pragma unroll
-        for (int j4 = 0; j4 < 8; ++j4) {
-          const float4 ww = __ldg(w4 + j4);
-          const float wv[4] = {ww.x, ww.y, ww.z, ww.w};
-#pragma unroll
-          for (int t = 0; t < 4; ++t)
-            if (fmaf(P.a, __uint_as_float(v[4 * j4 + t]), -wv[t]) >= e_thr) mask |= 1u << (4 * j4 + t);
-        }
-        while (mask) {
-          const int jj = __ffs(mask) - 1;
-          mask &= mask - 1;
-          const int64_t r = r0 + jj;
-          if (P.self && r == q) continue;
-          float s = 0.f;
-#pragma unroll
-          for (int t = 0; t < 32; ++t) s = (t == jj) ? __uint_as_float(v[t]) : s;
-          const float Nr = (P.method == COSINE) ? 0.f : P.norm2[r];
-          float key, err;
-          dense_key(P.method, 0, d, s, Nq, Nr, key, err);
-          const float lo = key - err, hi = key + err;
-          if (hi >= dense_cut(T)) {
-            if (cnt < P.ecap) { my_idx[cnt] = (int32_t)r; my_hi[cnt] = hi; }
-            ++cnt;
-          }
-          if (lo > T) {
-            // sorted insert: the new lst[i] is the median of lst[i - 1], lo, lst[i]
-#pragma unroll
-            for (int i = KL - 1; i > 0; --i) lst[i] = fmaxf(lst[i], fminf(lst[i - 1], lo));
-            lst[0] = fmaxf(lst[0], lo);
-            T = lst[KL - 1];
-            const float cut = dense_cut(T);
-            // hi >= cut implies x >= e_thr (the hot-test bound in the file
-            // header), with 2^-12 slack for the FP32 roundings of x and e_thr
-            e_thr = (P.method == COSINE)
-                        ? cut - rel - (2.44140625e-4f * (fabsf(cut) + 1.f) + 1e-30f)
-                        : cut + P.one_minus_c * Nq - (2.44140625e-4f * (fabsf(cut) + Nq) + 1e-30f);
-            e_thr = fmaxf(-FLT_MAX, e_thr);
-          }
+      } else {
+        // longer lists leave registers for one chunk at a time
+#pragma unroll 1
+        for (int hh = 0; hh < BN / 32; ++hh) {
+          uint32_t va[32];
+          tmem_ld32(tb + hh * 32, va);
+          const uint32_t ma = hot_mask(va, rtile + hh * 32);
+          if (__any_sync(0xffffffffu, ma != 0u)) take(va, ma, rtile + hh * 32);
         }
       }
       fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(acc_empty + buf);
     }
+    flush();
     if (active) {
       float* out = P.lists + slot * K;
 #pragma unroll

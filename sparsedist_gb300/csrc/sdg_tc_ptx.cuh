@@ -45,6 +45,22 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
+// try_wait with a suspend-time hint: the thread sleeps until the phase
+// completes or about `ns` nanoseconds pass, instead of spinning on the issue
+// slots that the warps sharing its scheduler need.
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t* bar, uint32_t parity, uint32_t ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(ns)
+      : "memory");
+  return ok != 0;
+}
+constexpr uint32_t SLEEP_NS = 20000;
+
 // Bounded wait for the phase of the given parity; false when it ran out or the
 // CTA aborted (then *abort_flag is set).
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
@@ -52,7 +68,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volati
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = gtimer();
   for (uint32_t spin = 1;; ++spin) {
-    if (mbar_try_wait(bar, parity)) return true;
+    if (mbar_try_wait_sleep(bar, parity, SLEEP_NS)) return true;
     if ((spin & 255u) == 0) {
       if (*abort_flag) return false;
       if (gtimer() - t0 > WAIT_NS) {
@@ -67,7 +83,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volati
 // issued will complete: the drain before a CTA exits.
 __device__ __forceinline__ void mbar_drain(uint64_t* bar, uint32_t parity) {
   const uint64_t t0 = gtimer();
-  while (!mbar_try_wait(bar, parity) && gtimer() - t0 < WAIT_NS) {}
+  while (!mbar_try_wait_sleep(bar, parity, SLEEP_NS) && gtimer() - t0 < WAIT_NS) {}
 }
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
   asm volatile(
@@ -144,6 +160,28 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
       : "r"(taddr));
   asm volatile("tcgen05.wait::ld.sync.aligned;" : SDG_P8(0), SDG_P8(8), SDG_P8(16), SDG_P8(24) :: "memory");
 #undef SDG_R8
+#undef SDG_P8
+}
+
+// tmem_ld32 in two halves, so that the next chunk's load is in flight while
+// the current one is processed: the issue writes v, the wait (which waits for
+// every load this thread issued) carries v as operands so that no use of v is
+// scheduled before it.
+__device__ __forceinline__ void tmem_ld32_issue(uint32_t taddr, uint32_t (&v)[32]) {
+#define SDG_R8(o) "=r"(v[o]), "=r"(v[o + 1]), "=r"(v[o + 2]), "=r"(v[o + 3]), "=r"(v[o + 4]), "=r"(v[o + 5]), \
+                  "=r"(v[o + 6]), "=r"(v[o + 7])
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : SDG_R8(0), SDG_R8(8), SDG_R8(16), SDG_R8(24)
+      : "r"(taddr));
+#undef SDG_R8
+}
+__device__ __forceinline__ void tmem_ld_wait(uint32_t (&v)[32]) {
+#define SDG_P8(o) "+r"(v[o]), "+r"(v[o + 1]), "+r"(v[o + 2]), "+r"(v[o + 3]), "+r"(v[o + 4]), "+r"(v[o + 5]), \
+                  "+r"(v[o + 6]), "+r"(v[o + 7])
+  asm volatile("tcgen05.wait::ld.sync.aligned;" : SDG_P8(0), SDG_P8(8), SDG_P8(16), SDG_P8(24) :: "memory");
 #undef SDG_P8
 }
 
