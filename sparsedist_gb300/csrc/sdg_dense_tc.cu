@@ -1,35 +1,51 @@
 // sdg_dense_tc.cu -- the dense screen fused on the 5th-generation tensor cores.
 //
-// The BF16 screen of the dense path without a slab in HBM: each CTA owns 256
-// query columns (two 128-row UMMA A tiles, resident in shared memory) and a
-// range of reference columns, streamed by TMA in 128-column x 64-row K chunks
-// (SWIZZLE_128B, five-stage ring).  One thread issues tcgen05.mma
-// (M = 128 queries, N = 128 references, K = 16, BF16 in, FP32 accumulate) into
-// TMEM: two query tiles x two accumulator buffers = 4 x 128 = 512 columns, so
-// the MMAs of reference tile j + 1 run while eight epilogue warps read tile j
-// back with tcgen05.ld.  An epilogue thread owns one query: it keeps the top k
-// pessimistic keys of its reference range in shared memory and appends every
-// reference whose optimistic key reaches its running cut to a per-(query,
-// range) candidate list.  The running cut is the k-th best of a subset, never
-// above the query's final cut, so the union of the lists holds every reference
-// that the slab screen keeps; k_tc_merge applies the final cut (the k-th best
-// over all ranges' lists) exactly as the slab screen does.
+// The BF16 screen of the dense path without a slab in HBM.  The work of a
+// query block is the grid of (query group, reference tile) items: a query
+// group is 128 query columns (one UMMA A tile, M = 128), a reference tile 256
+// reference columns (UMMA N = 256).  The items, query-group-major, are split
+// into equal contiguous spans, one per CTA (a persistent grid of at most one
+// CTA per SM), so every SM gets the same work whatever the block size; a span
+// usually covers the tail of one query group and the head of the next, and
+// each (query group, CTA) piece of a span is a "segment".
 //
-// Hot test.  An epilogue thread first tests x = a s - w[r] against one
-// threshold e_thr per query (a = 1, w = 0 for cosine; a = 2,
-// w = (1 - c) Nr for euclidean, c = rel + 2^-20; w = +inf for degenerate and
-// padding references), and only references passing it get their exact key
-// bounds.  For euclidean 2 rel sqrt(Nq Nr) <= rel (Nq + Nr), so
-// hi <= 2 s - (1 - c)(Nq + Nr) + 1e-30 and hi >= cut implies
-// x >= cut + (1 - c) Nq; for cosine hi = s + rel.  e_thr subtracts 2^-12
-// (|cut| + Nq) (euclidean) or 2^-12 (|cut| + 1) (cosine) more, far above the
-// FP32 rounding of x.
+// Per segment the query group's 128 x d BF16 columns are loaded into shared
+// memory once (TMA, SWIZZLE_128B, K-major, 64-row chunks); reference tiles of
+// 256 columns x 64 rows stream through a four-stage TMA ring.  One thread
+// issues tcgen05.mma.cta_group::1.kind::f16 (M = 128 queries, N = 256
+// references, K = 16, BF16 in, FP32 accumulate) into TMEM: two accumulator
+// buffers of 256 columns fill all 512, so the MMAs of tile j + 1 run while
+// the epilogue reads tile j back with tcgen05.ld.
+//
+// Epilogue: eight warps; warp w reads TMEM lanes 32 (w % 4) .. + 31 (its 32
+// queries) and one half of the tile's 256 columns ((w - 2) / 4).  A thread
+// owns one (query, column half): it keeps the top k pessimistic keys of its
+// half of the segment's references in registers and appends every reference
+// whose optimistic key reaches its running cut to a per-(query, segment,
+// half) list.  The running cut is the k-th best of a subset, never above the
+// query's final cut, so the union of the lists holds every reference that the
+// slab screen keeps; k_tc_merge applies the final cut (the k-th best over all
+// the query's lists) exactly as the slab screen does.
+//
+// Hot test.  An epilogue thread tests x = a s - w[r] against one threshold
+// e_thr per query (a = 1, w = 0 for cosine; a = 2, w = (1 - c) Nr for
+// euclidean, c = rel + 2^-20; w = +inf for degenerate and padding references),
+// and only references passing it get their exact key bounds.  For euclidean
+// 2 rel sqrt(Nq Nr) <= rel (Nq + Nr), so hi <= 2 s - (1 - c)(Nq + Nr) + 1e-30
+// and hi >= cut implies x >= cut + (1 - c) Nq; for cosine hi = s + rel.
+// e_thr subtracts 2^-12 (|cut| + Nq) (euclidean) or 2^-12 (|cut| + 1)
+// (cosine) more, far above the FP32 rounding of x.  The test's maximum, the
+// pass mask and the pick of a passing value are trees five levels deep, and
+// two 32-column chunks are tested together.  Passing references wait in eight
+// shared-memory slots per thread and are processed by the whole warp at once
+// when some lane's slots run out, so the slow path (key bounds, append,
+// sorted insert) runs with most lanes active.
 //
 // Warp roles (320 threads): warp 0 TMA producer, warp 1 TMEM allocator + MMA
-// issuer, warps 2..9 epilogue (warp w reads TMEM lanes 32 (w % 4) .. + 31, of
-// query tile (w - 2) / 4).  Every mbarrier wait is bounded (1 s of
-// %globaltimer); a wait that runs out sets *status, raises the CTA's abort
-// flag, and the CTA drains its own copies and MMAs, frees TMEM and returns.
+// issuer, warps 2..9 epilogue.  Every mbarrier wait is bounded (1 s of
+// %globaltimer, sdg_tc_ptx.cuh) and sleeps instead of spinning; a wait that
+// runs out sets *status, raises the CTA's abort flag, and the CTA drains its
+// own copies and MMAs, frees TMEM and returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 
@@ -44,57 +60,74 @@
 namespace sdg {
 namespace {
 
-constexpr int BM = 128;                 // queries per UMMA tile (TMEM lanes)
-constexpr int BN = 128;                 // references per tile (UMMA N)
+using namespace tc;
+
+constexpr int BM = 128;                 // queries per group (UMMA M, TMEM lanes)
+constexpr int BN = 256;                 // references per tile (UMMA N)
 constexpr int BK = 64;                  // rows of a K chunk: 64 BF16 = one 128-byte swizzle row
-constexpr int QT = 2;                   // query tiles per CTA
-constexpr int STAGES = 5;               // reference chunk ring
+constexpr int STAGES = 4;               // reference chunk ring
 constexpr int NB = 8;                   // buffered passing references per epilogue thread
 constexpr int EPI_THREADS = 256;
 constexpr int KT = 64;                  // largest k of the fused screen
 constexpr int THREADS = 320;
-constexpr uint32_t TILE_BYTES = BN * BK * 2;   // 16 KB (a 128 x 64 BF16 tile)
-constexpr uint32_t TMEM_COLS = 512;
+constexpr uint32_t A_BYTES = BM * BK * 2;      // 16 KB: a 128 x 64 BF16 query chunk
+constexpr uint32_t B_BYTES = BN * BK * 2;      // 32 KB: a 256 x 64 BF16 reference chunk
+constexpr uint32_t TMEM_COLS = 2 * BN;         // two accumulator buffers
 constexpr int MAX_DCH = 4;              // dpad <= 256
-// 1 KB alignment slack, A tiles, B ring, barriers
-constexpr size_t SMEM_BYTES = 1024 + (size_t)(QT * MAX_DCH + STAGES) * TILE_BYTES + (size_t)NB * EPI_THREADS * 8 + 256;
+// 1 KB alignment slack, A chunks, B ring, candidate slots, barriers
+constexpr size_t SMEM_BYTES = 1024 + (size_t)MAX_DCH * A_BYTES + (size_t)STAGES * B_BYTES +
+                              (size_t)NB * EPI_THREADS * 8 + 256;
+constexpr uint32_t IDESC = idesc_f16(BM, BN, true);
 
 struct TcArgs {
-  int method, k, dch, nqg, nrr, tiles_per_range, ecap;
+  int method, k, dch, ecap;
   int self;                   // queries are columns of the reference (skip r == q)
   int32_t d;
-  int64_t n, q0, nq, ntiles;
+  int64_t n, q0, nq;          // references; the block's first query (index in Q) and size
+  int64_t ntiles, tiles_per_cta, nslots;   // reference tiles; items per CTA; list slots per query
   float a;                    // x = a * s - w[r] (1 cosine, 2 euclidean)
   float one_minus_c;          // euclidean hot-test coefficient
-  const float* w;             // [npad]: +inf for degenerate / padding references
-  const float* norm2;         // [npad] reference sums of squares
-  const float* qnorm2;        // query sums of squares
+  const float* w;             // [ntiles * BN]: +inf for degenerate / padding references
+  const float* norm2;         // reference sums of squares
+  const float* qnorm2;        // query sums of squares (index in Q)
   const uint8_t* qempty;      // degenerate queries (no list)
-  float* lists;               // [nq][nrr][k]
-  int32_t* ecount;            // [nq][nrr]
-  int32_t* eidx;              // [nq][nrr][ecap]
-  float* ehi;                 // [nq][nrr][ecap]
+  unsigned* tshared;          // [nq]: the best running k-th pessimistic key of any list (ordered bits)
+  float* lists;               // [nq][nslots][k]
+  int32_t* ecount;            // [nq][nslots]
+  int32_t* eidx;              // [nq][nslots][ecap]
+  float* ehi;                 // [nq][nslots][ecap]
   int* status;
 };
 
-using namespace tc;
-constexpr uint32_t IDESC = idesc_f16(BM, BN, true);
+// Order-preserving map of a float onto uint32 (ascending value -> ascending
+// key), so that atomicMax on the keys is a max on the floats.
+__device__ __forceinline__ unsigned fkey(float f) {
+  const unsigned b = __float_as_uint(f);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float fkey_value(unsigned k) {
+  return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
+}
+constexpr int SHARE_TILES = 8;          // tiles between exchanges of the shared running key
 
-__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accum) {
-  umma_f16(d_tmem, adesc, bdesc, IDESC, accum);
+// the first and the last CTA whose span holds an item of query group g
+__host__ __device__ __forceinline__ int64_t first_cta(int64_t g, int64_t ntiles, int64_t per) {
+  return (g * ntiles) / per;
+}
+__host__ __device__ __forceinline__ int64_t last_cta(int64_t g, int64_t ntiles, int64_t per) {
+  return ((g + 1) * ntiles - 1) / per;
 }
 
-// ---- the fused screen ------------------------------------------------------
 template <int KL>
 __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__ CUtensorMap qmap,
                                                        const __grid_constant__ CUtensorMap rmap, TcArgs P) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint8_t* sA = base;                                    // QT * dch tiles
-  uint8_t* sB = base + (size_t)QT * MAX_DCH * TILE_BYTES;  // STAGES tiles
+  uint8_t* sA = base;                                     // MAX_DCH query chunks
+  uint8_t* sB = base + (size_t)MAX_DCH * A_BYTES;          // STAGES reference chunks
   // per epilogue thread NB (reference, GEMM value) slots, slot-major so that a
   // warp's accesses to one slot are conflict-free
-  int32_t* buf_r = (int32_t*)(sB + (size_t)STAGES * TILE_BYTES);
+  int32_t* buf_r = (int32_t*)(sB + (size_t)STAGES * B_BYTES);
   float* buf_s = (float*)(buf_r + NB * EPI_THREADS);
   uint64_t* bars = (uint64_t*)(buf_s + NB * EPI_THREADS);
   uint64_t* full = bars;
@@ -102,32 +135,27 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
   uint64_t* acc_full = bars + 2 * STAGES;
   uint64_t* acc_empty = acc_full + 2;
   uint64_t* a_full = acc_empty + 2;
-  uint64_t* mma_done = a_full + 1;
+  uint64_t* a_empty = a_full + 1;
+  uint64_t* mma_done = a_empty + 1;
   uint32_t* tmem_slot = (uint32_t*)(mma_done + 1);
   volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int qg = blockIdx.x % P.nqg, rr = blockIdx.x / P.nqg;
-  const int64_t qbase = P.q0 + (int64_t)qg * (QT * BM);
-  const int64_t t0 = (int64_t)rr * P.tiles_per_range;
-  const int64_t t1 = min(P.ntiles, t0 + (int64_t)P.tiles_per_range);
-  const int ntile = (int)max((int64_t)0, t1 - t0);
+  const int64_t per = P.tiles_per_cta, ntiles = P.ntiles;
+  const int64_t f0 = (int64_t)blockIdx.x * per;
+  const int64_t f1 = min(f0 + per, ((P.nq + BM - 1) / BM) * ntiles);
   const int dch = P.dch;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) { mbar_init(full + s, 1); mbar_init(emptyb + s, 1); }
     for (int b = 0; b < 2; ++b) { mbar_init(acc_full + b, 1); mbar_init(acc_empty + b, 8); }
     mbar_init(a_full, 1);
+    mbar_init(a_empty, 1);
     mbar_init(mma_done, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                 ::"r"(smem_u32(tmem_slot)), "r"(TMEM_COLS)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-  }
+  if (warp == 1) tmem_alloc(tmem_slot, TMEM_COLS);
   fence_before();
   __syncthreads();
   fence_after();
@@ -135,58 +163,73 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
 
   if (warp == 0) {
     // ---- TMA producer ----
-    if (lane == 0 && ntile > 0) {
-      asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&qmap) : "memory");
-      asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&rmap) : "memory");
-      mbar_expect_tx(a_full, (uint32_t)(QT * dch) * TILE_BYTES);
-      for (int qt = 0; qt < QT; ++qt)
-        for (int c = 0; c < dch; ++c)
-          tma_load_2d(sA + (size_t)(qt * MAX_DCH + c) * TILE_BYTES, &qmap, a_full, c * BK,
-                      (int)(qbase + qt * BM));
-      int it = 0;
+    if (lane == 0 && f1 > f0) {
+      prefetch_map(&qmap);
+      prefetch_map(&rmap);
+      int it = 0, seg = 0;
       bool ok = true;
-      for (int j = 0; j < ntile && ok; ++j) {
-        for (int c = 0; c < dch; ++c, ++it) {
-          const int s = it % STAGES;
-          const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
-          if (!mbar_wait(emptyb + s, ph ^ 1u, abort_flag, P.status)) { ok = false; break; }
-          mbar_expect_tx(full + s, TILE_BYTES);
-          tma_load_2d(sB + (size_t)s * TILE_BYTES, &rmap, full + s, c * BK, (int)((t0 + j) * BN));
+      for (int64_t f = f0; f < f1 && ok; ++seg) {
+        const int64_t g = f / ntiles;
+        const int64_t fe = min(f1, (g + 1) * ntiles);
+        // the previous segment's MMAs have finished reading the query chunks
+        if (!mbar_wait(a_empty, ((uint32_t)seg & 1u) ^ 1u, abort_flag, P.status)) break;
+        mbar_expect_tx(a_full, (uint32_t)dch * A_BYTES);
+        for (int c = 0; c < dch; ++c)
+          tma_load_2d(sA + (size_t)c * A_BYTES, &qmap, a_full, c * BK, (int)(P.q0 + g * BM));
+        for (; f < fe && ok; ++f) {
+          const int rcol = (int)((f - g * ntiles) * BN);
+          for (int c = 0; c < dch; ++c, ++it) {
+            const int s = it % STAGES;
+            const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+            if (!mbar_wait(emptyb + s, ph ^ 1u, abort_flag, P.status)) { ok = false; break; }
+            mbar_expect_tx(full + s, B_BYTES);
+            tma_load_2d(sB + (size_t)s * B_BYTES, &rmap, full + s, c * BK, rcol);
+          }
         }
       }
       // every issued copy lands before the CTA can exit
       for (int x = max(0, it - STAGES); x < it; ++x) mbar_drain(full + x % STAGES, (uint32_t)(x / STAGES) & 1u);
-      mbar_drain(a_full, 0);
+      if (seg > 0) mbar_drain(a_full, (uint32_t)(seg - 1) & 1u);
     }
     __syncwarp();
   } else if (warp == 1) {
     // ---- MMA issuer ----
-    if (lane == 0 && ntile > 0) {
-      bool ok = mbar_wait(a_full, 0, abort_flag, P.status);
-      fence_after();
-      int it = 0;
-      for (int j = 0; j < ntile && ok; ++j) {
-        const int buf = j & 1;
-        const uint32_t aph = (uint32_t)(j >> 1) & 1u;
-        if (!mbar_wait(acc_empty + buf, aph ^ 1u, abort_flag, P.status)) { ok = false; break; }
+    if (lane == 0 && f1 > f0) {
+      int it = 0, seg = 0;
+      int64_t j = 0;
+      bool ok = true;
+      for (int64_t f = f0; f < f1 && ok; ++seg) {
+        const int64_t g = f / ntiles;
+        const int64_t fe = min(f1, (g + 1) * ntiles);
+        if (!mbar_wait(a_full, (uint32_t)seg & 1u, abort_flag, P.status)) break;
         fence_after();
-        for (int c = 0; c < dch; ++c, ++it) {
-          const int s = it % STAGES;
-          const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
-          if (!mbar_wait(full + s, ph, abort_flag, P.status)) { ok = false; break; }
+        const uint32_t a0 = smem_u32(sA);
+        for (; f < fe && ok; ++f, ++j) {
+          const int buf = (int)(j & 1);
+          // the epilogue has drained this buffer's previous tile
+          if (!mbar_wait(acc_empty + buf, ((uint32_t)(j >> 1) & 1u) ^ 1u, abort_flag, P.status)) {
+            ok = false;
+            break;
+          }
           fence_after();
-          const uint32_t b_addr = smem_u32(sB + (size_t)s * TILE_BYTES);
-          for (int qt = 0; qt < QT; ++qt) {
-            const uint32_t a_addr = smem_u32(sA + (size_t)(qt * MAX_DCH + c) * TILE_BYTES);
-            const uint32_t d_addr = tmem + (uint32_t)((buf * QT + qt) * BN);
+          const uint32_t d_addr = tmem + (uint32_t)(buf * BN);
+          for (int c = 0; c < dch; ++c, ++it) {
+            const int s = it % STAGES;
+            const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+            if (!mbar_wait(full + s, ph, abort_flag, P.status)) { ok = false; break; }
+            fence_after();
+            const uint32_t b_addr = smem_u32(sB + (size_t)s * B_BYTES);
+            const uint32_t a_addr = a0 + (uint32_t)c * A_BYTES;
 #pragma unroll
             for (int kk = 0; kk < BK / 16; ++kk)
-              umma_bf16(d_addr, sw128_desc(a_addr + kk * 32), sw128_desc(b_addr + kk * 32), (c | kk) != 0);
+              umma_f16(d_addr, sw128_desc(a_addr + kk * 32), sw128_desc(b_addr + kk * 32), IDESC,
+                       (c | kk) != 0);
+            umma_commit(emptyb + s);            // the stage is free once these MMAs have read it
           }
-          umma_commit(emptyb + s);            // the stage is free once these MMAs have read it
+          if (!ok) break;
+          umma_commit(acc_full + buf);          // the tile's accumulators are complete
         }
-        if (!ok) break;
-        umma_commit(acc_full + buf);          // tile j's accumulators are complete
+        umma_commit(a_empty);                   // the query chunks are free once the segment's MMAs are done
       }
       // all issued MMAs complete before TMEM is freed
       umma_commit(mma_done);
@@ -194,35 +237,44 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
     }
     __syncwarp();
   } else {
-    // ---- epilogue: one thread per query ----
-    const int qt = (warp - 2) >> 2, quarter = warp & 3;
+    // ---- epilogue: one thread per (query, column half) ----
+    const int quarter = warp & 3, half = (warp - 2) >> 2;
     const int row = quarter * 32 + lane;
-    const int64_t q = qbase + qt * BM + row;
     const int K = P.k;
-    bool active = q < P.q0 + P.nq;
-    float Nq = 0.f;
-    if (active) {
-      active = !P.qempty[q];                 // a degenerate query has no list
-      Nq = P.qnorm2[q];
-    }
     const int32_t d = P.d;
     const float rel = 0.0040f + (float)d * 2.384185791015625e-7f;
     const bool cosine = P.method == COSINE;
+    const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+    const int et = threadIdx.x - 64;                  // epilogue thread 0 .. 255
+
+    // per-segment state
+    bool active = false;
+    int64_t q = 0;
+    float Nq = 0.f;
     // this thread's top k pessimistic keys, sorted descending, in registers:
     // KL - k leading +inf sentinels, so that lst[KL - 1] is the k-th best
     float lst[KL];
-#pragma unroll
-    for (int i = 0; i < KL; ++i) lst[i] = (i < KL - K) ? INFINITY : -INFINITY;
-    float T = -INFINITY;                       // k-th best pessimistic key so far
+    float T = -INFINITY;                       // k-th best pessimistic key of this list so far
+    // the best running k-th key of any of the query's lists (segments and
+    // halves running on other warps and CTAs), exchanged every SHARE_TILES
+    // tiles: each is the k-th best of a subset, so their maximum never
+    // exceeds the query's final k-th best and may stand in for T in every test
+    float Ts = -INFINITY;
     // hot-loop threshold on x; finite, so that x = -inf (degenerate or padding
     // references) never passes
     float e_thr = -FLT_MAX;
-    int cnt = 0;
-    const int64_t slot = active ? ((q - P.q0) * P.nrr + rr) : 0;
-    int32_t* my_idx = P.eidx + slot * P.ecap;
-    float* my_hi = P.ehi + slot * P.ecap;
-    const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+    int cnt = 0, nbuf = 0;
+    int32_t* my_idx = P.eidx;
+    float* my_hi = P.ehi;
 
+    // hi >= cut implies x >= e_thr (the hot-test bound in the file header),
+    // with 2^-12 slack for the FP32 roundings of x and e_thr
+    auto set_thr = [&]() {
+      const float cut = dense_cut(fmaxf(T, Ts));
+      e_thr = cosine ? cut - rel - (2.44140625e-4f * (fabsf(cut) + 1.f) + 1e-30f)
+                     : cut + P.one_minus_c * Nq - (2.44140625e-4f * (fabsf(cut) + Nq) + 1e-30f);
+      e_thr = fmaxf(-FLT_MAX, e_thr);
+    };
     // The exact key bounds of one reference r with GEMM value s (the slow
     // path): append it if its optimistic key reaches the running cut, insert
     // its pessimistic key into the running top k and tighten the hot test.
@@ -235,31 +287,24 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
       float key, err;
       dense_key(P.method, 0, d, s, Nq, Nr, key, err);
       const float lo = key - err, hi = key + err;
-      if (hi >= dense_cut(T)) {
+      const float Te = fmaxf(T, Ts);
+      if (hi >= dense_cut(Te)) {
         if (cnt < P.ecap) { my_idx[cnt] = (int32_t)r; my_hi[cnt] = hi; }
         ++cnt;
       }
-      if (lo > T) {
+      if (lo > Te) {
         // sorted insert: the new lst[i] is the median of lst[i - 1], lo, lst[i]
 #pragma unroll
         for (int i = KL - 1; i > 0; --i) lst[i] = fmaxf(lst[i], fminf(lst[i - 1], lo));
         lst[0] = fmaxf(lst[0], lo);
         T = lst[KL - 1];
-        const float cut = dense_cut(T);
-        // hi >= cut implies x >= e_thr (the hot-test bound in the file
-        // header), with 2^-12 slack for the FP32 roundings of x and e_thr
-        e_thr = cosine ? cut - rel - (2.44140625e-4f * (fabsf(cut) + 1.f) + 1e-30f)
-                       : cut + P.one_minus_c * Nq - (2.44140625e-4f * (fabsf(cut) + Nq) + 1e-30f);
-        e_thr = fmaxf(-FLT_MAX, e_thr);
+        set_thr();
       }
     };
-    // Passing references wait in this thread's NB shared-memory slots and are
-    // processed by the whole warp at once when some lane's slots run out (and
-    // at the end), so that the slow path runs with most lanes active instead
-    // of one lane at a time; a deferred reference is judged against the cut
-    // current when it is processed, which only tightens the test.
-    const int et = threadIdx.x - 64;                  // epilogue thread 0 .. 255
-    int nbuf = 0;
+    // Passing references wait in this thread's NB slots and are processed by
+    // the whole warp at once when some lane's slots run out (and at the end of
+    // a segment); a deferred reference is judged against the cut current when
+    // it is processed, which is never above the final one.
     auto flush = [&]() {
       const int nmax = __reduce_max_sync(0xffffffffu, nbuf);
       for (int i = 0; i < nmax; ++i)
@@ -267,10 +312,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
       nbuf = 0;
       __syncwarp();
     };
-    // The hot test of one 32-reference chunk: x = s (cosine) or x = 2 s - w[r]
-    // (euclidean), the maximum as a tree; the mask of the references with
-    // x >= e_thr (0 for an inactive lane), built as a tree of ORs.  Trees keep
-    // the dependent chains five instructions deep.
+    // The hot test of one 32-reference chunk: the mask of the references with
+    // x >= e_thr (0 for an inactive lane); maximum and mask as trees.
     auto hot_mask = [&](const uint32_t (&v)[32], int64_t r0) -> uint32_t {
       if (!active) return 0u;
       float x[32];
@@ -292,18 +335,18 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
 #pragma unroll
       for (int t = 0; t < 16; ++t) m[t] = fmaxf(x[2 * t], x[2 * t + 1]);
 #pragma unroll
-      for (int w = 8; w > 0; w >>= 1)
+      for (int wdt = 8; wdt > 0; wdt >>= 1)
 #pragma unroll
-        for (int t = 0; t < w; ++t) m[t] = fmaxf(m[t], m[t + w]);
+        for (int t = 0; t < wdt; ++t) m[t] = fmaxf(m[t], m[t + wdt]);
       if (!(m[0] >= e_thr)) return 0u;
       uint32_t b[16];
 #pragma unroll
       for (int t = 0; t < 16; ++t)
         b[t] = (x[2 * t] >= e_thr ? 1u << (2 * t) : 0u) | (x[2 * t + 1] >= e_thr ? 2u << (2 * t) : 0u);
 #pragma unroll
-      for (int w = 8; w > 0; w >>= 1)
+      for (int wdt = 8; wdt > 0; wdt >>= 1)
 #pragma unroll
-        for (int t = 0; t < w; ++t) b[t] |= b[t + w];
+        for (int t = 0; t < wdt; ++t) b[t] |= b[t + wdt];
       return b[0];
     };
     // v[jj] as a five-level tree of selects on the bits of jj
@@ -312,9 +355,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
 #pragma unroll
       for (int t = 0; t < 16; ++t) a[t] = (jj & 1) ? v[2 * t + 1] : v[2 * t];
 #pragma unroll
-      for (int lvl = 1, w = 8; w > 0; ++lvl, w >>= 1)
+      for (int lvl = 1, wdt = 8; wdt > 0; ++lvl, wdt >>= 1)
 #pragma unroll
-        for (int t = 0; t < w; ++t) a[t] = ((jj >> lvl) & 1) ? a[2 * t + 1] : a[2 * t];
+        for (int t = 0; t < wdt; ++t) a[t] = ((jj >> lvl) & 1) ? a[2 * t + 1] : a[2 * t];
       return __uint_as_float(a[0]);
     };
     // The passing references of one chunk into this lane's slots (lanes
@@ -341,68 +384,90 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
       }
       __syncwarp();
     };
-    // two chunks at once: their hot tests are independent, so they overlap
-    auto chunk2 = [&](const uint32_t (&va)[32], int64_t ra, const uint32_t (&vb)[32], int64_t rb) {
-      const uint32_t ma = hot_mask(va, ra), mb = hot_mask(vb, rb);
-      if (__any_sync(0xffffffffu, (ma | mb) != 0u)) {
-        take(va, ma, ra);
-        take(vb, mb, rb);
-      }
-    };
 
-    for (int j = 0; j < ntile; ++j) {
-      const int buf = j & 1;
-      const uint32_t aph = (uint32_t)(j >> 1) & 1u;
-      const bool ok = mbar_wait(acc_full + buf, aph, abort_flag, P.status);
-      if (!__all_sync(0xffffffffu, ok)) break;     // the warp leaves together (tcgen05.ld is .aligned)
-      fence_after();
-      const int64_t rtile = (t0 + j) * BN;
-      const uint32_t tb = tmem + lane_base + (uint32_t)((buf * QT + qt) * BN);
-      static_assert(BN % 64 == 0, "pairs of 32-column chunks");
-      if constexpr (KL <= 32) {
-        // chunks in pairs (the TMEM loads take a few tens of cycles; the
-        // pair's hot tests overlap)
+    int64_t j = 0;                                    // tile counter (the MMA's order)
+    bool ok = true;
+    for (int64_t f = f0; f < f1 && ok;) {
+      const int64_t g = f / ntiles;
+      const int64_t fe = min(f1, (g + 1) * ntiles);
+      const int64_t ql = g * BM + row;
+      q = P.q0 + ql;
+      active = ql < P.nq;
+      if (active) active = !P.qempty[q];           // a degenerate query has no list
+      Nq = active ? P.qnorm2[q] : 0.f;
+#pragma unroll
+      for (int i = 0; i < KL; ++i) lst[i] = (i < KL - K) ? INFINITY : -INFINITY;
+      T = -INFINITY;
+      Ts = active ? fkey_value(*(volatile unsigned*)(P.tshared + ql)) : -INFINITY;
+      e_thr = -FLT_MAX;
+      if (Ts > -INFINITY) set_thr();
+      cnt = 0;
+      nbuf = 0;
+      const int64_t slot =
+          active ? (ql * P.nslots + ((int64_t)blockIdx.x - first_cta(g, ntiles, per)) * 2 + half) : 0;
+      my_idx = P.eidx + slot * P.ecap;
+      my_hi = P.ehi + slot * P.ecap;
+      for (; f < fe; ++f, ++j) {
+        const int buf = (int)(j & 1);
+        const bool got = mbar_wait(acc_full + buf, (uint32_t)(j >> 1) & 1u, abort_flag, P.status);
+        if (!__all_sync(0xffffffffu, got)) { ok = false; break; }   // the warp leaves together
+        fence_after();
+        const int64_t r_half = (f - g * ntiles) * BN + half * (BN / 2);
+        const uint32_t tb = tmem + lane_base + (uint32_t)(buf * BN + half * (BN / 2));
+        if constexpr (KL <= 32) {
+          // chunks in pairs (the TMEM loads take a few tens of cycles; the
+          // pair's hot tests overlap)
 #pragma unroll 1
-        for (int hh = 0; hh < BN / 32; hh += 2) {
-          uint32_t va[32], vb[32];
-          tmem_ld32_issue(tb + hh * 32, va);
-          tmem_ld32_issue(tb + hh * 32 + 32, vb);
-          tmem_ld_wait(va);
-          tmem_ld_wait(vb);
-          chunk2(va, rtile + hh * 32, vb, rtile + hh * 32 + 32);
+          for (int hh = 0; hh < BN / 64; hh += 2) {
+            uint32_t va[32], vb[32];
+            tmem_ld32_issue(tb + hh * 32, va);
+            tmem_ld32_issue(tb + hh * 32 + 32, vb);
+            tmem_ld_wait(va);
+            tmem_ld_wait(vb);
+            const uint32_t ma = hot_mask(va, r_half + hh * 32), mb = hot_mask(vb, r_half + hh * 32 + 32);
+            if (__any_sync(0xffffffffu, (ma | mb) != 0u)) {
+              take(va, ma, r_half + hh * 32);
+              take(vb, mb, r_half + hh * 32 + 32);
+            }
+          }
+        } else {
+          // longer lists leave registers for one chunk at a time
+#pragma unroll 1
+          for (int hh = 0; hh < BN / 64; ++hh) {
+            uint32_t va[32];
+            tmem_ld32(tb + hh * 32, va);
+            const uint32_t ma = hot_mask(va, r_half + hh * 32);
+            if (__any_sync(0xffffffffu, ma != 0u)) take(va, ma, r_half + hh * 32);
+          }
         }
-      } else {
-        // longer lists leave registers for one chunk at a time
-#pragma unroll 1
-        for (int hh = 0; hh < BN / 32; ++hh) {
-          uint32_t va[32];
-          tmem_ld32(tb + hh * 32, va);
-          const uint32_t ma = hot_mask(va, rtile + hh * 32);
-          if (__any_sync(0xffffffffu, ma != 0u)) take(va, ma, rtile + hh * 32);
+        fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(acc_empty + buf);
+        if ((j & (SHARE_TILES - 1)) == SHARE_TILES - 1 && active) {
+          // publish this list's running key and take the best one published
+          const unsigned prev = atomicMax(P.tshared + ql, fkey(T));
+          const float best = fmaxf(fkey_value(prev), T);
+          if (best > Ts) { Ts = best; set_thr(); }
         }
       }
-      fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(acc_empty + buf);
-    }
-    flush();
-    if (active) {
-      float* out = P.lists + slot * K;
+      flush();
+      if (active) atomicMax(P.tshared + ql, fkey(T));
+      if (active) {
+        float* out = P.lists + slot * K;
 #pragma unroll
-      for (int i = 0; i < KL; ++i)
-        if (i >= KL - K) out[i - (KL - K)] = lst[i];
-      P.ecount[slot] = cnt;
+        for (int i = 0; i < KL; ++i)
+          if (i >= KL - K) out[i - (KL - K)] = lst[i];
+        P.ecount[slot] = cnt;
+      }
     }
   }
   fence_before();
   __syncthreads();
   fence_after();
-  if (warp == 1) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
-  }
+  if (warp == 1) tmem_dealloc(tmem, TMEM_COLS);
 }
 
-// ---- merge: the final cut of each query over its ranges ---------------------
+// ---- merge: the final cut of each query over its lists ---------------------
 constexpr int MW = 8;   // warps per block
 
 __device__ __forceinline__ void warp_insert_desc_tc(float* lst, int K, int& n, unsigned m, float v, int lane) {
@@ -423,32 +488,44 @@ __device__ __forceinline__ void warp_insert_desc_tc(float* lst, int K, int& n, u
   }
 }
 
-__global__ void k_tc_merge(int64_t q0, int64_t nq, int nrr, int K, int ecap, const uint8_t* empty,
-                           const float* lists, const int32_t* ecount, const int32_t* eidx, const float* ehi,
-                           int cap, int32_t* cand, int32_t* count, int32_t* over) {
+// Per query: T = the k-th largest pessimistic key over the lists of every
+// (segment, half) that covered it (the exact k-th over all references: the top
+// k of a union is the top k of the parts' top k), cut = dense_cut(T); the
+// candidates are the appended references with hi >= cut.
+__global__ void k_tc_merge(int64_t q0, int64_t nq, int64_t ntiles, int64_t per, int64_t nslots, int K, int ecap,
+                           const uint8_t* qempty, const unsigned* tshared, const float* lists,
+                           const int32_t* ecount, const int32_t* eidx, const float* ehi, int cap, int32_t* cand,
+                           int32_t* count, int32_t* over) {
   __shared__ float sl[MW][KT];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t ql = (int64_t)blockIdx.x * MW + warp;
   if (ql >= nq) return;
-  if (empty[q0 + ql]) {
+  if (qempty[q0 + ql]) {
     if (lane == 0) { count[ql] = 0; over[ql] = 0; }
     return;
   }
+  const int64_t g = ql / BM;
+  const int64_t used = 2 * (last_cta(g, ntiles, per) - first_cta(g, ntiles, per) + 1);
   float* lst = sl[warp];
   int n = 0;
-  const float* in = lists + ql * nrr * (int64_t)K;
-  const int64_t tot = (int64_t)nrr * K;
+  const float* in = lists + ql * nslots * (int64_t)K;
+  const int64_t tot = used * K;
   for (int64_t p0 = 0; p0 < tot; p0 += 32) {
     const float v = p0 + lane < tot ? in[p0 + lane] : -INFINITY;
     const unsigned m = __ballot_sync(0xffffffffu, v > -INFINITY && (n < K || v > lst[K - 1]));
     if (m) warp_insert_desc_tc(lst, K, n, m, v, lane);
   }
-  const float cut = dense_cut((n == K) ? lst[K - 1] : -INFINITY);
+  // A list keeps only keys above the shared key it saw, so when some list's
+  // view of the shared key reached the final k-th best, fewer than k keys at
+  // or above it may be listed; the shared key (the k-th best of a subset,
+  // never above the final) then is the final k-th best.
+  const float T = fmaxf((n == K) ? lst[K - 1] : -INFINITY, fkey_value(tshared[ql]));
+  const float cut = dense_cut(T);
   bool ovf = false;
   int total = 0;
   int32_t* out = cand + ql * (int64_t)cap;
-  for (int r = 0; r < nrr && !ovf; ++r) {
-    const int64_t slot = ql * nrr + r;
+  for (int64_t r = 0; r < used && !ovf; ++r) {
+    const int64_t slot = ql * nslots + r;
     const int c = ecount[slot];
     if (c > ecap) { ovf = true; break; }
     for (int p0 = 0; p0 < c; p0 += 32) {
@@ -464,12 +541,17 @@ __global__ void k_tc_merge(int64_t q0, int64_t nq, int nrr, int K, int ecap, con
   if (lane == 0) { count[ql] = ovf ? 0 : total; over[ql] = ovf ? 1 : 0; }
 }
 
+__global__ void k_tc_key_init(int64_t nq, unsigned* keys) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < nq) keys[i] = fkey(-INFINITY);
+}
+
 // w[r]: +inf for degenerate references and the padding; 0 (cosine) or
 // (1 - c) Nr (euclidean) otherwise
-__global__ void k_tc_weights(int method, int64_t n, int64_t npad, float one_minus_c, const float* norm2,
+__global__ void k_tc_weights(int method, int64_t n, int64_t nw, float one_minus_c, const float* norm2,
                              const uint8_t* empty, float* w) {
   const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (r >= npad) return;
+  if (r >= nw) return;
   float v = INFINITY;
   if (r < n && !empty[r]) v = (method == COSINE) ? 0.f : one_minus_c * norm2[r];
   w[r] = v;
@@ -508,55 +590,69 @@ int tc_screen(sdg_ctx* ctx, const sdg_dense* Q, const sdg_dense* D, bool self, i
   if (Q->dpad != D->dpad || Q->n >= (int64_t)1 << 30) return fail(SDG_E_ARG, "query and reference shapes differ");
   const int64_t n = D->n;
   const int dch = D->dpad / BK;
-  // one map per operand: 64-row x 128-column boxes of the K-major BF16 copy
-  // (rows padded to dpad with zeros; columns beyond the matrix read as zero)
-  auto encode = [&](const sdg_dense* M, CUtensorMap* map) {
-    const __nv_bfloat16* base = (method == COSINE) ? M->ubp : M->xbp;
+  // one map per operand: 64-row x 128-column (query) / 256-column (reference)
+  // boxes of the K-major BF16 copy (rows padded to dpad with zeros; columns
+  // beyond the matrix read as zero)
+  auto encode = [&](const sdg_dense* M, int box_cols, CUtensorMap* map) {
+    const __nv_bfloat16* base_ptr = (method == COSINE) ? M->ubp : M->xbp;
     const cuuint64_t gdim[2] = {(cuuint64_t)M->dpad, (cuuint64_t)M->n};
     const cuuint64_t gstride[1] = {(cuuint64_t)M->dpad * 2};
-    const cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)BN};
+    const cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_cols};
     const cuuint32_t estr[2] = {1, 1};
-    return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)base, gdim, gstride, box, estr,
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)base_ptr, gdim, gstride, box, estr,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
   };
   CUtensorMap qmap, rmap;
-  if (!encode(Q, &qmap) || !encode(D, &rmap)) return fail(SDG_E_CUDA, "cuTensorMapEncodeTiled failed");
+  if (!encode(Q, BM, &qmap) || !encode(D, BN, &rmap)) return fail(SDG_E_CUDA, "cuTensorMapEncodeTiled failed");
 
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, D->device);
   if (sms < 1) sms = 1;
-  const int nqg = (int)((nq + QT * BM - 1) / (QT * BM));
+  // (query group, reference tile) items in equal contiguous spans, one per CTA
+  const int64_t G = (nq + BM - 1) / BM;
   const int64_t ntiles = (n + BN - 1) / BN;
-  int nrr = std::max(1, sms / nqg);
-  nrr = (int)std::min<int64_t>(nrr, ntiles);
-  const int tpr = (int)((ntiles + nrr - 1) / nrr);
-  nrr = (int)((ntiles + tpr - 1) / tpr);
+  const int64_t items = G * ntiles;
+  int64_t grid = std::min<int64_t>(sms, items);
+  const int64_t per = (items + grid - 1) / grid;
+  grid = (items + per - 1) / per;
+  // list slots per query: two halves per CTA whose span meets its group
+  int64_t maxc = 1;
+  for (int64_t g = 0; g < G; ++g)
+    maxc = std::max<int64_t>(maxc, last_cta(g, ntiles, per) - first_cta(g, ntiles, per) + 1);
+  const int64_t nslots = 2 * maxc;
   const int ecap = 768;
   const float rel = 0.0040f + (float)D->d * 2.384185791015625e-7f;
   const float omc = 1.f - (rel + 9.5367431640625e-7f);
 
   float *w = nullptr, *lists = nullptr, *ehi = nullptr;
   int32_t *ecount = nullptr, *eidx = nullptr;
+  unsigned* tshared = nullptr;
   int* status = nullptr;
   cudaError_t e = cudaSuccess;
   auto chk = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
-  chk(cudaMallocAsync(&w, sizeof(float) * (size_t)D->npad, s));
-  chk(cudaMallocAsync(&lists, sizeof(float) * (size_t)(nq * nrr * k), s));
-  chk(cudaMallocAsync(&ecount, sizeof(int32_t) * (size_t)(nq * nrr), s));
-  chk(cudaMallocAsync(&eidx, sizeof(int32_t) * (size_t)(nq * nrr * ecap), s));
-  chk(cudaMallocAsync(&ehi, sizeof(float) * (size_t)(nq * nrr * ecap), s));
+  const int64_t nw = ntiles * BN;
+  chk(cudaMallocAsync(&w, sizeof(float) * (size_t)nw, s));
+  chk(cudaMallocAsync(&lists, sizeof(float) * (size_t)(nq * nslots * k), s));
+  chk(cudaMallocAsync(&ecount, sizeof(int32_t) * (size_t)(nq * nslots), s));
+  chk(cudaMallocAsync(&eidx, sizeof(int32_t) * (size_t)(nq * nslots * ecap), s));
+  chk(cudaMallocAsync(&ehi, sizeof(float) * (size_t)(nq * nslots * ecap), s));
   chk(cudaMallocAsync(&status, sizeof(int), s));
+  chk(cudaMallocAsync(&tshared, sizeof(unsigned) * (size_t)nq, s));
   if (e == cudaSuccess) {
     chk(cudaMemsetAsync(status, 0, sizeof(int), s));
-    chk(cudaMemsetAsync(ecount, 0, sizeof(int32_t) * (size_t)(nq * nrr), s));
-    k_tc_weights<<<(unsigned)((D->npad + 255) / 256), 256, 0, s>>>(method, n, D->npad, omc, D->norm2, D->empty, w);
+    // every query's shared key starts at fkey(-inf)
+    k_tc_key_init<<<(unsigned)((nq + 255) / 256), 256, 0, s>>>(nq, tshared);
+    chk(cudaMemsetAsync(ecount, 0, sizeof(int32_t) * (size_t)(nq * nslots), s));
+    k_tc_weights<<<(unsigned)((nw + 255) / 256), 256, 0, s>>>(method, n, nw, omc, D->norm2, D->empty, w);
     TcArgs P;
-    P.method = method; P.k = k; P.dch = dch; P.nqg = nqg; P.nrr = nrr; P.tiles_per_range = tpr; P.ecap = ecap;
+    P.method = method; P.k = k; P.dch = dch; P.ecap = ecap;
     P.self = self ? 1 : 0;
-    P.d = D->d; P.n = n; P.q0 = q0; P.nq = nq; P.ntiles = ntiles;
+    P.d = D->d; P.n = n; P.q0 = q0; P.nq = nq;
+    P.ntiles = ntiles; P.tiles_per_cta = per; P.nslots = nslots;
     P.a = (method == COSINE) ? 1.f : 2.f; P.one_minus_c = omc;
     P.w = w; P.norm2 = D->norm2; P.qnorm2 = Q->norm2; P.qempty = Q->empty;
+    P.tshared = tshared;
     P.lists = lists; P.ecount = ecount; P.eidx = eidx; P.ehi = ehi;
     P.status = status;
     // the list length: the smallest of 16 / 24 / 32 / 48 / 64 that holds k
@@ -564,17 +660,18 @@ int tc_screen(sdg_ctx* ctx, const sdg_dense* Q, const sdg_dense* D, bool self, i
               : (k <= 48) ? k_dense_tc<48> : k_dense_tc<64>;
     chk(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
     sdg_time_begin(ctx);
-    if (e == cudaSuccess) kern<<<(unsigned)(nqg * nrr), THREADS, SMEM_BYTES, s>>>(qmap, rmap, P);
+    if (e == cudaSuccess) kern<<<(unsigned)grid, THREADS, SMEM_BYTES, s>>>(qmap, rmap, P);
     sdg_time_end(ctx);
     chk(cudaGetLastError());
-    k_tc_merge<<<(unsigned)((nq + MW - 1) / MW), MW * 32, 0, s>>>(q0, nq, nrr, k, ecap, Q->empty, lists, ecount,
-                                                                  eidx, ehi, cap, cand, count, over);
+    k_tc_merge<<<(unsigned)((nq + MW - 1) / MW), MW * 32, 0, s>>>(q0, nq, ntiles, per, nslots, k, ecap, Q->empty,
+                                                                  tshared, lists, ecount, eidx, ehi, cap, cand,
+                                                                  count, over);
     chk(cudaGetLastError());
   }
   int hstatus = 0;
   if (e == cudaSuccess) chk(cudaMemcpyAsync(&hstatus, status, sizeof(int), cudaMemcpyDeviceToHost, s));
   if (e == cudaSuccess) chk(cudaStreamSynchronize(s));
-  for (void* p : {(void*)w, (void*)lists, (void*)ecount, (void*)eidx, (void*)ehi, (void*)status})
+  for (void* p : {(void*)w, (void*)lists, (void*)ecount, (void*)eidx, (void*)ehi, (void*)status, (void*)tshared})
     if (p) cudaFreeAsync(p, s);
   if (e != cudaSuccess) {
     set_error(cudaGetErrorString(e));
