@@ -72,16 +72,22 @@ def parse():
     ap.add_argument("--dist-long", action="store_true",
                     help="long columns (the 30,000-row log-count generator)")
     ap.add_argument("--config", default="dense",
-                    choices=["dense", "logcount", "uniform", "serve", "dist", "snn"],
+                    choices=["dense", "logcount", "uniform", "serve", "dist", "snn", "batched"],
                     help="dense: the default line (256 x 2,000,000 embeddings, BF16-screened vs plain "
                          "FP32, served e2e); logcount: 30,000 x 200,000 log-count sparse kNN; uniform: "
                          "the CPU-runnable 2,000 x 10,000 case; serve: the sparse serving loop; dist: "
-                         "full-matrix sparseDist; snn: sparseSNN")
+                         "full-matrix sparseDist; snn: sparseSNN; batched: 512 uneven sparseKNNCross "
+                         "problems through sdg_knn_cross_batch")
     ap.add_argument("--serve-ref-cols", type=int, default=1000000)
     ap.add_argument("--dense-cols", type=int, default=2000000)
     ap.add_argument("--dense-block", type=int, default=4096)
     ap.add_argument("--dense-cpu-cols", type=int, default=128,
                     help="query columns of the dense CPU-baseline / parity sample")
+    ap.add_argument("--batch-problems", type=int, default=512)
+    ap.add_argument("--batch-scale", type=float, default=1.0, help="multiplies the batched problems' column counts")
+    ap.add_argument("--batch-check", type=int, default=16, help="smallest problems checked against the oracle")
+    ap.add_argument("--batch-group", type=int, default=32,
+                    help="problems per sdg_knn_cross_batch call (bounds host memory)")
     ap.add_argument("--ref-cols", type=int, default=16,
                     help="query columns per step of the dense --impl reference arm")
     ap.add_argument("--serve-requests", type=int, default=80)
@@ -607,10 +613,14 @@ def run_dense_main(args):
         clk = ClockSampler(local) if sample_clocks else None
         if clk:
             clk.__enter__()
+        if sample_clocks:
+            torch.cuda.nvtx.range_push("sdg_timed")  # ncu --nvtx --nvtx-include sdg_timed/
         e0.record(stream)
         for s in range(K):
             step(starts[W + s], mode)
         e1.record(stream)
+        if sample_clocks:
+            torch.cuda.nvtx.range_pop()
         torch.cuda.synchronize()
         if clk:
             clk.__exit__()
@@ -638,7 +648,8 @@ def run_dense_main(args):
             "frac": (achieved / bf16_peak) if achieved else None,
             "peak_kind": peak_kind + " (cuBLAS bf16 burst)", "kernel": "k_dense_tc (fused BF16 tcgen05 screen)",
             "flops_per_launch": flops, "kernel_ms_per_launch": per_launch_ms,
-            "launches_per_step": klaunch / max(K, 1), "traffic": DENSE_TRAFFIC}
+            "launches_per_step": klaunch / max(K, 1),
+            "traffic": DENSE_TRAFFIC if (n == 2000000 and B == 4096 and args.method == "cosine") else None}
 
     # e2e: the serving loop with host query vectors, two requests in flight
     e2e = None
@@ -716,9 +727,89 @@ def run_dense_main(args):
         dist.destroy_process_group()
 
 
-# dram__bytes_read.sum + dram__bytes_write.sum of one k_dense_tc launch (ncu, see
-# profiles/); None until captured
-DENSE_TRAFFIC = None
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch of the bounding
+# kernel at the bench's full size, from a one-pass ncu capture
+# (profiles/k_dense_tc_cosine_2000000x256_q4096.md,
+# profiles/launches_logcount_cosine_30000x200000_q4096.md)
+DENSE_TRAFFIC = 7.03e9 + 0.145e9
+LOGCOUNT_TRAFFIC = 65.22e9 + 0.181e9
+
+
+def run_batched(args):
+    """Batched uneven sparseKNNCross problems (the 512-problem draw of
+    synth.cross_draw: nq log-U[100, 50,000], nr log-U[1,000, 200,000], rows
+    U[5,000, 30,000], density log-U[0.1 %, 10 %], methods cycling binary /
+    cosine / manhattan / js, k in {10, 20, 50}) through sdg_knn_cross_batch,
+    --batch-group problems per call (host CSC in, host results out: each call
+    uploads its problems, runs every exact-path search in one persistent
+    launch and the others on the engines the autotuner picks, and copies the
+    results back).  value = forward + reverse query columns / the calls' wall
+    time; the problems are generated on the GPU outside the timed calls.  The
+    smallest problems are checked against the oracle, which also gives the
+    CPU baseline on them."""
+    import torch
+    from sparsedist_gb300 import _lib, synth
+    from oracle import build as obuild
+    from oracle.pyoracle import Oracle
+    specs = synth.cross_draw(args.batch_problems, seed=4, scale=args.batch_scale)
+    ctx = _lib.Context()
+    t_calls, cols, pairs = 0.0, 0, 0.0
+    engines = {}
+    kept = []
+    by_size = sorted(range(len(specs)), key=lambda p: specs[p]["nq"] * specs[p]["nr"])
+    check_set = set(by_size[:args.batch_check])
+    for g0 in range(0, len(specs), args.batch_group):
+        group = specs[g0:g0 + args.batch_group]
+        probs = [synth.cross_problem(sp_) for sp_ in group]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rc, res = _lib.knn_cross_batch(ctx, [(X, Y, METHOD_CODES[sp_["method"]], True, sp_["k"])
+                                             for (X, Y), sp_ in zip(probs, group)])
+        t_calls += time.perf_counter() - t0
+        if rc != 0:
+            raise RuntimeError("sdg_knn_cross_batch: %s" % [r["status"] for r in res])
+        for j, ((X, Y), sp_, r) in enumerate(zip(probs, group, res)):
+            cols += X.shape[1] + Y.shape[1]
+            pairs += 2.0 * X.shape[1] * Y.shape[1]
+            for d, e in zip(("forward", "reverse"), r["engines"]):
+                key = "%s/engine%d" % (sp_["method"], e)
+                engines[key] = engines.get(key, 0) + 1
+            if g0 + j in check_set:
+                kept.append((X, Y, sp_, r))
+        del probs
+    obuild.build_oracle()
+    threads = os.cpu_count() or 1
+    orc = Oracle(threads=threads)
+    identical, close, total = 0, 0, 0
+    t_cpu, cpu_cols = 0.0, 0
+    for X, Y, sp_, r in kept:
+        t0 = time.perf_counter()
+        (wfi, wfd), (wri, wrd), _ = orc.knn_cross(X, Y, k=sp_["k"], method=sp_["method"])
+        t_cpu += time.perf_counter() - t0
+        cpu_cols += X.shape[1] + Y.shape[1]
+        total += 1
+        same = all(np.array_equal(a, b) for a, b in ((r["forward"][0], wfi), (r["reverse"][0], wri))) and all(
+            np.array_equal(a.view(np.uint64), b.view(np.uint64)) for a, b in ((r["forward"][1], wfd), (r["reverse"][1], wrd)))
+        identical += int(same)
+        if not same:
+            ok = all(np.allclose(a, b, rtol=1e-12, atol=0, equal_nan=True)
+                     for a, b in ((r["forward"][1], wfd), (r["reverse"][1], wrd)))
+            close += int(ok)
+    print(json.dumps({
+        "metric": "batched sparseKNNCross query columns/s (%d uneven problems, forward + reverse, e2e through "
+                  "sdg_knn_cross_batch)" % len(specs),
+        "value": cols / t_calls, "unit": "columns/s", "n_gpus": 1, "higher_is_better": True,
+        "seconds": t_calls, "columns": cols, "pairs": pairs, "calls": (len(specs) + args.batch_group - 1) // args.batch_group,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "synth.cross_draw(%d, seed=4, scale=%g): nq log-U[100,50000], nr log-U[1000,200000], "
+                               "rows U[5000,30000], density log-U[0.1%%,10%%], binary/cosine/manhattan/js, "
+                               "k in {10,20,50}" % (len(specs), args.batch_scale),
+                   "problems_per_call": args.batch_group},
+        "engines": engines,
+        "parity": {"problems": total, "bit_identical": identical, "js_within_1e-12": close,
+                   "vs": "oracle (the reference's algorithm), the %d smallest problems" % total},
+        "cpu_baseline": {"value": cpu_cols / t_cpu if t_cpu else None, "unit": "columns/s", "cores": threads,
+                         "kind": "port", "sample": "the %d smallest problems, forward + reverse" % total}}))
 
 
 def main():
@@ -740,6 +831,9 @@ def main():
         return
     if args.config == "snn":
         run_snn(args)
+        return
+    if args.config == "batched":
+        run_batched(args)
         return
     if args.impl == "reference":
         run_reference(args)
@@ -834,7 +928,8 @@ def run_logcount(args):
         roof = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "peak_kind": peak_kind, "kernel": "k_screen", "alg_bytes_per_launch": alg / launches_per_step}
     roof["frac"] = (roof["achieved"] / roof["peak"]) if roof["achieved"] else None
-    roof["traffic"] = None
+    roof["traffic"] = LOGCOUNT_TRAFFIC if (roof["bound"] == "tensor" and args.ncol == 200000 and
+                                          args.nrow == 30000 and B == 4096) else None
     roof["kernel_ms_per_launch"] = per_launch_ms
     # the sparse-slab figure of merit (operand bytes a pairwise merge walk streams)
     roof["sparse_alg_gbs"] = achieved

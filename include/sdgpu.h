@@ -175,6 +175,28 @@ SDG_API int sdg_knn_cross(sdg_ctx* ctx, const sdg_csc* X, const sdg_csc* Y, int 
                           int32_t* fwd_idx, double* fwd_dist, int32_t* rev_idx,
                           double* rev_dist, int* k_fwd, int* k_rev, int* flags);
 
+/* Many independent sparseKNNCross problems in one call: problem p is
+ * sparseKNNCross(X[p], Y[p], k[p], method[p], dist[p], drop_degenerate), with
+ * its results written to fwd_idx[p] / fwd_dist[p] (ncol(X[p]) * k[p] values)
+ * and rev_idx[p] / rev_dist[p] (ncol(Y[p]) * k[p]), clamped k in k_fwd[p] /
+ * k_rev[p], warnings in flags[p] and the problem's own status in status[p] (a
+ * failing problem leaves the others untouched; the call returns the first
+ * failure's code and message, or SDG_OK).  An autotuner picks each search
+ * direction's engine (exact FP64, FP32 sparse screen or tensor-core screen)
+ * from the problem's shape, with corrections learned from measured times
+ * and kept per shape class for the process; every exact-path search of the
+ * call (up to a device-memory budget per wave of problems) runs in ONE
+ * persistent launch over a work queue of (problem, direction, query column,
+ * reference range) items sized by their merge-walk cost.  engines (optional,
+ * 2 * nprob) receives the engine of each problem's forward and reverse
+ * search.  Replaces a loop of R/sparseKNNCross.R:44-199 over the problems;
+ * each problem's result equals sdg_knn_cross's. */
+SDG_API int sdg_knn_cross_batch(sdg_ctx* ctx, int nprob, const sdg_csc* X, const sdg_csc* Y,
+                                const int* method, const int* dist, const int* k, int drop_degenerate,
+                                int32_t* const* fwd_idx, double* const* fwd_dist,
+                                int32_t* const* rev_idx, double* const* rev_dist, int* k_fwd,
+                                int* k_rev, int* flags, int* status, int* engines);
+
 /* sparseSNN(idx, include_self, prune, symmetrise, edges = "knn") as the slots
  * of the n x n dgCMatrix.  Call once with p == NULL to learn *nnz, then with
  * p (n + 1), i and x (nnz each).  The size query keeps its graph on the

@@ -33,6 +33,7 @@ EXPORTED = ["sdg_version", "sdg_last_error", "sdg_ctx_create", "sdg_ctx_destroy"
             "sdg_server_cancel", "sdg_server_stats", "sdg_server_destroy",
             "sdg_matrix_upload_device", "sdg_dense_upload", "sdg_dense_free", "sdg_dense_knn_block",
             "sdg_dense_knn_query", "sdg_server_create_dense", "sdg_server_submit_dense",
+            "sdg_knn_cross_batch",
             "sdg_snn_graph_shared"]
 
 
@@ -102,6 +103,7 @@ def load() -> C.CDLL:
             lib.sdg_server_create.argtypes = [v, v, C.c_int, C.c_int, C.c_int64, v, C.c_int,
                                               C.POINTER(v)]
             lib.sdg_server_submit.argtypes = [v, v, C.c_int, C.c_int, C.c_int, C.c_int, v]
+            lib.sdg_knn_cross_batch.argtypes = [v, C.c_int, v, v, v, v, v, C.c_int, v, v, v, v, v, v, v, v, v]
             lib.sdg_server_create_dense.argtypes = [v, v, C.c_int, C.c_int, C.c_int64, C.POINTER(v)]
             lib.sdg_server_submit_dense.argtypes = [v, v, C.c_int32, C.c_int32, C.c_int, C.c_int, v]
             lib.sdg_server_wait.argtypes = [v, C.c_int64, C.c_int]
@@ -324,6 +326,41 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def knn_cross_batch(ctx, problems, drop_degenerate=True):
+    """sdg_knn_cross_batch over a list of (X, Y, method_code, dist, k) with X, Y
+    scipy CSC matrices.  Returns one dict per problem: forward / reverse
+    (idx, dist) as (n, k_eff) arrays, flags, status (0 or the sdg_status) and
+    the engines chosen for the two directions."""
+    n = len(problems)
+    held = [(HeldCSC(X.shape[0], X.shape[1], X.indptr, X.indices, X.data),
+             HeldCSC(Y.shape[0], Y.shape[1], Y.indptr, Y.indices, Y.data)) for X, Y, _, _, _ in problems]
+    Xs = (CSC * max(n, 1))(*[h[0].s for h in held])
+    Ys = (CSC * max(n, 1))(*[h[1].s for h in held])
+    meth = np.array([p[2] for p in problems] or [0], np.int32)
+    dist = np.array([int(bool(p[3])) for p in problems] or [0], np.int32)
+    ks = np.array([p[4] for p in problems] or [1], np.int32)
+    outs = []
+    for (X, Y, _, _, k) in problems:
+        outs.append((np.empty(max(X.shape[1] * k, 1), np.int32), np.empty(max(X.shape[1] * k, 1), np.float64),
+                     np.empty(max(Y.shape[1] * k, 1), np.int32), np.empty(max(Y.shape[1] * k, 1), np.float64)))
+    ptrs = [(C.c_void_p * max(n, 1))(*[o[j].ctypes.data for o in outs]) for j in range(4)]
+    kf, kr, fl, st = (np.zeros(max(n, 1), np.int32) for _ in range(4))
+    eng = np.zeros(2 * max(n, 1), np.int32)
+    rc = ctx.lib.sdg_knn_cross_batch(ctx.handle, n, C.cast(Xs, C.c_void_p), C.cast(Ys, C.c_void_p),
+                                     meth.ctypes.data, dist.ctypes.data, ks.ctypes.data, int(bool(drop_degenerate)),
+                                     C.cast(ptrs[0], C.c_void_p), C.cast(ptrs[1], C.c_void_p),
+                                     C.cast(ptrs[2], C.c_void_p), C.cast(ptrs[3], C.c_void_p), kf.ctypes.data,
+                                     kr.ctypes.data, fl.ctypes.data, st.ctypes.data, eng.ctypes.data)
+    res = []
+    for p, (X, Y, _, _, k) in enumerate(problems):
+        nx, ny, a, b = X.shape[1], Y.shape[1], int(kf[p]), int(kr[p])
+        fi, fd, ri, rd = outs[p]
+        res.append({"forward": (fi[:nx * a].reshape(a, nx).T.copy(), fd[:nx * a].reshape(a, nx).T.copy()),
+                    "reverse": (ri[:ny * b].reshape(b, ny).T.copy(), rd[:ny * b].reshape(b, ny).T.copy()),
+                    "flags": int(fl[p]), "status": int(st[p]), "engines": (int(eng[2 * p]), int(eng[2 * p + 1]))})
+    return rc, res
 
 
 def na_real(shape) -> np.ndarray:

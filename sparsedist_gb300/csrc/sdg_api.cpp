@@ -14,7 +14,10 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
+#include <tuple>
 #include <new>
 #include <string>
 #include <vector>
@@ -1181,6 +1184,355 @@ SDG_API int sdg_knn_resident(sdg_ctx* c, const sdg_matrix* X, const sdg_matrix* 
     CK(cudaMemcpyAsync(idx, hi.p, sizeof(int32_t) * cnt, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(dist_out, hv.p, sizeof(double) * cnt, cudaMemcpyDeviceToHost, c->stream));
     end_stats(c);
+  });
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// batched sparseKNNCross: many independent problems, an autotuned engine per
+// search direction, one persistent launch for every exact-path search
+// ---------------------------------------------------------------------------
+namespace {
+
+// The features that decide an engine, bucketed on a log2 scale: searches of
+// one shape class take the same engine and share the learned corrections.
+struct ShapeClass {
+  int method, lq, lr, ln, lk;
+  bool operator<(const ShapeClass& o) const {
+    return std::tie(method, lq, lr, ln, lk) < std::tie(o.method, o.lq, o.lr, o.ln, o.lk);
+  }
+};
+
+int ilog2(double v) { return v < 1.0 ? 0 : (int)std::floor(std::log2(v)); }
+
+// One search direction of one problem: nq query columns against nr reference
+// columns of nrow rows.
+struct SearchShape {
+  int method = 0, k = 1;
+  int64_t nq = 0, nr = 0, nnz_q = 0, nnz_r = 0;
+  int32_t nrow = 0;
+  ShapeClass cls() const {
+    const double per_col = nr > 0 ? (double)nnz_r / (double)nr : 0.0;
+    return ShapeClass{method, ilog2((double)nq), ilog2((double)nr), ilog2(per_col), ilog2((double)k)};
+  }
+};
+
+// Engine choice per search direction.  A cost model predicts each engine's
+// time from the shape (merge steps of the exact walk at the measured exact
+// rate; screened stored entries and slab bytes of the FP32 screen; dense flops
+// and copy bytes of the tensor screen), corrected per (shape class, engine) by
+// the ratio of measured to predicted time (exponential average, learned from
+// every timed search and kept for the process); an engine a class has not
+// tried yet is tried once when its prediction is within 2x of the best.  The
+// persistent exact launch's work-item size (merge steps per item) is tuned the
+// same way over {2^20, 2^22, 2^24}.
+struct Autotuner {
+  std::mutex mu;
+  std::map<std::pair<ShapeClass, int>, std::pair<double, int>> corr;   // (ratio, samples)
+  double exact_rate = 2.0e11;            // merge steps per second, batched exact kernel
+  std::map<int, std::pair<double, int>> item_rate;                      // log2 size -> (steps/s, samples)
+
+  static double predict(int engine, const SearchShape& sh) {
+    const double nq = (double)sh.nq, nr = (double)sh.nr;
+    if (engine == 1) return 0.0;                                        // scaled by exact_rate
+    if (engine == 2) return nq / 16.0 * (double)sh.nnz_r / 1.1e11 + nq * nr * 8.0 / 4.0e12 + 2e-3;
+    const double ld = std::ceil((double)sh.nrow / 64.0) * 64.0;
+    return 2.0 * ld * nq * nr / 1.9e15 + ld * (nq + nr) * 2.0 / 3.0e12 + 3e-3;
+  }
+  double predict_exact(const SearchShape& sh) const {
+    return ((double)sh.nr * (double)sh.nnz_q + (double)sh.nq * (double)sh.nnz_r) / exact_rate;
+  }
+  double cost(int engine, const SearchShape& sh) {
+    const double base = engine == 1 ? predict_exact(sh) : predict(engine, sh);
+    auto it = corr.find({sh.cls(), engine});
+    return base * (it == corr.end() ? 1.0 : it->second.first);
+  }
+  int choose(const SearchShape& sh, const std::vector<int>& engines) {
+    std::lock_guard<std::mutex> lock(mu);
+    int best = engines.front();
+    double bc = cost(best, sh);
+    for (int e : engines) {
+      const double c = cost(e, sh);
+      if (c < bc) { bc = c; best = e; }
+    }
+    for (int e : engines)
+      if (e != best && corr.find({sh.cls(), e}) == corr.end() && cost(e, sh) <= 2.0 * bc) return e;
+    return best;
+  }
+  void learn(int engine, const SearchShape& sh, double seconds) {
+    std::lock_guard<std::mutex> lock(mu);
+    const double pred = engine == 1 ? predict_exact(sh) : predict(engine, sh);
+    if (!(pred > 0.0) || !(seconds > 0.0)) return;
+    auto& c = corr[{sh.cls(), engine}];
+    const double r = seconds / pred;
+    c.first = c.second == 0 ? r : 0.7 * c.first + 0.3 * r;
+    ++c.second;
+  }
+  int item_log2() {
+    std::lock_guard<std::mutex> lock(mu);
+    for (int l : {22, 20, 24})
+      if (item_rate.find(l) == item_rate.end()) return l;
+    int best = 22;
+    double br = 0.0;
+    for (auto& kv : item_rate)
+      if (kv.second.first > br) { br = kv.second.first; best = kv.first; }
+    return best;
+  }
+  void learn_exact(int l, double steps, double seconds) {
+    std::lock_guard<std::mutex> lock(mu);
+    if (!(steps > 0.0) || !(seconds > 0.0)) return;
+    const double rate = steps / seconds;
+    auto& r = item_rate[l];
+    r.first = r.second == 0 ? rate : 0.7 * r.first + 0.3 * rate;
+    ++r.second;
+    exact_rate = 0.7 * exact_rate + 0.3 * rate;
+  }
+};
+
+Autotuner& autotuner() {
+  static Autotuner t;
+  return t;
+}
+
+// engines that can run a search: 1 (exact) always where k fits the batched
+// launch, 2 and 3 where the method and k admit the screens
+std::vector<int> candidate_engines(const SearchShape& sh, bool drop) {
+  (void)drop;
+  std::vector<int> e;
+  if (sh.k <= kBatchMaxK) e.push_back(1);
+  if (screen_supported(sh.method, sh.k) && screen_fits(sh.nrow)) {
+    e.push_back(2);
+    const double density = (sh.nrow > 0 && sh.nr > 0) ? (double)sh.nnz_r / ((double)sh.nrow * (double)sh.nr) : 0.0;
+    if (tensor_supported(sh.method) && stc_supported(sh.k) && density >= 0.005) {
+      const size_t bytes = tensor_cache_bytes(sh.nrow, sh.nr) + tensor_cache_bytes(sh.nrow, sh.nq);
+      size_t fr = 0, tot = 0;
+      if (cudaMemGetInfo(&fr, &tot) == cudaSuccess && bytes <= fr / 2) e.push_back(3);
+      cudaGetLastError();
+    }
+  }
+  if (e.empty()) e.push_back(sh.k <= kMaxK ? 2 : 1);
+  return e;
+}
+
+double elapsed_s(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  CK(cudaEventSynchronize(b));
+  CK(cudaEventElapsedTime(&ms, a, b));
+  return ms / 1000.0;
+}
+
+}  // namespace
+
+extern "C" {
+
+SDG_API int sdg_knn_cross_batch(sdg_ctx* c, int nprob, const sdg_csc* X, const sdg_csc* Y, const int* method,
+                                const int* dist, const int* k, int drop_degenerate, int32_t* const* fwd_idx,
+                                double* const* fwd_dist, int32_t* const* rev_idx, double* const* rev_dist,
+                                int* k_fwd, int* k_rev, int* flags, int* status, int* engines) {
+  return guarded([&] {
+    if (!c || nprob < 0 || (nprob > 0 && (!X || !Y || !method || !dist || !k || !fwd_idx || !fwd_dist ||
+                                          !rev_idx || !rev_dist || !k_fwd || !k_rev || !flags || !status)))
+      fail(SDG_E_ARG, "NULL argument");
+    CK(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    // per-problem validation on the host, in the reference's order
+    // (R/sparseKNNCross.R:44-127); a failing problem keeps its own status
+    std::string first_err;
+    int first_code = SDG_OK;
+    auto record = [&](int p, int code) {
+      status[p] = code;
+      if (code != SDG_OK && first_code == SDG_OK) { first_code = code; first_err.assign(g_err.data(), g_err.size()); }
+    };
+    std::vector<int> ok_probs;
+    for (int p = 0; p < nprob; ++p) {
+      flags[p] = 0; k_fwd[p] = 0; k_rev[p] = 0;
+      if (engines) engines[2 * p] = engines[2 * p + 1] = 0;
+      record(p, guarded([&] {
+        check_counts(k[p], 1, 0);
+        check_method(method[p], dist[p]);
+        check_csc_host(&X[p], "X");
+        check_csc_host(&Y[p], "Y");
+        if (X[p].nrow != Y[p].nrow) fail(SDG_E_ROWS, "'X' and 'Y' must have the same number of rows.");
+        if (X[p].ncol < 1) fail(SDG_E_ARG, "'X' must have at least one column.");
+        if (Y[p].ncol < 1) fail(SDG_E_ARG, "'Y' must have at least one column.");
+      }));
+      if (status[p] == SDG_OK) ok_probs.push_back(p);
+    }
+    // waves of problems within a device-memory budget
+    size_t fr = 0, tot = 0;
+    CK(cudaMemGetInfo(&fr, &tot));
+    const int64_t budget = std::max<int64_t>((int64_t)1 << 30, std::min<int64_t>((int64_t)fr / 2, (int64_t)64 << 30));
+    size_t w0 = 0;
+    Autotuner& T = autotuner();
+    while (w0 < ok_probs.size()) {
+      std::vector<int> wave;
+      int64_t used = 0;
+      for (size_t w = w0; w < ok_probs.size(); ++w) {
+        const int p = ok_probs[w];
+        const int64_t nnz = (int64_t)X[p].p[X[p].ncol] + Y[p].p[Y[p].ncol];
+        const int64_t need = nnz * 32 + ((int64_t)X[p].ncol + Y[p].ncol) * (16 + 12 * (int64_t)k[p]);
+        if (!wave.empty() && used + need > budget) break;
+        wave.push_back(p);
+        used += need;
+      }
+      w0 += wave.size();
+      struct Held {
+        int p;
+        std::unique_ptr<sdg_matrix> xm, ym;
+        DevBuf fi, fv, ri, rv;
+        int ef = 0, er = 0;
+        SearchShape fs, rs;
+        std::vector<uint8_t> xe, ye;
+      };
+      std::vector<Held> held;
+      held.reserve(wave.size());
+      std::vector<BatchProb> probs;
+      std::vector<int> prob_of;                       // index into held of each BatchProb
+      cudaEvent_t e0 = c->ev[2], e1 = c->ev[3];
+      for (int p : wave) {
+        Held h;
+        h.p = p;
+        const int st = guarded([&] {
+          h.xm = upload(c, &X[p], "X");
+          h.ym = upload(c, &Y[p], "Y");
+          ensure_empty(h.xm.get());
+          ensure_empty(h.ym.get());
+          const bool drop = drop_degenerate != 0;
+          const int64_t av_f = drop ? h.ym->ncol - h.ym->n_empty : h.ym->ncol;
+          const int64_t av_r = drop ? h.xm->ncol - h.xm->n_empty : h.xm->ncol;
+          if (av_f < 1) fail(SDG_E_NOCAND, "No candidate neighbours available for the forward direction.");
+          if (av_r < 1) fail(SDG_E_NOCAND, "No candidate neighbours available for the reverse direction.");
+          prepare(method[p], h.ym.get(), h.xm.get());
+          int kf = k[p], kr = k[p];
+          if (kf > av_f) { kf = (int)av_f; flags[p] |= SDG_WARN_CLAMP_FWD; }
+          if (kr > av_r) { kr = (int)av_r; flags[p] |= SDG_WARN_CLAMP_REV; }
+          k_fwd[p] = kf; k_rev[p] = kr;
+          const int64_t nx = h.xm->ncol, ny = h.ym->ncol;
+          h.fs = SearchShape{method[p], kf, nx, ny, h.xm->nnz, h.ym->nnz, h.xm->nrow};
+          h.rs = SearchShape{method[p], kr, ny, nx, h.ym->nnz, h.xm->nnz, h.xm->nrow};
+          h.ef = T.choose(h.fs, candidate_engines(h.fs, drop));
+          h.er = T.choose(h.rs, candidate_engines(h.rs, drop));
+          if (engines) { engines[2 * p] = h.ef; engines[2 * p + 1] = h.er; }
+          h.fi = DevBuf(sizeof(int32_t) * (size_t)(nx * kf), s);
+          h.fv = DevBuf(sizeof(double) * (size_t)(nx * kf), s);
+          h.ri = DevBuf(sizeof(int32_t) * (size_t)(ny * kr), s);
+          h.rv = DevBuf(sizeof(double) * (size_t)(ny * kr), s);
+          // the screened searches run now, one at a time (each fills the GPU)
+          const int saved = c->engine;
+          for (int dir = 0; dir < 2; ++dir) {
+            const int eng = dir == 0 ? h.ef : h.er;
+            if (eng == 1) continue;
+            c->engine = eng;
+            int ke = 0, fl = 0;
+            DevBuf hi_, hv_;
+            CK(cudaEventRecord(e0, s));
+            if (dir == 0)
+              knn_device(c, h.xm.get(), h.ym.get(), method[p], dist[p], k[p], 0, drop_degenerate, true, 0,
+                         h.fi.as<int32_t>(), h.fv.as<double>(), &ke, &fl, &hi_, &hv_);
+            else
+              knn_device(c, h.ym.get(), h.xm.get(), method[p], dist[p], k[p], 0, drop_degenerate, true, 1,
+                         h.ri.as<int32_t>(), h.rv.as<double>(), &ke, &fl, &hi_, &hv_);
+            CK(cudaEventRecord(e1, s));
+            c->engine = saved;
+            T.learn(eng, dir == 0 ? h.fs : h.rs, elapsed_s(e0, e1));
+          }
+          if (h.ef == 1 || h.er == 1) {
+            h.xe.resize((size_t)nx);
+            h.ye.resize((size_t)ny);
+            CK(cudaMemcpyAsync(h.xe.data(), h.xm->empty.p, (size_t)nx, cudaMemcpyDeviceToHost, s));
+            CK(cudaMemcpyAsync(h.ye.data(), h.ym->empty.p, (size_t)ny, cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            BatchProb b;
+            b.X = h.xm->dev(); b.Y = h.ym->dev();
+            b.xa = aux_of(h.xm.get()); b.ya = aux_of(h.ym.get());
+            b.method = method[p]; b.dist = dist[p]; b.decreasing = decreasing_for(method[p], dist[p]) ? 1 : 0;
+            b.kf = kf; b.kr = kr;
+            b.xmask = drop ? h.xm->empty.as<uint8_t>() : nullptr;
+            b.ymask = drop ? h.ym->empty.as<uint8_t>() : nullptr;
+            b.fidx = h.fi.as<int32_t>(); b.fval = h.fv.as<double>();
+            b.ridx = h.ri.as<int32_t>(); b.rval = h.rv.as<double>();
+            probs.push_back(b);
+            prob_of.push_back((int)held.size());
+          }
+        });
+        record(p, st);
+        if (st == SDG_OK) held.push_back(std::move(h));
+      }
+      // the exact-path searches of the wave: one persistent launch
+      if (!probs.empty()) {
+        const int lg = T.item_log2();
+        std::vector<BatchItem> items;
+        std::vector<BatchRow> rows;
+        double total_steps = 0.0;
+        int kmax = 1;
+        for (size_t b = 0; b < probs.size(); ++b) {
+          Held& h = held[(size_t)prob_of[b]];
+          for (int dir = 0; dir < 2; ++dir) {
+            if ((dir == 0 ? h.ef : h.er) != 1) continue;
+            const sdg_csc& Qc = dir == 0 ? X[h.p] : Y[h.p];
+            const sdg_csc& Rc = dir == 0 ? Y[h.p] : X[h.p];
+            const std::vector<uint8_t>& qe = dir == 0 ? h.xe : h.ye;
+            const int kk = dir == 0 ? probs[b].kf : probs[b].kr;
+            kmax = std::max(kmax, kk);
+            const int64_t nnz_r = Rc.p[Rc.ncol];
+            for (int32_t q = 0; q < Qc.ncol; ++q) {
+              BatchRow rw;
+              rw.prob = (int32_t)b; rw.dir = dir; rw.q = q; rw.nparts = 0; rw.part0 = (int64_t)items.size();
+              if (!(drop_degenerate && qe[(size_t)q])) {
+                const double steps = (double)Rc.ncol * (double)(Qc.p[q + 1] - Qc.p[q]) + (double)nnz_r;
+                total_steps += steps;
+                const int64_t parts = std::max<int64_t>(
+                    1, std::min<int64_t>((Rc.ncol + 31) / 32, (int64_t)std::ceil(steps / std::ldexp(1.0, lg))));
+                for (int64_t t = 0; t < parts; ++t) {
+                  BatchItem it;
+                  it.prob = (int32_t)b; it.dir = dir; it.q = q; it.pad = 0;
+                  it.r0 = (int32_t)(Rc.ncol * t / parts);
+                  it.r1 = (int32_t)(Rc.ncol * (t + 1) / parts);
+                  it.part = (int64_t)items.size();
+                  items.push_back(it);
+                }
+                rw.nparts = (int32_t)parts;
+              }
+              rows.push_back(rw);
+            }
+          }
+        }
+        DevBuf dp(sizeof(BatchProb) * probs.size(), s), di(sizeof(BatchItem) * std::max<size_t>(1, items.size()), s);
+        DevBuf dr(sizeof(BatchRow) * rows.size(), s), dc(sizeof(unsigned long long), s);
+        const size_t slots = std::max<size_t>(1, items.size()) * (size_t)kmax;
+        DevBuf pk(slots * 8, s), pi(slots * 4, s), pv(slots * 8, s);
+        CK(cudaMemcpyAsync(dp.p, probs.data(), sizeof(BatchProb) * probs.size(), cudaMemcpyHostToDevice, s));
+        if (!items.empty())
+          CK(cudaMemcpyAsync(di.p, items.data(), sizeof(BatchItem) * items.size(), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dr.p, rows.data(), sizeof(BatchRow) * rows.size(), cudaMemcpyHostToDevice, s));
+        CK(cudaMemsetAsync(dc.p, 0, sizeof(unsigned long long), s));
+        CK(cudaEventRecord(e0, s));
+        launch_batch_exact(dp.as<BatchProb>(), di.as<BatchItem>(), (int64_t)items.size(), dc.as<unsigned long long>(),
+                           kmax, pk.as<uint64_t>(), pi.as<int32_t>(), pv.as<double>(), sms, s);
+        CK(cudaEventRecord(e1, s));
+        launch_batch_merge(dp.as<BatchProb>(), dr.as<BatchRow>(), (int64_t)rows.size(), kmax, pk.as<uint64_t>(),
+                           pi.as<int32_t>(), pv.as<double>(), s);
+        CK(cudaGetLastError());
+        const double secs = elapsed_s(e0, e1);
+        T.learn_exact(lg, total_steps, secs);
+        c->stats[1] += (int64_t)total_steps;
+        c->stats[3] += 2;
+      }
+      // results to the caller's host buffers
+      for (Held& h : held) {
+        const int p = h.p;
+        const size_t cf = (size_t)h.xm->ncol * (size_t)k_fwd[p], cr = (size_t)h.ym->ncol * (size_t)k_rev[p];
+        CK(cudaMemcpyAsync(fwd_idx[p], h.fi.p, sizeof(int32_t) * cf, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(fwd_dist[p], h.fv.p, sizeof(double) * cf, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(rev_idx[p], h.ri.p, sizeof(int32_t) * cr, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(rev_dist[p], h.rv.p, sizeof(double) * cr, cudaMemcpyDeviceToHost, s));
+      }
+      CK(cudaStreamSynchronize(s));
+    }
+    if (first_code != SDG_OK) fail(first_code, first_err);
   });
 }
 

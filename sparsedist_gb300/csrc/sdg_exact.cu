@@ -8,6 +8,7 @@
 #include <cmath>
 
 #include "sdg_kernels.h"
+#include "sdg_topk.cuh"
 
 namespace sdg {
 namespace {
@@ -704,6 +705,102 @@ inline unsigned blocks_for(int64_t n, int threads) {
   return (unsigned)((n + threads - 1) / threads);
 }
 
+// ---- batched exact kNN of many independent problems ------------------------
+//
+// One persistent launch serves every (problem, direction, query column,
+// reference range) item of a batch: a warp takes the next item from a global
+// counter, computes the exact FP64 value of each pair of its range (one pair
+// per lane, the reference's arithmetic through pair_value, reference column
+// first as in the slab) and keeps the item's top k under the reference's
+// comparator (topk::insert_batch); the item's list goes to its partial slot.
+// k_batch_merge then takes each output row's top k over its items' lists:
+// the top k of a union is the top k of the parts' top k, so the rows equal
+// topKBlock / topKRowsAccum over whole slabs (src/topK.cpp:104-148,
+// src/topKRows.cpp:201-248).
+constexpr int BATCH_WARPS = 8;
+
+__global__ void __launch_bounds__(BATCH_WARPS * 32) k_batch_exact(const BatchProb* probs, const BatchItem* items,
+                                                                  int64_t nitems, unsigned long long* counter,
+                                                                  int kmax, uint64_t* pkey, int32_t* pidx,
+                                                                  double* pval) {
+  extern __shared__ unsigned char bsm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint64_t* lk = reinterpret_cast<uint64_t*>(bsm) + (int64_t)warp * kmax;
+  double* lv = reinterpret_cast<double*>(bsm) + (int64_t)BATCH_WARPS * kmax + (int64_t)warp * kmax;
+  int32_t* li = reinterpret_cast<int32_t*>(reinterpret_cast<double*>(bsm) + 2 * (int64_t)BATCH_WARPS * kmax) +
+                (int64_t)warp * kmax;
+  for (;;) {
+    unsigned long long it = 0;
+    if (lane == 0) it = atomicAdd(counter, 1ull);
+    it = __shfl_sync(topk::FULL, it, 0);
+    if (it >= (unsigned long long)nitems) break;
+    const BatchItem I = items[it];
+    const BatchProb& P = probs[I.prob];
+    const bool fwd = I.dir == 0;
+    const DevCsc R = fwd ? P.Y : P.X, Q = fwd ? P.X : P.Y;
+    const ColAux ra = fwd ? P.ya : P.xa, qa = fwd ? P.xa : P.ya;
+    const uint8_t* rmask = fwd ? P.ymask : P.xmask;
+    const int K = fwd ? P.kf : P.kr;
+    const bool dec = P.decreasing != 0;
+    int n = 0;
+    for (int32_t b = I.r0; b < I.r1; b += 32) {
+      const int32_t r = b + lane;
+      bool ok = r < I.r1 && !(rmask && rmask[r]);
+      double v = 0.0;
+      if (ok) {
+        v = pair_value(P.method, P.dist != 0, R, ra, r, Q, qa, I.q);
+        ok = isfinite(v);
+      }
+      topk::insert_batch(ok, ok ? order_key(v, dec) : 0, r, v, lk, li, lv, n, K, lane);
+    }
+    const int64_t base = I.part * (int64_t)kmax;
+    for (int t = lane; t < K; t += 32) {
+      pkey[base + t] = (t < n) ? lk[t] : ~0ull;
+      pidx[base + t] = (t < n) ? li[t] : 0;
+      pval[base + t] = (t < n) ? lv[t] : 0.0;
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void __launch_bounds__(BATCH_WARPS * 32) k_batch_merge(const BatchProb* probs, const BatchRow* rows,
+                                                                  int64_t nrows, int kmax, const uint64_t* pkey,
+                                                                  const int32_t* pidx, const double* pval) {
+  extern __shared__ unsigned char bsm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t rw = (int64_t)blockIdx.x * BATCH_WARPS + warp;
+  if (rw >= nrows) return;
+  uint64_t* lk = reinterpret_cast<uint64_t*>(bsm) + (int64_t)warp * kmax;
+  double* lv = reinterpret_cast<double*>(bsm) + (int64_t)BATCH_WARPS * kmax + (int64_t)warp * kmax;
+  int32_t* li = reinterpret_cast<int32_t*>(reinterpret_cast<double*>(bsm) + 2 * (int64_t)BATCH_WARPS * kmax) +
+                (int64_t)warp * kmax;
+  const BatchRow W = rows[rw];
+  const BatchProb& P = probs[W.prob];
+  const bool fwd = W.dir == 0;
+  const int K = fwd ? P.kf : P.kr;
+  const int64_t ld = fwd ? P.X.ncol : P.Y.ncol;
+  int32_t* oi = fwd ? P.fidx : P.ridx;
+  double* ov = fwd ? P.fval : P.rval;
+  const uint8_t* qmask = fwd ? P.xmask : P.ymask;
+  int n = 0;
+  if (!(qmask && qmask[W.q])) {
+    for (int64_t part = W.part0; part < W.part0 + W.nparts; ++part) {
+      for (int t0 = 0; t0 < K; t0 += 32) {
+        const int t = t0 + lane;
+        const uint64_t key = (t < K) ? pkey[part * kmax + t] : ~0ull;
+        const bool ok = key != ~0ull;
+        topk::insert_batch(ok, key, ok ? pidx[part * kmax + t] : 0, ok ? pval[part * kmax + t] : 0.0, lk, li, lv, n,
+                           K, lane);
+      }
+    }
+  }
+  for (int t = lane; t < K; t += 32) {
+    const int64_t at = (int64_t)t * ld + W.q;
+    if (t < n) { oi[at] = li[t] + 1; ov[at] = lv[t]; }
+    else       { oi[at] = NA_INT;    ov[at] = na_real(); }
+  }
+}
+
 }  // namespace
 
 void launch_col_empty(const DevCsc& M, uint8_t* empty, cudaStream_t s) {
@@ -819,6 +916,33 @@ void launch_exact_pairs_sparse(int method, int dist, const DevCsc& ref, const Co
   if (npairs > 0)
     k_exact_pairs_sparse<<<blocks_for(npairs, 128), 128, 0, s>>>(
         method, dist, ref, ra, qry, qa, ref_idx, qry_idx, npairs, restore_self, self_value, out);
+}
+
+}  // namespace sdg
+
+namespace sdg {
+
+size_t batch_smem(int kmax) { return (size_t)BATCH_WARPS * kmax * 20; }
+
+void launch_batch_exact(const BatchProb* probs, const BatchItem* items, int64_t nitems, unsigned long long* counter,
+                        int kmax, uint64_t* pkey, int32_t* pidx, double* pval, int sms, cudaStream_t s) {
+  if (nitems <= 0) return;
+  const size_t smem = batch_smem(kmax);
+  if (smem > 48 * 1024) cudaFuncSetAttribute(k_batch_exact, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int per_sm = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_exact, BATCH_WARPS * 32, smem);
+  const int64_t grid = std::min<int64_t>((int64_t)std::max(1, per_sm) * std::max(1, sms),
+                                         (nitems + BATCH_WARPS - 1) / BATCH_WARPS);
+  k_batch_exact<<<(unsigned)grid, BATCH_WARPS * 32, smem, s>>>(probs, items, nitems, counter, kmax, pkey, pidx, pval);
+}
+
+void launch_batch_merge(const BatchProb* probs, const BatchRow* rows, int64_t nrows, int kmax, const uint64_t* pkey,
+                        const int32_t* pidx, const double* pval, cudaStream_t s) {
+  if (nrows <= 0) return;
+  const size_t smem = batch_smem(kmax);
+  if (smem > 48 * 1024) cudaFuncSetAttribute(k_batch_merge, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_batch_merge<<<(unsigned)((nrows + BATCH_WARPS - 1) / BATCH_WARPS), BATCH_WARPS * 32, smem, s>>>(
+      probs, rows, nrows, kmax, pkey, pidx, pval);
 }
 
 }  // namespace sdg

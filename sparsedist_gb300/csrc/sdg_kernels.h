@@ -116,6 +116,37 @@ struct SelectArgs {
   int64_t cand_ld = 0;
 };
 constexpr int kMaxK = 1024;   // largest k the selection kernels hold on chip
+
+// ---- sdg_exact.cu: batched exact kNN of many independent problems -------------
+// Problem p of a batch: the forward direction searches the columns of X among
+// the columns of Y, the reverse one the columns of Y among those of X.
+struct BatchProb {
+  DevCsc X, Y;
+  ColAux xa, ya;
+  int method, dist, decreasing;
+  int kf, kr;                              // clamped k of each direction
+  const uint8_t* xmask;                    // dropped (degenerate) columns, or null
+  const uint8_t* ymask;
+  int32_t* fidx; double* fval;             // device results: ncol(X) x kf, column-major
+  int32_t* ridx; double* rval;             // ncol(Y) x kr
+};
+// one unit of the persistent launch: query column q of direction dir against
+// the reference columns [r0, r1); its top k goes to partial slot `part`
+struct BatchItem {
+  int32_t prob, dir, q, r0, r1, pad;
+  int64_t part;
+};
+// one output row: its items' lists are the partial slots part0 .. + nparts
+struct BatchRow {
+  int32_t prob, dir, q, nparts;
+  int64_t part0;
+};
+constexpr int kBatchMaxK = 256;          // largest k of the batched exact path
+size_t batch_smem(int kmax);
+void launch_batch_exact(const BatchProb* probs, const BatchItem* items, int64_t nitems, unsigned long long* counter,
+                        int kmax, uint64_t* pkey, int32_t* pidx, double* pval, int sms, cudaStream_t s);
+void launch_batch_merge(const BatchProb* probs, const BatchRow* rows, int64_t nrows, int kmax, const uint64_t* pkey,
+                        const int32_t* pidx, const double* pval, cudaStream_t s);
 void launch_select(const SelectArgs& a, cudaStream_t s);
 
 // ---- sdg_snn.cu: SNN weights and graph ------------------------------------------

@@ -14,6 +14,12 @@ for them).
   s_c ~ lognormal(0, col_sdlog); zero counts are dropped, so no explicit zeros
   are stored.  Generated on the GPU with torch (seeded), returned as host
   numpy CSC arrays.
+* ``cross_draw`` / ``cross_problem``: the batched uneven sparseKNNCross
+  problems: per problem nq log-U[100, 50,000] query and nr log-U[1,000,
+  200,000] reference columns, rows U[5,000, 30,000], density
+  log-U[0.1 %, 10 %] (a uniform pattern: positions drawn uniformly and made
+  unique), |N(0,1)| values; methods cycle binary / cosine / manhattan / js (js
+  on column-normalised data), k drawn from {10, 20, 50}.
 """
 from __future__ import annotations
 
@@ -98,3 +104,52 @@ def logcount_csc(nrow=30000, ncol=200000, mean_nnz=1800.0, sdlog=0.6, row_sdlog=
         return (torch.from_numpy(p.astype(np.int32)).to(device), torch.cat(rows_parts),
                 torch.cat(vals_parts))
     return p.astype(np.int32), np.concatenate(rows_parts), np.concatenate(vals_parts)
+
+
+CROSS_METHODS = ("binary", "cosine", "manhattan", "js")
+
+
+def cross_draw(n=512, seed=4, scale=1.0):
+    """The parameters of the batched problems: a list of dicts (nq, nr, rows,
+    density, method, k, seed); ``scale`` multiplies the column counts."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for p in range(n):
+        nq = int(round(math.exp(rng.uniform(math.log(100), math.log(50000))) * scale))
+        nr = int(round(math.exp(rng.uniform(math.log(1000), math.log(200000))) * scale))
+        rows = int(rng.integers(5000, 30001))
+        dens = math.exp(rng.uniform(math.log(0.001), math.log(0.1)))
+        k = int(rng.choice([10, 20, 50]))
+        out.append(dict(nq=max(1, nq), nr=max(1, nr), rows=rows, density=dens, method=CROSS_METHODS[p % 4], k=k,
+                        seed=int(seed) * 100003 + p))
+    return out
+
+
+def _uniform_pattern(nrow, ncol, density, g, device):
+    import torch
+    m = int(round(density * nrow * ncol))
+    keys = torch.unique(torch.randint(0, nrow * ncol, (max(m, 1),), generator=g, device=device))
+    cols = keys // nrow
+    rows = (keys - cols * nrow).to(torch.int32)
+    vals = torch.randn(keys.numel(), generator=g, device=device, dtype=torch.float64).abs()
+    counts = torch.bincount(cols, minlength=ncol)
+    return counts, rows, vals, cols
+
+
+def cross_problem(spec, device="cuda"):
+    """(X, Y) of one batched problem as scipy CSC matrices (host)."""
+    import scipy.sparse as sp
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(spec["seed"])
+    mats = []
+    for ncol in (spec["nq"], spec["nr"]):
+        counts, rows, vals, cols = _uniform_pattern(spec["rows"], ncol, spec["density"], g, device)
+        if spec["method"] == "js":
+            sums = torch.zeros(ncol, dtype=torch.float64, device=device).index_add_(0, cols, vals)
+            vals = vals / sums[cols]
+        p = np.zeros(ncol + 1, np.int64)
+        p[1:] = np.cumsum(counts.cpu().numpy())
+        M = sp.csc_matrix((vals.cpu().numpy(), rows.cpu().numpy(), p.astype(np.int32)), shape=(spec["rows"], ncol))
+        mats.append(M)
+    return mats[0], mats[1]

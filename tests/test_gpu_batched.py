@@ -96,3 +96,52 @@ def test_batched_uneven_cross_problems_all_in_flight(wanted):
     assert sorted(got) == list(range(len(PROBLEMS)))
     for t, (p, want) in enumerate(zip(PROBLEMS, wanted)):
         check(p, got[t], want)
+
+
+def _batch(problems, ctx=None):
+    from backends import METHODS as CODES
+    from sparsedist_gb300 import _lib
+    ctx = ctx or _lib.Context()
+    return _lib.knn_cross_batch(ctx, [(p["X"], p["Y"], CODES[p["method"]], True, p["k"]) for p in problems])
+
+
+def test_batch_call_equals_oracle_twice(wanted):
+    """Every problem in ONE sdg_knn_cross_batch call (the exact-path searches
+    of the call in one persistent launch, the others on the screened engines
+    the autotuner picks), twice in a row on one context: the autotuner has
+    learned from the first call's timings and may pick other engines in the
+    second, whose results must still equal the oracle's."""
+    from sparsedist_gb300 import _lib
+    ctx = _lib.Context()
+    for rnd in range(2):
+        rc, res = _batch(PROBLEMS, ctx)
+        assert rc == 0
+        for p, r, want in zip(PROBLEMS, res, wanted):
+            assert r["status"] == 0, p["tag"]
+            assert all(e in (1, 2, 3) for e in r["engines"]), p["tag"]
+            check(p, (r["forward"], r["reverse"], r["flags"]), want)
+    used = {e for r in res for e in r["engines"]}
+    assert 1 in used                               # the persistent exact launch ran
+
+
+def test_batch_call_keeps_each_problems_status():
+    """A problem that fails validation (row dimensions differ) or has no
+    candidate (every reference column empty) reports its own status and
+    message; the problems around it are computed as usual, and clamped k
+    sets the warning flags as sparseKNNCross's clamp does."""
+    import scipy.sparse as sp
+    from sparsedist_gb300 import _lib
+    good = PROBLEMS[:3]
+    X = make_x(300, 40, 0.05, 7)
+    bad_rows = dict(X=X, Y=make_x(301, 30, 0.05, 8), method="cosine", k=5, tag="rows")
+    empty = dict(X=X, Y=sp.csc_matrix((300, 12)), method="binary", k=5, tag="no candidates")
+    clamp = dict(X=make_x(300, 6, 0.2, 9), Y=make_x(300, 4, 0.2, 10), method="cosine", k=10, tag="clamp")
+    probs = good + [bad_rows, empty, clamp]
+    rc, res = _batch(probs)
+    assert rc == -3                                # the first failure: SDG_E_ROWS
+    assert [r["status"] for r in res[3:5]] == [-3, -4]
+    orc = OracleBackend()
+    for p, r in zip(good + [clamp], res[:3] + res[5:]):
+        want = orc.knn_cross(p["X"], p["Y"], k=p["k"], method=p["method"])
+        check(p, (r["forward"], r["reverse"], r["flags"]), want)
+    assert res[5]["flags"] == 3 and res[5]["forward"][0].shape == (6, 4) and res[5]["reverse"][0].shape == (4, 6)
