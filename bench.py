@@ -755,6 +755,7 @@ def run_batched(args):
     ctx = _lib.Context()
     t_calls, cols, pairs = 0.0, 0, 0.0
     engines = {}
+    eng_s = [0.0, 0.0, 0.0]
     kept = []
     by_size = sorted(range(len(specs)), key=lambda p: specs[p]["nq"] * specs[p]["nr"])
     check_set = set(by_size[:args.batch_check])
@@ -766,6 +767,8 @@ def run_batched(args):
         rc, res = _lib.knn_cross_batch(ctx, [(X, Y, METHOD_CODES[sp_["method"]], True, sp_["k"])
                                              for (X, Y), sp_ in zip(probs, group)])
         t_calls += time.perf_counter() - t0
+        for e, sec in enumerate(_lib.knn_cross_batch.engine_seconds):
+            eng_s[e] += sec
         if rc != 0:
             raise RuntimeError("sdg_knn_cross_batch: %s" % [r["status"] for r in res])
         for j, ((X, Y), sp_, r) in enumerate(zip(probs, group, res)):
@@ -806,6 +809,8 @@ def run_batched(args):
                                "k in {10,20,50}" % (len(specs), args.batch_scale),
                    "problems_per_call": args.batch_group},
         "engines": engines,
+        "engine_seconds": {"exact_batched": eng_s[0], "fp32_screen": eng_s[1], "tensor_screen": eng_s[2],
+                           "other (uploads, preparation, copies)": t_calls - sum(eng_s)},
         "parity": {"problems": total, "bit_identical": identical, "js_within_1e-12": close,
                    "vs": "oracle (the reference's algorithm), the %d smallest problems" % total},
         "cpu_baseline": {"value": cpu_cols / t_cpu if t_cpu else None, "unit": "columns/s", "cores": threads,

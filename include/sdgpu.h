@@ -189,13 +189,15 @@ SDG_API int sdg_knn_cross(sdg_ctx* ctx, const sdg_csc* X, const sdg_csc* Y, int 
  * persistent launch over a work queue of (problem, direction, query column,
  * reference range) items sized by their merge-walk cost.  engines (optional,
  * 2 * nprob) receives the engine of each problem's forward and reverse
- * search.  Replaces a loop of R/sparseKNNCross.R:44-199 over the problems;
+ * search (1 exact, 2 FP32 screen, 3 tensor-core screen) and engine_seconds
+ * (optional, 3) the device time spent in each engine over the call.  Replaces a loop of R/sparseKNNCross.R:44-199 over the problems;
  * each problem's result equals sdg_knn_cross's. */
 SDG_API int sdg_knn_cross_batch(sdg_ctx* ctx, int nprob, const sdg_csc* X, const sdg_csc* Y,
                                 const int* method, const int* dist, const int* k, int drop_degenerate,
                                 int32_t* const* fwd_idx, double* const* fwd_dist,
                                 int32_t* const* rev_idx, double* const* rev_dist, int* k_fwd,
-                                int* k_rev, int* flags, int* status, int* engines);
+                                int* k_rev, int* flags, int* status, int* engines,
+                                double* engine_seconds);
 
 /* sparseSNN(idx, include_self, prune, symmetrise, edges = "knn") as the slots
  * of the n x n dgCMatrix.  Call once with p == NULL to learn *nnz, then with
@@ -353,5 +355,15 @@ SDG_API int sdg_kernel_time(sdg_ctx* ctx, double* ms, int64_t* launches);
  * beyond FP16's range, use 2).  Results are identical; only speed differs.
  * Used by tests to cross-check the engines. */
 SDG_API int sdg_ctx_set_engine(sdg_ctx* ctx, int engine);
+
+/* Failure-detection test hook: the next `launches` launches of the fused
+ * tensor-core screens (the dense BF16 screen and the sparse FP16 screen) make
+ * their MMA issuer wait on a pipeline phase that nothing completes.  Every
+ * wait of those kernels is bounded (1 s); the one that runs out raises the
+ * CTA's abort flag, the other roles leave their loops, issued copies and MMAs
+ * are drained, TMEM is freed and the kernel returns, so the call fails with
+ * SDG_E_CUDA ("... timed out") and the context stays usable.  0 clears it.
+ * Process-wide; used by the tests only. */
+SDG_API int sdg_debug_stall_tc(int launches);
 
 #endif

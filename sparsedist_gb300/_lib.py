@@ -28,7 +28,7 @@ EXPORTED = ["sdg_version", "sdg_last_error", "sdg_ctx_create", "sdg_ctx_destroy"
             "sdg_ctx_reset_cancel", "sdg_dist_cross", "sdg_dist", "sdg_topk_block", "sdg_topk_rows_accum",
             "sdg_snn_jaccard", "sdg_knn", "sdg_knn_cross", "sdg_snn_graph", "sdg_matrix_upload",
             "sdg_matrix_free", "sdg_knn_resident", "sdg_knn_resident_device", "sdg_ctx_set_stream",
-            "sdg_last_stats", "sdg_ctx_set_engine", "sdg_kernel_time", "sdg_knn_block",
+            "sdg_last_stats", "sdg_ctx_set_engine", "sdg_debug_stall_tc", "sdg_kernel_time", "sdg_knn_block",
             "sdg_server_create", "sdg_server_submit", "sdg_server_wait", "sdg_server_result",
             "sdg_server_cancel", "sdg_server_stats", "sdg_server_destroy",
             "sdg_matrix_upload_device", "sdg_dense_upload", "sdg_dense_free", "sdg_dense_knn_block",
@@ -72,6 +72,7 @@ def load() -> C.CDLL:
             lib.sdg_ctx_cancel.argtypes = [v]
             lib.sdg_ctx_reset_cancel.argtypes = [v]
             lib.sdg_ctx_set_engine.argtypes = [v, C.c_int]
+            lib.sdg_debug_stall_tc.argtypes = [C.c_int]
             lib.sdg_last_stats.argtypes = [v, v, C.c_int]
             lib.sdg_dist_cross.argtypes = [v, C.c_int, C.c_int, v, v, v]
             lib.sdg_dist.argtypes = [v, C.c_int, C.c_int, v, C.c_int, C.c_int, v]
@@ -103,7 +104,7 @@ def load() -> C.CDLL:
             lib.sdg_server_create.argtypes = [v, v, C.c_int, C.c_int, C.c_int64, v, C.c_int,
                                               C.POINTER(v)]
             lib.sdg_server_submit.argtypes = [v, v, C.c_int, C.c_int, C.c_int, C.c_int, v]
-            lib.sdg_knn_cross_batch.argtypes = [v, C.c_int, v, v, v, v, v, C.c_int, v, v, v, v, v, v, v, v, v]
+            lib.sdg_knn_cross_batch.argtypes = [v, C.c_int, v, v, v, v, v, C.c_int, v, v, v, v, v, v, v, v, v, v]
             lib.sdg_server_create_dense.argtypes = [v, v, C.c_int, C.c_int, C.c_int64, C.POINTER(v)]
             lib.sdg_server_submit_dense.argtypes = [v, v, C.c_int32, C.c_int32, C.c_int, C.c_int, v]
             lib.sdg_server_wait.argtypes = [v, C.c_int64, C.c_int]
@@ -348,11 +349,13 @@ def knn_cross_batch(ctx, problems, drop_degenerate=True):
     ptrs = [(C.c_void_p * max(n, 1))(*[o[j].ctypes.data for o in outs]) for j in range(4)]
     kf, kr, fl, st = (np.zeros(max(n, 1), np.int32) for _ in range(4))
     eng = np.zeros(2 * max(n, 1), np.int32)
+    secs = np.zeros(3, np.float64)
     rc = ctx.lib.sdg_knn_cross_batch(ctx.handle, n, C.cast(Xs, C.c_void_p), C.cast(Ys, C.c_void_p),
                                      meth.ctypes.data, dist.ctypes.data, ks.ctypes.data, int(bool(drop_degenerate)),
                                      C.cast(ptrs[0], C.c_void_p), C.cast(ptrs[1], C.c_void_p),
                                      C.cast(ptrs[2], C.c_void_p), C.cast(ptrs[3], C.c_void_p), kf.ctypes.data,
-                                     kr.ctypes.data, fl.ctypes.data, st.ctypes.data, eng.ctypes.data)
+                                     kr.ctypes.data, fl.ctypes.data, st.ctypes.data, eng.ctypes.data,
+                                     secs.ctypes.data)
     res = []
     for p, (X, Y, _, _, k) in enumerate(problems):
         nx, ny, a, b = X.shape[1], Y.shape[1], int(kf[p]), int(kr[p])
@@ -360,6 +363,7 @@ def knn_cross_batch(ctx, problems, drop_degenerate=True):
         res.append({"forward": (fi[:nx * a].reshape(a, nx).T.copy(), fd[:nx * a].reshape(a, nx).T.copy()),
                     "reverse": (ri[:ny * b].reshape(b, ny).T.copy(), rd[:ny * b].reshape(b, ny).T.copy()),
                     "flags": int(fl[p]), "status": int(st[p]), "engines": (int(eng[2 * p]), int(eng[2 * p + 1]))})
+    knn_cross_batch.engine_seconds = secs.tolist()
     return rc, res
 
 

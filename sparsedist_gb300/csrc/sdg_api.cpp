@@ -229,6 +229,8 @@ struct sdg_matrix {
   DevBuf s1, s2;                // pearson moments
   bool have_moments = false;
   int js_status = 1;
+  DevBuf xl;                    // js: xlogx of each stored value
+  DevBuf xsum;                  // js: column sums
   ScreenCache screen[4];        // screening data per method (sdg_screen.h), binary..manhattan
   TensorCache tensor[4];        // dense BF16 screen values per method (tensor-core screen)
 
@@ -238,7 +240,7 @@ struct sdg_matrix {
       for (auto& tc : tensor) tensor_cache_free(&tc, ctx->stream);
       cudaStreamSynchronize(ctx->stream);
     }
-    for (DevBuf* b : {&p, &i, &x, &empty, &uval, &scale, &s1, &s2}) b->detach();
+    for (DevBuf* b : {&p, &i, &x, &empty, &uval, &scale, &s1, &s2, &xl, &xsum}) b->detach();
   }
 
   DevCsc dev() const {
@@ -348,6 +350,12 @@ void ensure_js(sdg_matrix* m, const char* msg = kMsgJS) {
   CK(cudaStreamSynchronize(s));
   m->js_status = herr ? SDG_E_NONFINITE : 0;
   if (herr) fail(SDG_E_NONFINITE, msg);
+  m->xl = DevBuf(sizeof(double) * (size_t)std::max<int64_t>(m->nnz, 1), s);
+  launch_xlogx_values(m->x.as<double>(), m->nnz, m->xl.as<double>(), s);
+  // column sums in row order (the moments' sums; the squares are not needed)
+  m->xsum = DevBuf(sizeof(double) * (size_t)std::max<int64_t>(m->ncol, 1), s);
+  DevBuf sq(sizeof(double) * (size_t)std::max<int64_t>(m->ncol, 1), s);
+  launch_moments(m->dev(), m->xsum.as<double>(), sq.as<double>(), s);
 }
 
 // Method-specific preparation of the reference-side (m) and query-side (m2)
@@ -365,6 +373,8 @@ ColAux aux_of(const sdg_matrix* m) {
   a.scale = m->scale.as<double>();
   a.s = m->s1.as<double>();
   a.ss = m->s2.as<double>();
+  a.xl = m->xl.as<double>();
+  a.xsum = m->xsum.as<double>();
   return a;
 }
 
@@ -476,9 +486,6 @@ void knn_device(sdg_ctx* c, sdg_matrix* X, sdg_matrix* Y, int method, int dist, 
     k = (int)avail;
   }
   *k_eff = k;
-  if (k > kMaxK)
-    fail(SDG_E_UNSUPPORTED, "k above " + std::to_string(kMaxK) +
-                                " neighbours is not supported by this build.");
   prepare(method, ref, X);
 
   KnnPlan P;
@@ -641,6 +648,12 @@ SDG_API int sdg_ctx_set_engine(sdg_ctx* c, int engine) {
   return SDG_OK;
 }
 
+SDG_API int sdg_debug_stall_tc(int launches) {
+  if (launches < 0) { g_err = "launches must be >= 0"; return SDG_E_ARG; }
+  tc_set_stall(launches);
+  return SDG_OK;
+}
+
 SDG_API int sdg_kernel_time(sdg_ctx* c, double* ms, int64_t* launches) {
   return guarded([&] {
     if (!c || !ms || !launches) fail(SDG_E_ARG, "NULL argument");
@@ -790,8 +803,6 @@ SDG_API int sdg_topk_block(sdg_ctx* c, const double* D, int64_t nrow, int64_t nc
         fail(SDG_E_ARG, "self_row entries must be 0 or valid 1-based rows of D.");
       skip[(size_t)b] = sr > 0 ? sr - 1 : -1;
     }
-    if (k > kMaxK)
-      fail(SDG_E_UNSUPPORTED, "k above " + std::to_string(kMaxK) + " is not supported by this build.");
     if (ncol == 0) return;
     cudaStream_t s = c->stream;
     DevBuf dD(sizeof(double) * (size_t)(nrow * ncol), s), dskip(sizeof(int64_t) * (size_t)ncol, s);
@@ -827,8 +838,6 @@ SDG_API int sdg_topk_rows_accum(sdg_ctx* c, const double* D, int64_t nrow, int64
         fail(SDG_E_ARG, "self_col entries must be 0 or a positive 1-based query index.");
       skip[(size_t)r] = sc > 0 ? (int64_t)sc - 1 : -1;
     }
-    if (k > kMaxK)
-      fail(SDG_E_UNSUPPORTED, "k above " + std::to_string(kMaxK) + " is not supported by this build.");
     if (nrow == 0) return;
     cudaStream_t s = c->stream;
     DevBuf dD(sizeof(double) * (size_t)std::max<int64_t>(nrow * ncol, 1), s);
@@ -1311,7 +1320,9 @@ std::vector<int> candidate_engines(const SearchShape& sh, bool drop) {
       cudaGetLastError();
     }
   }
-  if (e.empty()) e.push_back(sh.k <= kMaxK ? 2 : 1);
+  // no batched exact item and no screen: the problem's own search, whose
+  // engine choice falls back to the exact slab (engine 2 = "run it alone")
+  if (e.empty()) e.push_back(2);
   return e;
 }
 
@@ -1329,8 +1340,10 @@ extern "C" {
 SDG_API int sdg_knn_cross_batch(sdg_ctx* c, int nprob, const sdg_csc* X, const sdg_csc* Y, const int* method,
                                 const int* dist, const int* k, int drop_degenerate, int32_t* const* fwd_idx,
                                 double* const* fwd_dist, int32_t* const* rev_idx, double* const* rev_dist,
-                                int* k_fwd, int* k_rev, int* flags, int* status, int* engines) {
+                                int* k_fwd, int* k_rev, int* flags, int* status, int* engines,
+                                double* engine_seconds) {
   return guarded([&] {
+    if (engine_seconds) for (int e = 0; e < 3; ++e) engine_seconds[e] = 0.0;
     if (!c || nprob < 0 || (nprob > 0 && (!X || !Y || !method || !dist || !k || !fwd_idx || !fwd_dist ||
                                           !rev_idx || !rev_dist || !k_fwd || !k_rev || !flags || !status)))
       fail(SDG_E_ARG, "NULL argument");
@@ -1437,7 +1450,9 @@ SDG_API int sdg_knn_cross_batch(sdg_ctx* c, int nprob, const sdg_csc* X, const s
                          h.ri.as<int32_t>(), h.rv.as<double>(), &ke, &fl, &hi_, &hv_);
             CK(cudaEventRecord(e1, s));
             c->engine = saved;
-            T.learn(eng, dir == 0 ? h.fs : h.rs, elapsed_s(e0, e1));
+            const double secs = elapsed_s(e0, e1);
+            T.learn(eng, dir == 0 ? h.fs : h.rs, secs);
+            if (engine_seconds) engine_seconds[eng - 1] += secs;
           }
           if (h.ef == 1 || h.er == 1) {
             h.xe.resize((size_t)nx);
@@ -1467,11 +1482,12 @@ SDG_API int sdg_knn_cross_batch(sdg_ctx* c, int nprob, const sdg_csc* X, const s
         std::vector<BatchItem> items;
         std::vector<BatchRow> rows;
         double total_steps = 0.0;
-        int kmax = 1;
+        int kmax = 1, lwords = 0;
         for (size_t b = 0; b < probs.size(); ++b) {
           Held& h = held[(size_t)prob_of[b]];
           for (int dir = 0; dir < 2; ++dir) {
             if ((dir == 0 ? h.ef : h.er) != 1) continue;
+            lwords = std::max(lwords, batch_lookup_words(probs[b].method, probs[b].X.nrow));
             const sdg_csc& Qc = dir == 0 ? X[h.p] : Y[h.p];
             const sdg_csc& Rc = dir == 0 ? Y[h.p] : X[h.p];
             const std::vector<uint8_t>& qe = dir == 0 ? h.xe : h.ye;
@@ -1511,13 +1527,14 @@ SDG_API int sdg_knn_cross_batch(sdg_ctx* c, int nprob, const sdg_csc* X, const s
         CK(cudaMemsetAsync(dc.p, 0, sizeof(unsigned long long), s));
         CK(cudaEventRecord(e0, s));
         launch_batch_exact(dp.as<BatchProb>(), di.as<BatchItem>(), (int64_t)items.size(), dc.as<unsigned long long>(),
-                           kmax, pk.as<uint64_t>(), pi.as<int32_t>(), pv.as<double>(), sms, s);
+                           kmax, lwords, pk.as<uint64_t>(), pi.as<int32_t>(), pv.as<double>(), sms, s);
         CK(cudaEventRecord(e1, s));
         launch_batch_merge(dp.as<BatchProb>(), dr.as<BatchRow>(), (int64_t)rows.size(), kmax, pk.as<uint64_t>(),
                            pi.as<int32_t>(), pv.as<double>(), s);
         CK(cudaGetLastError());
         const double secs = elapsed_s(e0, e1);
         T.learn_exact(lg, total_steps, secs);
+        if (engine_seconds) engine_seconds[0] += secs;
         c->stats[1] += (int64_t)total_steps;
         c->stats[3] += 2;
       }
@@ -1612,13 +1629,21 @@ namespace {
 
 // Device memory a request needs while it runs: its query CSC, its share of
 // the FP32 screen slab (capped by the engine's per-pass slab), the candidate
-// table and exact values, and the result buffers.
-int64_t request_mem(const sdg_server* S, int64_t ncol, int64_t nnz, int k) {
+// table and exact values, and the result buffers; where the reference holds
+// the method's tensor-screen copy, the query block's own FP16 copy too (the
+// tensor screen builds one for the queries: ld x ncol halves plus per-column
+// bounds).
+int64_t request_mem(const sdg_server* S, int method, int64_t ncol, int64_t nnz, int k) {
   if (S->dref) return dense_query_bytes(S->dref, ncol, k);
   const int64_t nr = S->ref->ncol;
   const int64_t slab_cols = std::min<int64_t>(ncol, std::max<int64_t>(16, ((int64_t)4 << 30) / (4 * std::max<int64_t>(nr, 1))));
   const int64_t cap = std::max(256, std::min(8192, 16 * k + 64));
-  return nnz * 12 + (ncol + 1) * 8 + slab_cols * nr * 4 + ncol * cap * 24 + ncol * (int64_t)k * 12;
+  int64_t bytes = nnz * 12 + (ncol + 1) * 8 + slab_cols * nr * 4 + ncol * cap * 24 + ncol * (int64_t)k * 12;
+  constexpr int kTensorSlots = (int)(sizeof(sdg_matrix::tensor) / sizeof(sdg_matrix::tensor[0]));
+  if (method >= 0 && method < kTensorSlots && S->ref->tensor[method].method == method &&
+      S->ref->tensor[method].usable)
+    bytes += (int64_t)tensor_cache_bytes(S->ref->nrow, ncol);
+  return bytes;
 }
 
 void admit_locked(sdg_server* S) {
@@ -1901,7 +1926,7 @@ SDG_API int sdg_server_submit_dense(sdg_server* S, const float* Q, int32_t d, in
     r->method = method; r->dist = 1; r->k = k; r->drop = 1;
     r->nrow = d; r->ncol = nq;
     r->q.assign(Q, Q + (size_t)d * (size_t)nq);
-    r->mem = request_mem(S, nq, 0, k);
+    r->mem = request_mem(S, method, nq, 0, k);
     r->t_submit = now_s();
     std::lock_guard<std::mutex> lock(S->mu);
     r->id = S->next_id++;
@@ -1932,7 +1957,7 @@ SDG_API int sdg_server_submit(sdg_server* S, const sdg_csc* Q, int method, int d
     r->p.assign(Q->p, Q->p + Q->ncol + 1);
     r->i.assign(Q->i, Q->i + Q->p[Q->ncol]);
     r->x.assign(Q->x, Q->x + Q->p[Q->ncol]);
-    r->mem = request_mem(S, Q->ncol, Q->p[Q->ncol], k);
+    r->mem = request_mem(S, method, Q->ncol, Q->p[Q->ncol], k);
     r->t_submit = now_s();
     std::lock_guard<std::mutex> lock(S->mu);
     r->id = S->next_id++;

@@ -31,6 +31,8 @@ struct ColAux {
   const float* fval = nullptr;      // screening: float copy of the values the
                                     // screen multiplies (unit values for cosine)
   const float* norm = nullptr;      // screening: per-column norm term (method-specific)
+  const double* xl = nullptr;       // js: xlogx of each stored value (nnz), or null
+  const double* xsum = nullptr;     // js: sum of each column's values, or null
 };
 
 __host__ __device__ inline double na_real() {

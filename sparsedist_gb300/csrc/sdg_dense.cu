@@ -428,9 +428,43 @@ int dense_search(sdg_ctx* ctx, const sdg_dense* Q, int64_t q0, int64_t nq, const
   const int64_t avail = D->n - D->n_empty - (self ? 1 : 0);   // include_self = FALSE
   if (avail < 1) return fail_with(SDG_E_NOCAND, "No candidate neighbours available.");
   if (k > avail) { k = (int)avail; *flags |= SDG_WARN_CLAMP_FWD; }
-  if (k > kMaxK) return fail_with(SDG_E_UNSUPPORTED, "k above 1024 is not supported by this build.");
   *k_eff = k;
   const int64_t n = D->n;
+  if (k > kMaxK) {
+    // more neighbours than the screens' lists hold: every query is valued
+    // exactly against every reference and selected with lists in device
+    // scratch (the same kernels as the screens' overflow path)
+    int32_t* o_idx = idx;
+    double *o_val = dist_out, *row = nullptr;
+    if (!device_out) {
+      DK(cudaMallocAsync(&o_idx, sizeof(int32_t) * (size_t)(nq * k), s));
+      DK(cudaMallocAsync(&o_val, sizeof(double) * (size_t)(nq * k), s));
+    }
+    DK(cudaMallocAsync(&row, sizeof(double) * (size_t)n, s));
+    ctx_stats_reset(ctx);
+    for (int64_t q = q0; q < q0 + nq; ++q) {
+      k_dense_exact_row<<<blocks_for(n, 256), 256, 0, s>>>(method, D->d, D->x64, D->u64, Q->x64, Q->u64,
+                                                            D->empty, n, q, self ? 1 : 0, row);
+      SelectArgs sa;
+      sa.vals = row; sa.seg_stride = 0; sa.elem_stride = 1; sa.len = n; sa.nseg = 1;
+      sa.seg_blank = Q->empty + q0;
+      sa.out_idx = o_idx; sa.out_val = o_val; sa.out_ld = nq; sa.out_row0 = q - q0;
+      sa.k = k; sa.decreasing = 0;
+      launch_select(sa, s);
+    }
+    DK(cudaGetLastError());
+    if (!device_out) {
+      DK(cudaMemcpyAsync(idx, o_idx, sizeof(int32_t) * (size_t)(nq * k), cudaMemcpyDeviceToHost, s));
+      DK(cudaMemcpyAsync(dist_out, o_val, sizeof(double) * (size_t)(nq * k), cudaMemcpyDeviceToHost, s));
+      DK(cudaFreeAsync(o_idx, s));
+      DK(cudaFreeAsync(o_val, s));
+    }
+    DK(cudaFreeAsync(row, s));
+    DK(cudaStreamSynchronize(s));
+    ctx_stats_add(ctx, 1, n * nq);
+    ctx_stats_add(ctx, 3, 2 * nq);
+    return SDG_OK;
+  }
   const int cap = std::max(512, std::min(16384, 64 * k + 256));
   // mode 0 runs the fused tensor-core screen where it applies (no slab in
   // HBM), else the BF16 slab screen of mode 2; smode is the bound in force
@@ -497,7 +531,7 @@ int dense_search(sdg_ctx* ctx, const sdg_dense* Q, int64_t q0, int64_t nq, const
     A.qnorm2 = Q->norm2; A.qempty = Q->empty;
     A.nseg = nseg; A.segtop = segtop; A.cut = cut;
     A.cap = cap; A.cand = cand; A.count = count; A.overflow = over;
-    const size_t smem = sizeof(float) * (size_t)DSEL_WARPS * k;     // <= 32 KB (k <= 1024)
+    const size_t smem = sizeof(float) * (size_t)DSEL_WARPS * k;     // <= 32 KB (k <= kMaxK here)
     const dim3 grid(blocks_for(nb, DSEL_WARPS), (unsigned)nseg);
     k_dense_segtop<<<grid, DSEL_WARPS * 32, smem, s>>>(A);
     k_dense_thresh<<<blocks_for(nb, DSEL_WARPS), DSEL_WARPS * 32, smem, s>>>(A);

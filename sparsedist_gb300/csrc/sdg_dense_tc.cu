@@ -97,6 +97,7 @@ struct TcArgs {
   int32_t* eidx;              // [nq][nslots][ecap]
   float* ehi;                 // [nq][nslots][ecap]
   int* status;
+  int stall;                  // failure-detection test: the MMA issuer's first wait never completes
 };
 
 // Order-preserving map of a float onto uint32 (ascending value -> ascending
@@ -207,7 +208,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
         for (; f < fe && ok; ++f, ++j) {
           const int buf = (int)(j & 1);
           // the epilogue has drained this buffer's previous tile
-          if (!mbar_wait(acc_empty + buf, ((uint32_t)(j >> 1) & 1u) ^ 1u, abort_flag, P.status)) {
+          // (with P.stall the first wait asks for the phase the epilogue has not
+          // begun, so it runs out: the failure-detection test's path)
+          const uint32_t flip = (P.stall && j == 0) ? 0u : 1u;
+          if (!mbar_wait(acc_empty + buf, ((uint32_t)(j >> 1) & 1u) ^ flip, abort_flag, P.status)) {
             ok = false;
             break;
           }
@@ -655,6 +659,7 @@ int tc_screen(sdg_ctx* ctx, const sdg_dense* Q, const sdg_dense* D, bool self, i
     P.tshared = tshared;
     P.lists = lists; P.ecount = ecount; P.eidx = eidx; P.ehi = ehi;
     P.status = status;
+    P.stall = tc_take_stall() ? 1 : 0;
     // the list length: the smallest of 16 / 24 / 32 / 48 / 64 that holds k
     auto kern = (k <= 16) ? k_dense_tc<16> : (k <= 24) ? k_dense_tc<24> : (k <= 32) ? k_dense_tc<32>
               : (k <= 48) ? k_dense_tc<48> : k_dense_tc<64>;

@@ -119,6 +119,14 @@ __global__ void k_check_js(const double* x, int64_t nnz, int* err) {
 
 // ---- exact pair values ---------------------------------------------------------
 
+// jacc_value from the two columns' stored counts and the common count
+__device__ __forceinline__ double binary_finish(double ni, double nj, int64_t common, bool dist) {
+  const double c = (double)common;
+  const double denom = dsub(dadd(ni, nj), c);
+  const double sim = (denom > 0.0) ? (c / denom) : 1.0;
+  return dist ? dsub(1.0, sim) : sim;
+}
+
 // jacc_common / jacc_value: src/sparseDist.cpp:535-556
 __device__ double pair_binary(const DevCsc& A, int32_t i, const DevCsc& B, int32_t j, bool dist) {
   int64_t a = A.p[i], ae = A.p[i + 1], b = B.p[j], be = B.p[j + 1];
@@ -130,34 +138,35 @@ __device__ double pair_binary(const DevCsc& A, int32_t i, const DevCsc& B, int32
     a += (ra <= rb);
     b += (rb <= ra);
   }
-  const double c = (double)common;
-  const double denom = dsub(dadd(ni, nj), c);
-  const double sim = (denom > 0.0) ? (c / denom) : 1.0;
-  return dist ? dsub(1.0, sim) : sim;
+  return binary_finish(ni, nj, common, dist);
+}
+
+// unit_cosine's clamp of the unit dot product s (NaN -> 0)
+__device__ __forceinline__ double cosine_finish(double s, bool dist) {
+  double c = s;
+  if (!(c == c)) c = 0.0;
+  else if (c > 1.0) c = 1.0;
+  else if (c < -1.0) c = -1.0;
+  return dist ? dsub(1.0, c) : c;
 }
 
 // unit_dot / unit_cosine: src/sparseDist.cpp:287-331
 __device__ double pair_cosine(const DevCsc& A, const ColAux& aa, int32_t i, const DevCsc& B,
                               const ColAux& ba, int32_t j, bool dist) {
   const bool ea = (aa.scale[i] == 0.0), eb = (ba.scale[j] == 0.0);
-  double c;
   if (ea || eb) {
-    c = (ea && eb) ? 1.0 : 0.0;
-  } else {
-    int64_t a = A.p[i], ae = A.p[i + 1], b = B.p[j], be = B.p[j + 1];
-    double s = 0.0;
-    while (a < ae && b < be) {
-      const int32_t ra = __ldg(A.i + a), rb = __ldg(B.i + b);
-      if (ra == rb) { s = dadd(s, dmul(aa.uval[a], ba.uval[b])); ++a; ++b; }
-      else if (ra < rb) { ++a; }
-      else { ++b; }
-    }
-    c = s;
-    if (!(c == c)) c = 0.0;
-    else if (c > 1.0) c = 1.0;
-    else if (c < -1.0) c = -1.0;
+    const double c = (ea && eb) ? 1.0 : 0.0;
+    return dist ? dsub(1.0, c) : c;
   }
-  return dist ? dsub(1.0, c) : c;
+  int64_t a = A.p[i], ae = A.p[i + 1], b = B.p[j], be = B.p[j + 1];
+  double s = 0.0;
+  while (a < ae && b < be) {
+    const int32_t ra = __ldg(A.i + a), rb = __ldg(B.i + b);
+    if (ra == rb) { s = dadd(s, dmul(aa.uval[a], ba.uval[b])); ++a; ++b; }
+    else if (ra < rb) { ++a; }
+    else { ++b; }
+  }
+  return cosine_finish(s, dist);
 }
 
 // fastEuclidean2 pair loop: src/sparseDist.cpp:855-871
@@ -194,6 +203,22 @@ __device__ double pair_manhattan(const DevCsc& A, int32_t i, const DevCsc& B, in
   return num;
 }
 
+// arma::cor's single-pass form from the matched-product sum sab and the
+// columns' moments
+__device__ __forceinline__ double pearson_finish(double sab, int32_t nrow, const ColAux& aa, int32_t i,
+                                                 const ColAux& ba, int32_t j, bool dist) {
+  const double N = (double)nrow;
+  const double norm = (nrow > 1) ? dsub(N, 1.0) : 1.0;
+  const double cov = dsub(sab, dmul(aa.s[i], ba.s[j]) / N) / norm;
+  const double va = dsub(aa.ss[i], dmul(aa.s[i], aa.s[i]) / N) / norm;
+  const double vb = dsub(ba.ss[j], dmul(ba.s[j], ba.s[j]) / N) / norm;
+  double c = cov / dmul(sqrt(va), sqrt(vb));
+  if (!isfinite(c)) c = 0.0;
+  if (c > 1.0) c = 1.0;
+  if (c < -1.0) c = -1.0;
+  return dist ? dsub(1.0, c) : c;
+}
+
 // fastCorr2 (src/sparseDist.cpp:424-431) with arma::cor in the single-pass
 // vector form: sums in ascending row order over stored entries.
 __device__ double pair_pearson(const DevCsc& A, const ColAux& aa, int32_t i, const DevCsc& B,
@@ -206,16 +231,7 @@ __device__ double pair_pearson(const DevCsc& A, const ColAux& aa, int32_t i, con
     else if (ra < rb) { ++a; }
     else { ++b; }
   }
-  const double N = (double)A.nrow;
-  const double norm = (A.nrow > 1) ? dsub(N, 1.0) : 1.0;
-  const double cov = dsub(sab, dmul(aa.s[i], ba.s[j]) / N) / norm;
-  const double va = dsub(aa.ss[i], dmul(aa.s[i], aa.s[i]) / N) / norm;
-  const double vb = dsub(ba.ss[j], dmul(ba.s[j], ba.s[j]) / N) / norm;
-  double c = cov / dmul(sqrt(va), sqrt(vb));
-  if (!isfinite(c)) c = 0.0;
-  if (c > 1.0) c = 1.0;
-  if (c < -1.0) c = -1.0;
-  return dist ? dsub(1.0, c) : c;
+  return pearson_finish(sab, A.nrow, aa, i, ba, j, dist);
 }
 
 // fastJS2 (src/sparseDist.cpp:1099-1108, xlogx :206-210): per row
@@ -224,6 +240,13 @@ __device__ double pair_pearson(const DevCsc& A, const ColAux& aa, int32_t i, con
 __device__ __forceinline__ double xlogx(double x) {
   const double r = dmul(x, log(x));
   return isnan(r) ? 0.0 : r;
+}
+
+__device__ __forceinline__ double covariance_finish(double sab, int32_t nrow, const ColAux& aa, int32_t i,
+                                                    const ColAux& ba, int32_t j) {
+  const double N = (double)nrow;
+  const double norm = (nrow > 1) ? dsub(N, 1.0) : 1.0;
+  return dsub(sab, dmul(aa.s[i], ba.s[j]) / N) / norm;
 }
 
 // covariance: fastCov2, src/sparseDist.cpp:480-510 -- arma::cov of the two
@@ -239,29 +262,99 @@ __device__ double pair_covariance(const DevCsc& A, const ColAux& aa, int32_t i, 
     else if (ra < rb) { ++a; }
     else { ++b; }
   }
-  const double N = (double)A.nrow;
-  const double norm = (A.nrow > 1) ? dsub(N, 1.0) : 1.0;
-  return dsub(sab, dmul(aa.s[i], ba.s[j]) / N) / norm;
+  return covariance_finish(sab, A.nrow, aa, i, ba, j);
 }
 
-__device__ double pair_js(const DevCsc& A, int32_t i, const DevCsc& B, int32_t j) {
+// A row stored in one column only (Q = 0) contributes exactly P log 2: xlogx(0)
+// is 0, P + 0 is P, and (xlogx(P) + 0) - xlogx(P) is +0, so no logarithm is
+// taken there; a shared row takes xlogx(P), xlogx(Q) from the columns'
+// precomputed values (ColAux::xl, the same function of the same double) and
+// one logarithm for xlogx(P + Q).  The terms and their order of summation
+// are the formula's above: pair_js_walk evaluates every stored row.
+__device__ double pair_js_walk(const DevCsc& A, const ColAux& aa, int32_t i, const DevCsc& B, const ColAux& ba,
+                               int32_t j) {
   const double log2v = 0.69314718055994530942;   // log(2.0), correctly rounded
   int64_t a = A.p[i], ae = A.p[i + 1], b = B.p[j], be = B.p[j + 1];
   double acc0 = 0.0, acc1 = 0.0;
   while (a < ae || b < be) {
-    int32_t r;
-    double P = 0.0, Q = 0.0;
     const int32_t ra = (a < ae) ? __ldg(A.i + a) : INT32_MAX;
     const int32_t rb = (b < be) ? __ldg(B.i + b) : INT32_MAX;
-    if (ra < rb) { r = ra; P = A.x[a]; ++a; }
-    else if (rb < ra) { r = rb; Q = B.x[b]; ++b; }
-    else { r = ra; P = A.x[a]; Q = B.x[b]; ++a; ++b; }
-    const double PQ = dadd(P, Q);
-    const double t = dadd(dsub(dadd(xlogx(P), xlogx(Q)), xlogx(PQ)), dmul(PQ, log2v));
+    int32_t r;
+    double t;
+    if (ra < rb) {
+      r = ra; t = dmul(A.x[a], log2v); ++a;
+    } else if (rb < ra) {
+      r = rb; t = dmul(B.x[b], log2v); ++b;
+    } else {
+      r = ra;
+      const double P = A.x[a], Q = B.x[b];
+      const double xp = aa.xl ? aa.xl[a] : xlogx(P), xq = ba.xl ? ba.xl[b] : xlogx(Q);
+      const double PQ = dadd(P, Q);
+      t = dadd(dsub(dadd(xp, xq), xlogx(PQ)), dmul(PQ, log2v));
+      ++a; ++b;
+    }
     if (r & 1) acc1 = dadd(acc1, t); else acc0 = dadd(acc0, t);
   }
   const double v = dmul(0.5, dadd(acc0, acc1));
   return (v > 0.0) ? sqrt(v) : 0.0;
+}
+
+// fastJS2's value with the rows stored in one column only summed in bulk.
+// Every row's term is >= 0 (P log 2 for a one-sided row; (P + Q) log 2 minus
+// g(P, Q) = xlogx(P + Q) - xlogx(P) - xlogx(Q) <= (P + Q) log 2 for a shared
+// one), so the order of summation moves the result by a few units of 2^-53 of
+// it.  The one-sided rows add log 2 times the columns' one-sided masses,
+// S_P - (shared P) and S_Q - (shared Q) from the columns' sums: the walk
+// touches only the shared rows' values.  The difference is taken only when
+// each one-sided mass is at least half its column's sum (then its relative
+// error is below ~2e-13); a pair sharing most of its mass is walked in full.
+// The value is fastJS2's within 1e-12 relative (the reference sums with
+// Armadillo's accu, whose order is not pinned either).
+// The bulk form's value from the column sums SA, SB, the shared rows' value
+// sums sp, sq and their terms' sum; false when a one-sided mass is below half
+// its column's sum (the caller then walks the pair in full).
+__device__ __forceinline__ bool js_bulk(double SA, double SB, double sp, double sq, double shared, double* out) {
+  const double log2v = 0.69314718055994530942;
+  const double oa = dsub(SA, sp), ob = dsub(SB, sq);
+  if (!(oa >= 0.5 * SA) || !(ob >= 0.5 * SB)) return false;
+  const double v = dmul(0.5, dadd(dmul(dadd(oa, ob), log2v), shared));
+  *out = (v > 0.0) ? sqrt(v) : 0.0;
+  return true;
+}
+// the term of a row stored in both columns (P, Q and their xlogx values)
+__device__ __forceinline__ double js_shared_term(double P, double Q, double xp, double xq) {
+  const double log2v = 0.69314718055994530942;
+  const double PQ = dadd(P, Q);
+  return dadd(dsub(dadd(xp, xq), xlogx(PQ)), dmul(PQ, log2v));
+}
+
+__device__ double pair_js(const DevCsc& A, const ColAux& aa, int32_t i, const DevCsc& B, const ColAux& ba,
+                          int32_t j) {
+  if (!aa.xsum || !ba.xsum || !aa.xl || !ba.xl) return pair_js_walk(A, aa, i, B, ba, j);
+  int64_t a = A.p[i], ae = A.p[i + 1], b = B.p[j], be = B.p[j + 1];
+  double shared = 0.0, sp = 0.0, sq = 0.0;
+  while (a < ae && b < be) {
+    const int32_t ra = __ldg(A.i + a), rb = __ldg(B.i + b);
+    if (ra == rb) {
+      const double P = A.x[a], Q = B.x[b];
+      shared = dadd(shared, js_shared_term(P, Q, aa.xl[a], ba.xl[b]));
+      sp = dadd(sp, P);
+      sq = dadd(sq, Q);
+      ++a; ++b;
+    } else {
+      a += (ra < rb);
+      b += (rb < ra);
+    }
+  }
+  double v;
+  if (!js_bulk(aa.xsum[i], ba.xsum[j], sp, sq, shared, &v)) return pair_js_walk(A, aa, i, B, ba, j);
+  return v;
+}
+
+// xlogx of each stored value (the per-entry half of pair_js's shared rows)
+__global__ void k_xlogx_values(const double* x, int64_t nnz, double* xl) {
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < nnz; a += (int64_t)gridDim.x * blockDim.x)
+    xl[a] = xlogx(x[a]);
 }
 
 __device__ __forceinline__ double pair_value(int method, bool dist, const DevCsc& A,
@@ -274,20 +367,136 @@ __device__ __forceinline__ double pair_value(int method, bool dist, const DevCsc
     case MANHATTAN: return pair_manhattan(A, i, B, j);
     case PEARSON: return pair_pearson(A, aa, i, B, ba, j, dist);
     case COVARIANCE: return pair_covariance(A, aa, i, B, ba, j);
-    default: return pair_js(A, i, B, j);
+    default: return pair_js(A, aa, i, B, ba, j);
   }
 }
 
+// ---- the query column as a row lookup -----------------------------------------
+//
+// For the match-only methods (binary, cosine, pearson, covariance) and js's
+// bulk form, a pair's value needs only the rows stored in both columns, in
+// ascending row order.  With the query column held in shared memory as a row
+// lookup -- bit r % 32 of bits[r / 32] set when row r is stored, base[w] the
+// position in the column of the first stored row of word w (read only for
+// words that hold one) -- a thread walks its reference column alone: every
+// stored row is tested with one shared-memory load, no load's address waits
+// on a comparison (the merge walk's serial dependence), and the matched rows
+// come in the same ascending order as in the merge walk, so every sum is the
+// same sequence of operations and the values are the merge walk's bit for bit.
+constexpr int32_t LOOKUP_MAX_ROWS = 32768;
+
+__host__ __device__ __forceinline__ bool lookup_method(int method) {
+  return method == BINARY || method == COSINE || method == PEARSON || method == COVARIANCE || method == JS;
+}
+
+// The lookup of column q, built by the threads t = 0 .. nt - 1 of the calling
+// group (a warp or a block): first lookup_clear, then (after the group
+// synchronises) lookup_fill, then the group synchronises again.
+__device__ __forceinline__ void lookup_clear(uint32_t* bits, int32_t nrow, int t, int nt) {
+  for (int32_t w = t; w < ((nrow + 31) >> 5); w += nt) bits[w] = 0u;
+}
+__device__ __forceinline__ void lookup_fill(const DevCsc& Q, int32_t q, uint32_t* bits, int32_t* base, int t,
+                                            int nt) {
+  const int64_t b0 = Q.p[q], b1 = Q.p[q + 1];
+  for (int64_t b = b0 + t; b < b1; b += nt) {
+    const int32_t row = __ldg(Q.i + b);
+    atomicOr(bits + (row >> 5), 1u << (row & 31));
+    if (b == b0 || (__ldg(Q.i + b - 1) >> 5) != (row >> 5)) base[row >> 5] = (int32_t)(b - b0);
+  }
+}
+
+// pair_value(method, dist, R, ra, r, Q, qa, q) for a lookup method, with
+// column q of Q given as its lookup.
+__device__ double pair_value_lookup(int method, bool dist, const DevCsc& R, const ColAux& ra, int32_t r,
+                                    const DevCsc& Q, const ColAux& qa, int32_t q, const uint32_t* bits,
+                                    const int32_t* base) {
+  const int64_t a0 = R.p[r], a1 = R.p[r + 1], qb = Q.p[q];
+  switch (method) {
+    case BINARY: {
+      int64_t common = 0;
+      for (int64_t a = a0; a < a1; ++a) {
+        const int32_t row = __ldg(R.i + a);
+        common += (bits[row >> 5] >> (row & 31)) & 1u;
+      }
+      return binary_finish((double)(a1 - a0), (double)(Q.p[q + 1] - qb), common, dist);
+    }
+    case COSINE: {
+      const bool ea = (ra.scale[r] == 0.0), eb = (qa.scale[q] == 0.0);
+      if (ea || eb) {
+        const double c = (ea && eb) ? 1.0 : 0.0;
+        return dist ? dsub(1.0, c) : c;
+      }
+      double sum = 0.0;
+      for (int64_t a = a0; a < a1; ++a) {
+        const int32_t row = __ldg(R.i + a);
+        const uint32_t w = bits[row >> 5];
+        if ((w >> (row & 31)) & 1u) {
+          const int64_t b = qb + base[row >> 5] + __popc(w & ((1u << (row & 31)) - 1u));
+          sum = dadd(sum, dmul(ra.uval[a], qa.uval[b]));
+        }
+      }
+      return cosine_finish(sum, dist);
+    }
+    case PEARSON:
+    case COVARIANCE: {
+      double sab = 0.0;
+      for (int64_t a = a0; a < a1; ++a) {
+        const int32_t row = __ldg(R.i + a);
+        const uint32_t w = bits[row >> 5];
+        if ((w >> (row & 31)) & 1u) {
+          const int64_t b = qb + base[row >> 5] + __popc(w & ((1u << (row & 31)) - 1u));
+          sab = dadd(sab, dmul(R.x[a], Q.x[b]));
+        }
+      }
+      return method == PEARSON ? pearson_finish(sab, R.nrow, ra, r, qa, q, dist)
+                               : covariance_finish(sab, R.nrow, ra, r, qa, q);
+    }
+    case JS: {
+      if (!ra.xsum || !qa.xsum || !ra.xl || !qa.xl) return pair_js_walk(R, ra, r, Q, qa, q);
+      double shared = 0.0, sp = 0.0, sq = 0.0;
+      for (int64_t a = a0; a < a1; ++a) {
+        const int32_t row = __ldg(R.i + a);
+        const uint32_t w = bits[row >> 5];
+        if ((w >> (row & 31)) & 1u) {
+          const int64_t b = qb + base[row >> 5] + __popc(w & ((1u << (row & 31)) - 1u));
+          const double P = R.x[a], Qv = Q.x[b];
+          shared = dadd(shared, js_shared_term(P, Qv, ra.xl[a], qa.xl[b]));
+          sp = dadd(sp, P);
+          sq = dadd(sq, Qv);
+        }
+      }
+      double v;
+      if (!js_bulk(ra.xsum[r], qa.xsum[q], sp, sq, shared, &v)) return pair_js_walk(R, ra, r, Q, qa, q);
+      return v;
+    }
+    default:
+      return pair_value(method, dist, R, ra, r, Q, qa, q);
+  }
+}
+
+// One query column per blockIdx.y, one reference column per thread.  With
+// `lookup` (a lookup method and nrow <= LOOKUP_MAX_ROWS) the block first holds
+// its query column as a row lookup in dynamic shared memory.
 __global__ void k_exact_slab(int method, int dist, DevCsc ref, ColAux ra, DevCsc qry, ColAux qa,
                              int64_t q0, const uint8_t* ref_mask, int restore_self,
-                             double self_value, double* D) {
+                             double self_value, double* D, int lookup) {
+  extern __shared__ uint32_t lk_bits[];
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t b = blockIdx.y;
-  if (i >= ref.ncol) return;
   const int64_t q = q0 + b;
+  const int32_t words = (qry.nrow + 31) >> 5;
+  int32_t* lk_base = reinterpret_cast<int32_t*>(lk_bits + words);
+  if (lookup) {
+    lookup_clear(lk_bits, qry.nrow, threadIdx.x, blockDim.x);
+    __syncthreads();
+    lookup_fill(qry, (int32_t)q, lk_bits, lk_base, threadIdx.x, blockDim.x);
+    __syncthreads();
+  }
+  if (i >= ref.ncol) return;
   double v;
   if (ref_mask && ref_mask[i]) v = na_real();
   else if (restore_self && i == q) v = self_value;
+  else if (lookup) v = pair_value_lookup(method, dist != 0, ref, ra, (int32_t)i, qry, qa, (int32_t)q, lk_bits, lk_base);
   else v = pair_value(method, dist != 0, ref, ra, (int32_t)i, qry, qa, (int32_t)q);
   D[b * (int64_t)ref.ncol + i] = v;
 }
@@ -721,14 +930,18 @@ constexpr int BATCH_WARPS = 8;
 
 __global__ void __launch_bounds__(BATCH_WARPS * 32) k_batch_exact(const BatchProb* probs, const BatchItem* items,
                                                                   int64_t nitems, unsigned long long* counter,
-                                                                  int kmax, uint64_t* pkey, int32_t* pidx,
-                                                                  double* pval) {
+                                                                  int kmax, int lwords, uint64_t* pkey,
+                                                                  int32_t* pidx, double* pval) {
   extern __shared__ unsigned char bsm[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   uint64_t* lk = reinterpret_cast<uint64_t*>(bsm) + (int64_t)warp * kmax;
   double* lv = reinterpret_cast<double*>(bsm) + (int64_t)BATCH_WARPS * kmax + (int64_t)warp * kmax;
   int32_t* li = reinterpret_cast<int32_t*>(reinterpret_cast<double*>(bsm) + 2 * (int64_t)BATCH_WARPS * kmax) +
                 (int64_t)warp * kmax;
+  // this warp's query-column lookup (lwords words of bits, then of bases)
+  uint32_t* lbits = reinterpret_cast<uint32_t*>(bsm + (size_t)BATCH_WARPS * kmax * 20) + (int64_t)warp * 2 * lwords;
+  int32_t* lbase = reinterpret_cast<int32_t*>(lbits + lwords);
+  int32_t held_prob = -1, held_dir = -1, held_q = -1;        // the column the lookup holds
   for (;;) {
     unsigned long long it = 0;
     if (lane == 0) it = atomicAdd(counter, 1ull);
@@ -742,13 +955,22 @@ __global__ void __launch_bounds__(BATCH_WARPS * 32) k_batch_exact(const BatchPro
     const uint8_t* rmask = fwd ? P.ymask : P.xmask;
     const int K = fwd ? P.kf : P.kr;
     const bool dec = P.decreasing != 0;
+    const bool lookup = lookup_method(P.method) && Q.nrow <= lwords * 32;
+    if (lookup && (held_prob != I.prob || held_dir != I.dir || held_q != I.q)) {
+      lookup_clear(lbits, Q.nrow, lane, 32);
+      __syncwarp();
+      lookup_fill(Q, I.q, lbits, lbase, lane, 32);
+      __syncwarp();
+      held_prob = I.prob; held_dir = I.dir; held_q = I.q;
+    }
     int n = 0;
     for (int32_t b = I.r0; b < I.r1; b += 32) {
       const int32_t r = b + lane;
       bool ok = r < I.r1 && !(rmask && rmask[r]);
       double v = 0.0;
       if (ok) {
-        v = pair_value(P.method, P.dist != 0, R, ra, r, Q, qa, I.q);
+        v = lookup ? pair_value_lookup(P.method, P.dist != 0, R, ra, r, Q, qa, I.q, lbits, lbase)
+                   : pair_value(P.method, P.dist != 0, R, ra, r, Q, qa, I.q);
         ok = isfinite(v);
       }
       topk::insert_batch(ok, ok ? order_key(v, dec) : 0, r, v, lk, li, lv, n, K, lane);
@@ -812,6 +1034,10 @@ void launch_unit_csc(const DevCsc& M, double* uval, double* scale, int* err, cud
 void launch_moments(const DevCsc& M, double* sum, double* sumsq, cudaStream_t s) {
   if (M.ncol > 0) k_moments<<<blocks_for(M.ncol, 128), 128, 0, s>>>(M, sum, sumsq);
 }
+void launch_xlogx_values(const double* x, int64_t nnz, double* xl, cudaStream_t s) {
+  if (nnz > 0) k_xlogx_values<<<(unsigned)std::min<int64_t>((nnz + 255) / 256, 152 * 32), 256, 0, s>>>(x, nnz, xl);
+}
+
 void launch_check_js(const double* x, int64_t nnz, int* err, cudaStream_t s) {
   if (nnz > 0) {
     unsigned g = blocks_for(nnz, 256);
@@ -828,8 +1054,10 @@ void launch_exact_slab(int method, int dist, const DevCsc& ref, const ColAux& ra
   for (int64_t b0 = 0; b0 < nb; b0 += 65535) {            // gridDim.y limit
     const int64_t cnt = (nb - b0 < 65535) ? nb - b0 : 65535;
     dim3 grid(blocks_for(ref.ncol, 128), (unsigned)cnt);
-    k_exact_slab<<<grid, 128, 0, s>>>(method, dist, ref, ra, qry, qa, q0 + b0, ref_mask,
-                                      restore_self, self_value, D + b0 * (int64_t)ref.ncol);
+    const bool lookup = lookup_method(method) && qry.nrow <= LOOKUP_MAX_ROWS;
+    const size_t smem = lookup ? (size_t)((qry.nrow + 31) / 32) * 8 : 0;
+    k_exact_slab<<<grid, 128, smem, s>>>(method, dist, ref, ra, qry, qa, q0 + b0, ref_mask,
+                                         restore_self, self_value, D + b0 * (int64_t)ref.ncol, lookup ? 1 : 0);
   }
 }
 
@@ -924,16 +1152,21 @@ namespace sdg {
 
 size_t batch_smem(int kmax) { return (size_t)BATCH_WARPS * kmax * 20; }
 
+int batch_lookup_words(int method, int32_t nrow) {
+  return (lookup_method(method) && nrow <= LOOKUP_MAX_ROWS) ? (nrow + 31) / 32 : 0;
+}
+
 void launch_batch_exact(const BatchProb* probs, const BatchItem* items, int64_t nitems, unsigned long long* counter,
-                        int kmax, uint64_t* pkey, int32_t* pidx, double* pval, int sms, cudaStream_t s) {
+                        int kmax, int lwords, uint64_t* pkey, int32_t* pidx, double* pval, int sms, cudaStream_t s) {
   if (nitems <= 0) return;
-  const size_t smem = batch_smem(kmax);
+  const size_t smem = batch_smem(kmax) + (size_t)BATCH_WARPS * lwords * 8;
   if (smem > 48 * 1024) cudaFuncSetAttribute(k_batch_exact, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int per_sm = 1;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_exact, BATCH_WARPS * 32, smem);
   const int64_t grid = std::min<int64_t>((int64_t)std::max(1, per_sm) * std::max(1, sms),
                                          (nitems + BATCH_WARPS - 1) / BATCH_WARPS);
-  k_batch_exact<<<(unsigned)grid, BATCH_WARPS * 32, smem, s>>>(probs, items, nitems, counter, kmax, pkey, pidx, pval);
+  k_batch_exact<<<(unsigned)grid, BATCH_WARPS * 32, smem, s>>>(probs, items, nitems, counter, kmax, lwords, pkey,
+                                                                pidx, pval);
 }
 
 void launch_batch_merge(const BatchProb* probs, const BatchRow* rows, int64_t nrows, int kmax, const uint64_t* pkey,

@@ -31,6 +31,15 @@ void launch_col_empty(const DevCsc& M, uint8_t* empty, cudaStream_t s);
 void launch_unit_csc(const DevCsc& M, double* uval, double* scale, int* err, cudaStream_t s);
 void launch_moments(const DevCsc& M, double* sum, double* sumsq, cudaStream_t s);
 void launch_check_js(const double* x, int64_t nnz, int* err, cudaStream_t s);
+// xl[a] = xlogx(x[a]) for every stored value (js pair values reuse them)
+void launch_xlogx_values(const double* x, int64_t nnz, double* xl, cudaStream_t s);
+
+// Failure-detection test hook of the tcgen05 screens (sdg_sparse_tc.cu):
+// tc_set_stall(n) makes the next n launches of k_dense_tc / k_sparse_tc wait
+// on a phase that nothing completes, so that the bounded wait runs out and
+// the launch returns its timeout status; tc_take_stall() consumes one.
+void tc_set_stall(int n);
+bool tc_take_stall();
 
 // Exact values of every pair (ref column i, query column q0 + b) for
 // b < nb into D (nb columns of length ref.ncol).  Masked reference columns
@@ -115,7 +124,7 @@ struct SelectArgs {
   const int32_t* cand_count = nullptr;
   int64_t cand_ld = 0;
 };
-constexpr int kMaxK = 1024;   // largest k the selection kernels hold on chip
+constexpr int kMaxK = 1024;   // largest k whose selection lists sit in shared memory (and the screens' limit)
 
 // ---- sdg_exact.cu: batched exact kNN of many independent problems -------------
 // Problem p of a batch: the forward direction searches the columns of X among
@@ -143,8 +152,11 @@ struct BatchRow {
 };
 constexpr int kBatchMaxK = 256;          // largest k of the batched exact path
 size_t batch_smem(int kmax);
+// words of a query-column row lookup per warp for a problem of this method and
+// row count (0: the problem's pairs use the merge walk)
+int batch_lookup_words(int method, int32_t nrow);
 void launch_batch_exact(const BatchProb* probs, const BatchItem* items, int64_t nitems, unsigned long long* counter,
-                        int kmax, uint64_t* pkey, int32_t* pidx, double* pval, int sms, cudaStream_t s);
+                        int kmax, int lwords, uint64_t* pkey, int32_t* pidx, double* pval, int sms, cudaStream_t s);
 void launch_batch_merge(const BatchProb* probs, const BatchRow* rows, int64_t nrows, int kmax, const uint64_t* pkey,
                         const int32_t* pidx, const double* pval, cudaStream_t s);
 void launch_select(const SelectArgs& a, cudaStream_t s);

@@ -8,6 +8,8 @@
 // of the candidate set whatever order candidates arrive in: it equals the
 // bounded-heap results of topKBlock (src/topK.cpp:104-131) and of
 // topKRowsAccum's strictly-better replacement (src/topKRows.cpp:201-228).
+#include <algorithm>
+
 #include "sdg_kernels.h"
 #include "sdg_topk.cuh"
 
@@ -16,17 +18,9 @@ namespace {
 
 using namespace topk;
 
-__global__ void k_select(SelectArgs a) {
-  extern __shared__ unsigned char smem[];
-  const int warps = blockDim.x >> 5;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t seg = (int64_t)blockIdx.x * warps + warp;
-  if (seg >= a.nseg) return;                         // uniform per warp
+// Selects output row seg of the call into the list (lk, li, lv) of k slots.
+__device__ void select_row(const SelectArgs& a, int64_t seg, uint64_t* lk, double* lv, int32_t* li, int lane) {
   const int K = a.k;
-  uint64_t* lk = reinterpret_cast<uint64_t*>(smem) + (int64_t)warp * K;
-  double* lv = reinterpret_cast<double*>(smem) + (int64_t)warps * K + (int64_t)warp * K;
-  int32_t* li = reinterpret_cast<int32_t*>(reinterpret_cast<uint64_t*>(smem) + 2 * (int64_t)warps * K) +
-                (int64_t)warp * K;
   const bool dec = a.decreasing != 0;
   const int64_t row = a.out_row0 + seg;
   int n = 0;
@@ -76,15 +70,67 @@ __global__ void k_select(SelectArgs a) {
   }
 }
 
+// k <= kMaxK: a warp's list in shared memory, one row per warp.
+__global__ void k_select(SelectArgs a) {
+  extern __shared__ unsigned char smem[];
+  const int warps = blockDim.x >> 5;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t seg = (int64_t)blockIdx.x * warps + warp;
+  if (seg >= a.nseg) return;                         // uniform per warp
+  const int K = a.k;
+  uint64_t* lk = reinterpret_cast<uint64_t*>(smem) + (int64_t)warp * K;
+  double* lv = reinterpret_cast<double*>(smem) + (int64_t)warps * K + (int64_t)warp * K;
+  int32_t* li = reinterpret_cast<int32_t*>(reinterpret_cast<uint64_t*>(smem) + 2 * (int64_t)warps * K) +
+                (int64_t)warp * K;
+  select_row(a, seg, lk, lv, li, lane);
+}
+
+// Bytes of one warp's list in device scratch: k keys (8 B), values (8 B) and
+// indices (4 B), rounded up to 16 so that every warp's keys stay 8-byte aligned.
+__host__ __device__ __forceinline__ int64_t wide_list_bytes(int64_t k) { return (k * 20 + 15) / 16 * 16; }
+
+// Any k: each warp owns wide_list_bytes(k) of device scratch and takes rows
+// warp, warp + (all warps), ...  The list's operations are the same, in
+// global memory (a row's list is private to its warp; L1 holds its tail).
+__global__ void k_select_wide(SelectArgs a, unsigned char* scratch) {
+  const int warps = blockDim.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int64_t w = (int64_t)blockIdx.x * warps + (threadIdx.x >> 5);
+  const int64_t stride = (int64_t)gridDim.x * warps;
+  const int64_t K = a.k;
+  unsigned char* base = scratch + w * wide_list_bytes(K);
+  uint64_t* lk = reinterpret_cast<uint64_t*>(base);
+  double* lv = reinterpret_cast<double*>(base + K * 8);
+  int32_t* li = reinterpret_cast<int32_t*>(base + K * 16);
+  for (int64_t seg = w; seg < a.nseg; seg += stride) {
+    select_row(a, seg, lk, lv, li, lane);
+    __syncwarp();
+  }
+}
+
 }  // namespace
 
 void launch_select(const SelectArgs& a, cudaStream_t s) {
   if (a.nseg <= 0) return;
-  int warps = 8;
-  while (warps > 1 && (size_t)warps * a.k * 20 > 48 * 1024) warps >>= 1;
-  const size_t smem = (size_t)warps * a.k * 20;
-  const int64_t blocks = (a.nseg + warps - 1) / warps;
-  k_select<<<(unsigned)blocks, warps * 32, smem, s>>>(a);
+  if (a.k <= kMaxK) {
+    int warps = 8;
+    while (warps > 1 && (size_t)warps * a.k * 20 > 48 * 1024) warps >>= 1;
+    const size_t smem = (size_t)warps * a.k * 20;
+    const int64_t blocks = (a.nseg + warps - 1) / warps;
+    k_select<<<(unsigned)blocks, warps * 32, smem, s>>>(a);
+    return;
+  }
+  // Lists in device scratch: at most 256 MiB of them and 64 warps per SM.
+  const int warps = 8;
+  const int64_t per = wide_list_bytes(a.k);
+  int64_t nw = std::min<int64_t>(a.nseg, std::max<int64_t>(1, ((int64_t)256 << 20) / per));
+  nw = std::min<int64_t>(nw, 152 * 64);
+  const int64_t blocks = (nw + warps - 1) / warps;
+  unsigned char* scratch = nullptr;
+  // a failed allocation is left as the thread's last error for the caller's check
+  if (cudaMallocAsync(reinterpret_cast<void**>(&scratch), (size_t)(blocks * warps * per), s) != cudaSuccess) return;
+  k_select_wide<<<(unsigned)blocks, warps * 32, 0, s>>>(a, scratch);
+  cudaFreeAsync(scratch, s);
 }
 
 }  // namespace sdg

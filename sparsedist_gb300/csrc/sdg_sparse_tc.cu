@@ -47,6 +47,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
 #include <cmath>
 
@@ -100,6 +101,7 @@ struct SArgs {
   int32_t* eidx;                           // [nq][nrr][ECAP]
   float* ehi;
   int* status;
+  int stall;                               // failure-detection test: the MMA issuer's first wait never completes
 };
 
 // Per-thread hot-test coefficients (x = a s - b w >= C) for running cut `cut`
@@ -197,7 +199,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_sparse_tc(const __grid_constant_
       bool ok = true;
       for (int j = 0; j < ntile && ok; ++j) {
         // the epilogue has drained tile j - 1
-        if (!mbar_wait(acc_empty, ((uint32_t)j & 1u) ^ 1u, abort_flag, P.status)) break;
+        // (with P.stall the first wait asks for the phase the epilogue has not
+        // begun, so it runs out: the failure-detection test's path)
+        const uint32_t flip = (P.stall && j == 0) ? 0u : 1u;
+        if (!mbar_wait(acc_empty, ((uint32_t)j & 1u) ^ flip, abort_flag, P.status)) break;
         fence_after();
         for (int c = 0; c < kch; ++c, ++it) {
           const int s = it % STAGES;
@@ -523,6 +528,7 @@ int stc_screen(const StcRun& R, cudaStream_t s, int32_t* cand, int32_t* count, i
     P.qnnz = R.qnnz; P.qnorm = R.qnorm; P.qerr = R.qerr; P.qbn = R.qbn;
     P.qskip = qskip;
     P.lists = lists; P.ecount = ecount; P.eidx = eidx; P.ehi = ehi; P.status = status;
+    P.stall = tc_take_stall() ? 1 : 0;
     k_stc_skip<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(nb, R.q0, R.qry_blank, R.qry_force, qskip);
     const int k = R.k;
     auto kern = (k <= 16) ? k_sparse_tc<16> : (k <= 32) ? k_sparse_tc<32> : k_sparse_tc<64>;
@@ -549,6 +555,16 @@ int stc_screen(const StcRun& R, cudaStream_t s, int32_t* cand, int32_t* count, i
     return (int)cudaErrorLaunchTimeout;
   }
   return 0;
+}
+
+namespace {
+std::atomic<int> g_stall{0};
+}
+void tc_set_stall(int n) { g_stall.store(n > 0 ? n : 0); }
+bool tc_take_stall() {
+  int v = g_stall.load();
+  while (v > 0 && !g_stall.compare_exchange_weak(v, v - 1)) {}
+  return v > 0;
 }
 
 }  // namespace sdg

@@ -49,22 +49,19 @@ def sharded_knn(X, search, *, world: int, rank: int, group=None, gather: bool = 
     ``search`` returns the rows of the kNN result for query columns
     [lo, hi) as (hi - lo, k) arrays (idx 1-based into the reference, NA
     padded).  With ``gather`` the full (ncol, k) result is assembled on every
-    rank with torch.distributed.all_gather_object; the shards are disjoint and
-    ordered by rank, so the assembled matrix is exactly the single-process
-    result."""
+    rank with one tensor all-gather (NCCL on GPUs, gloo on CPUs); the shards
+    are disjoint and ordered by rank, so the assembled matrix is exactly the
+    single-process result."""
     ncol = X.shape[1]
     lo, hi = shard_bounds(ncol, world, rank)
     idx, dist = search(lo, hi)
     if not gather or world == 1:
         return (lo, hi), idx, dist
-    import torch.distributed as tdist
-    parts = [None] * world
-    tdist.all_gather_object(parts, (lo, hi, np.asarray(idx), np.asarray(dist)), group=group)
-    parts.sort(key=lambda t: t[0])
-    k = max(p[2].shape[1] for p in parts)
-    full_idx = np.concatenate([p[2] for p in parts], axis=0)
-    full_dist = np.concatenate([p[3] for p in parts], axis=0)
-    assert full_idx.shape == (ncol, k)
+    rows = [shard_bounds(ncol, world, r) for r in range(world)]
+    parts = _all_gather_lists(np.asarray(idx), np.asarray(dist), [b - a for a, b in rows], group)
+    full_idx = np.concatenate([p[0] for p in parts], axis=0)
+    full_dist = np.concatenate([p[1] for p in parts], axis=0)
+    assert full_idx.shape[0] == ncol
     return (0, ncol), full_idx, full_dist
 
 
@@ -108,10 +105,37 @@ def global_count(local: int, group=None) -> int:
     return int(t.item())
 
 
-def _gather_parts(obj, world, group):
+def _all_gather_lists(idx, dist, rows, group):
+    """Every rank's (rows[r], k) idx / dist lists on every rank, in rank order.
+
+    One all-gather of a (max(rows), 2k) int64 tensor per rank: idx widened in
+    the first k columns, the float64 bit patterns of dist (NA payloads
+    included) in the last k.  On an NCCL group the tensors live on the current
+    CUDA device; on gloo, on the host.  k is the same on every rank (the
+    whole search's clamp), which the lengths exchanged first confirm."""
+    import torch
     import torch.distributed as tdist
-    parts = [None] * world
-    tdist.all_gather_object(parts, obj, group=group)
+    idx = np.asarray(idx, np.int32)
+    dist = np.ascontiguousarray(np.asarray(dist, np.float64))
+    n, k = idx.shape
+    dev = torch.device("cuda", torch.cuda.current_device()) if tdist.get_backend(group) == "nccl" \
+        else torch.device("cpu")
+    world = len(rows)
+    ks = [torch.zeros(1, dtype=torch.int64, device=dev) for _ in range(world)]
+    tdist.all_gather(ks, torch.tensor([k], dtype=torch.int64, device=dev), group=group)
+    if any(int(t.item()) != k for t in ks):
+        raise RuntimeError("ranks disagree on k: " + str([int(t.item()) for t in ks]))
+    m = max(max(rows), 1)
+    buf = np.zeros((m, 2 * k), np.int64)
+    buf[:n, :k] = idx
+    buf[:n, k:] = dist.view(np.int64)
+    mine = torch.from_numpy(buf).to(dev)
+    got = [torch.empty_like(mine) for _ in range(world)]
+    tdist.all_gather(got, mine, group=group)
+    parts = []
+    for r, t in enumerate(got):
+        a = t.cpu().numpy()[:rows[r]]
+        parts.append((a[:, :k].astype(np.int32), np.ascontiguousarray(a[:, k:]).view(np.float64)))
     return parts
 
 
@@ -126,7 +150,8 @@ def sharded_knn_reference(ncol_ref: int, search_shard, *, k_eff: int, decreasing
     idx, dist = search_shard(r0, r1)
     if world == 1:
         return merge_topk([(idx, dist)], k_eff, decreasing)
-    parts = _gather_parts((np.asarray(idx), np.asarray(dist)), world, group)
+    idx, dist = np.asarray(idx), np.asarray(dist)
+    parts = _all_gather_lists(idx, dist, [idx.shape[0]] * world, group)
     return merge_topk(parts, k_eff, decreasing)
 
 
@@ -145,11 +170,12 @@ def sharded_knn_cross(ncol_x: int, forward_search, reverse_search, *, k_rev: int
     ri, rd = reverse_search(lo, hi)
     if world == 1:
         return (np.asarray(fi), np.asarray(fd)), merge_topk([(ri, rd)], k_rev, decreasing)
-    parts = _gather_parts((lo, np.asarray(fi), np.asarray(fd), np.asarray(ri), np.asarray(rd)),
-                          world, group)
-    parts.sort(key=lambda t: t[0])
-    fwd = (np.concatenate([p[1] for p in parts], axis=0), np.concatenate([p[2] for p in parts], axis=0))
-    rev = merge_topk([(p[3], p[4]) for p in parts], k_rev, decreasing)
+    rows = [shard_bounds(ncol_x, world, r) for r in range(world)]
+    fparts = _all_gather_lists(fi, fd, [b - a for a, b in rows], group)
+    ri, rd = np.asarray(ri), np.asarray(rd)
+    rparts = _all_gather_lists(ri, rd, [ri.shape[0]] * world, group)
+    fwd = (np.concatenate([p[0] for p in fparts], axis=0), np.concatenate([p[1] for p in fparts], axis=0))
+    rev = merge_topk(rparts, k_rev, decreasing)
     return fwd, rev
 
 
