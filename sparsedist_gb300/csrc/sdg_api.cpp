@@ -231,8 +231,8 @@ struct sdg_matrix {
   int js_status = 1;
   DevBuf xl;                    // js: xlogx of each stored value
   DevBuf xsum;                  // js: column sums
-  ScreenCache screen[4];        // screening data per method (sdg_screen.h), binary..manhattan
-  TensorCache tensor[4];        // dense BF16 screen values per method (tensor-core screen)
+  ScreenCache screen[kMethodCount];   // screening data per method (sdg_screen.h)
+  TensorCache tensor[kMethodCount];   // dense FP16 screen values per method (tensor-core screen)
 
   ~sdg_matrix() {
     if (ctx) {
@@ -528,7 +528,7 @@ void knn_device(sdg_ctx* c, sdg_matrix* X, sdg_matrix* Y, int method, int dist, 
     h.exact_range = [&](int64_t q0, int64_t n) { exact_engine(c, P, ref, X, d_idx, d_val, q0, q0 + n); };
     const int st = screen_knn(c->stream, r, ref->dev(), aux_of(ref), &ref->screen[method], &ref->tensor[method],
                               X->dev(), aux_of(X), &X->screen[method], &X->tensor[method], d_idx, d_val, c->stats, h);
-    if (st) cuda_check((cudaError_t)st, "screen_knn");
+    if (st) cuda_check((cudaError_t)st, (std::string("screen_knn (") + screen_error_site() + ")").c_str());
   } else {
     exact_engine(c, P, ref, X, d_idx, d_val, q_lo, q_hi);
   }

@@ -8,6 +8,7 @@
 namespace sdg {
 
 enum Method { BINARY = 0, COSINE = 1, EUCLIDEAN = 2, MANHATTAN = 3, PEARSON = 4, JS = 5, COVARIANCE = 6 };
+constexpr int kMethodCount = 7;
 
 constexpr int32_t NA_INT = INT32_MIN;
 constexpr uint64_t NA_REAL_BITS = 0x7FF00000000007A2ULL;   // R's NA_real_

@@ -51,7 +51,13 @@ inline unsigned blocks_for(int64_t n, int threads) {
   return (unsigned)((n + threads - 1) / threads);
 }
 
-#define SK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return (int)e_; } while (0)
+// the failing call of the last screen error on this thread (for the message)
+thread_local const char* g_screen_site = "";
+#define SK_STR2(l) #l
+#define SK_STR(l) SK_STR2(l)
+#define SK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { g_screen_site = #x " at line " SK_STR(__LINE__); return (int)e_; } } while (0)
+// a call of a function that records its own failing site
+#define SKN(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return (int)e_; } while (0)
 
 // ---------------------------------------------------------------------------
 // validation used at upload
@@ -76,12 +82,16 @@ __global__ void k_check_rows(DevCsc M, int* err) {
 // One warp per column: the FP32 screen values (coalesced) and the column's
 // norm term (a warp sum in FP64, rounded to FP32: the screen bounds allow for
 // its rounding whatever the summation order).
-__global__ void k_screen_prep(DevCsc M, int method, const double* uval, float* fval, float* cnorm,
-                              int32_t* nnz) {
+// js: fval = the value, fxl = its x log x (from the FP64 values the exact path
+// uses), cnorm = the column's sum of |x log x| + x rounded up, and *range_err
+// set when a nonzero value lies outside [2^-100, 2^100].
+__global__ void k_screen_prep(DevCsc M, int method, const double* uval, const double* xl, float* fval,
+                              float* fxl, float* cnorm, int32_t* nnz, int* range_err) {
   const int64_t j = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (j >= M.ncol) return;
   double acc = 0.0;
+  bool bad = false;
   const int64_t a0 = M.p[j], a1 = M.p[j + 1];
   for (int64_t a = a0 + lane; a < a1; a += 32) {
     const double v = M.x[a];
@@ -92,11 +102,17 @@ __global__ void k_screen_prep(DevCsc M, int method, const double* uval, float* f
     fval[a] = f;
     if (method == EUCLIDEAN) acc += v * v;
     else if (method == MANHATTAN) acc += fabs(v);
+    else if (method == JS) {
+      fxl[a] = (float)xl[a];
+      acc += fabs(xl[a]) + v;
+      bad = bad || (v != 0.0 && !(v >= 0x1p-100 && v <= 0x1p100));
+    }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(range_err, 1);
   if (lane == 0) {
-    cnorm[j] = (float)acc;
+    cnorm[j] = (method == JS) ? __double2float_ru(acc * (1.0 + 1e-12)) : (float)acc;
     nnz[j] = (int32_t)(a1 - a0);
   }
 }
@@ -118,10 +134,12 @@ struct ScreenArgs {
   int vcap;                   // tile value capacity (floats)
   // reference
   const int64_t* rp; const int32_t* ri; const float* rv;
+  const float* rxl;           // js: x log x of each reference value
   const int32_t* rperm;       // position -> reference column
   int64_t nr;
   // queries (columns of the query matrix)
   const int64_t* qp; const int32_t* qi; const float* qv;
+  const float* qxl;           // js: x log x of each query value
   const int32_t* tile_q;      // first local query of each tile
   const int32_t* tile_n;      // queries in each tile
   int64_t q_begin;            // local query 0 = query column q_begin
@@ -159,12 +177,32 @@ __device__ __forceinline__ void accumulate_word(int method, float (&acc)[QT], ui
   if (m) accumulate(method, acc, m, w & 0xffffu, v, vals);   // rows outside the tile: skip
 }
 
-template <int METHOD_KIND>   // 0: product, 1: manhattan
+// js: the shared row's g = S log S - P log P - Q log Q (S = P + Q) in FP32,
+// every operation rounded on its own (no contraction), summed in order:
+// the error analysis of js_key_and_bound below follows these steps.
+__device__ __forceinline__ void accumulate_js(float (&acc)[QT], uint32_t w, float v, float vx,
+                                              const float* __restrict__ vals, const float* __restrict__ vxl) {
+  uint32_t m = w >> 16;
+  uint32_t base = w & 0xffffu;
+#pragma unroll
+  for (int j = 0; j < QT; ++j) {
+    if (m & (1u << j)) {
+      const float q = vals[base], qx = vxl[base];
+      const float S = __fadd_rn(v, q);
+      const float g = __fsub_rn(__fsub_rn(__fmul_rn(S, logf(S)), vx), qx);
+      acc[j] = __fadd_rn(acc[j], g);
+      ++base;
+    }
+  }
+}
+
+template <int METHOD_KIND>   // 0: product, 1: manhattan, 2: js
 __global__ void __launch_bounds__(SCREEN_THREADS, 1) k_screen(ScreenArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   // row[r] = (mask16 << 16) | offset of row r's first value in vals[]
   uint32_t* row = reinterpret_cast<uint32_t*>(smem);
   float* vals = reinterpret_cast<float*>(row + A.nrow);
+  float* vxl = vals + A.vcap;                       // js: the values' x log x
   __shared__ int s_item;
   __shared__ uint32_t s_warp[SCREEN_THREADS / 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -229,7 +267,10 @@ __global__ void __launch_bounds__(SCREEN_THREADS, 1) k_screen(ScreenArgs A) {
         for (int64_t e = e0 + tid; e < e1; e += SCREEN_THREADS) {
           const uint32_t w = row[A.qi[e]];
           const uint32_t pos = (w & 0xffffu) + __popc((w >> 16) & below);
-          if (pos < (uint32_t)A.vcap) vals[pos] = A.qv[e];
+          if (pos < (uint32_t)A.vcap) {
+            vals[pos] = A.qv[e];
+            if (METHOD_KIND == 2) vxl[pos] = A.qxl[e];
+          }
         }
       }
       __syncthreads();
@@ -246,6 +287,12 @@ __global__ void __launch_bounds__(SCREEN_THREADS, 1) k_screen(ScreenArgs A) {
       for (int j = 0; j < QT; ++j) acc[j] = 0.f;
       int64_t e = A.rp[c];
       const int64_t e1 = A.rp[c + 1];
+      if (METHOD_KIND == 2) {
+        for (; e < e1; ++e) {
+          const uint32_t w = row[__ldg(A.ri + e)];
+          if (w >> 16) accumulate_js(acc, w, __ldg(A.rv + e), __ldg(A.rxl + e), vals, vxl);
+        }
+      }
       for (; e < e1 && (e & 3); ++e)
         accumulate_word(method, acc, row[__ldg(A.ri + e)], __ldg(A.rv + e), vals);
       if (e + 4 <= e1) {
@@ -284,6 +331,8 @@ struct SelectScreenArgs {
   const int32_t* rperm;
   const int32_t* rnnz; const float* rnorm;
   const int32_t* qnnz; const float* qnorm;   // indexed by query column
+  const double* rsum;                        // js: reference column sums
+  const double* qsum;                        // js: query column sums (indexed by query column)
   const uint8_t* ref_mask;                   // eligible reference columns
   const uint8_t* qry_blank;                  // query rows written all-NA
   const uint8_t* qry_force_exact;            // queries the screen cannot bound
@@ -316,6 +365,28 @@ __device__ __forceinline__ void key_and_bound(int method, float s, int32_t nq_, 
     key = (denom > 0.f) ? s / denom : 1.f;
     err = key * (4.f * U32) + 1e-30f;
   }
+}
+
+// js (fastJS2, src/sparseDist.cpp:1099-1108): the value is sqrt(0.5 t) with
+// t = (S_P + S_Q) log 2 - G, G = sum over shared rows of g = S log S - P log P
+// - Q log Q (every other row adds its value times log 2), so with the query
+// fixed the order is that of key = G - S_P log 2 (larger = better).  Error of
+// the FP32 G (values in [2^-100, 2^100], u = 2^-24): per shared row, with
+// p, q, S, logf (<= 1 ulp), the product and the two differences each rounded
+// once and x log x stored to FP32, |g~ - g| <= 10.01 u (|P log P| + |Q log Q|
+// + S) (using |S log S| <= |P log P| + |Q log Q| + S); summed over the shared
+// rows <= 10.01 u (A_P + A_Q), A = a column's sum of |x log x| + x.  The
+// recursive FP32 sum of n <= min(nnz) terms adds <= n u / (1 - n u) times
+// sum |g~| <= log 2 (C_P + C_Q) + 10.01 u (A_P + A_Q) (0 <= g <= S log 2,
+// C = a column's sum).  With n u <= 1/16 (n is below the row table's 56 K
+// rows) the two give E_G = u (10.8 (A_P + A_Q) + 0.75 n (C_P + C_Q)) 1.01; the
+// key's own rounding (u |key|, the FP64 S_P log 2 rounded once) is added.
+__device__ __forceinline__ void js_key_and_bound(float G, double SP, double SQ, float AP, float AQ,
+                                                 int32_t n_, float& key, float& err) {
+  const float n = (float)n_;
+  key = (float)((double)G - SP * 0.69314718055994530942);
+  const float C = (float)(SP + SQ);
+  err = U32 * (10.8f * (AP + AQ) + 0.75f * n * C) * 1.01f + 2.f * U32 * fabsf(key) + 1e-30f;
 }
 
 __global__ void k_screen_select(SelectScreenArgs A) {
@@ -351,7 +422,10 @@ __global__ void k_screen_select(SelectScreenArgs A) {
         if (A.include_self) lo = INFINITY; else ok = false;
       } else {
         float key, err;
-        key_and_bound(A.method, Srow[pos], nq_, Nq, A.rnnz[c], A.rnorm ? A.rnorm[c] : 0.f, key, err);
+        if (A.method == JS)
+          js_key_and_bound(Srow[pos], A.rsum[c], A.qsum[q], A.rnorm[c], Nq, min(nq_, A.rnnz[c]), key, err);
+        else
+          key_and_bound(A.method, Srow[pos], nq_, Nq, A.rnnz[c], A.rnorm ? A.rnorm[c] : 0.f, key, err);
         lo = key - err;
       }
     }
@@ -397,7 +471,10 @@ __global__ void k_screen_select(SelectScreenArgs A) {
       else if (c == self_c) keep = A.include_self != 0;
       else {
         float key, err;
-        key_and_bound(A.method, Srow[pos], nq_, Nq, A.rnnz[c], A.rnorm ? A.rnorm[c] : 0.f, key, err);
+        if (A.method == JS)
+          js_key_and_bound(Srow[pos], A.rsum[c], A.qsum[q], A.rnorm[c], Nq, min(nq_, A.rnnz[c]), key, err);
+        else
+          key_and_bound(A.method, Srow[pos], nq_, Nq, A.rnnz[c], A.rnorm ? A.rnorm[c] : 0.f, key, err);
         keep = (key + err) >= T - margin;
       }
     }
@@ -709,7 +786,7 @@ void launch_check_rows(const DevCsc& M, int* err, cudaStream_t s) {
 }
 
 bool screen_supported(int method, int k) {
-  return (method == BINARY || method == COSINE || method == EUCLIDEAN || method == MANHATTAN) &&
+  return (method == BINARY || method == COSINE || method == EUCLIDEAN || method == MANHATTAN || method == JS) &&
          k >= 1 && k <= 1024;
 }
 
@@ -723,6 +800,10 @@ static int ensure_cache(ScreenCache* c, int method, const DevCsc& M, const ColAu
                         cudaStream_t s) {
   const int family = method;
   if (c->method == family) return 0;
+  if (method == JS && !aux.xl) {                 // the js values' x log x come first
+    g_screen_site = "js x log x values missing";
+    return (int)cudaErrorInvalidValue;
+  }
   if (c->blob) { SK(cudaFreeAsync(c->blob, s)); *c = ScreenCache(); }
   const int64_t nnz = M.ncol > 0 ? -1 : 0;
   (void)nnz;
@@ -733,11 +814,17 @@ static int ensure_cache(ScreenCache* c, int method, const DevCsc& M, const ColAu
   auto seg = [](size_t bytes) { return (bytes + 255) & ~(size_t)255; };
   const size_t b_fval = seg(sizeof(float) * ((size_t)h_nnz + 4));
   const size_t b_col = seg(sizeof(float) * ((size_t)M.ncol + 4));
-  const size_t bytes = b_fval + 3 * b_col;
+  const bool js = method == JS;
+  const size_t bytes = (js ? 2 : 1) * b_fval + 3 * b_col + 256;
   SK(cudaMallocAsync(&c->blob, bytes, s));
   char* b = static_cast<char*>(c->blob);
   c->fval = reinterpret_cast<float*>(b);
   b += b_fval;
+  if (js) {
+    c->fxl = reinterpret_cast<float*>(b);
+    b += b_fval;
+  }
+  int* range_err = reinterpret_cast<int*>(static_cast<char*>(c->blob) + bytes - 256);
   c->cnorm = reinterpret_cast<float*>(b);
   b += b_col;
   c->nnz = reinterpret_cast<int32_t*>(b);
@@ -745,8 +832,9 @@ static int ensure_cache(ScreenCache* c, int method, const DevCsc& M, const ColAu
   c->perm = reinterpret_cast<int32_t*>(b);
   c->nnz_total = h_nnz;
   if (M.ncol > 0) {
-    k_screen_prep<<<blocks_for(M.ncol * 32, 256), 256, 0, s>>>(M, method, aux.uval, c->fval, c->cnorm,
-                                                                c->nnz);
+    SK(cudaMemsetAsync(range_err, 0, sizeof(int), s));
+    k_screen_prep<<<blocks_for(M.ncol * 32, 256), 256, 0, s>>>(M, method, aux.uval, aux.xl, c->fval, c->fxl,
+                                                                c->cnorm, c->nnz, range_err);
     // descending-nnz order of the columns (radix sort on 32-bit keys)
     uint32_t *k_in = nullptr, *k_out = nullptr;
     int32_t* ids = nullptr;
@@ -765,6 +853,13 @@ static int ensure_cache(ScreenCache* c, int method, const DevCsc& M, const ColAu
     SK(cudaFreeAsync(ids, s));
   }
   SK(cudaGetLastError());
+  c->values_ok = true;
+  if (js && M.ncol > 0) {
+    int h_err = 0;
+    SK(cudaMemcpyAsync(&h_err, range_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SK(cudaStreamSynchronize(s));
+    c->values_ok = h_err == 0;
+  }
   c->method = family;
   return 0;
 }
@@ -772,19 +867,27 @@ static int ensure_cache(ScreenCache* c, int method, const DevCsc& M, const ColAu
 int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColAux& ra,
                ScreenCache* rc, TensorCache* rt, const DevCsc& qry, const ColAux& qa, ScreenCache* qc,
                TensorCache* qt, int32_t* d_idx, double* d_val, int64_t* stats, const ScreenHooks& hooks) {
-  SK((cudaError_t)ensure_cache(rc, r.method, ref, ra, s));
-  SK((cudaError_t)ensure_cache(qc, r.method, qry, qa, s));
+  SKN((cudaError_t)ensure_cache(rc, r.method, ref, ra, s));
+  SKN((cudaError_t)ensure_cache(qc, r.method, qry, qa, s));
+  if (r.method == JS && !(rc->values_ok && qc->values_ok)) {
+    // values outside the range the FP32 js bound covers: every query exactly
+    const int64_t lo = r.q_lo, hi = (r.q_hi < 0) ? qry.ncol : r.q_hi;
+    if (hi > lo) hooks.exact_range(lo, hi - lo);
+    return 0;
+  }
   bool use_t = r.tensor && rt && qt && tensor_supported(r.method) && stc_supported(r.k);
   if (use_t) {
-    SK((cudaError_t)ensure_tensor(rt, r.method, ref, ra, rc, s));
-    if (qt != rt) SK((cudaError_t)ensure_tensor(qt, r.method, qry, qa, qc, s));
+    SKN((cudaError_t)ensure_tensor(rt, r.method, ref, ra, rc, s));
+    if (qt != rt) SKN((cudaError_t)ensure_tensor(qt, r.method, qry, qa, qc, s));
     use_t = rt->usable && qt->usable && rt->ld == qt->ld;
   }
   const int64_t nr = ref.ncol, nq = qry.ncol;
   const int32_t nrow = ref.nrow;
   const size_t tbytes = table_bytes(nrow);
-  // row offsets are 16-bit: a tile holds at most 65,535 values
-  const int vcap = (int)std::min<size_t>((kSmemMax - tbytes - 256) / 4, 65535);
+  // row offsets are 16-bit: a tile holds at most 65,535 values (js keeps each
+  // value's x log x beside it)
+  const size_t vbytes = (r.method == JS) ? 8 : 4;
+  const int vcap = (int)std::min<size_t>((kSmemMax - tbytes - 256) / vbytes, 65535);
   const int groups = (nrow + 63) / 64;
 
   // host copy of the query column sizes (tile formation)
@@ -832,11 +935,12 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
   // product): such queries go to the exact engine.
   if (r.method == COSINE && r.qry_empty) force = const_cast<uint8_t*>(r.qry_empty);
 
-  const size_t smem = tbytes + (size_t)vcap * 4 + 64;
+  const size_t smem = tbytes + (size_t)vcap * vbytes + 64;
   // a function attribute is per device: set on every call (cheap, thread-safe),
   // never cached process-wide
   SK(cudaFuncSetAttribute(k_screen<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax));
   SK(cudaFuncSetAttribute(k_screen<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax));
+  SK(cudaFuncSetAttribute(k_screen<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax));
   int nsm = 152;
   {
     int dev = 0;
@@ -914,21 +1018,24 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
 
     ScreenArgs A;
     A.method = r.method; A.nrow = nrow; A.groups = groups; A.vcap = vcap;
-    A.rp = ref.p; A.ri = ref.i; A.rv = rc->fval; A.rperm = rc->perm; A.nr = nr;
-    A.qp = qry.p; A.qi = qry.i; A.qv = qc->fval;
+    A.rp = ref.p; A.ri = ref.i; A.rv = rc->fval; A.rxl = rc->fxl; A.rperm = rc->perm; A.nr = nr;
+    A.qp = qry.p; A.qi = qry.i; A.qv = qc->fval; A.qxl = qc->fxl;
     A.tile_q = tile_q; A.tile_n = tile_n; A.q_begin = q0; A.ntiles = ntiles; A.nparts = nparts;
     A.part_len = part_len; A.S = S; A.work = work;
     const int grid = std::min<int64_t>((int64_t)nsm, (int64_t)ntiles * nparts);
     hooks.time_begin();
     if (r.method == MANHATTAN) k_screen<1><<<grid, SCREEN_THREADS, smem, s>>>(A);
+    else if (r.method == JS) k_screen<2><<<grid, SCREEN_THREADS, smem, s>>>(A);
     else k_screen<0><<<grid, SCREEN_THREADS, smem, s>>>(A);
     hooks.time_end();
     SK(cudaGetLastError());
 
     SelectScreenArgs B;
     B.method = r.method; B.k = r.k; B.S = S; B.nr = nr; B.rperm = rc->perm;
-    B.rnnz = rc->nnz; B.rnorm = (r.method == EUCLIDEAN || r.method == MANHATTAN) ? rc->cnorm : nullptr;
-    B.qnnz = qc->nnz; B.qnorm = (r.method == EUCLIDEAN || r.method == MANHATTAN) ? qc->cnorm : nullptr;
+    const bool normed = r.method == EUCLIDEAN || r.method == MANHATTAN || r.method == JS;
+    B.rnnz = rc->nnz; B.rnorm = normed ? rc->cnorm : nullptr;
+    B.qnnz = qc->nnz; B.qnorm = normed ? qc->cnorm : nullptr;
+    B.rsum = ra.xsum; B.qsum = qa.xsum;
     B.ref_mask = r.ref_mask; B.qry_blank = r.qry_blank; B.qry_force_exact = force;
     B.q_begin = q0; B.nq = nb; B.selfmode = r.selfmode; B.include_self = r.include_self;
     B.cap = cap; B.cand = cand; B.count = count; B.overflow = over;
@@ -995,5 +1102,7 @@ void screen_cache_free(ScreenCache* c, cudaStream_t s) {
   if (c && c->blob) cudaFreeAsync(c->blob, s);
   if (c) *c = ScreenCache();
 }
+
+const char* screen_error_site() { return g_screen_site; }
 
 }  // namespace sdg

@@ -18,10 +18,14 @@ struct ScreenCache {
   int method = -1;
   void* blob = nullptr;      // one device allocation holding the arrays below
   float* fval = nullptr;     // per stored entry: value the screen multiplies
-  float* cnorm = nullptr;    // per column: norm term of the method
+  float* fxl = nullptr;      // js: per stored entry, x log x of the value (FP32)
+  float* cnorm = nullptr;    // per column: norm term of the method (js: sum of |x log x| + x, rounded up)
   int32_t* nnz = nullptr;    // per column: stored entries
   int32_t* perm = nullptr;   // columns in descending-nnz order
   int64_t nnz_total = 0;
+  // js: every nonzero stored value lies in [2^-100, 2^100], the range the FP32
+  // js bound is derived for; else the js searches of this matrix are exact
+  bool values_ok = true;
 };
 
 // Dense FP16 copy of one matrix's screen values for the tensor-core screen
@@ -84,6 +88,8 @@ struct StcRun {
   const uint8_t* qry_force = nullptr;
 };
 bool stc_supported(int k);
+// the call that failed in the last screen_knn error on this thread
+const char* screen_error_site();
 // 0 or a cudaError_t value (the message is set)
 int stc_screen(const StcRun& r, cudaStream_t s, int32_t* cand, int32_t* count, int32_t* over, int cap,
                const std::function<void()>& time_begin, const std::function<void()>& time_end);

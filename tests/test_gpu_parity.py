@@ -73,3 +73,22 @@ def test_gpu_engines_agree_bit_for_bit(gpu):
         assert same_bits(a[0], b[0]) and same_bits(a[1], b[1]), method
         assert same_bits(a[0], c[0]) and same_bits(a[1], c[1]), method
     gpu.set_engine(0)
+
+
+def test_js_screen_equals_exact_engine(gpu):
+    """js on the FP32 screen (engine 2: FP32 G with its bound, exact FP64
+    re-rank of the survivors) returns the exact engine's result bit for bit;
+    a matrix with values outside the bound's range (1e-40) is searched
+    exactly by the same call."""
+    X = normalise_cols(make_x(3000, 4000, 0.05, 41))
+    Y = normalise_cols(make_x(3000, 2500, 0.05, 42))
+    T = X.copy()
+    T.data[::97] = 1e-40
+    for A, B in ((X, None), (X, Y), (T, None)):
+        gpu.set_engine(1)
+        a = gpu.knn(A, B, k=20, method="js")
+        gpu.set_engine(2)
+        b = gpu.knn(A, B, k=20, method="js")
+        assert a[2] == b[2]
+        assert same_bits(a[0], b[0]) and same_bits(a[1], b[1])
+    gpu.set_engine(0)

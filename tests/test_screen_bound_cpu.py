@@ -96,3 +96,96 @@ def test_bound_covers_raw_values_and_patterns():
     check_pairs(lambda rng: _sparse_pair(rng, 5000, 0.1, logcounts), unit=False, trials=30, seed=3)
     check_pairs(lambda rng: _sparse_pair(rng, 5000, 0.1, lambda g, m: np.ones(m)), unit=False, trials=30,
                 seed=4)
+
+
+# ---- js: the FP32 screen of fastJS2 (sparsedist_gb300/csrc/sdg_screen.cu,
+# accumulate_js and js_key_and_bound).  Per shared row the kernel computes
+# g = ((S log S) - xlogx(P)) - xlogx(Q) with p, q the FP32 values, S = p + q,
+# logf within 1 ulp, the stored FP32 x log x values and every operation
+# rounded once, and sums the rows in FP32.  Here logf is emulated by either
+# FP32 neighbour of the FP64 logarithm (both are within 1 ulp), rows are
+# summed in random orders, and |G~ - G| must stay within
+# u (10.8 (A_P + A_Q) + 0.75 n (C_P + C_Q)) 1.01, A = a column's sum of
+# |x log x| + x, C = its sum.
+
+def _f32(x):
+    return np.float32(x)
+
+
+def _logf_1ulp(S, rng):
+    t = np.log(np.float64(S))
+    r = np.float32(t)
+    other = np.nextafter(r, np.float32(np.inf) if np.float64(r) < t else np.float32(-np.inf))
+    return r if rng.random() < 0.5 else other
+
+
+def _js_case(P, Q, rng):
+    """P, Q: the two columns' values (dense vectors, 0 = not stored)."""
+    shared = (P != 0) & (Q != 0)
+    def xlx(v):
+        with np.errstate(divide="ignore", invalid="ignore"):
+            r = v * np.log(v)
+        return np.where(v > 0, r, 0.0)
+    def A(v):
+        return float(np.float32(np.sum(np.abs(xlx(v)) + v) * (1 + 1e-12)))   # ~rounded up
+    AP, AQ = A(P), A(Q)
+    n = int(min(np.count_nonzero(P), np.count_nonzero(Q)))
+    idx = np.flatnonzero(shared)
+    # exact G without cancellation: g = P log1p(Q/P) + Q log1p(P/Q)
+    Ps, Qs = P[idx], Q[idx]
+    G = float(np.sum(Ps * np.log1p(Qs / Ps) + Qs * np.log1p(Ps / Qs)))
+    terms = []
+    for a, b in zip(Ps, Qs):
+        p, q = _f32(a), _f32(b)
+        xp, xq = _f32(a * np.log(a)), _f32(b * np.log(b))
+        S = _f32(p + q)
+        t1 = _f32(S * _logf_1ulp(S, rng))
+        terms.append(_f32(_f32(t1 - xp) - xq))
+    CP, CQ = float(P.sum()), float(Q.sum())
+    bound = 2.0 ** -24 * (10.8 * (AP + AQ) + 0.75 * n * (CP + CQ)) * 1.01
+    worst = 0.0
+    for _ in range(3):
+        acc = np.float32(0)
+        for t in np.asarray(terms, np.float32)[rng.permutation(len(terms))]:
+            acc = _f32(acc + t)
+        err = abs(float(acc) - G)
+        assert err <= bound, (err, bound, n)
+        worst = max(worst, err / bound if bound > 0 else 0.0)
+    return worst
+
+
+def _js_pair(rng, nrow, density, draw):
+    P = np.zeros(nrow)
+    Q = np.zeros(nrow)
+    ip = rng.random(nrow) < density
+    iq = rng.random(nrow) < density
+    P[ip] = draw(rng, ip.sum())
+    Q[iq] = draw(rng, iq.sum())
+    return P, Q
+
+
+def test_js_bound_normalised_columns():
+    rng = np.random.default_rng(21)
+    for _ in range(25):
+        P, Q = _js_pair(rng, 3000, 0.2, lambda g, m: g.random(m) + 1e-3)
+        P /= P.sum()
+        Q /= Q.sum()
+        assert _js_case(P, Q, rng) < 1.0
+
+
+def test_js_bound_skewed_ratios_and_ranges():
+    rng = np.random.default_rng(22)
+    # values over [2^-90, 2^90] in log scale, so that shared rows pair tiny
+    # with huge values (Q << P), plus exact ties P == Q
+    for _ in range(20):
+        P, Q = _js_pair(rng, 2000, 0.3, lambda g, m: np.exp2(g.uniform(-90, 90, m)))
+        tie = (P != 0) & (Q != 0) & (rng.random(2000) < 0.2)
+        Q[tie] = P[tie]
+        assert _js_case(P, Q, rng) < 1.0
+
+
+def test_js_bound_counts_above_one():
+    rng = np.random.default_rng(23)
+    for _ in range(20):
+        P, Q = _js_pair(rng, 4000, 0.1, lambda g, m: g.negative_binomial(2, 0.1, m).astype(float) + 1.0)
+        assert _js_case(P, Q, rng) < 1.0
