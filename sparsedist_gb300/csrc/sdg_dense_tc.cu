@@ -110,9 +110,6 @@ __device__ __forceinline__ float fkey_value(unsigned k) {
   return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
 }
 constexpr int SHARE_TILES = 8;          // tiles between exchanges of the shared running key
-// reference tiles ahead of the ring whose chunks the producer asks L2 to fetch:
-// the ring holds one tile, and a chunk that misses L2 waits on DRAM
-constexpr int PF_TILES = 2;
 
 // the first and the last CTA whose span holds an item of query group g
 __host__ __device__ __forceinline__ int64_t first_cta(int64_t g, int64_t ntiles, int64_t per) {
@@ -188,7 +185,6 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
             if (!mbar_wait(emptyb + s, ph ^ 1u, abort_flag, P.status)) { ok = false; break; }
             mbar_expect_tx(full + s, B_BYTES);
             tma_load_2d(sB + (size_t)s * B_BYTES, &rmap, full + s, c * BK, rcol);
-            if (f + PF_TILES < fe) tma_prefetch_l2_2d(&rmap, c * BK, rcol + PF_TILES * BN);
           }
         }
       }
