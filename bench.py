@@ -80,6 +80,8 @@ def parse():
                          "problems through sdg_knn_cross_batch")
     ap.add_argument("--serve-ref-cols", type=int, default=1000000)
     ap.add_argument("--dense-cols", type=int, default=2000000)
+    ap.add_argument("--dense-mode", type=int, default=0, choices=[0, 3],
+                    help="BF16-screened mode of the dense line: 0 (one CTA per query group), 3 (CTA pairs)")
     ap.add_argument("--dense-block", type=int, default=4096)
     ap.add_argument("--dense-cpu-cols", type=int, default=128,
                     help="query columns of the dense CPU-baseline / parity sample")
@@ -633,7 +635,7 @@ def run_dense_main(args):
         kms, kl = ctx.kernel_time()
         return float(t.item()), kms, kl, ctx.stats(), (clk.summary() if clk else None)
 
-    ms, kms, klaunch, st, clocks = timed(0, True)
+    ms, kms, klaunch, st, clocks = timed(args.dense_mode, True)
     value = world * B * K / (ms / 1000.0)
     launches = int(st["kernels"]) * K
     ms1, _, _, _, _ = timed(1, False)

@@ -244,9 +244,12 @@ SDG_API int sdg_knn_resident(sdg_ctx* ctx, const sdg_matrix* X, const sdg_matrix
  * drop_degenerate = TRUE) for cosine (dist) or euclidean.  mode 0: BF16
  * tensor-core screen with a rigorous bound and exact FP64 re-rank (the
  * reference's idx and distances), fused in one tcgen05 kernel (no slab in
- * HBM) for k <= 64 and d <= 256, else as mode 2; mode 2: the same screen
- * through a cuBLAS BF16 GEMM slab; mode 1: the plain FP32 path (FP32 GEMM,
- * top-k on FP32 values, no re-rank).  No counterpart in the reference, whose
+ * HBM, one CTA per 128-query group) for k <= 64 and d <= 256, else as
+ * mode 2; mode 3: the fused screen on CTA pairs (clusters of two CTAs sharing
+ * cta_group::2 UMMAs of 256 queries; the same results) when the block has
+ * more than 128 queries; mode 2: the same screen through a cuBLAS BF16 GEMM slab; mode 1:
+ * the plain FP32 path (FP32 GEMM, top-k on FP32 values, no re-rank).  k above
+ * 1,024: every mode values every pair exactly.  No counterpart in the reference, whose
  * dense inputs are coerced to dgCMatrix (R/sparseKNN.R:194-200); the FP64
  * values are those sparseKNN computes on the same data. */
 typedef struct sdg_dense sdg_dense;

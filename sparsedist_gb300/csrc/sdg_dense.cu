@@ -416,12 +416,15 @@ int dense_search(sdg_ctx* ctx, const sdg_dense* Q, int64_t q0, int64_t nq, const
                  int* flags) {
   if (!ctx || !Q || !D || !idx || !dist_out || !k_eff || !flags) return fail_with(SDG_E_ARG, "NULL argument");
   if (method != COSINE && method != EUCLIDEAN) return fail_with(SDG_E_UNSUPPORTED, "dense kNN supports cosine and euclidean");
-  if (mode < 0 || mode > 2)
-    return fail_with(SDG_E_ARG, "mode must be 0 (BF16 screen), 1 (plain FP32) or 2 (BF16 slab screen)");
+  if (mode < 0 || mode > 3)
+    return fail_with(SDG_E_ARG,
+                     "mode must be 0 (BF16 screen), 1 (plain FP32), 2 (BF16 slab screen) or 3 (BF16 screen on "
+                     "CTA pairs)");
   if (k < 1) return fail_with(SDG_E_ARG, "'k' must be a positive integer no larger than .Machine$integer.max.");
   if (q0 < 0 || nq < 1 || q0 + nq > Q->n) return fail_with(SDG_E_ARG, "invalid query column range");
   if (Q->d != D->d) return fail_with(SDG_E_ROWS, "'X' and 'Y' must have the same number of rows.");
-  if (mode != 0 && !D->blas) return fail_with(SDG_E_ARG, "modes 1 and 2 need the reference's cuBLAS handle");
+  if ((mode == 1 || mode == 2) && !D->blas)
+    return fail_with(SDG_E_ARG, "modes 1 and 2 need the reference's cuBLAS handle");
   DK(cudaSetDevice(D->device));
   cudaStream_t s = ctx_stream(ctx);
   *flags = 0;
@@ -466,9 +469,10 @@ int dense_search(sdg_ctx* ctx, const sdg_dense* Q, int64_t q0, int64_t nq, const
     return SDG_OK;
   }
   const int cap = std::max(512, std::min(16384, 64 * k + 256));
-  // mode 0 runs the fused tensor-core screen where it applies (no slab in
-  // HBM), else the BF16 slab screen of mode 2; smode is the bound in force
-  const bool fused = mode == 0 && tc_screen_supported(D, method, k);
+  // modes 0 and 3 run the fused tensor-core screen where it applies (no slab
+  // in HBM; mode 0 one CTA per query group, mode 3 on CTA pairs), else the
+  // BF16 slab screen of mode 2; smode is the bound in force
+  const bool fused = (mode == 0 || mode == 3) && tc_screen_supported(D, method, k);
   const int smode = (mode == 1) ? 1 : 0;
   const int64_t ldS = (n + 127) / 128 * 128;
   const int nseg = (int)((n + DSEG - 1) / DSEG);
@@ -504,7 +508,7 @@ int dense_search(sdg_ctx* ctx, const sdg_dense* Q, int64_t q0, int64_t nq, const
   for (int64_t c0 = q0; c0 < q0 + nq; c0 += chunk) {
     const int64_t nb = std::min(chunk, q0 + nq - c0);
     if (fused) {
-      const int st = tc_screen(ctx, Q, D, self, method, k, c0, nb, cand, count, over, cap, s);
+      const int st = tc_screen(ctx, Q, D, self, method, k, c0, nb, cand, count, over, cap, s, mode == 3);
       if (st != SDG_OK) return st;
       ctx_stats_add(ctx, 6, 2 * (int64_t)D->dpad * n * nb);
     } else {

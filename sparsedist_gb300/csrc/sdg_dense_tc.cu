@@ -46,6 +46,20 @@
 // %globaltimer, sdg_tc_ptx.cuh) and sleeps instead of spinning; a wait that
 // runs out sets *status, raises the CTA's abort flag, and the CTA drains its
 // own copies and MMAs, frees TMEM and returns.
+//
+// CTA pairs (PAIR = true, dense mode 3).  A cluster of two CTAs shares each
+// UMMA: the even CTA issues tcgen05.mma.cta_group::2 with M = 256 (its 128
+// queries in rows 0-127, the odd CTA's in 128-255) and N = 256, each CTA
+// holding its own query tile and one 128-column half of every reference chunk
+// (16 KB, an 8-stage ring).  Both CTAs' TMA loads (cta_group::2) count their
+// bytes on the even CTA's barriers, whose commits multicast to both CTAs; the
+// odd CTA's epilogue releases the even CTA's accumulator barrier remotely;
+// TMEM is allocated and freed by a warp of each CTA, and a cluster barrier
+// keeps either CTA from leaving while the other may still touch its memory.
+// Measured on the 256 x 2,000,000 workload it is no faster than one CTA per
+// group (3.55 against 3.41 ms): the loop is bound by the per-tile hand-off
+// between the MMAs and the epilogue through the two TMEM buffers, not by the
+// reference chunks' supply that the pairs halve.
 #include <cuda.h>
 #include <cuda_bf16.h>
 
@@ -65,19 +79,34 @@ using namespace tc;
 constexpr int BM = 128;                 // queries per group (UMMA M, TMEM lanes)
 constexpr int BN = 256;                 // references per tile (UMMA N)
 constexpr int BK = 64;                  // rows of a K chunk: 64 BF16 = one 128-byte swizzle row
-constexpr int STAGES = 4;               // reference chunk ring
 constexpr int NB = 8;                   // buffered passing references per epilogue thread
 constexpr int EPI_THREADS = 256;
 constexpr int KT = 64;                  // largest k of the fused screen
 constexpr int THREADS = 320;
 constexpr uint32_t A_BYTES = BM * BK * 2;      // 16 KB: a 128 x 64 BF16 query chunk
-constexpr uint32_t B_BYTES = BN * BK * 2;      // 32 KB: a 256 x 64 BF16 reference chunk
+constexpr uint32_t RING_BYTES = 128 * 1024;    // the reference chunk ring
 constexpr uint32_t TMEM_COLS = 2 * BN;         // two accumulator buffers
 constexpr int MAX_DCH = 4;              // dpad <= 256
+constexpr int MAX_STAGES = 8;
 // 1 KB alignment slack, A chunks, B ring, candidate slots, barriers
-constexpr size_t SMEM_BYTES = 1024 + (size_t)MAX_DCH * A_BYTES + (size_t)STAGES * B_BYTES +
-                              (size_t)NB * EPI_THREADS * 8 + 256;
-constexpr uint32_t IDESC = idesc_f16(BM, BN, true);
+constexpr size_t SMEM_BYTES = 1024 + (size_t)MAX_DCH * A_BYTES + RING_BYTES + (size_t)NB * EPI_THREADS * 8 + 256;
+
+// One CTA (PAIR = false): a query group is 128 queries, the CTA loads whole
+// 256-column reference chunks (32 KB, a 4-stage ring) and issues
+// cta_group::1 MMAs (M = 128).  A CTA pair (PAIR = true, a cluster of two): a
+// query group is 256 queries, 128 per CTA; each CTA loads its 128-column half
+// of every reference chunk (16 KB, an 8-stage ring in the same bytes, so the
+// ring covers twice the MMA time) and the even CTA issues cta_group::2 MMAs
+// (M = 256, N = 256) over both CTAs' operands.
+template <bool PAIR>
+struct Cfg {
+  static constexpr int GM = PAIR ? 2 * BM : BM;            // queries per group
+  static constexpr int BNL = PAIR ? BN / 2 : BN;           // reference columns a CTA loads per chunk
+  static constexpr uint32_t B_BYTES = BNL * BK * 2;
+  static constexpr int STAGES = (int)(RING_BYTES / B_BYTES);
+  static constexpr uint32_t IDESC = idesc_f16(GM, BN, true);
+};
+static_assert(Cfg<true>::STAGES <= MAX_STAGES && Cfg<false>::STAGES <= MAX_STAGES, "barrier space");
 
 struct TcArgs {
   int method, k, dch, ecap;
@@ -111,7 +140,8 @@ __device__ __forceinline__ float fkey_value(unsigned k) {
 }
 constexpr int SHARE_TILES = 8;          // tiles between exchanges of the shared running key
 
-// the first and the last CTA whose span holds an item of query group g
+// the first and the last work unit (a CTA, or a CTA pair) whose span holds an
+// item of query group g
 __host__ __device__ __forceinline__ int64_t first_cta(int64_t g, int64_t ntiles, int64_t per) {
   return (g * ntiles) / per;
 }
@@ -119,21 +149,24 @@ __host__ __device__ __forceinline__ int64_t last_cta(int64_t g, int64_t ntiles, 
   return ((g + 1) * ntiles - 1) / per;
 }
 
-template <int KL>
+template <int KL, bool PAIR>
 __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__ CUtensorMap qmap,
                                                        const __grid_constant__ CUtensorMap rmap, TcArgs P) {
+  using C = Cfg<PAIR>;
+  constexpr int STAGES = C::STAGES;
+  constexpr uint32_t B_BYTES = C::B_BYTES;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint8_t* sA = base;                                     // MAX_DCH query chunks
   uint8_t* sB = base + (size_t)MAX_DCH * A_BYTES;          // STAGES reference chunks
   // per epilogue thread NB (reference, GEMM value) slots, slot-major so that a
   // warp's accesses to one slot are conflict-free
-  int32_t* buf_r = (int32_t*)(sB + (size_t)STAGES * B_BYTES);
+  int32_t* buf_r = (int32_t*)(sB + (size_t)RING_BYTES);
   float* buf_s = (float*)(buf_r + NB * EPI_THREADS);
   uint64_t* bars = (uint64_t*)(buf_s + NB * EPI_THREADS);
   uint64_t* full = bars;
-  uint64_t* emptyb = bars + STAGES;
-  uint64_t* acc_full = bars + 2 * STAGES;
+  uint64_t* emptyb = bars + MAX_STAGES;
+  uint64_t* acc_full = bars + 2 * MAX_STAGES;
   uint64_t* acc_empty = acc_full + 2;
   uint64_t* a_full = acc_empty + 2;
   uint64_t* a_empty = a_full + 1;
@@ -142,23 +175,38 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
   volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // this CTA's rank in its pair (0: the MMA issuer) and its work unit
+  const uint32_t crank = PAIR ? cluster_rank() : 0u;
+  const bool leader = crank == 0;
+  const int64_t unit = PAIR ? (int64_t)(blockIdx.x >> 1) : (int64_t)blockIdx.x;
   const int64_t per = P.tiles_per_cta, ntiles = P.ntiles;
-  const int64_t f0 = (int64_t)blockIdx.x * per;
-  const int64_t f1 = min(f0 + per, ((P.nq + BM - 1) / BM) * ntiles);
+  const int64_t f0 = unit * per;
+  const int64_t f1 = min(f0 + per, ((P.nq + C::GM - 1) / C::GM) * ntiles);
   const int dch = P.dch;
+  // the bounded waits (CTA-scope acquire: the pair's barriers are completed
+  // by TMA transactions, tcgen05 commits and the other CTA's arrivals, each
+  // ordered by the barrier itself)
+  auto wait = [&](uint64_t* bar, uint32_t parity) -> bool { return mbar_wait(bar, parity, abort_flag, P.status); };
+  auto drain = [&](uint64_t* bar, uint32_t parity) { mbar_drain(bar, parity); };
 
   if (threadIdx.x == 0) {
+    // a pair's MMA waits on the even CTA's barriers: both CTAs' loads count
+    // their bytes there, and both CTAs' epilogues release its buffers
     for (int s = 0; s < STAGES; ++s) { mbar_init(full + s, 1); mbar_init(emptyb + s, 1); }
-    for (int b = 0; b < 2; ++b) { mbar_init(acc_full + b, 1); mbar_init(acc_empty + b, 8); }
+    for (int b = 0; b < 2; ++b) { mbar_init(acc_full + b, 1); mbar_init(acc_empty + b, PAIR ? 16 : 8); }
     mbar_init(a_full, 1);
     mbar_init(a_empty, 1);
     mbar_init(mma_done, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 1) tmem_alloc(tmem_slot, TMEM_COLS);
+  if (warp == 1) {
+    if constexpr (PAIR) tmem_alloc_pair(tmem_slot, TMEM_COLS);
+    else tmem_alloc(tmem_slot, TMEM_COLS);
+  }
   fence_before();
   __syncthreads();
+  if constexpr (PAIR) cluster_sync();            // both CTAs' barriers exist before any remote arrival
   fence_after();
   const uint32_t tmem = *tmem_slot;
 
@@ -173,71 +221,101 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
         const int64_t g = f / ntiles;
         const int64_t fe = min(f1, (g + 1) * ntiles);
         // the previous segment's MMAs have finished reading the query chunks
-        if (!mbar_wait(a_empty, ((uint32_t)seg & 1u) ^ 1u, abort_flag, P.status)) break;
-        mbar_expect_tx(a_full, (uint32_t)dch * A_BYTES);
-        for (int c = 0; c < dch; ++c)
-          tma_load_2d(sA + (size_t)c * A_BYTES, &qmap, a_full, c * BK, (int)(P.q0 + g * BM));
+        if (!wait(a_empty, ((uint32_t)seg & 1u) ^ 1u)) break;
+        const int qy = (int)(P.q0 + g * C::GM + crank * BM);
+        if constexpr (PAIR) {
+          // both CTAs' query chunks are counted on the even CTA's barrier
+          if (leader) mbar_expect_tx(a_full, 2u * (uint32_t)dch * A_BYTES);
+          const uint32_t bar = cluster_addr(a_full, 0);
+          for (int c = 0; c < dch; ++c) tma_load_2d_pair(sA + (size_t)c * A_BYTES, &qmap, bar, c * BK, qy);
+        } else {
+          mbar_expect_tx(a_full, (uint32_t)dch * A_BYTES);
+          for (int c = 0; c < dch; ++c) tma_load_2d(sA + (size_t)c * A_BYTES, &qmap, a_full, c * BK, qy);
+        }
         for (; f < fe && ok; ++f) {
-          const int rcol = (int)((f - g * ntiles) * BN);
+          const int rcol = (int)((f - g * ntiles) * BN + crank * C::BNL);
           for (int c = 0; c < dch; ++c, ++it) {
             const int s = it % STAGES;
             const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
-            if (!mbar_wait(emptyb + s, ph ^ 1u, abort_flag, P.status)) { ok = false; break; }
-            mbar_expect_tx(full + s, B_BYTES);
-            tma_load_2d(sB + (size_t)s * B_BYTES, &rmap, full + s, c * BK, rcol);
+            if (!wait(emptyb + s, ph ^ 1u)) { ok = false; break; }
+            if constexpr (PAIR) {
+              if (leader) mbar_expect_tx(full + s, 2u * B_BYTES);
+              tma_load_2d_pair(sB + (size_t)s * B_BYTES, &rmap, cluster_addr(full + s, 0), c * BK, rcol);
+            } else {
+              mbar_expect_tx(full + s, B_BYTES);
+              tma_load_2d(sB + (size_t)s * B_BYTES, &rmap, full + s, c * BK, rcol);
+            }
           }
         }
       }
-      // every issued copy lands before the CTA can exit
-      for (int x = max(0, it - STAGES); x < it; ++x) mbar_drain(full + x % STAGES, (uint32_t)(x / STAGES) & 1u);
-      if (seg > 0) mbar_drain(a_full, (uint32_t)(seg - 1) & 1u);
+      // every issued copy lands before the CTA can exit; a pair's copies are
+      // counted on the even CTA's barriers, so the even CTA waits for both
+      // CTAs' (the odd CTA leaves only after it, at the final cluster barrier)
+      if (!PAIR || leader) {
+        for (int x = max(0, it - STAGES); x < it; ++x) drain(full + x % STAGES, (uint32_t)(x / STAGES) & 1u);
+        if (seg > 0) drain(a_full, (uint32_t)(seg - 1) & 1u);
+      }
     }
     __syncwarp();
   } else if (warp == 1) {
-    // ---- MMA issuer ----
-    if (lane == 0 && f1 > f0) {
-      int it = 0, seg = 0;
-      int64_t j = 0;
-      bool ok = true;
-      for (int64_t f = f0; f < f1 && ok; ++seg) {
-        const int64_t g = f / ntiles;
-        const int64_t fe = min(f1, (g + 1) * ntiles);
-        if (!mbar_wait(a_full, (uint32_t)seg & 1u, abort_flag, P.status)) break;
-        fence_after();
-        const uint32_t a0 = smem_u32(sA);
-        for (; f < fe && ok; ++f, ++j) {
-          const int buf = (int)(j & 1);
-          // the epilogue has drained this buffer's previous tile
-          // (with P.stall the first wait asks for the phase the epilogue has not
-          // begun, so it runs out: the failure-detection test's path)
-          const uint32_t flip = (P.stall && j == 0) ? 0u : 1u;
-          if (!mbar_wait(acc_empty + buf, ((uint32_t)(j >> 1) & 1u) ^ flip, abort_flag, P.status)) {
-            ok = false;
-            break;
-          }
+    if (!PAIR || leader) {
+      // ---- MMA issuer ----
+      if (lane == 0 && f1 > f0) {
+        int it = 0, seg = 0;
+        int64_t j = 0;
+        bool ok = true;
+        for (int64_t f = f0; f < f1 && ok; ++seg) {
+          const int64_t g = f / ntiles;
+          const int64_t fe = min(f1, (g + 1) * ntiles);
+          if (!wait(a_full, (uint32_t)seg & 1u)) break;
           fence_after();
-          const uint32_t d_addr = tmem + (uint32_t)(buf * BN);
-          for (int c = 0; c < dch; ++c, ++it) {
-            const int s = it % STAGES;
-            const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
-            if (!mbar_wait(full + s, ph, abort_flag, P.status)) { ok = false; break; }
+          const uint32_t a0 = smem_u32(sA);
+          for (; f < fe && ok; ++f, ++j) {
+            const int buf = (int)(j & 1);
+            // the epilogue has drained this buffer's previous tile
+            // (with P.stall the first wait asks for the phase the epilogue has not
+            // begun, so it runs out: the failure-detection test's path)
+            const uint32_t flip = (P.stall && j == 0) ? 0u : 1u;
+            if (!wait(acc_empty + buf, ((uint32_t)(j >> 1) & 1u) ^ flip)) {
+              ok = false;
+              break;
+            }
             fence_after();
-            const uint32_t b_addr = smem_u32(sB + (size_t)s * B_BYTES);
-            const uint32_t a_addr = a0 + (uint32_t)c * A_BYTES;
+            const uint32_t d_addr = tmem + (uint32_t)(buf * BN);
+            for (int c = 0; c < dch; ++c, ++it) {
+              const int s = it % STAGES;
+              const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+              if (!wait(full + s, ph)) { ok = false; break; }
+              fence_after();
+              const uint32_t b_addr = smem_u32(sB + (size_t)s * B_BYTES);
+              const uint32_t a_addr = a0 + (uint32_t)c * A_BYTES;
 #pragma unroll
-            for (int kk = 0; kk < BK / 16; ++kk)
-              umma_f16(d_addr, sw128_desc(a_addr + kk * 32), sw128_desc(b_addr + kk * 32), IDESC,
-                       (c | kk) != 0);
-            umma_commit(emptyb + s);            // the stage is free once these MMAs have read it
+              for (int kk = 0; kk < BK / 16; ++kk) {
+                if constexpr (PAIR)
+                  umma_f16_pair(d_addr, sw128_desc(a_addr + kk * 32), sw128_desc(b_addr + kk * 32), C::IDESC,
+                                (c | kk) != 0);
+                else
+                  umma_f16(d_addr, sw128_desc(a_addr + kk * 32), sw128_desc(b_addr + kk * 32), C::IDESC,
+                           (c | kk) != 0);
+              }
+              // the stage is free (in both CTAs of a pair) once these MMAs have read it
+              if constexpr (PAIR) umma_commit_pair(emptyb + s, 3); else umma_commit(emptyb + s);
+            }
+            if (!ok) break;
+            // the tile's accumulators are complete
+            if constexpr (PAIR) umma_commit_pair(acc_full + buf, 3); else umma_commit(acc_full + buf);
           }
-          if (!ok) break;
-          umma_commit(acc_full + buf);          // the tile's accumulators are complete
+          // the query chunks are free once the segment's MMAs are done
+          if constexpr (PAIR) umma_commit_pair(a_empty, 3); else umma_commit(a_empty);
         }
-        umma_commit(a_empty);                   // the query chunks are free once the segment's MMAs are done
+        // all issued MMAs complete before TMEM is freed
+        if constexpr (PAIR) umma_commit_pair(mma_done, 3); else umma_commit(mma_done);
+        drain(mma_done, 0);
       }
-      // all issued MMAs complete before TMEM is freed
-      umma_commit(mma_done);
-      mbar_drain(mma_done, 0);
+    } else if constexpr (PAIR) {
+      // the odd CTA: the even CTA's last commit also arrives on this CTA's
+      // barriers; it lands before they go away
+      if (lane == 0 && f1 > f0) drain(mma_done, 0);
     }
     __syncwarp();
   } else {
@@ -394,7 +472,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
     for (int64_t f = f0; f < f1 && ok;) {
       const int64_t g = f / ntiles;
       const int64_t fe = min(f1, (g + 1) * ntiles);
-      const int64_t ql = g * BM + row;
+      const int64_t ql = g * C::GM + crank * BM + row;
       q = P.q0 + ql;
       active = ql < P.nq;
       if (active) active = !P.qempty[q];           // a degenerate query has no list
@@ -408,12 +486,12 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
       cnt = 0;
       nbuf = 0;
       const int64_t slot =
-          active ? (ql * P.nslots + ((int64_t)blockIdx.x - first_cta(g, ntiles, per)) * 2 + half) : 0;
+          active ? (ql * P.nslots + (unit - first_cta(g, ntiles, per)) * 2 + half) : 0;
       my_idx = P.eidx + slot * P.ecap;
       my_hi = P.ehi + slot * P.ecap;
       for (; f < fe; ++f, ++j) {
         const int buf = (int)(j & 1);
-        const bool got = mbar_wait(acc_full + buf, (uint32_t)(j >> 1) & 1u, abort_flag, P.status);
+        const bool got = wait(acc_full + buf, (uint32_t)(j >> 1) & 1u);
         if (!__all_sync(0xffffffffu, got)) { ok = false; break; }   // the warp leaves together
         fence_after();
         const int64_t r_half = (f - g * ntiles) * BN + half * (BN / 2);
@@ -446,7 +524,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
         }
         fence_before();
         __syncwarp();
-        if (lane == 0) mbar_arrive(acc_empty + buf);
+        if (lane == 0) {
+          if constexpr (PAIR) mbar_arrive_remote(acc_empty + buf, 0);   // the even CTA's MMA waits on it
+          else mbar_arrive(acc_empty + buf);
+        }
         if ((j & (SHARE_TILES - 1)) == SHARE_TILES - 1 && active) {
           // publish this list's running key and take the best one published
           const unsigned prev = atomicMax(P.tshared + ql, fkey(T));
@@ -467,8 +548,14 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
   }
   fence_before();
   __syncthreads();
+  // a pair's MMAs read both CTAs' shared memory and write both TMEMs: neither
+  // CTA frees TMEM or exits before the other is done
+  if constexpr (PAIR) cluster_sync();
   fence_after();
-  if (warp == 1) tmem_dealloc(tmem, TMEM_COLS);
+  if (warp == 1) {
+    if constexpr (PAIR) tmem_dealloc_pair(tmem, TMEM_COLS);
+    else tmem_dealloc(tmem, TMEM_COLS);
+  }
 }
 
 // ---- merge: the final cut of each query over its lists ---------------------
@@ -496,7 +583,7 @@ __device__ __forceinline__ void warp_insert_desc_tc(float* lst, int K, int& n, u
 // (segment, half) that covered it (the exact k-th over all references: the top
 // k of a union is the top k of the parts' top k), cut = dense_cut(T); the
 // candidates are the appended references with hi >= cut.
-__global__ void k_tc_merge(int64_t q0, int64_t nq, int64_t ntiles, int64_t per, int64_t nslots, int K, int ecap,
+__global__ void k_tc_merge(int64_t q0, int64_t nq, int gm, int64_t ntiles, int64_t per, int64_t nslots, int K, int ecap,
                            const uint8_t* qempty, const unsigned* tshared, const float* lists,
                            const int32_t* ecount, const int32_t* eidx, const float* ehi, int cap, int32_t* cand,
                            int32_t* count, int32_t* over) {
@@ -508,7 +595,7 @@ __global__ void k_tc_merge(int64_t q0, int64_t nq, int64_t ntiles, int64_t per, 
     if (lane == 0) { count[ql] = 0; over[ql] = 0; }
     return;
   }
-  const int64_t g = ql / BM;
+  const int64_t g = ql / gm;
   const int64_t used = 2 * (last_cta(g, ntiles, per) - first_cta(g, ntiles, per) + 1);
   float* lst = sl[warp];
   int n = 0;
@@ -588,7 +675,7 @@ bool tc_screen_supported(const sdg_dense* R, int method, int k) {
 }
 
 int tc_screen(sdg_ctx* ctx, const sdg_dense* Q, const sdg_dense* D, bool self, int method, int k, int64_t q0,
-              int64_t nq, int32_t* cand, int32_t* count, int32_t* over, int cap, cudaStream_t s) {
+              int64_t nq, int32_t* cand, int32_t* count, int32_t* over, int cap, cudaStream_t s, bool allow_pairs) {
   EncodeTiledFn enc = encode_fn();
   if (!enc) return fail(SDG_E_CUDA, "cuTensorMapEncodeTiled is unavailable");
   if (Q->dpad != D->dpad || Q->n >= (int64_t)1 << 30) return fail(SDG_E_ARG, "query and reference shapes differ");
@@ -607,17 +694,49 @@ int tc_screen(sdg_ctx* ctx, const sdg_dense* Q, const sdg_dense* D, bool self, i
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
   };
+  // the list length: the smallest of 16 / 24 / 32 / 48 / 64 that holds k
+  auto pick_kernel = [&](bool pair) {
+    if (pair)
+      return (k <= 16) ? k_dense_tc<16, true> : (k <= 24) ? k_dense_tc<24, true> : (k <= 32) ? k_dense_tc<32, true>
+           : (k <= 48) ? k_dense_tc<48, true> : k_dense_tc<64, true>;
+    return (k <= 16) ? k_dense_tc<16, false> : (k <= 24) ? k_dense_tc<24, false> : (k <= 32) ? k_dense_tc<32, false>
+         : (k <= 48) ? k_dense_tc<48, false> : k_dense_tc<64, false>;
+  };
+  // CTA pairs (clusters of two) where the block has more than one 128-query
+  // group and the device can hold such clusters; the work unit is then a pair
+  int64_t units = 0;
+  bool pair = false;
+  if (allow_pairs && nq > BM) {
+    auto kp = pick_kernel(true);
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2; attr[0].val.clusterDim.y = 1; attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(2, 1, 1); cfg.blockDim = dim3(THREADS, 1, 1); cfg.dynamicSmemBytes = SMEM_BYTES;
+    cfg.attrs = attr; cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaFuncSetAttribute(kp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES) == cudaSuccess &&
+        cudaOccupancyMaxActiveClusters(&clusters, kp, &cfg) == cudaSuccess && clusters > 0) {
+      pair = true;
+      units = clusters;
+    }
+    cudaGetLastError();
+  }
+  if (!pair) {
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, D->device);
+    units = std::max(sms, 1);
+  }
+  const int GM = pair ? Cfg<true>::GM : Cfg<false>::GM;
   CUtensorMap qmap, rmap;
-  if (!encode(Q, BM, &qmap) || !encode(D, BN, &rmap)) return fail(SDG_E_CUDA, "cuTensorMapEncodeTiled failed");
+  if (!encode(Q, BM, &qmap) || !encode(D, pair ? Cfg<true>::BNL : Cfg<false>::BNL, &rmap))
+    return fail(SDG_E_CUDA, "cuTensorMapEncodeTiled failed");
 
-  int sms = 0;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, D->device);
-  if (sms < 1) sms = 1;
-  // (query group, reference tile) items in equal contiguous spans, one per CTA
-  const int64_t G = (nq + BM - 1) / BM;
+  // (query group, reference tile) items in equal contiguous spans, one per unit
+  const int64_t G = (nq + GM - 1) / GM;
   const int64_t ntiles = (n + BN - 1) / BN;
   const int64_t items = G * ntiles;
-  int64_t grid = std::min<int64_t>(sms, items);
+  int64_t grid = std::min<int64_t>(units, items);
   const int64_t per = (items + grid - 1) / grid;
   grid = (items + per - 1) / per;
   // list slots per query: two halves per CTA whose span meets its group
@@ -660,15 +779,26 @@ int tc_screen(sdg_ctx* ctx, const sdg_dense* Q, const sdg_dense* D, bool self, i
     P.lists = lists; P.ecount = ecount; P.eidx = eidx; P.ehi = ehi;
     P.status = status;
     P.stall = tc_take_stall() ? 1 : 0;
-    // the list length: the smallest of 16 / 24 / 32 / 48 / 64 that holds k
-    auto kern = (k <= 16) ? k_dense_tc<16> : (k <= 24) ? k_dense_tc<24> : (k <= 32) ? k_dense_tc<32>
-              : (k <= 48) ? k_dense_tc<48> : k_dense_tc<64>;
+    auto kern = pick_kernel(pair);
     chk(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
     sdg_time_begin(ctx);
-    if (e == cudaSuccess) kern<<<(unsigned)grid, THREADS, SMEM_BYTES, s>>>(qmap, rmap, P);
+    if (e == cudaSuccess) {
+      if (pair) {
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = 2; attr[0].val.clusterDim.y = 1; attr[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3((unsigned)(2 * grid), 1, 1); cfg.blockDim = dim3(THREADS, 1, 1);
+        cfg.dynamicSmemBytes = SMEM_BYTES; cfg.stream = s;
+        cfg.attrs = attr; cfg.numAttrs = 1;
+        chk(cudaLaunchKernelEx(&cfg, kern, qmap, rmap, P));
+      } else {
+        kern<<<(unsigned)grid, THREADS, SMEM_BYTES, s>>>(qmap, rmap, P);
+      }
+    }
     sdg_time_end(ctx);
     chk(cudaGetLastError());
-    k_tc_merge<<<(unsigned)((nq + MW - 1) / MW), MW * 32, 0, s>>>(q0, nq, ntiles, per, nslots, k, ecap, Q->empty,
+    k_tc_merge<<<(unsigned)((nq + MW - 1) / MW), MW * 32, 0, s>>>(q0, nq, GM, ntiles, per, nslots, k, ecap, Q->empty,
                                                                   tshared, lists, ecount, eidx, ehi, cap, cand,
                                                                   count, over);
     chk(cudaGetLastError());

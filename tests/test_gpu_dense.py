@@ -1,5 +1,7 @@
-"""Dense embedding columns (the 256 x 2,000,000 embedding path): both BF16 screens (mode 0,
-the fused tcgen05 kernel; mode 2, the cuBLAS slab) with the exact FP64 re-rank
+"""Dense embedding columns (the 256 x 2,000,000 embedding path): the BF16 screens (mode 0,
+the fused tcgen05 kernel, one CTA per 128-query group; mode 3, the same screen on CTA
+pairs (cta_group::2 UMMAs of 256 queries) for blocks of more than 128 queries; mode 2, the
+cuBLAS slab) with the exact FP64 re-rank
 must return the oracle's sparseKNN result on the same data bit for bit (idx
 and distances), near-duplicate columns included; the plain FP32 path (mode 1)
 is only reported (its recall is not exact)."""
@@ -23,7 +25,7 @@ def dense_knn(ctx, D, q0, nq, method, k, mode):
     return idx[:nq * e].reshape(e, nq).T.copy(), dst[:nq * e].reshape(e, nq).T.copy()
 
 
-@pytest.mark.parametrize("mode", [0, 2])
+@pytest.mark.parametrize("mode", [0, 2, 3])
 @pytest.mark.parametrize("method,code", [("cosine", 1), ("euclidean", 2)])
 def test_bf16_screen_with_exact_rerank_equals_oracle(method, code, mode):
     import ctypes as C
@@ -45,7 +47,7 @@ def test_bf16_screen_with_exact_rerank_equals_oracle(method, code, mode):
 
 
 @pytest.mark.parametrize("k", [10, 20, 30])
-@pytest.mark.parametrize("mode", [0, 2])
+@pytest.mark.parametrize("mode", [0, 2, 3])
 @pytest.mark.parametrize("method,code", [("cosine", 1), ("euclidean", 2)])
 def test_bf16_screen_many_segments_and_zero_columns(method, code, mode, k):
     """70,001 references (three 32,768-reference segments, the last one ragged
@@ -58,7 +60,7 @@ def test_bf16_screen_many_segments_and_zero_columns(method, code, mode, k):
     import ctypes as C
     import torch
     from sparsedist_gb300 import _lib, synth
-    d, n, q0, nq = 32, 70001, 1000, 64
+    d, n, q0, nq = 32, 70001, 1000, 300
     X = synth.dense_embeddings(d=d, n=n, centres=50, seed=7)
     X[q0 + 5] = 0.0
     X[40000] = 0.0
@@ -106,18 +108,18 @@ def as_csc(X):
     return M
 
 
-@pytest.mark.parametrize("mode", [0, 2])
+@pytest.mark.parametrize("mode", [0, 2, 3])
 @pytest.mark.parametrize("method,code", [("cosine", 1), ("euclidean", 2)])
 def test_d256_block_equals_oracle(method, code, mode):
     """The target configuration's kernel shape: d = 256 (four 64-row K chunks),
     200,000 references from the embedding generator (Gaussian clusters and
-    1 % near duplicates at 1e-6), a 64-query block from the middle of the
+    1 % near duplicates at 1e-6), a 300-query block (a CTA pair and a partial one) from the middle of the
     matrix, k = 20; idx and distances bit for bit against the oracle's
     two-matrix search with k + 1 neighbours minus each query's own column."""
     import ctypes as C
     import torch
     from sparsedist_gb300 import _lib, synth
-    d, n, q0, nq, k = 256, 200000, 123456, 64, 20
+    d, n, q0, nq, k = 256, 200000, 123456, 300, 20
     X = synth.dense_embeddings(d=d, n=n, seed=5)
     ctx = _lib.Context()
     h = C.c_void_p()
@@ -134,7 +136,7 @@ def test_d256_block_equals_oracle(method, code, mode):
 
 
 @pytest.mark.parametrize("k", [20, 50, 64])
-@pytest.mark.parametrize("mode", [0, 2])
+@pytest.mark.parametrize("mode", [0, 2, 3])
 @pytest.mark.parametrize("method,code", [("cosine", 1), ("euclidean", 2)])
 def test_query_entry_equals_oracle(method, code, mode, k):
     """sdg_dense_knn_query: new query embeddings (host memory, drawn from the

@@ -63,3 +63,26 @@ def test_stall_hook_rejects_negative_counts():
     lib = _lib.load()
     assert lib.sdg_debug_stall_tc(-1) != 0
     assert lib.sdg_debug_stall_tc(0) == 0
+
+
+def test_dense_screen_pair_wait_runs_out():
+    # the CTA-pair form of the dense kernel (mode 3) the same way
+    import torch
+    from sparsedist_gb300 import _lib, synth
+    from test_gpu_dense import dense_knn
+    X = synth.dense_embeddings(d=64, n=3000, centres=20, seed=6)
+    ctx = _lib.Context()
+    h = C.c_void_p()
+    _lib.check(ctx.lib.sdg_dense_upload(ctx.handle, X.data_ptr(), 64, 3000, C.byref(h)))
+    try:
+        _lib.check(ctx.lib.sdg_debug_stall_tc(1))
+        with pytest.raises(_lib.SdgError) as ei:
+            dense_knn(ctx, h, 0, 3000, 1, 15, 3)
+        assert ei.value.code == SDG_E_CUDA and "timed out" in str(ei.value)
+        got = dense_knn(ctx, h, 0, 3000, 1, 15, 3)
+    finally:
+        ctx.lib.sdg_debug_stall_tc(0)
+        ctx.lib.sdg_dense_free(h)
+    want = OracleBackend().knn(sp.csc_matrix(X.double().cpu().numpy().T), k=15, method="cosine")
+    assert same_bits(got[0], want[0]) and same_bits(got[1], want[1])
+    torch.cuda.synchronize()
