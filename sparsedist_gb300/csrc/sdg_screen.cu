@@ -84,7 +84,9 @@ __global__ void k_check_rows(DevCsc M, int* err) {
 // its rounding whatever the summation order).
 // js: fval = the value, fxl = its x log x (from the FP64 values the exact path
 // uses), cnorm = the column's sum of |x log x| + x rounded up, and *range_err
-// set when a nonzero value lies outside [2^-100, 2^100].
+// set when a nonzero value lies outside [2^-100, 2^100]; pearson /
+// covariance: fval = the value, *range_err when a nonzero |value| lies outside
+// [2^-50, 2^50].
 __global__ void k_screen_prep(DevCsc M, int method, const double* uval, const double* xl, float* fval,
                               float* fxl, float* cnorm, int32_t* nnz, int* range_err) {
   const int64_t j = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
@@ -106,6 +108,9 @@ __global__ void k_screen_prep(DevCsc M, int method, const double* uval, const do
       fxl[a] = (float)xl[a];
       acc += fabs(xl[a]) + v;
       bad = bad || (v != 0.0 && !(v >= 0x1p-100 && v <= 0x1p100));
+    } else if (method == PEARSON || method == COVARIANCE) {
+      // FP32 products of values within 2^+-50 stay normal and their sums finite
+      bad = bad || (v != 0.0 && !(fabs(v) >= 0x1p-50 && fabs(v) <= 0x1p50));
     }
   }
 #pragma unroll
@@ -358,6 +363,9 @@ struct SelectScreenArgs {
   const int32_t* qnnz; const float* qnorm;   // indexed by query column
   const double* rsum;                        // js: reference column sums
   const double* qsum;                        // js: query column sums (indexed by query column)
+  // pearson / covariance: the columns' FP64 sums and sums of squares, nrow
+  const double *rs, *rss, *qs, *qss;
+  int32_t nrow;
   const uint8_t* ref_mask;                   // eligible reference columns
   const uint8_t* qry_blank;                  // query rows written all-NA
   const uint8_t* qry_force_exact;            // queries the screen cannot bound
@@ -414,6 +422,48 @@ __device__ __forceinline__ void js_key_and_bound(float G, double SP, double SQ, 
   err = U32 * (10.8f * (AP + AQ) + 0.75f * n * C) * 1.01f + 2.f * U32 * fabsf(key) + 1e-30f;
 }
 
+// pearson / covariance (fastCorr2 / fastCov2 in the single-pass form of the
+// exact path, pearson_finish / covariance_finish): the screen's s~ is the FP32
+// FMA chain over the matched rows' FP32 values; with u = 2^-24 and n <= min(nnz)
+// terms, |s~ - s| <= (n + 3) u (1 + n u 1.1) sum |ab| <= (n + 4) u 1.01 sqrt(SS_P
+// SS_Q) (Cauchy-Schwarz over the full columns' sums of squares; the exact
+// path's own FP64 sum is within n 2^-53 of s, inside the factor).  The key is
+// the exact path's formula evaluated in FP64 on s~ with the same rounded
+// operations, so the decisions that depend only on the moments (a zero or
+// non-finite denominator, which makes the exact value 0) are the exact path's:
+// cov = (s - S_P S_Q / N) / (N - 1), errs by E_s / (N - 1) plus 2^-50 of its
+// terms; pearson c = cov / (sqrt(v_P) sqrt(v_Q)) by E_cov / den plus 2^-50 |c|,
+// and both bounds are clamped to [-1, 1] as the exact value is.  A pearson
+// denominator below 1e-200 could let cov / den overflow (exact value 0 then):
+// the bounds are [-1, 1].  Larger key = better for both methods.
+__device__ __forceinline__ void moment_key_and_bound(bool pearson, float s, int32_t n_, int32_t nrow, double SP,
+                                                     double SSP, double SQ, double SSQ, float& key, float& err) {
+  const double N = (double)nrow;
+  const double norm = (nrow > 1) ? __dsub_rn(N, 1.0) : 1.0;
+  const double sd = (double)s;
+  const double Es = (((double)n_ + 4.0) * 5.9604644775390625e-8 * 1.01) * sqrt(SSP * SSQ) + 1e-300;
+  const double m = __dmul_rn(SP, SQ) / N;
+  const double cov = __dsub_rn(sd, m) / norm;
+  const double Ecov = (Es + 0x1p-50 * (fabs(sd) + fabs(m))) / norm;
+  double lo, hi;
+  if (!pearson) {
+    lo = cov - Ecov * 1.0001;
+    hi = cov + Ecov * 1.0001;
+  } else {
+    const double vp = __dsub_rn(SSP, __dmul_rn(SP, SP) / N) / norm;
+    const double vq = __dsub_rn(SSQ, __dmul_rn(SQ, SQ) / N) / norm;
+    const double den = __dmul_rn(sqrt(vp), sqrt(vq));
+    if (!(den > 0.0) || !isfinite(den)) { key = 0.f; err = 0.f; return; }   // the exact value is 0
+    if (den < 1e-200) { key = 0.f; err = 1.0001f; return; }
+    const double c = cov / den;
+    const double e = (Ecov / den + 0x1p-50 * fabs(c)) * 1.0001;
+    lo = fmin(1.0, fmax(-1.0, c - e));
+    hi = fmin(1.0, fmax(-1.0, c + e));
+  }
+  key = (float)(0.5 * (lo + hi));
+  err = (float)(0.5 * (hi - lo)) + 2.f * U32 * (fabsf(key) + 1.f) + 1e-30f;
+}
+
 __global__ void k_screen_select(SelectScreenArgs A) {
   extern __shared__ float lists[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -449,6 +499,9 @@ __global__ void k_screen_select(SelectScreenArgs A) {
         float key, err;
         if (A.method == JS)
           js_key_and_bound(Srow[pos], A.rsum[c], A.qsum[q], A.rnorm[c], Nq, min(nq_, A.rnnz[c]), key, err);
+        else if (A.method == PEARSON || A.method == COVARIANCE)
+          moment_key_and_bound(A.method == PEARSON, Srow[pos], min(nq_, A.rnnz[c]), A.nrow, A.rs[c], A.rss[c],
+                               A.qs[q], A.qss[q], key, err);
         else
           key_and_bound(A.method, Srow[pos], nq_, Nq, A.rnnz[c], A.rnorm ? A.rnorm[c] : 0.f, key, err);
         lo = key - err;
@@ -498,6 +551,9 @@ __global__ void k_screen_select(SelectScreenArgs A) {
         float key, err;
         if (A.method == JS)
           js_key_and_bound(Srow[pos], A.rsum[c], A.qsum[q], A.rnorm[c], Nq, min(nq_, A.rnnz[c]), key, err);
+        else if (A.method == PEARSON || A.method == COVARIANCE)
+          moment_key_and_bound(A.method == PEARSON, Srow[pos], min(nq_, A.rnnz[c]), A.nrow, A.rs[c], A.rss[c],
+                               A.qs[q], A.qss[q], key, err);
         else
           key_and_bound(A.method, Srow[pos], nq_, Nq, A.rnnz[c], A.rnorm ? A.rnorm[c] : 0.f, key, err);
         keep = (key + err) >= T - margin;
@@ -811,7 +867,8 @@ void launch_check_rows(const DevCsc& M, int* err, cudaStream_t s) {
 }
 
 bool screen_supported(int method, int k) {
-  return (method == BINARY || method == COSINE || method == EUCLIDEAN || method == MANHATTAN || method == JS) &&
+  return (method == BINARY || method == COSINE || method == EUCLIDEAN || method == MANHATTAN || method == JS ||
+          method == PEARSON || method == COVARIANCE) &&
          k >= 1 && k <= 1024;
 }
 
@@ -879,7 +936,7 @@ static int ensure_cache(ScreenCache* c, int method, const DevCsc& M, const ColAu
   }
   SK(cudaGetLastError());
   c->values_ok = true;
-  if (js && M.ncol > 0) {
+  if ((js || method == PEARSON || method == COVARIANCE) && M.ncol > 0) {
     int h_err = 0;
     SK(cudaMemcpyAsync(&h_err, range_err, sizeof(int), cudaMemcpyDeviceToHost, s));
     SK(cudaStreamSynchronize(s));
@@ -894,8 +951,8 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
                TensorCache* qt, int32_t* d_idx, double* d_val, int64_t* stats, const ScreenHooks& hooks) {
   SKN((cudaError_t)ensure_cache(rc, r.method, ref, ra, s));
   SKN((cudaError_t)ensure_cache(qc, r.method, qry, qa, s));
-  if (r.method == JS && !(rc->values_ok && qc->values_ok)) {
-    // values outside the range the FP32 js bound covers: every query exactly
+  if ((r.method == JS || r.method == PEARSON || r.method == COVARIANCE) && !(rc->values_ok && qc->values_ok)) {
+    // values outside the range the method's FP32 bound covers: every query exactly
     const int64_t lo = r.q_lo, hi = (r.q_hi < 0) ? qry.ncol : r.q_hi;
     if (hi > lo) hooks.exact_range(lo, hi - lo);
     return 0;
@@ -1061,6 +1118,7 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
     B.rnnz = rc->nnz; B.rnorm = normed ? rc->cnorm : nullptr;
     B.qnnz = qc->nnz; B.qnorm = normed ? qc->cnorm : nullptr;
     B.rsum = ra.xsum; B.qsum = qa.xsum;
+    B.rs = ra.s; B.rss = ra.ss; B.qs = qa.s; B.qss = qa.ss; B.nrow = ref.nrow;
     B.ref_mask = r.ref_mask; B.qry_blank = r.qry_blank; B.qry_force_exact = force;
     B.q_begin = q0; B.nq = nb; B.selfmode = r.selfmode; B.include_self = r.include_self;
     B.cap = cap; B.cand = cand; B.count = count; B.overflow = over;

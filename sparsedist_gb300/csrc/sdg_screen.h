@@ -23,8 +23,10 @@ struct ScreenCache {
   int32_t* nnz = nullptr;    // per column: stored entries
   int32_t* perm = nullptr;   // columns in descending-nnz order
   int64_t nnz_total = 0;
-  // js: every nonzero stored value lies in [2^-100, 2^100], the range the FP32
-  // js bound is derived for; else the js searches of this matrix are exact
+  // js / pearson / covariance: every nonzero stored value lies in the range
+  // the method's FP32 bound is derived for ([2^-100, 2^100] for js, |value| in
+  // [2^-50, 2^50] for the moment methods); else the searches of this matrix
+  // with that method are exact
   bool values_ok = true;
 };
 

@@ -92,3 +92,31 @@ def test_js_screen_equals_exact_engine(gpu):
         assert a[2] == b[2]
         assert same_bits(a[0], b[0]) and same_bits(a[1], b[1])
     gpu.set_engine(0)
+
+
+def test_moment_methods_screen_equals_exact_engine(gpu):
+    """pearson and covariance on the FP32 screen (engine 2: the matched-product
+    sum in FP32, the exact path's moment formula on it with a rigorous bound,
+    exact FP64 re-rank of the survivors) return the exact engine's result bit
+    for bit: signed values, a constant column, a near-constant one, dist and
+    similarity forms; a matrix with a value beyond 2^50 is searched exactly by
+    the same call."""
+    X = make_x(1500, 3000, 0.06, 51, signed=True)
+    Y = make_x(1500, 2200, 0.06, 52, signed=True)
+    X = X.tolil()
+    X[:, 7] = 2.5                                   # constant column (zero variance)
+    X[:750, 8] = 1.0                                # near-constant pattern
+    X = X.tocsc()
+    X.sort_indices()
+    T = X.copy()
+    T.data[::101] = 1e20
+    for A, B in ((X, None), (X, Y), (T, None)):
+        for method, dists in (("pearson", (True, False)), ("covariance", (True,))):
+            for d in dists:
+                gpu.set_engine(1)
+                a = gpu.knn(A, B, k=20, method=method, dist=d)
+                gpu.set_engine(2)
+                b = gpu.knn(A, B, k=20, method=method, dist=d)
+                assert a[2] == b[2]
+                assert same_bits(a[0], b[0]) and same_bits(a[1], b[1]), (method, d)
+    gpu.set_engine(0)

@@ -189,3 +189,88 @@ def test_js_bound_counts_above_one():
     for _ in range(20):
         P, Q = _js_pair(rng, 4000, 0.1, lambda g, m: g.negative_binomial(2, 0.1, m).astype(float) + 1.0)
         assert _js_case(P, Q, rng) < 1.0
+
+
+# ---- pearson / covariance: the FP32 product screen with the moment key
+# (sparsedist_gb300/csrc/sdg_screen.cu, moment_key_and_bound).  The screen's
+# s~ is the FP32 FMA chain over the matched rows' FP32 values (emulated here as
+# the FP64 product-plus-sum rounded once to FP32); the interval [key - err,
+# key + err] must contain the exact path's value (pearson_finish /
+# covariance_finish: FP64 sums in row order, then the clamp and the
+# non-finite-to-0 rule) for signed values, tiny and near-constant columns.
+
+U = 2.0 ** -24
+
+
+def _moment_bounds(pearson, s, n, N, SP, SSP, SQ, SSQ):
+    norm = N - 1.0 if N > 1 else 1.0
+    Es = ((n + 4.0) * U * 1.01) * np.sqrt(SSP * SSQ) + 1e-300
+    m = (SP * SQ) / N
+    cov = (s - m) / norm
+    Ecov = (Es + 2.0 ** -50 * (abs(s) + abs(m))) / norm
+    if not pearson:
+        lo, hi = cov - Ecov * 1.0001, cov + Ecov * 1.0001
+    else:
+        vp = (SSP - (SP * SP) / N) / norm
+        vq = (SSQ - (SQ * SQ) / N) / norm
+        with np.errstate(invalid="ignore"):
+            den = np.sqrt(vp) * np.sqrt(vq)
+        if not (den > 0.0) or not np.isfinite(den):
+            return 0.0, 0.0
+        if den < 1e-200:
+            return 0.0, 1.0001
+        c = cov / den
+        e = (Ecov / den + 2.0 ** -50 * abs(c)) * 1.0001
+        lo, hi = min(1.0, max(-1.0, c - e)), min(1.0, max(-1.0, c + e))
+    key = np.float32(0.5 * (lo + hi))
+    err = np.float32(0.5 * (hi - lo)) + np.float32(2 * U * (abs(float(key)) + 1.0)) + np.float32(1e-30)
+    return float(key), float(err)
+
+
+def _exact_value(pearson, A, B):
+    N = float(len(A))
+    norm = N - 1.0 if N > 1 else 1.0
+    sab = 0.0
+    for a, b in zip(A, B):
+        if a != 0 and b != 0:
+            sab = sab + a * b
+    cov = (sab - (A.sum() * B.sum()) / N) / norm
+    if not pearson:
+        return cov
+    va = (np.dot(A, A) - (A.sum() * A.sum()) / N) / norm
+    vb = (np.dot(B, B) - (B.sum() * B.sum()) / N) / norm
+    with np.errstate(invalid="ignore", divide="ignore"):
+        c = cov / (np.sqrt(va) * np.sqrt(vb))
+    if not np.isfinite(c):
+        c = 0.0
+    return min(1.0, max(-1.0, c))
+
+
+def _moment_case(A, B, rng):
+    shared = np.flatnonzero((A != 0) & (B != 0))
+    n = int(min(np.count_nonzero(A), np.count_nonzero(B)))
+    acc = np.float32(0)
+    for i in shared:                                        # the reference column's row order
+        acc = np.float32(float(np.float32(A[i])) * float(np.float32(B[i])) + float(acc))
+    for pearson in (True, False):
+        key, err = _moment_bounds(pearson, float(acc), n, float(len(A)), float(A.sum()), float(np.dot(A, A)),
+                                  float(B.sum()), float(np.dot(B, B)))
+        v = _exact_value(pearson, A, B)
+        assert key - err <= v <= key + err, (pearson, key, err, v)
+
+
+def test_moment_bounds_cover_signed_and_degenerate_columns():
+    rng = np.random.default_rng(31)
+    for trial in range(60):
+        nrow = int(rng.integers(50, 3000))
+        dens = float(rng.uniform(0.02, 0.6))
+        A = np.where(rng.random(nrow) < dens, rng.standard_normal(nrow) * 10 ** rng.uniform(-3, 3), 0.0)
+        B = np.where(rng.random(nrow) < dens, rng.standard_normal(nrow) * 10 ** rng.uniform(-3, 3), 0.0)
+        if trial % 5 == 0:
+            B = A * 3.0 + (A != 0) * 1e-9              # nearly collinear: c close to 1
+        if trial % 7 == 0:
+            A[:] = 0.0
+            A[:nrow // 2] = 2.5                        # near-constant pattern
+        if trial % 11 == 0:
+            B[:] = 1.25                                # constant column: zero variance, value 0
+        _moment_case(A, B, rng)
