@@ -66,6 +66,26 @@ __global__ void k_dense_cast(int64_t total, const double* u64, const float* x32,
   }
 }
 
+// Per column: ||v - bf16(v)|| and ||bf16(v)|| of the unit column and of the
+// column, in FP64 from the copies the screen multiplies, rounded up to FP32.
+__global__ void k_dense_errnorm(int32_t d, int64_t n, const double* u64, const double* x64,
+                                const __nv_bfloat16* ub, const __nv_bfloat16* xb, float* ue, float* un, float* xe,
+                                float* xn) {
+  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  double eu = 0.0, nu = 0.0, ex = 0.0, nx = 0.0;
+  for (int32_t r = 0; r < d; ++r) {
+    const int64_t a = j * d + r;
+    const double bu = (double)__bfloat162float(ub[a]), bx = (double)__bfloat162float(xb[a]);
+    const double du = u64[a] - bu, dx = x64[a] - bx;
+    eu += du * du; nu += bu * bu; ex += dx * dx; nx += bx * bx;
+  }
+  ue[j] = __double2float_ru(sqrt(eu) * (1.0 + 1e-12));
+  un[j] = __double2float_ru(sqrt(nu) * (1.0 + 1e-12));
+  xe[j] = __double2float_ru(sqrt(ex) * (1.0 + 1e-12));
+  xn[j] = __double2float_ru(sqrt(nx) * (1.0 + 1e-12));
+}
+
 // A query's scan over the n references is split into segments of DSEG
 // references, one warp per (query, segment), so that the slab is streamed at
 // full bandwidth: (1) each warp keeps the top k of its segment's pessimistic
@@ -360,6 +380,8 @@ int dense_build(sdg_ctx* ctx, const float* X, int32_t d, int64_t n, bool async, 
   chk(alloc(&D->xb, tot * 2)); chk(alloc(&D->ub, tot * 2));
   chk(alloc(&D->norm2, npad * 4)); chk(alloc(&D->scale, n * 8));
   chk(alloc(&D->empty, npad)); chk(alloc(&D->pview, (n + 1) * 8));
+  chk(alloc(&D->ue, npad * 4)); chk(alloc(&D->un, npad * 4));
+  chk(alloc(&D->xe, npad * 4)); chk(alloc(&D->xn, npad * 4));
   chk(alloc(&err, sizeof(int)));
   if (D->dpad != d) {
     const size_t ptot = (size_t)D->dpad * (size_t)n;
@@ -368,6 +390,7 @@ int dense_build(sdg_ctx* ctx, const float* X, int32_t d, int64_t n, bool async, 
   if (e != cudaSuccess) { sdg_dense_free(D); return cuda_fail(e); }
   chk(cudaMemsetAsync(D->norm2, 0, npad * 4, s));
   chk(cudaMemsetAsync(D->empty, 1, npad, s));
+  for (float* p : {D->ue, D->un, D->xe, D->xn}) chk(cudaMemsetAsync(p, 0, npad * 4, s));
   chk(cudaMemsetAsync(err, 0, sizeof(int), s));
   chk(cudaMemcpyAsync(D->x32, X, tot * 4, cudaMemcpyDefault, s));
   if (e == cudaSuccess) {
@@ -377,6 +400,8 @@ int dense_build(sdg_ctx* ctx, const float* X, int32_t d, int64_t n, bool async, 
     M.nrow = d; M.ncol = (int32_t)n; M.p = D->pview; M.i = nullptr; M.x = D->x64;
     launch_unit_csc(M, D->u64, D->scale, err, s);
     k_dense_cast<<<152 * 16, 256, 0, s>>>((int64_t)tot, D->u64, D->x32, D->u32, D->ub, D->xb);
+    k_dense_errnorm<<<blocks_for(n, 128), 128, 0, s>>>(d, n, D->u64, D->x64, D->ub, D->xb, D->ue, D->un, D->xe,
+                                                        D->xn);
   }
   if (D->dpad == d) {
     D->ubp = D->ub;
@@ -633,6 +658,7 @@ SDG_API int sdg_dense_free(sdg_dense* D) {
   cudaSetDevice(D->device);
   void* bufs[] = {(void*)D->x64, (void*)D->u64, (void*)D->x32, (void*)D->u32, (void*)D->xb, (void*)D->ub,
                   (void*)D->norm2, (void*)D->scale, (void*)D->empty, (void*)D->pview,
+                  (void*)D->ue, (void*)D->un, (void*)D->xe, (void*)D->xn,
                   (void*)(D->ubp != D->ub ? D->ubp : nullptr), (void*)(D->xbp != D->xb ? D->xbp : nullptr)};
   if (D->async) {
     // a per-request matrix: stream-ordered frees after the work queued on its stream

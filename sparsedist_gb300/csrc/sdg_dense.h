@@ -25,6 +25,13 @@ struct sdg_dense {
   __nv_bfloat16* xbp = nullptr;   // dpad x n, zero rows below d (aliases xb when dpad == d)
   __nv_bfloat16* ubp = nullptr;
   float* norm2 = nullptr;         // sum of squares (FP64, rounded), padded to npad with 0
+  // per column, for the fused screen's per-pair bound: the exact norm of each
+  // BF16 copy's rounding error and of the copy (FP64, rounded up), unit
+  // columns (cosine) and columns (euclidean); [npad], 0 past n
+  float* ue = nullptr;
+  float* un = nullptr;
+  float* xe = nullptr;
+  float* xn = nullptr;
   double* scale = nullptr;        // unit_csc scale (0 = empty column)
   uint8_t* empty = nullptr;       // padded to npad with 1
   int64_t* pview = nullptr;       // column offsets j * d, for the CSC kernels

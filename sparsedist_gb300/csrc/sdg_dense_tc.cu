@@ -25,7 +25,9 @@
 // half) list.  The running cut is the k-th best of a subset, never above the
 // query's final cut, so the union of the lists holds every reference that the
 // slab screen keeps; k_tc_merge applies the final cut (the k-th best over all
-// the query's lists) exactly as the slab screen does.
+// the query's lists) exactly as the slab screen does, then a second, tighter
+// cut from per-pair bounds (the columns' BF16 rounding-error norms) on the
+// candidates alone.
 //
 // Hot test.  An epilogue thread tests x = a s - w[r] against one threshold
 // e_thr per query (a = 1, w = 0 for cosine; a = 2, w = (1 - c) Nr for
@@ -124,7 +126,7 @@ struct TcArgs {
   float* lists;               // [nq][nslots][k]
   int32_t* ecount;            // [nq][nslots]
   int32_t* eidx;              // [nq][nslots][ecap]
-  float* ehi;                 // [nq][nslots][ecap]
+  float* es;                  // [nq][nslots][ecap]: the appended references' GEMM values
   int* status;
   int stall;                  // failure-detection test: the MMA issuer's first wait never completes
 };
@@ -347,7 +349,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
     float e_thr = -FLT_MAX;
     int cnt = 0, nbuf = 0;
     int32_t* my_idx = P.eidx;
-    float* my_hi = P.ehi;
+    float* my_s = P.es;
 
     // hi >= cut implies x >= e_thr (the hot-test bound in the file header),
     // with 2^-12 slack for the FP32 roundings of x and e_thr
@@ -371,7 +373,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
       const float lo = key - err, hi = key + err;
       const float Te = fmaxf(T, Ts);
       if (hi >= dense_cut(Te)) {
-        if (cnt < P.ecap) { my_idx[cnt] = (int32_t)r; my_hi[cnt] = hi; }
+        if (cnt < P.ecap) { my_idx[cnt] = (int32_t)r; my_s[cnt] = s; }
         ++cnt;
       }
       if (lo > Te) {
@@ -488,7 +490,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
       const int64_t slot =
           active ? (ql * P.nslots + (unit - first_cta(g, ntiles, per)) * 2 + half) : 0;
       my_idx = P.eidx + slot * P.ecap;
-      my_hi = P.ehi + slot * P.ecap;
+      my_s = P.es + slot * P.ecap;
       for (; f < fe; ++f, ++j) {
         const int buf = (int)(j & 1);
         const bool got = wait(acc_full + buf, (uint32_t)(j >> 1) & 1u);
@@ -579,27 +581,79 @@ __device__ __forceinline__ void warp_insert_desc_tc(float* lst, int K, int& n, u
   }
 }
 
+struct MergeArgs {
+  int64_t q0, nq;
+  int gm;                      // queries per group
+  int64_t ntiles, per, nslots;
+  int K, ecap, method;
+  int32_t d;
+  const uint8_t* qempty;
+  const unsigned* tshared;
+  const float* lists;
+  const int32_t* ecount;
+  const int32_t* eidx;
+  const float* es;
+  const float* norm2;          // reference sums of squares
+  const float* qnorm2;         // query sums of squares (index in Q)
+  const float *re, *rn;        // reference copies: rounding-error norm, norm (the method's copy)
+  const float *qe, *qn;        // query copies (index in Q)
+  int cap;
+  int32_t* cand;
+  float* cand_s;               // [nq][cap] the candidates' GEMM values
+  int32_t* count;
+  int32_t* over;
+};
+
+// The per-pair bound of one candidate from the columns' BF16 copies: with v
+// the exact (unit) columns and b their BF16 copies, |sum v_q v_r - sum b_q b_r|
+// <= e_q ||v_r|| + ||b_q|| e_r (Cauchy-Schwarz; e = ||v - b||, computed in
+// FP64 and rounded up at upload), the BF16 products are exact in FP32 and the
+// tensor cores' FP32 accumulation of d products is allowed (d + 64) 2^-21
+// ||b_q|| ||b_r||; ||v_r|| is 1 (unit columns) or sqrt(Nr).  The key is the
+// screen's (s for cosine, 2 s - Nq - Nr for euclidean) with the FP32 roundings
+// of Nq, Nr and the key allowed 2^-20 of the terms.
+__device__ __forceinline__ void tight_bounds(const MergeArgs& A, float s, int64_t r, float Nq, float qe, float qn,
+                                             float& lo, float& hi) {
+  const float acc = (float)(A.d + 64) * 4.76837158203125e-7f;     // 2^-21
+  if (A.method == COSINE) {
+    const float E = (1.000001f * qe * 1.000001f + qn * A.re[r] + acc * qn * A.rn[r]) * 1.01f + 1e-12f +
+                    2.384185791015625e-7f * fabsf(s);               // 2^-22 |s|
+    lo = s - E;
+    hi = s + E;
+  } else {
+    const float Nr = A.norm2[r];
+    const float Es = (qe * sqrtf(Nr) * 1.000001f + qn * A.re[r] + acc * qn * A.rn[r]) * 1.01f + 1e-30f;
+    const float key = 2.f * s - (Nq + Nr);
+    const float E = 2.f * Es + 9.5367431640625e-7f * (Nq + Nr + 2.f * fabsf(s)) + 1e-30f;
+    lo = key - E;
+    hi = key + E;
+  }
+}
+
 // Per query: T = the k-th largest pessimistic key over the lists of every
 // (segment, half) that covered it (the exact k-th over all references: the top
 // k of a union is the top k of the parts' top k), cut = dense_cut(T); the
-// candidates are the appended references with hi >= cut.
-__global__ void k_tc_merge(int64_t q0, int64_t nq, int gm, int64_t ntiles, int64_t per, int64_t nslots, int K, int ecap,
-                           const uint8_t* qempty, const unsigned* tshared, const float* lists,
-                           const int32_t* ecount, const int32_t* eidx, const float* ehi, int cap, int32_t* cand,
-                           int32_t* count, int32_t* over) {
+// candidates are the appended references with hi >= cut, hi the uniform bound
+// of the screen.  A second, tighter cut follows on the candidates alone: T2 =
+// the k-th largest per-pair lower bound (tight_bounds) among them is again at
+// most the exact k-th best key (k candidates reach it), so every member of the
+// exact top k (ties included) has its per-pair upper bound at or above
+// dense_cut(max(T, T2)) and is kept.
+__global__ void k_tc_merge(MergeArgs A) {
   __shared__ float sl[MW][KT];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t ql = (int64_t)blockIdx.x * MW + warp;
-  if (ql >= nq) return;
-  if (qempty[q0 + ql]) {
-    if (lane == 0) { count[ql] = 0; over[ql] = 0; }
+  if (ql >= A.nq) return;
+  const int K = A.K;
+  if (A.qempty[A.q0 + ql]) {
+    if (lane == 0) { A.count[ql] = 0; A.over[ql] = 0; }
     return;
   }
-  const int64_t g = ql / gm;
-  const int64_t used = 2 * (last_cta(g, ntiles, per) - first_cta(g, ntiles, per) + 1);
+  const int64_t g = ql / A.gm;
+  const int64_t used = 2 * (last_cta(g, A.ntiles, A.per) - first_cta(g, A.ntiles, A.per) + 1);
   float* lst = sl[warp];
   int n = 0;
-  const float* in = lists + ql * nslots * (int64_t)K;
+  const float* in = A.lists + ql * A.nslots * (int64_t)K;
   const int64_t tot = used * K;
   for (int64_t p0 = 0; p0 < tot; p0 += 32) {
     const float v = p0 + lane < tot ? in[p0 + lane] : -INFINITY;
@@ -610,26 +664,72 @@ __global__ void k_tc_merge(int64_t q0, int64_t nq, int gm, int64_t ntiles, int64
   // view of the shared key reached the final k-th best, fewer than k keys at
   // or above it may be listed; the shared key (the k-th best of a subset,
   // never above the final) then is the final k-th best.
-  const float T = fmaxf((n == K) ? lst[K - 1] : -INFINITY, fkey_value(tshared[ql]));
+  const float T = fmaxf((n == K) ? lst[K - 1] : -INFINITY, fkey_value(A.tshared[ql]));
   const float cut = dense_cut(T);
+  const int64_t q = A.q0 + ql;
+  const float Nq = A.qnorm2[q];
   bool ovf = false;
   int total = 0;
-  int32_t* out = cand + ql * (int64_t)cap;
+  int32_t* out = A.cand + ql * (int64_t)A.cap;
+  float* out_s = A.cand_s + ql * (int64_t)A.cap;
   for (int64_t r = 0; r < used && !ovf; ++r) {
-    const int64_t slot = ql * nslots + r;
-    const int c = ecount[slot];
-    if (c > ecap) { ovf = true; break; }
+    const int64_t slot = ql * A.nslots + r;
+    const int c = A.ecount[slot];
+    if (c > A.ecap) { ovf = true; break; }
     for (int p0 = 0; p0 < c; p0 += 32) {
       const int p = p0 + lane;
-      const bool keep = p < c && ehi[slot * ecap + p] >= cut;
+      bool keep = false;
+      int32_t ref = 0;
+      float sv = 0.f;
+      if (p < c) {
+        ref = A.eidx[slot * A.ecap + p];
+        sv = A.es[slot * A.ecap + p];
+        float key, err;
+        dense_key(A.method, 0, A.d, sv, Nq, A.norm2[ref], key, err);
+        keep = key + err >= cut;
+      }
       const unsigned m = __ballot_sync(0xffffffffu, keep);
       const int rank = __popc(m & ((1u << lane) - 1u));
-      if (keep && total + rank < cap) out[total + rank] = eidx[slot * ecap + p];
+      if (keep && total + rank < A.cap) { out[total + rank] = ref; out_s[total + rank] = sv; }
       total += __popc(m);
     }
-    if (total > cap) ovf = true;
+    if (total > A.cap) ovf = true;
   }
-  if (lane == 0) { count[ql] = ovf ? 0 : total; over[ql] = ovf ? 1 : 0; }
+  if (!ovf && total > K) {
+    const float qe = A.qe[q], qn = A.qn[q];
+    n = 0;
+    __syncwarp();
+    for (int p0 = 0; p0 < total; p0 += 32) {
+      const int p = p0 + lane;
+      float lo = -INFINITY, hi;
+      if (p < total) tight_bounds(A, out_s[p], out[p], Nq, qe, qn, lo, hi);
+      const unsigned m = __ballot_sync(0xffffffffu, p < total && (n < K || lo > lst[K - 1]));
+      if (m) warp_insert_desc_tc(lst, K, n, m, lo, lane);
+    }
+    const float T2 = (n == K) ? lst[K - 1] : -INFINITY;
+    const float cut2 = dense_cut(fmaxf(T, T2));
+    int kept = 0;
+    for (int p0 = 0; p0 < total; p0 += 32) {
+      const int p = p0 + lane;
+      bool keep = false;
+      int32_t ref = 0;
+      float sv = 0.f;
+      if (p < total) {
+        ref = out[p];
+        sv = out_s[p];
+        float lo, hi;
+        tight_bounds(A, sv, ref, Nq, qe, qn, lo, hi);
+        keep = hi >= cut2;
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, keep);   // every lane has read slot p first
+      const int rank = __popc(m & ((1u << lane) - 1u));
+      if (keep) { out[kept + rank] = ref; out_s[kept + rank] = sv; }
+      kept += __popc(m);
+      __syncwarp();
+    }
+    total = kept;
+  }
+  if (lane == 0) { A.count[ql] = ovf ? 0 : total; A.over[ql] = ovf ? 1 : 0; }
 }
 
 __global__ void k_tc_key_init(int64_t nq, unsigned* keys) {
@@ -748,7 +848,7 @@ int tc_screen(sdg_ctx* ctx, const sdg_dense* Q, const sdg_dense* D, bool self, i
   const float rel = 0.0040f + (float)D->d * 2.384185791015625e-7f;
   const float omc = 1.f - (rel + 9.5367431640625e-7f);
 
-  float *w = nullptr, *lists = nullptr, *ehi = nullptr;
+  float *w = nullptr, *lists = nullptr, *es = nullptr, *cand_s = nullptr;
   int32_t *ecount = nullptr, *eidx = nullptr;
   unsigned* tshared = nullptr;
   int* status = nullptr;
@@ -759,7 +859,8 @@ int tc_screen(sdg_ctx* ctx, const sdg_dense* Q, const sdg_dense* D, bool self, i
   chk(cudaMallocAsync(&lists, sizeof(float) * (size_t)(nq * nslots * k), s));
   chk(cudaMallocAsync(&ecount, sizeof(int32_t) * (size_t)(nq * nslots), s));
   chk(cudaMallocAsync(&eidx, sizeof(int32_t) * (size_t)(nq * nslots * ecap), s));
-  chk(cudaMallocAsync(&ehi, sizeof(float) * (size_t)(nq * nslots * ecap), s));
+  chk(cudaMallocAsync(&es, sizeof(float) * (size_t)(nq * nslots * ecap), s));
+  chk(cudaMallocAsync(&cand_s, sizeof(float) * (size_t)(nq * cap), s));
   chk(cudaMallocAsync(&status, sizeof(int), s));
   chk(cudaMallocAsync(&tshared, sizeof(unsigned) * (size_t)nq, s));
   if (e == cudaSuccess) {
@@ -776,7 +877,7 @@ int tc_screen(sdg_ctx* ctx, const sdg_dense* Q, const sdg_dense* D, bool self, i
     P.a = (method == COSINE) ? 1.f : 2.f; P.one_minus_c = omc;
     P.w = w; P.norm2 = D->norm2; P.qnorm2 = Q->norm2; P.qempty = Q->empty;
     P.tshared = tshared;
-    P.lists = lists; P.ecount = ecount; P.eidx = eidx; P.ehi = ehi;
+    P.lists = lists; P.ecount = ecount; P.eidx = eidx; P.es = es;
     P.status = status;
     P.stall = tc_take_stall() ? 1 : 0;
     auto kern = pick_kernel(pair);
@@ -798,15 +899,22 @@ int tc_screen(sdg_ctx* ctx, const sdg_dense* Q, const sdg_dense* D, bool self, i
     }
     sdg_time_end(ctx);
     chk(cudaGetLastError());
-    k_tc_merge<<<(unsigned)((nq + MW - 1) / MW), MW * 32, 0, s>>>(q0, nq, GM, ntiles, per, nslots, k, ecap, Q->empty,
-                                                                  tshared, lists, ecount, eidx, ehi, cap, cand,
-                                                                  count, over);
+    MergeArgs M;
+    M.q0 = q0; M.nq = nq; M.gm = GM; M.ntiles = ntiles; M.per = per; M.nslots = nslots;
+    M.K = k; M.ecap = ecap; M.method = method; M.d = D->d;
+    M.qempty = Q->empty; M.tshared = tshared; M.lists = lists; M.ecount = ecount; M.eidx = eidx; M.es = es;
+    M.norm2 = D->norm2; M.qnorm2 = Q->norm2;
+    M.re = (method == COSINE) ? D->ue : D->xe; M.rn = (method == COSINE) ? D->un : D->xn;
+    M.qe = (method == COSINE) ? Q->ue : Q->xe; M.qn = (method == COSINE) ? Q->un : Q->xn;
+    M.cap = cap; M.cand = cand; M.cand_s = cand_s; M.count = count; M.over = over;
+    k_tc_merge<<<(unsigned)((nq + MW - 1) / MW), MW * 32, 0, s>>>(M);
     chk(cudaGetLastError());
   }
   int hstatus = 0;
   if (e == cudaSuccess) chk(cudaMemcpyAsync(&hstatus, status, sizeof(int), cudaMemcpyDeviceToHost, s));
   if (e == cudaSuccess) chk(cudaStreamSynchronize(s));
-  for (void* p : {(void*)w, (void*)lists, (void*)ecount, (void*)eidx, (void*)ehi, (void*)status, (void*)tshared})
+  for (void* p : {(void*)w, (void*)lists, (void*)ecount, (void*)eidx, (void*)es, (void*)cand_s, (void*)status,
+                  (void*)tshared})
     if (p) cudaFreeAsync(p, s);
   if (e != cudaSuccess) {
     set_error(cudaGetErrorString(e));

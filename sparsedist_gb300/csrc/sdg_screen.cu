@@ -493,7 +493,9 @@ __global__ void k_screen_select(SelectScreenArgs A) {
     if (ok) {
       const int32_t c = A.rperm[pos];
       if (A.ref_mask && A.ref_mask[c]) ok = false;
-      else if (c == self_c) {
+      else if (c == self_c && !(A.include_self && A.method == COVARIANCE)) {
+        // a restored self value (R/sparseKNN.R:270-279) is the best key; a
+        // covariance self pair keeps its computed value and is an ordinary pair
         if (A.include_self) lo = INFINITY; else ok = false;
       } else {
         float key, err;
@@ -546,7 +548,7 @@ __global__ void k_screen_select(SelectScreenArgs A) {
     if (pos < A.nr) {
       c = A.rperm[pos];
       if (A.ref_mask && A.ref_mask[c]) keep = false;
-      else if (c == self_c) keep = A.include_self != 0;
+      else if (c == self_c && !(A.include_self && A.method == COVARIANCE)) keep = A.include_self != 0;
       else {
         float key, err;
         if (A.method == JS)
@@ -1132,12 +1134,12 @@ int screen_knn(cudaStream_t s, const ScreenRun& r, const DevCsc& ref, const ColA
     // exact FP64 values of the kept pairs, then the exact top-k
     if (rerank_warp_supported(r.method)) {
       launch_rerank_warp(r.method, r.dist, ref, ra, qry, qa, cand, count, cap, nb, q0,
-                         r.selfmode && r.include_self, r.self_value, rvals, s);
+                         r.selfmode && r.include_self && r.method != COVARIANCE, r.self_value, rvals, s);
     } else {
       k_exact_candidates_prep<<<blocks_for(nb * cap, 256), 256, 0, s>>>(count, nb, cap, qidx,
                                                                           cand, ridx, q0);
       launch_exact_pairs_sparse(r.method, r.dist, ref, ra, qry, qa, ridx, qidx, nb * cap,
-                                r.selfmode && r.include_self, r.self_value, rvals, s);
+                                r.selfmode && r.include_self && r.method != COVARIANCE, r.self_value, rvals, s);
     }
     SelectArgs sa;
     sa.vals = rvals; sa.seg_stride = cap; sa.elem_stride = 1; sa.nseg = nb;

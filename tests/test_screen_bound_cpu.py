@@ -274,3 +274,53 @@ def test_moment_bounds_cover_signed_and_degenerate_columns():
         if trial % 11 == 0:
             B[:] = 1.25                                # constant column: zero variance, value 0
         _moment_case(A, B, rng)
+
+
+# ---- the dense screen's per-pair bound (sparsedist_gb300/csrc/sdg_dense_tc.cu,
+# tight_bounds): BF16 copies (FP64 -> FP32 -> BF16, round to nearest even as
+# __float2bfloat16_rn), exact BF16 products in FP32, FP32 sums in random
+# orders; |sum b_q b_r - sum v_q v_r| <= (e_q ||v_r|| + ||b_q|| e_r + (d + 64)
+# 2^-21 ||b_q|| ||b_r||) 1.01 for unit columns (cosine) and raw columns
+# (euclidean's inner product).
+
+def _bf16(x):
+    f = np.asarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    lsb = (f >> 16) & 1
+    r = ((f + 0x7FFF + lsb) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def _dense_case(vq, vr, rng, unit):
+    bq, br = _bf16(vq), _bf16(vr)
+    eq, er = np.linalg.norm(vq - bq) * (1 + 1e-12), np.linalg.norm(vr - br) * (1 + 1e-12)
+    nq, nr = np.linalg.norm(bq) * (1 + 1e-12), np.linalg.norm(br) * (1 + 1e-12)
+    d = len(vq)
+    vnorm = 1.000001 if unit else float(np.linalg.norm(vr)) * 1.000001
+    bound = (eq * vnorm + nq * er + (d + 64) * 2.0 ** -21 * nq * nr) * 1.01 + 1e-12
+    exact = float(np.dot(vq, vr))
+    prods = (bq * br).astype(np.float32)
+    assert np.all(prods.astype(np.float64) == bq * br)          # exact in FP32
+    worst = 0.0
+    for _ in range(3):
+        acc = np.float32(0)
+        for t in prods[rng.permutation(d)]:
+            acc = np.float32(acc + t)
+        err = abs(float(acc) - exact)
+        assert err <= bound, (err, bound)
+        worst = max(worst, err / bound)
+    return worst
+
+
+def test_dense_bf16_pair_bound():
+    rng = np.random.default_rng(41)
+    worst = 0.0
+    for trial in range(40):
+        d = int(rng.choice([32, 64, 96, 256]))
+        vq, vr = rng.standard_normal(d), rng.standard_normal(d)
+        if trial % 3 == 0:
+            vr = vq + 1e-6 * rng.standard_normal(d)                # near duplicate
+        unit = trial % 2 == 0
+        if unit:
+            vq, vr = vq / np.linalg.norm(vq), vr / np.linalg.norm(vr)
+        worst = max(worst, _dense_case(vq, vr, rng, unit))
+    assert worst < 1.0
