@@ -360,8 +360,9 @@ def knn_cross_batch(ctx, problems, drop_degenerate=True):
     for p, (X, Y, _, _, k) in enumerate(problems):
         nx, ny, a, b = X.shape[1], Y.shape[1], int(kf[p]), int(kr[p])
         fi, fd, ri, rd = outs[p]
-        res.append({"forward": (fi[:nx * a].reshape(a, nx).T.copy(), fd[:nx * a].reshape(a, nx).T.copy()),
-                    "reverse": (ri[:ny * b].reshape(b, ny).T.copy(), rd[:ny * b].reshape(b, ny).T.copy()),
+        # (n, k) views of the column-major results (the R layout), no copies
+        res.append({"forward": (fi[:nx * a].reshape(a, nx).T, fd[:nx * a].reshape(a, nx).T),
+                    "reverse": (ri[:ny * b].reshape(b, ny).T, rd[:ny * b].reshape(b, ny).T),
                     "flags": int(fl[p]), "status": int(st[p]), "engines": (int(eng[2 * p]), int(eng[2 * p + 1]))})
     knn_cross_batch.engine_seconds = secs.tolist()
     return rc, res
