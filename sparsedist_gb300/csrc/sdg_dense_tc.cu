@@ -498,6 +498,17 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
         fence_after();
         const int64_t r_half = (f - g * ntiles) * BN + half * (BN / 2);
         const uint32_t tb = tmem + lane_base + (uint32_t)(buf * BN + half * (BN / 2));
+        // the buffer goes back to the MMAs as soon as its last TMEM reads are
+        // done (the values being processed are in registers by then): the
+        // hand-off to the next-but-one tile does not wait for the processing
+        auto release = [&]() {
+          fence_before();
+          __syncwarp();
+          if (lane == 0) {
+            if constexpr (PAIR) mbar_arrive_remote(acc_empty + buf, 0);   // the even CTA's MMA waits on it
+            else mbar_arrive(acc_empty + buf);
+          }
+        };
         if constexpr (KL <= 32) {
           // chunks in pairs (the TMEM loads take a few tens of cycles; the
           // pair's hot tests overlap)
@@ -508,6 +519,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
             tmem_ld32_issue(tb + hh * 32 + 32, vb);
             tmem_ld_wait(va);
             tmem_ld_wait(vb);
+            if (hh == BN / 64 - 2) release();
             const uint32_t ma = hot_mask(va, r_half + hh * 32), mb = hot_mask(vb, r_half + hh * 32 + 32);
             if (__any_sync(0xffffffffu, (ma | mb) != 0u)) {
               take(va, ma, r_half + hh * 32);
@@ -520,15 +532,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_dense_tc(const __grid_constant__
           for (int hh = 0; hh < BN / 64; ++hh) {
             uint32_t va[32];
             tmem_ld32(tb + hh * 32, va);
+            if (hh == BN / 64 - 1) release();
             const uint32_t ma = hot_mask(va, r_half + hh * 32);
             if (__any_sync(0xffffffffu, ma != 0u)) take(va, ma, r_half + hh * 32);
           }
-        }
-        fence_before();
-        __syncwarp();
-        if (lane == 0) {
-          if constexpr (PAIR) mbar_arrive_remote(acc_empty + buf, 0);   // the even CTA's MMA waits on it
-          else mbar_arrive(acc_empty + buf);
         }
         if ((j & (SHARE_TILES - 1)) == SHARE_TILES - 1 && active) {
           // publish this list's running key and take the best one published
