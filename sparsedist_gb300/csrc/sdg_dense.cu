@@ -35,24 +35,33 @@ inline unsigned blocks_for(int64_t n, int threads) {
   return (unsigned)((n + threads - 1) / threads);
 }
 
+// One warp per column (coalesced rows): the FP64 copy, the sum of squares
+// (FP64, any order: it only feeds the screens' bounds and the plain mode),
+// the empty flag and the finiteness check.
 __global__ void k_dense_prep(int32_t d, int64_t n, const float* x32, double* x64, float* norm2,
-                             uint8_t* empty, int64_t* pview, int* err) {
-  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (j > n) return;
-  pview[j] = j * d;
-  if (j == n) return;
+                             uint8_t* empty, int* err) {
+  const int lane = threadIdx.x & 31;
+  const int64_t j = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (j >= n) return;
   double s = 0.0;
-  uint8_t e = 1;
-  for (int32_t r = 0; r < d; ++r) {
+  bool nz = false, bad = false;
+  for (int32_t r = lane; r < d; r += 32) {
     const float v = x32[j * d + r];
-    if (!isfinite(v)) atomicOr(err, 1);
-    if (v != 0.f) e = 0;
+    bad |= !isfinite(v);
+    nz |= (v != 0.f);
     const double dv = (double)v;
     x64[j * d + r] = dv;
     s += dv * dv;
   }
-  norm2[j] = (float)s;
-  empty[j] = e;
+#pragma unroll
+  for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  nz = __any_sync(0xffffffffu, nz);
+  bad = __any_sync(0xffffffffu, bad);
+  if (lane == 0) {
+    norm2[j] = (float)s;
+    empty[j] = nz ? 0 : 1;
+    if (bad) atomicOr(err, 1);
+  }
 }
 
 __global__ void k_dense_cast(int64_t total, const double* u64, const float* x32, float* u32,
@@ -67,23 +76,35 @@ __global__ void k_dense_cast(int64_t total, const double* u64, const float* x32,
 }
 
 // Per column: ||v - bf16(v)|| and ||bf16(v)|| of the unit column and of the
-// column, in FP64 from the copies the screen multiplies, rounded up to FP32.
+// column, in FP64 from the copies the screen multiplies (one warp per column;
+// the FP64 sums' rounding, under d 2^-53 relative, is inside the 1e-12
+// allowance), rounded up to FP32.
 __global__ void k_dense_errnorm(int32_t d, int64_t n, const double* u64, const double* x64,
                                 const __nv_bfloat16* ub, const __nv_bfloat16* xb, float* ue, float* un, float* xe,
                                 float* xn) {
-  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int64_t j = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   if (j >= n) return;
   double eu = 0.0, nu = 0.0, ex = 0.0, nx = 0.0;
-  for (int32_t r = 0; r < d; ++r) {
+  for (int32_t r = lane; r < d; r += 32) {
     const int64_t a = j * d + r;
     const double bu = (double)__bfloat162float(ub[a]), bx = (double)__bfloat162float(xb[a]);
     const double du = u64[a] - bu, dx = x64[a] - bx;
     eu += du * du; nu += bu * bu; ex += dx * dx; nx += bx * bx;
   }
-  ue[j] = __double2float_ru(sqrt(eu) * (1.0 + 1e-12));
-  un[j] = __double2float_ru(sqrt(nu) * (1.0 + 1e-12));
-  xe[j] = __double2float_ru(sqrt(ex) * (1.0 + 1e-12));
-  xn[j] = __double2float_ru(sqrt(nx) * (1.0 + 1e-12));
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    eu += __shfl_xor_sync(0xffffffffu, eu, o);
+    nu += __shfl_xor_sync(0xffffffffu, nu, o);
+    ex += __shfl_xor_sync(0xffffffffu, ex, o);
+    nx += __shfl_xor_sync(0xffffffffu, nx, o);
+  }
+  if (lane == 0) {
+    ue[j] = __double2float_ru(sqrt(eu) * (1.0 + 1e-12));
+    un[j] = __double2float_ru(sqrt(nu) * (1.0 + 1e-12));
+    xe[j] = __double2float_ru(sqrt(ex) * (1.0 + 1e-12));
+    xn[j] = __double2float_ru(sqrt(nx) * (1.0 + 1e-12));
+  }
 }
 
 // A query's scan over the n references is split into segments of DSEG
@@ -274,42 +295,282 @@ __global__ void k_dense_overflow(int64_t nq, int cap, int32_t* count, int32_t* o
 
 // Exact FP64 value of each kept pair, in the reference's arithmetic; in the
 // plain mode the FP32 value of the slab instead.
+// Third cut, on the candidates of the BF16 screens: FP32 inner products of
+// the FP32 copies with a rigorous bound on their distance from the FP64 value
+// that k_dense_values computes.  A warp values up to 8 candidates of one
+// query at a time: each lane accumulates its share of the elements with FMA
+// (at most J roundings per product: J = 4 ceil(d / 128) when d is a multiple
+// of 4 and lane l takes the float4s l, l + 32, ...; else J = ceil(d / 32),
+// lane l taking elements l, l + 32, ...), and a five-level xor butterfly adds
+// the lanes (five more, the same sum on every lane).  With u = 2^-24 and
+// g(m) = m u / (1 - m u) (Higham's gamma; g53 the same for u = 2^-53):
+//   cosine:    s = fl32(sum u32_q u32_r) of the FP32 copies (|u32 - u| <= u |u|),
+//              |s - c| <= [g(J + 5) (1 + u)^2 + 2u + u^2 + g53(d + 1)] Nq Nr,
+//              c the FP64 sequential dot, N = ||b|| + ||u - b|| >= ||u|| (the
+//              BF16 copy's norm and error norm, both rounded up);
+//   euclidean: m = fl32(sum fl32(x_r - x_q)^2) of the FP32 inputs; every term is
+//              >= 0, so |m - num| <= (g(J + 7) + g53(d + 2)) / (1 - g(J + 7)) m.
+// Key = s (cosine) or -m (euclidean), larger is nearer.  The allowances get a
+// factor 1.01 and absolute terms (1e-15 cosine, 1e-36 euclidean) covering FP32
+// underflow and the keys that the FP64 distance rounds into a tie (1 - c: one
+// ulp of a value <= 2, at most 2^-52; sqrt(num): 2^-51 num relative, inside
+// the 1 % slack); lo and hi are formed with directed rounding.  T3 = the k-th
+// largest lo among the candidates is at most the k-th best exact key (k
+// candidates reach it), so every member of the exact top k, ties included,
+// has hi >= dense_cut(T3) and is kept.  A non-finite m keeps its pair.
+//
+// Candidate counts are very uneven (a query inside a cluster of near
+// duplicates has hundreds), so the products run over a flat list of items,
+// ceil(count / 8) per query that needs the cut (k_dense_refine_scan: their
+// exclusive offsets), dealt round-robin to a persistent grid of warps
+// (k_dense_refine_dot); a warp per query then makes the cut from the stored
+// values (k_dense_refine_cut).
+constexpr int RW = 8;        // warps per block of the cut
+constexpr int RG = 8;        // candidates per item of the products
+
+struct RefineArgs {
+  int method, k;
+  int32_t d;
+  int J;                       // FMA roundings per product in a lane (see above)
+  const float* rv;             // reference FP32 copies, d x n (u32 cosine, x32 euclidean)
+  const float* qv;             // query FP32 copies, column q0 + ql
+  const float *rn, *re;        // reference BF16 copy norm / error norm (unit columns)
+  const float *qn, *qe;        // query
+  int64_t q0, nq;
+  int cap;
+  int32_t* cand;               // [nq][cap], compacted in place
+  int32_t* count;              // [nq], updated
+  float* sv;                   // [nq][cap] scratch: the FP32 values
+  int64_t* off;                // [nq + 1] exclusive offsets of the items (0 for queries without the cut)
+};
+
+inline int refine_lane_terms(int32_t d) { return (d % 4 == 0) ? 4 * ((d + 127) / 128) : (d + 31) / 32; }
+
+__device__ __forceinline__ double gam(int m, double u) { return m * u / (1.0 - m * u); }
+
+__device__ __forceinline__ void refine_bounds(const RefineArgs& A, float s, int32_t r, float Nq, float C, float& lo,
+                                              float& hi) {
+  if (A.method == COSINE) {
+    const float Nr = __fadd_ru(A.rn[r], A.re[r]);
+    const float E = __fmaf_ru(C, __fmul_ru(Nq, Nr), 1e-15f);
+    lo = __fsub_rd(s, E);
+    hi = __fadd_ru(s, E);
+  } else if (isfinite(s)) {
+    const float E = __fmaf_ru(C, s, 1e-36f);
+    lo = __fsub_rd(-s, E);
+    hi = __fadd_ru(-s, E);
+  } else {
+    lo = -INFINITY;
+    hi = INFINITY;
+  }
+}
+
+__device__ __forceinline__ int refine_items(int c, int k) { return c > k ? (c + RG - 1) / RG : 0; }
+
+// One block of 1024 threads: off[ql] = the items of the queries before ql,
+// off[nq] = the total.
+__global__ void k_dense_refine_scan(RefineArgs A) {
+  __shared__ int64_t wsum[32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t per = (A.nq + blockDim.x - 1) / blockDim.x;
+  const int64_t b = tid * per, e = (b + per < A.nq) ? b + per : A.nq;
+  int64_t own = 0;
+  for (int64_t i = b; i < e; ++i) own += refine_items(A.count[i], A.k);
+  int64_t incl = own;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int64_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) wsum[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    int64_t w = (lane < (int)(blockDim.x >> 5)) ? wsum[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    wsum[lane] = w;                                  // inclusive over warps
+  }
+  __syncthreads();
+  int64_t run = incl - own + (warp ? wsum[warp - 1] : 0);
+  for (int64_t i = b; i < e; ++i) {
+    A.off[i] = run;
+    run += refine_items(A.count[i], A.k);
+  }
+  if (tid == (int)blockDim.x - 1) A.off[A.nq] = run;
+}
+
+__device__ __forceinline__ void refine_fma(bool cosine, float a, float b, float& acc) {
+  if (cosine) {
+    acc = __fmaf_rn(a, b, acc);
+  } else {
+    const float df = __fsub_rn(a, b);
+    acc = __fmaf_rn(df, df, acc);
+  }
+}
+
+__global__ void __launch_bounds__(128) k_dense_refine_dot(RefineArgs A) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t items = A.off[A.nq];
+  const int32_t d = A.d;
+  const bool cosine = (A.method == COSINE);
+  const bool vec = (d % 4 == 0);
+  for (int64_t it = w; it < items; it += warps) {
+    int64_t lo = 0, hi = A.nq;                       // off[lo] <= it < off[hi]
+    while (hi - lo > 1) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (__ldg(A.off + mid) <= it) lo = mid;
+      else hi = mid;
+    }
+    const int64_t ql = lo;
+    const int t0 = (int)(it - __ldg(A.off + ql)) * RG;
+    const int n = min(RG, A.count[ql] - t0);
+    const int32_t* cp = A.cand + ql * A.cap + t0;
+    const int32_t mine = lane < n ? cp[lane] : 0;
+    const float* qv = A.qv + (A.q0 + ql) * d;
+    const float* row[RG];
+#pragma unroll
+    for (int j = 0; j < RG; ++j) row[j] = A.rv + (int64_t)__shfl_sync(0xffffffffu, mine, j < n ? j : n - 1) * d;
+    float acc[RG];
+#pragma unroll
+    for (int j = 0; j < RG; ++j) acc[j] = 0.f;
+    if (vec) {
+      const int32_t d4 = d >> 2;
+      for (int32_t f0 = 0; f0 < d4; f0 += 64) {
+        float4 qa[2], ra[2][RG];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int32_t f = f0 + lane + 32 * h;
+          if (f < d4) {
+            qa[h] = __ldg(reinterpret_cast<const float4*>(qv) + f);
+#pragma unroll
+            for (int j = 0; j < RG; ++j) ra[h][j] = __ldg(reinterpret_cast<const float4*>(row[j]) + f);
+          }
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          if (f0 + lane + 32 * h < d4) {
+#pragma unroll
+            for (int j = 0; j < RG; ++j) {
+              refine_fma(cosine, ra[h][j].x, qa[h].x, acc[j]);
+              refine_fma(cosine, ra[h][j].y, qa[h].y, acc[j]);
+              refine_fma(cosine, ra[h][j].z, qa[h].z, acc[j]);
+              refine_fma(cosine, ra[h][j].w, qa[h].w, acc[j]);
+            }
+          }
+        }
+      }
+    } else {
+      for (int32_t e = lane; e < d; e += 32) {
+        const float b = __ldg(qv + e);
+#pragma unroll
+        for (int j = 0; j < RG; ++j) refine_fma(cosine, __ldg(row[j] + e), b, acc[j]);
+      }
+    }
+    float out = 0.f;
+#pragma unroll
+    for (int j = 0; j < RG; ++j) {
+#pragma unroll
+      for (int o = 16; o; o >>= 1) acc[j] = __fadd_rn(acc[j], __shfl_xor_sync(0xffffffffu, acc[j], o));
+      if (lane == j) out = acc[j];
+    }
+    if (lane < n) A.sv[ql * A.cap + t0 + lane] = out;
+  }
+}
+
+__global__ void k_dense_refine_cut(RefineArgs A) {
+  extern __shared__ float rl[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t ql = blockIdx.x * (int64_t)RW + warp;
+  if (ql >= A.nq) return;
+  const int c = A.count[ql], K = A.k;
+  if (c <= K) return;
+  const int64_t q = A.q0 + ql;
+  const int32_t d = A.d;
+  int32_t* cand = A.cand + ql * (int64_t)A.cap;
+  const float* sv = A.sv + ql * (int64_t)A.cap;
+  float* lst = rl + warp * K;
+  const int J = A.J;
+  const double u = 5.9604644775390625e-8;             // 2^-24
+  const double u53 = 1.1102230246251565e-16;          // 2^-53
+  double Cd;
+  if (A.method == COSINE) Cd = gam(J + 5, u) * (1.0 + u) * (1.0 + u) + 2.0 * u + u * u + gam(d + 1, u53);
+  else Cd = (gam(J + 7, u) + gam(d + 2, u53)) / (1.0 - gam(J + 7, u));
+  const float C = __double2float_ru(Cd * 1.01 * (1.0 + 1e-12));
+  const float Nq = (A.method == COSINE) ? __fadd_ru(A.qn[q], A.qe[q]) : 0.f;
+  int n = 0;
+  for (int t0 = 0; t0 < c; t0 += 32) {
+    const int t = t0 + lane;
+    float lo = -INFINITY, hi;
+    if (t < c) refine_bounds(A, sv[t], cand[t], Nq, C, lo, hi);
+    const unsigned m = __ballot_sync(0xffffffffu, t < c && (n < K || lo > lst[K - 1]));
+    if (m) warp_insert_desc(lst, K, n, m, lo, lane);
+  }
+  const float cut = dense_cut((n == K) ? lst[K - 1] : -INFINITY);
+  int kept = 0;
+  for (int t0 = 0; t0 < c; t0 += 32) {
+    const int t = t0 + lane;
+    bool keep = false;
+    int32_t r = 0;
+    if (t < c) {
+      r = cand[t];
+      float lo, hi;
+      refine_bounds(A, sv[t], r, Nq, C, lo, hi);
+      keep = hi >= cut;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, keep);    // every lane has read slot t first
+    if (keep) cand[kept + __popc(m & ((1u << lane) - 1u))] = r;
+    kept += __popc(m);
+    __syncwarp();
+  }
+  if (lane == 0) A.count[ql] = kept;
+}
+
+// Exact values of the candidates, one warp per query (lane t values
+// candidates t, t + 32, ...).
 __global__ void k_dense_values(int method, int mode, int32_t d, const double* x64, const double* u64,
                                const double* qx64, const double* qu64, const float* S, int64_t ldS,
                                const float* norm2, const float* qnorm2, const int32_t* cand,
                                const int32_t* count, int cap, int64_t q0, int64_t nq, double* out) {
-  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (s >= nq * cap) return;
-  const int64_t ql = s / cap, t = s % cap;
-  if (t >= count[ql]) return;
-  const int64_t q = q0 + ql, r = cand[s];
-  if (mode == 1) {
-    const float sv = S[ql * ldS + r];
-    out[s] = (method == COSINE) ? (double)(1.f - fminf(1.f, fmaxf(-1.f, sv)))
-                                : (double)sqrtf(fmaxf(0.f, qnorm2[q] + norm2[r] - 2.f * sv));
-    return;
-  }
-  if (method == COSINE) {
-    // unit_dot / unit_cosine (src/sparseDist.cpp:287-331), reference column first
-    const double* a = u64 + r * d;
-    const double* b = qu64 + q * d;
-    double acc = 0.0;
-    for (int32_t k = 0; k < d; ++k) acc = __dadd_rn(acc, __dmul_rn(a[k], b[k]));
-    double c = acc;
-    if (!(c == c)) c = 0.0;
-    else if (c > 1.0) c = 1.0;
-    else if (c < -1.0) c = -1.0;
-    out[s] = __dsub_rn(1.0, c);
-  } else {
-    // fastEuclidean2's pair loop with every row stored (src/sparseDist.cpp:855-871)
-    const double* a = x64 + r * d;
-    const double* b = qx64 + q * d;
-    double num = 0.0;
-    for (int32_t k = 0; k < d; ++k) {
-      const double diff = __dsub_rn(a[k], b[k]);
-      num = __dadd_rn(num, __dmul_rn(diff, diff));
+  const int64_t ql = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (ql >= nq) return;
+  const int lane = threadIdx.x & 31;
+  const int c = count[ql];
+  const int64_t q = q0 + ql;
+  for (int t = lane; t < c; t += 32) {
+    const int64_t s = ql * cap + t, r = cand[s];
+    if (mode == 1) {
+      const float sv = S[ql * ldS + r];
+      out[s] = (method == COSINE) ? (double)(1.f - fminf(1.f, fmaxf(-1.f, sv)))
+                                  : (double)sqrtf(fmaxf(0.f, qnorm2[q] + norm2[r] - 2.f * sv));
+      continue;
     }
-    out[s] = sqrt(num);
+    if (method == COSINE) {
+      // unit_dot / unit_cosine (src/sparseDist.cpp:287-331), reference column first
+      const double* a = u64 + r * d;
+      const double* b = qu64 + q * d;
+      double acc = 0.0;
+      for (int32_t k = 0; k < d; ++k) acc = __dadd_rn(acc, __dmul_rn(a[k], b[k]));
+      double cv = acc;
+      if (!(cv == cv)) cv = 0.0;
+      else if (cv > 1.0) cv = 1.0;
+      else if (cv < -1.0) cv = -1.0;
+      out[s] = __dsub_rn(1.0, cv);
+    } else {
+      // fastEuclidean2's pair loop with every row stored (src/sparseDist.cpp:855-871)
+      const double* a = x64 + r * d;
+      const double* b = qx64 + q * d;
+      double num = 0.0;
+      for (int32_t k = 0; k < d; ++k) {
+        const double diff = __dsub_rn(a[k], b[k]);
+        num = __dadd_rn(num, __dmul_rn(diff, diff));
+      }
+      out[s] = sqrt(num);
+    }
   }
 }
 
@@ -379,7 +640,7 @@ int dense_build(sdg_ctx* ctx, const float* X, int32_t d, int64_t n, bool async, 
   chk(alloc(&D->x32, tot * 4)); chk(alloc(&D->u32, tot * 4));
   chk(alloc(&D->xb, tot * 2)); chk(alloc(&D->ub, tot * 2));
   chk(alloc(&D->norm2, npad * 4)); chk(alloc(&D->scale, n * 8));
-  chk(alloc(&D->empty, npad)); chk(alloc(&D->pview, (n + 1) * 8));
+  chk(alloc(&D->empty, npad));
   chk(alloc(&D->ue, npad * 4)); chk(alloc(&D->un, npad * 4));
   chk(alloc(&D->xe, npad * 4)); chk(alloc(&D->xn, npad * 4));
   chk(alloc(&err, sizeof(int)));
@@ -394,14 +655,11 @@ int dense_build(sdg_ctx* ctx, const float* X, int32_t d, int64_t n, bool async, 
   chk(cudaMemsetAsync(err, 0, sizeof(int), s));
   chk(cudaMemcpyAsync(D->x32, X, tot * 4, cudaMemcpyDefault, s));
   if (e == cudaSuccess) {
-    k_dense_prep<<<blocks_for(n + 1, 128), 128, 0, s>>>(d, n, D->x32, D->x64, D->norm2, D->empty,
-                                                        D->pview, err);
-    DevCsc M;
-    M.nrow = d; M.ncol = (int32_t)n; M.p = D->pview; M.i = nullptr; M.x = D->x64;
-    launch_unit_csc(M, D->u64, D->scale, err, s);
+    k_dense_prep<<<blocks_for(n * 32, 256), 256, 0, s>>>(d, n, D->x32, D->x64, D->norm2, D->empty, err);
+    launch_unit_dense(d, n, D->x64, D->u64, D->scale, err, s);
     k_dense_cast<<<152 * 16, 256, 0, s>>>((int64_t)tot, D->u64, D->x32, D->u32, D->ub, D->xb);
-    k_dense_errnorm<<<blocks_for(n, 128), 128, 0, s>>>(d, n, D->u64, D->x64, D->ub, D->xb, D->ue, D->un, D->xe,
-                                                        D->xn);
+    k_dense_errnorm<<<blocks_for(n * 32, 256), 256, 0, s>>>(d, n, D->u64, D->x64, D->ub, D->xb, D->ue, D->un,
+                                                            D->xe, D->xn);
   }
   if (D->dpad == d) {
     D->ubp = D->ub;
@@ -506,6 +764,7 @@ int dense_search(sdg_ctx* ctx, const sdg_dense* Q, int64_t q0, int64_t nq, const
   float* S = nullptr;
   float *segtop = nullptr, *cut = nullptr;
   int32_t *cand = nullptr, *count = nullptr, *over = nullptr, *o_idx = idx;
+  int64_t* off = nullptr;
   double *vals = nullptr, *o_val = dist_out, *row = nullptr;
   if (!fused) {
     DK(cudaMallocAsync(&S, sizeof(float) * (size_t)(chunk * ldS), s));
@@ -516,6 +775,7 @@ int dense_search(sdg_ctx* ctx, const sdg_dense* Q, int64_t q0, int64_t nq, const
   DK(cudaMallocAsync(&count, sizeof(int32_t) * (size_t)chunk, s));
   DK(cudaMallocAsync(&over, sizeof(int32_t) * (size_t)chunk, s));
   DK(cudaMallocAsync(&vals, sizeof(double) * (size_t)(chunk * cap), s));
+  if (smode == 0) DK(cudaMallocAsync(&off, sizeof(int64_t) * (size_t)(chunk + 1), s));
   if (!device_out) {
     DK(cudaMallocAsync(&o_idx, sizeof(int32_t) * (size_t)(nq * k), s));
     DK(cudaMallocAsync(&o_val, sizeof(double) * (size_t)(nq * k), s));
@@ -567,9 +827,29 @@ int dense_search(sdg_ctx* ctx, const sdg_dense* Q, int64_t q0, int64_t nq, const
     k_dense_keep<<<grid, DSEL_WARPS * 32, 0, s>>>(A);
     k_dense_overflow<<<blocks_for(nb, 256), 256, 0, s>>>(nb, cap, count, over);
     }
-    k_dense_values<<<blocks_for(nb * cap, 128), 128, 0, s>>>(method, smode, D->d, D->x64, D->u64, Q->x64, Q->u64,
-                                                              S, ldS, D->norm2, Q->norm2, cand, count, cap, c0,
-                                                              nb, vals);
+    if (smode == 0) {
+      RefineArgs R;
+      R.method = method; R.k = k; R.d = D->d; R.J = refine_lane_terms(D->d);
+      R.rv = (method == COSINE) ? D->u32 : D->x32;
+      R.qv = (method == COSINE) ? Q->u32 : Q->x32;
+      R.rn = D->un; R.re = D->ue; R.qn = Q->un; R.qe = Q->ue;
+      R.q0 = c0; R.nq = nb; R.cap = cap; R.cand = cand; R.count = count;
+      R.sv = reinterpret_cast<float*>(vals);          // free until the exact values are written
+      R.off = off;
+      k_dense_refine_scan<<<1, 1024, 0, s>>>(R);
+      static int dot_blocks = 0;                      // persistent: every block resident at once
+      if (!dot_blocks) {
+        int per_sm = 0, sms = 0;
+        DK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dense_refine_dot, 128, 0));
+        DK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, D->device));
+        dot_blocks = std::max(1, per_sm * sms);
+      }
+      k_dense_refine_dot<<<dot_blocks, 128, 0, s>>>(R);
+      const size_t rsm = sizeof(float) * (size_t)RW * k;   // <= 32 KB (k <= kMaxK here)
+      k_dense_refine_cut<<<blocks_for(nb, RW), RW * 32, rsm, s>>>(R);
+    }
+    k_dense_values<<<blocks_for(nb, 8), 256, 0, s>>>(method, smode, D->d, D->x64, D->u64, Q->x64, Q->u64, S, ldS,
+                                                     D->norm2, Q->norm2, cand, count, cap, c0, nb, vals);
     SelectArgs sa;
     sa.vals = vals; sa.seg_stride = cap; sa.elem_stride = 1; sa.nseg = nb;
     sa.cand = cand; sa.cand_count = count; sa.cand_ld = cap;
@@ -610,11 +890,16 @@ int dense_search(sdg_ctx* ctx, const sdg_dense* Q, int64_t q0, int64_t nq, const
   if (cut) DK(cudaFreeAsync(cut, s));
   DK(cudaFreeAsync(cand, s)); DK(cudaFreeAsync(count, s));
   DK(cudaFreeAsync(over, s)); DK(cudaFreeAsync(vals, s));
+  if (off) DK(cudaFreeAsync(off, s));
   if (row) DK(cudaFreeAsync(row, s));
   if (!device_out) { DK(cudaFreeAsync(o_idx, s)); DK(cudaFreeAsync(o_val, s)); }
   DK(cudaStreamSynchronize(s));
   ctx_add_overflow(ctx, (int64_t)overflow.size());
-  ctx_stats_add(ctx, 3, fused ? 4 : 7);
+  // kernels per chunk: the screen (fused: key init, weights, k_dense_tc, merge;
+  // slab: the GEMM, segtop, thresh, keep, overflow), the FP32 cut, the exact
+  // values and the selection; two more per overflowing query
+  const int64_t chunks = (nq + chunk - 1) / chunk;
+  ctx_stats_add(ctx, 3, chunks * ((fused ? 4 : 5) + (smode == 0 ? 3 : 0) + 2) + 2 * (int64_t)overflow.size());
   return SDG_OK;
 }
 
@@ -641,6 +926,7 @@ int dense_query(sdg_ctx* ctx, const sdg_dense* D, const float* Q, int32_t d, int
   int st = dense_build(ctx, Q, d, nq, true, false, &QD);
   if (st != SDG_OK) return st;
   st = dense_search(ctx, QD, 0, nq, D, false, method, k, mode, idx, dist_out, device_out, k_eff, flags);
+  if (st == SDG_OK) ctx_stats_add(ctx, 3, 4);        // the query block's prep, unit columns, cast, error norms
   sdg_dense_free(QD);
   return st;
 }
@@ -657,7 +943,7 @@ SDG_API int sdg_dense_free(sdg_dense* D) {
   if (!D) return SDG_OK;
   cudaSetDevice(D->device);
   void* bufs[] = {(void*)D->x64, (void*)D->u64, (void*)D->x32, (void*)D->u32, (void*)D->xb, (void*)D->ub,
-                  (void*)D->norm2, (void*)D->scale, (void*)D->empty, (void*)D->pview,
+                  (void*)D->norm2, (void*)D->scale, (void*)D->empty,
                   (void*)D->ue, (void*)D->un, (void*)D->xe, (void*)D->xn,
                   (void*)(D->ubp != D->ub ? D->ubp : nullptr), (void*)(D->xbp != D->xb ? D->xbp : nullptr)};
   if (D->async) {

@@ -34,7 +34,6 @@ struct sdg_dense {
   float* xn = nullptr;
   double* scale = nullptr;        // unit_csc scale (0 = empty column)
   uint8_t* empty = nullptr;       // padded to npad with 1
-  int64_t* pview = nullptr;       // column offsets j * d, for the CSC kernels
   int64_t n_empty = 0;
   cublasHandle_t blas = nullptr;  // slab (mode 2) and plain (mode 1) GEMMs; resident references only
   std::mutex blas_mu;             // one caller at a time on `blas` (it is bound to a stream)

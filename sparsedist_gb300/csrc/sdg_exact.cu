@@ -95,6 +95,84 @@ __global__ void k_unit_csc_warp(DevCsc M, double* uval, double* scale_out, int* 
     uval[a] = (scale == 0.0) ? 0.0 : ((M.x[a]) / scale) / sq;
 }
 
+// unit_csc of dense columns (d values each, zeros included and skipped as
+// above): the same recurrence, ratios and branches, with the serial part
+// spread over columns instead of run by one lane.  A warp owns 32 columns;
+// for each 32-row chunk it computes every column's ratios and flags with the
+// lanes over the rows (prefix maximum of the magnitudes on their bit
+// patterns, which order non-negative doubles as integers), parks them in
+// shared memory, and then lane c runs column c's sum-of-squares chain over
+// the chunk in the reference's order.  The FP64 pipe issues one instruction
+// for cpw columns' chain steps instead of one per step; cpw (columns per
+// warp, <= 32) trades that against the number of warps for small n.
+constexpr int UD_WARPS = 2;
+
+__global__ void __launch_bounds__(UD_WARPS * 32) k_unit_dense(int32_t d, int64_t n, int cpw, const double* x,
+                                                              double* uval, double* scale_out, int* err) {
+  __shared__ double s_r[UD_WARPS][32][33];
+  __shared__ uint8_t s_f[UD_WARPS][32][33];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t j0 = ((int64_t)blockIdx.x * UD_WARPS + warp) * cpw;
+  if (j0 >= n) return;
+  const int nc = (int)((n - j0) < cpw ? (n - j0) : cpw);
+  long long scale_bits = 0;        // lane c: column c's running maximum magnitude (bits)
+  double ssq = 1.0;                // lane c: column c's sum of squares
+  bool bad = false;
+  for (int32_t k0 = 0; k0 < d; k0 += 32) {
+    const int kn = (d - k0) < 32 ? (d - k0) : 32;
+    for (int c = 0; c < nc; ++c) {
+      long long ab = 0;
+      if (lane < kn) {
+        const long long b = __double_as_longlong(x[(j0 + c) * d + k0 + lane]);
+        ab = b & 0x7fffffffffffffffLL;
+        if ((ab >> 52) == 0x7ff) bad = true;        // reported for the whole call below
+      }
+      long long incl = ab;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const long long y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl = incl > y ? incl : y;
+      }
+      long long prev = __shfl_up_sync(0xffffffffu, incl, 1);
+      if (lane == 0) prev = 0;
+      const long long sc = __shfl_sync(0xffffffffu, scale_bits, c);
+      prev = prev > sc ? prev : sc;
+      uint8_t flag = 0;              // 0: skip (zero), 1: new maximum, 2: below maximum
+      double r = 0.0;
+      if (ab != 0) {
+        const double av = __longlong_as_double(ab), pv = __longlong_as_double(prev);
+        if (prev < ab) { flag = 1; r = pv / av; }
+        else { flag = 2; r = av / pv; }
+      }
+      s_r[warp][lane][c] = r;
+      s_f[warp][lane][c] = flag;
+      const long long tot = __shfl_sync(0xffffffffu, incl, 31);
+      if (lane == c && tot > scale_bits) scale_bits = tot;
+    }
+    __syncwarp();
+    if (lane < nc) {
+      for (int t = 0; t < kn; ++t) {
+        const uint8_t f = s_f[warp][t][lane];
+        const double rr = s_r[warp][t][lane];
+        if (f == 1) ssq = dadd(1.0, dmul(dmul(ssq, rr), rr));
+        else if (f == 2) ssq = dadd(ssq, dmul(rr, rr));
+      }
+    }
+    __syncwarp();
+  }
+  if (__any_sync(0xffffffffu, bad)) { if (lane == 0) atomicOr(err, 1); return; }
+  const double sq = sqrt(ssq);
+  if (lane < nc) scale_out[j0 + lane] = __longlong_as_double(scale_bits);
+  for (int c = 0; c < nc; ++c) {
+    const double scale = __longlong_as_double(__shfl_sync(0xffffffffu, scale_bits, c));
+    const double q = __shfl_sync(0xffffffffu, sq, c);
+    for (int32_t a = lane; a < d; a += 32) {
+      const int64_t at = (j0 + c) * d + a;
+      uval[at] = (scale == 0.0) ? 0.0 : (x[at] / scale) / q;
+    }
+  }
+}
+
 __global__ void k_moments(DevCsc M, double* sum, double* sumsq) {
   const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (j >= M.ncol) return;
@@ -1030,6 +1108,14 @@ void launch_col_empty(const DevCsc& M, uint8_t* empty, cudaStream_t s) {
 }
 void launch_unit_csc(const DevCsc& M, double* uval, double* scale, int* err, cudaStream_t s) {
   if (M.ncol > 0) k_unit_csc_warp<<<blocks_for(M.ncol, 8), 256, 0, s>>>(M, uval, scale, err);
+}
+void launch_unit_dense(int32_t d, int64_t n, const double* x, double* uval, double* scale, int* err,
+                       cudaStream_t s) {
+  if (n <= 0) return;
+  const int cpw = (n >= (int64_t)152 * 64 * 32) ? 32 : 8;   // 32 once every SM has 64 warps' worth
+  const int64_t per_block = (int64_t)cpw * UD_WARPS;
+  k_unit_dense<<<(unsigned)((n + per_block - 1) / per_block), UD_WARPS * 32, 0, s>>>(d, n, cpw, x, uval, scale,
+                                                                                    err);
 }
 void launch_moments(const DevCsc& M, double* sum, double* sumsq, cudaStream_t s) {
   if (M.ncol > 0) k_moments<<<blocks_for(M.ncol, 128), 128, 0, s>>>(M, sum, sumsq);

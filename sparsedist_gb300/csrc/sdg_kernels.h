@@ -29,6 +29,11 @@ void ctx_stats_reset(sdg_ctx* c);
 // ---- sdg_exact.cu: per-column preparation and exact FP64 pair values --------
 void launch_col_empty(const DevCsc& M, uint8_t* empty, cudaStream_t s);
 void launch_unit_csc(const DevCsc& M, double* uval, double* scale, int* err, cudaStream_t s);
+// unit_csc of n dense columns of d values (column-major, zeros included and
+// skipped by the recurrence): the same values as launch_unit_csc on the
+// all-entries CSC view, bit for bit
+void launch_unit_dense(int32_t d, int64_t n, const double* x, double* uval, double* scale, int* err,
+                       cudaStream_t s);
 void launch_moments(const DevCsc& M, double* sum, double* sumsq, cudaStream_t s);
 void launch_check_js(const double* x, int64_t nnz, int* err, cudaStream_t s);
 // xl[a] = xlogx(x[a]) for every stored value (js pair values reuse them)

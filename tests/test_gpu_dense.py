@@ -135,6 +135,88 @@ def test_d256_block_equals_oracle(method, code, mode):
     torch.cuda.synchronize()
 
 
+@pytest.mark.parametrize("mode", [0, 2, 3])
+@pytest.mark.parametrize("method,code", [("cosine", 1), ("euclidean", 2)])
+def test_fp32_cut_near_ties_equal_oracle(method, code, mode):
+    """Neighbours that the FP32 third cut cannot tell apart: around each of 12
+    base columns (d = 256), 400 references at relative offsets from 2^-25
+    (a few FP32 ulps, most elements unchanged) to 2^-12 and 3 exact copies, so
+    the k-th neighbour of a base column sits among references closer than the
+    cut's FP32 allowance, with exact ties (the copies) broken by index.  The base columns are queries of the resident
+    matrix; idx and distances bit for bit against the oracle, and the pairs
+    valued exactly stay above k per query (the cut kept the near ties)."""
+    import ctypes as C
+    import torch
+    from sparsedist_gb300 import _lib
+    rng = np.random.default_rng(17)
+    d, nbase, per, k = 256, 12, 400, 20
+    base = rng.standard_normal((nbase, d)).astype(np.float32)
+    cols = [base]
+    for b in range(nbase):
+        scale = np.exp2(rng.uniform(-25, -12, per))[:, None]
+        cols.append((base[b] * (1 + scale * rng.standard_normal((per, d)))).astype(np.float32))
+        cols.append(np.repeat(base[b][None, :], 3, axis=0))
+    cols.append(rng.standard_normal((2000, d)).astype(np.float32))
+    X = torch.from_numpy(np.ascontiguousarray(np.concatenate(cols))).cuda()
+    n = X.shape[0]
+    ctx = _lib.Context()
+    h = C.c_void_p()
+    _lib.check(ctx.lib.sdg_dense_upload(ctx.handle, X.data_ptr(), d, n, C.byref(h)))
+    got = dense_knn(ctx, h, 0, nbase, code, k, mode)
+    exact_pairs = ctx.stats()["pairs_exact"]
+    ctx.lib.sdg_dense_free(h)
+    A = as_csc(X)
+    wi, wd, _ = OracleBackend().knn(A[:, 0:nbase], A, k=k + 1, method=method)
+    for t in range(nbase):
+        keep = wi[t] != t + 1
+        assert same_bits(got[0][t], wi[t][keep][:k]), t
+        assert same_bits(got[1][t], wd[t][keep][:k]), t
+    assert exact_pairs >= nbase * k
+    torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("mode", [0, 2])
+def test_unit_columns_of_wide_ragged_columns_equal_oracle(mode):
+    """The dense unit columns (unit_csc's recurrence, 8 and 32 columns per
+    warp): d = 45 (a ragged last 32-row chunk), values spread over 2^-40 ..
+    2^40 with 30 % exact zeros and some negative zeros, an all-zero column and
+    a one-entry column; then 320,000 columns of d = 8 (the 32-columns-per-warp
+    form).  Cosine idx and distances bit for bit against the oracle."""
+    import ctypes as C
+    import torch
+    from sparsedist_gb300 import _lib
+    rng = np.random.default_rng(29)
+    cases = []
+    d, n = 45, 3000
+    X = rng.standard_normal((n, d)) * np.exp2(rng.integers(-40, 40, (n, d)))
+    X[rng.random((n, d)) < 0.3] = 0.0
+    X[rng.random((n, d)) < 0.02] = -0.0
+    X[17] = 0.0
+    X[18] = 0.0
+    X[18, 44] = 3.5
+    cases.append((X.astype(np.float32), 0, 300, 10))
+    d, n = 8, 320000
+    cases.append((rng.standard_normal((n, d)).astype(np.float32), 1000, 64, 5))
+    for Xh, q0, nq, k in cases:
+        n, d = Xh.shape
+        X = torch.from_numpy(np.ascontiguousarray(Xh)).cuda()
+        ctx = _lib.Context()
+        h = C.c_void_p()
+        _lib.check(ctx.lib.sdg_dense_upload(ctx.handle, X.data_ptr(), d, n, C.byref(h)))
+        got = dense_knn(ctx, h, q0, nq, 1, k, mode)
+        ctx.lib.sdg_dense_free(h)
+        A = as_csc(X)
+        wi, wd, _ = OracleBackend().knn(A[:, q0:q0 + nq], A, k=k + 1, method="cosine")
+        for t in range(nq):
+            if q0 + t == 17:
+                assert np.all(got[0][t] == np.iinfo(np.int32).min)
+                continue
+            keep = wi[t] != q0 + t + 1
+            assert same_bits(got[0][t], wi[t][keep][:k]), t
+            assert same_bits(got[1][t], wd[t][keep][:k]), t
+    torch.cuda.synchronize()
+
+
 @pytest.mark.parametrize("k", [20, 50, 64])
 @pytest.mark.parametrize("mode", [0, 2, 3])
 @pytest.mark.parametrize("method,code", [("cosine", 1), ("euclidean", 2)])

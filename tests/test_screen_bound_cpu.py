@@ -331,3 +331,117 @@ def test_dense_bf16_pair_bound():
             vq, vr = vq / np.linalg.norm(vq), vr / np.linalg.norm(vr)
         worst = max(worst, _dense_case(vq, vr, rng, unit))
     assert worst < 1.0
+
+
+# The dense path's third cut (sdg_dense.cu, k_dense_refine_dot): a warp
+# accumulates lane l's share of the FP32 copies with FMA (the float4s l,
+# l + 32, ... when d is a multiple of 4, else the elements l, l + 32, ...), a
+# five-level xor butterfly adds the lanes, and the result must lie
+# within C Nq Nr + 1e-15 (cosine; N = ||bf16 copy|| + ||copy error|| rounded
+# up) or C m + 1e-36 (euclidean, m the FP32 sum of squares) of the FP64 value
+# the exact stage computes (sequential, unfused, ascending rows).
+
+def _gam(m, u):
+    return m * u / (1.0 - m * u)
+
+
+def _lane_elements(d):
+    """Each lane's elements in the kernel's order, and J (the longest chain)."""
+    if d % 4 == 0:
+        lanes = [[4 * f + c for f in range(lane, d // 4, 32) for c in range(4)] for lane in range(32)]
+        J = 4 * ((d + 127) // 128)
+    else:
+        lanes = [list(range(lane, d, 32)) for lane in range(32)]
+        J = (d + 31) // 32
+    assert max(len(e) for e in lanes) <= J and sorted(sum(lanes, [])) == list(range(d))
+    return lanes, J
+
+
+def _refine_constant(cosine, d):
+    u, u53, J = 2.0 ** -24, 2.0 ** -53, _lane_elements(d)[1]
+    if cosine:
+        c = _gam(J + 5, u) * (1 + u) ** 2 + 2 * u + u * u + _gam(d + 1, u53)
+    else:
+        c = (_gam(J + 7, u) + _gam(d + 2, u53)) / (1 - _gam(J + 7, u))
+    return ru32(c * 1.01 * (1 + 1e-12))
+
+
+def _fma32(a, b, c):
+    # a * b is exact in FP64 for FP32 a, b; one more FP64 rounding before the
+    # FP32 one (at most 2^-29 of an FP32 ulp beyond a single rounding)
+    return np.float32(np.float64(a) * np.float64(b) + np.float64(c))
+
+
+def _warp_dot(a32, b32, square_diff):
+    d = len(a32)
+    lanes = np.zeros(32, np.float32)
+    for lane, elems in enumerate(_lane_elements(d)[0]):
+        acc = np.float32(0)
+        for e in elems:
+            if square_diff:
+                df = np.float32(a32[e] - b32[e])
+                acc = _fma32(df, df, acc)
+            else:
+                acc = _fma32(a32[e], b32[e], acc)
+        lanes[lane] = acc
+    for o in (16, 8, 4, 2, 1):
+        lanes = (lanes + lanes[np.arange(32) ^ o]).astype(np.float32)
+    assert np.all(lanes == lanes[0])               # the butterfly leaves one value on every lane
+    return float(lanes[0])
+
+
+def _seq64(a, b, square_diff):
+    acc = 0.0
+    for x, y in zip(a, b):
+        if square_diff:
+            t = x - y
+            acc = acc + t * t
+        else:
+            acc = acc + x * y
+    return acc
+
+
+def _refine_cosine_case(vq, vr):
+    uq, ur = vq / np.linalg.norm(vq), vr / np.linalg.norm(vr)
+    Ns = []
+    for u in (uq, ur):
+        b = _bf16(u)
+        Ns.append(ru32(ru32(np.linalg.norm(b) * (1 + 1e-12)) + ru32(np.linalg.norm(u - b) * (1 + 1e-12))))
+    s = _warp_dot(ur.astype(np.float32), uq.astype(np.float32), False)
+    c = _seq64(ur, uq, False)
+    bound = _refine_constant(True, len(vq)) * Ns[0] * Ns[1] + 1e-15
+    assert abs(s - c) <= bound, (abs(s - c), bound)
+    return abs(s - c) / bound
+
+
+def _refine_euclid_case(xq, xr):
+    xq, xr = xq.astype(np.float32), xr.astype(np.float32)
+    m = _warp_dot(xr, xq, True)
+    num = _seq64(xr.astype(np.float64), xq.astype(np.float64), True)
+    bound = _refine_constant(False, len(xq)) * m + 1e-36
+    assert abs(m - num) <= bound, (abs(m - num), bound)
+    return abs(m - num) / bound
+
+
+def test_dense_fp32_cut_bound():
+    rng = np.random.default_rng(73)
+    worst = 0.0
+    for trial in range(60):
+        d = int(rng.choice([1, 5, 31, 33, 64, 100, 132, 256, 260]))
+        kind = trial % 5
+        vq = rng.standard_normal(d)
+        if kind == 0:
+            vr = rng.standard_normal(d)
+        elif kind == 1:
+            vr = vq + 1e-7 * rng.standard_normal(d)                # near duplicate
+        elif kind == 2:
+            vr = vq.copy()                                         # duplicate
+        elif kind == 3:
+            vq = np.abs(vq) + 1.0                                  # every product positive and alike:
+            vr = np.full(d, 1.0) + 1e-3 * rng.standard_normal(d)   # the roundings pile up one way
+        else:
+            vq = vq * np.exp2(rng.integers(-30, 30, d))            # wide exponent range
+            vr = vq * (1 + 1e-4 * rng.standard_normal(d))
+        worst = max(worst, _refine_cosine_case(vq, vr))
+        worst = max(worst, _refine_euclid_case(vq * 3.0, vr * 3.0))
+    assert worst < 1.0
