@@ -297,7 +297,7 @@ __global__ void k_dense_overflow(int64_t nq, int cap, int32_t* count, int32_t* o
 // plain mode the FP32 value of the slab instead.
 // Third cut, on the candidates of the BF16 screens: FP32 inner products of
 // the FP32 copies with a rigorous bound on their distance from the FP64 value
-// that k_dense_values computes.  A warp values up to 8 candidates of one
+// that k_dense_values_flat computes.  A warp values up to 8 candidates of one
 // query at a time: each lane accumulates its share of the elements with FMA
 // (at most J roundings per product: J = 4 ceil(d / 128) when d is a multiple
 // of 4 and lane l takes the float4s l, l + 32, ...; else J = ceil(d / 32),
@@ -342,6 +342,7 @@ struct RefineArgs {
   int32_t* count;              // [nq], updated
   float* sv;                   // [nq][cap] scratch: the FP32 values
   int64_t* off;                // [nq + 1] exclusive offsets of the items (0 for queries without the cut)
+  int unit;                    // k_dense_refine_scan: RG (the cut's items) or 1 (every candidate)
 };
 
 inline int refine_lane_terms(int32_t d) { return (d % 4 == 0) ? 4 * ((d + 127) / 128) : (d + 31) / 32; }
@@ -365,17 +366,20 @@ __device__ __forceinline__ void refine_bounds(const RefineArgs& A, float s, int3
   }
 }
 
-__device__ __forceinline__ int refine_items(int c, int k) { return c > k ? (c + RG - 1) / RG : 0; }
+__device__ __forceinline__ int refine_items(int c, int k, int unit) {
+  return unit == 1 ? c : (c > k ? (c + unit - 1) / unit : 0);
+}
 
 // One block of 1024 threads: off[ql] = the items of the queries before ql,
-// off[nq] = the total.
+// off[nq] = the total (unit RG: ceil(count / RG) items for each query with
+// more than k candidates; unit 1: every candidate).
 __global__ void k_dense_refine_scan(RefineArgs A) {
   __shared__ int64_t wsum[32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t per = (A.nq + blockDim.x - 1) / blockDim.x;
   const int64_t b = tid * per, e = (b + per < A.nq) ? b + per : A.nq;
   int64_t own = 0;
-  for (int64_t i = b; i < e; ++i) own += refine_items(A.count[i], A.k);
+  for (int64_t i = b; i < e; ++i) own += refine_items(A.count[i], A.k, A.unit);
   int64_t incl = own;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -397,7 +401,7 @@ __global__ void k_dense_refine_scan(RefineArgs A) {
   int64_t run = incl - own + (warp ? wsum[warp - 1] : 0);
   for (int64_t i = b; i < e; ++i) {
     A.off[i] = run;
-    run += refine_items(A.count[i], A.k);
+    run += refine_items(A.count[i], A.k, A.unit);
   }
   if (tid == (int)blockDim.x - 1) A.off[A.nq] = run;
 }
@@ -530,12 +534,82 @@ __global__ void k_dense_refine_cut(RefineArgs A) {
   if (lane == 0) A.count[ql] = kept;
 }
 
-// Exact values of the candidates, one warp per query (lane t values
-// candidates t, t + 32, ...).
-__global__ void k_dense_values(int method, int mode, int32_t d, const double* x64, const double* u64,
-                               const double* qx64, const double* qu64, const float* S, int64_t ldS,
-                               const float* norm2, const float* qnorm2, const int32_t* cand,
-                               const int32_t* count, int cap, int64_t q0, int64_t nq, double* out) {
+// Exact values of the candidates after the FP32 cut, over the flat list of
+// every candidate (k_dense_refine_scan with unit 1): lane l of a warp values
+// candidate base + l with the reference's sequential FP64 loop, so every lane
+// of the FP64 pipe works whatever the queries' counts.  The rows are read 32
+// elements at a time, coalesced, through a shared-memory tile.
+constexpr int VW = 4;        // warps per block
+
+__global__ void __launch_bounds__(VW * 32) k_dense_values_flat(int method, int32_t d, const double* rv,
+                                                               const double* qv, const int32_t* cand,
+                                                               int cap, int64_t q0, int64_t nq,
+                                                               const int64_t* off, double* out) {
+  __shared__ double tile[VW][32][33];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * VW;
+  const int64_t total = off[nq];
+  const bool cosine = (method == COSINE);
+  for (int64_t base = ((int64_t)blockIdx.x * VW + warp) * 32; base < total; base += warps * 32) {
+    const int64_t f = base + lane;
+    const int nv = (int)((total - base) < 32 ? (total - base) : 32);
+    int64_t ql = 0, slot = 0;
+    int32_t r = 0;
+    if (lane < nv) {
+      int64_t lo = 0, hi = nq;                       // off[lo] <= f < off[hi]
+      while (hi - lo > 1) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (__ldg(off + mid) <= f) lo = mid;
+        else hi = mid;
+      }
+      ql = lo;
+      slot = ql * cap + (f - __ldg(off + ql));
+      r = cand[slot];
+    }
+    const double* b = qv + (q0 + ql) * d;
+    double acc = 0.0;
+    for (int32_t k0 = 0; k0 < d; k0 += 32) {
+      const int kn = (d - k0) < 32 ? (d - k0) : 32;
+#pragma unroll 8
+      for (int j = 0; j < nv; ++j) {
+        const int32_t rj = __shfl_sync(0xffffffffu, r, j);
+        if (lane < kn) tile[warp][j][lane] = rv[(int64_t)rj * d + k0 + lane];
+      }
+      __syncwarp();
+      if (lane < nv) {
+        // unit_dot (src/sparseDist.cpp:287-331) / fastEuclidean2's pair loop
+        // (src/sparseDist.cpp:855-871), reference column first, ascending rows
+        for (int t = 0; t < kn; ++t) {
+          const double a = tile[warp][lane][t], bv = b[k0 + t];
+          if (cosine) {
+            acc = __dadd_rn(acc, __dmul_rn(a, bv));
+          } else {
+            const double diff = __dsub_rn(a, bv);
+            acc = __dadd_rn(acc, __dmul_rn(diff, diff));
+          }
+        }
+      }
+      __syncwarp();
+    }
+    if (lane < nv) {
+      if (cosine) {
+        double c = acc;
+        if (!(c == c)) c = 0.0;
+        else if (c > 1.0) c = 1.0;
+        else if (c < -1.0) c = -1.0;
+        out[slot] = __dsub_rn(1.0, c);
+      } else {
+        out[slot] = sqrt(acc);
+      }
+    }
+  }
+}
+
+// The plain mode's values (no exact re-rank): the FP32 slab values as
+// distances, one warp per query.
+__global__ void k_dense_values_plain(int method, const float* S, int64_t ldS, const float* norm2,
+                                     const float* qnorm2, const int32_t* cand, const int32_t* count, int cap,
+                                     int64_t q0, int64_t nq, double* out) {
   const int64_t ql = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
   if (ql >= nq) return;
   const int lane = threadIdx.x & 31;
@@ -543,34 +617,9 @@ __global__ void k_dense_values(int method, int mode, int32_t d, const double* x6
   const int64_t q = q0 + ql;
   for (int t = lane; t < c; t += 32) {
     const int64_t s = ql * cap + t, r = cand[s];
-    if (mode == 1) {
-      const float sv = S[ql * ldS + r];
-      out[s] = (method == COSINE) ? (double)(1.f - fminf(1.f, fmaxf(-1.f, sv)))
-                                  : (double)sqrtf(fmaxf(0.f, qnorm2[q] + norm2[r] - 2.f * sv));
-      continue;
-    }
-    if (method == COSINE) {
-      // unit_dot / unit_cosine (src/sparseDist.cpp:287-331), reference column first
-      const double* a = u64 + r * d;
-      const double* b = qu64 + q * d;
-      double acc = 0.0;
-      for (int32_t k = 0; k < d; ++k) acc = __dadd_rn(acc, __dmul_rn(a[k], b[k]));
-      double cv = acc;
-      if (!(cv == cv)) cv = 0.0;
-      else if (cv > 1.0) cv = 1.0;
-      else if (cv < -1.0) cv = -1.0;
-      out[s] = __dsub_rn(1.0, cv);
-    } else {
-      // fastEuclidean2's pair loop with every row stored (src/sparseDist.cpp:855-871)
-      const double* a = x64 + r * d;
-      const double* b = qx64 + q * d;
-      double num = 0.0;
-      for (int32_t k = 0; k < d; ++k) {
-        const double diff = __dsub_rn(a[k], b[k]);
-        num = __dadd_rn(num, __dmul_rn(diff, diff));
-      }
-      out[s] = sqrt(num);
-    }
+    const float sv = S[ql * ldS + r];
+    out[s] = (method == COSINE) ? (double)(1.f - fminf(1.f, fmaxf(-1.f, sv)))
+                                : (double)sqrtf(fmaxf(0.f, qnorm2[q] + norm2[r] - 2.f * sv));
   }
 }
 
@@ -836,6 +885,7 @@ int dense_search(sdg_ctx* ctx, const sdg_dense* Q, int64_t q0, int64_t nq, const
       R.q0 = c0; R.nq = nb; R.cap = cap; R.cand = cand; R.count = count;
       R.sv = reinterpret_cast<float*>(vals);          // free until the exact values are written
       R.off = off;
+      R.unit = RG;
       k_dense_refine_scan<<<1, 1024, 0, s>>>(R);
       static int dot_blocks = 0;                      // persistent: every block resident at once
       if (!dot_blocks) {
@@ -847,9 +897,22 @@ int dense_search(sdg_ctx* ctx, const sdg_dense* Q, int64_t q0, int64_t nq, const
       k_dense_refine_dot<<<dot_blocks, 128, 0, s>>>(R);
       const size_t rsm = sizeof(float) * (size_t)RW * k;   // <= 32 KB (k <= kMaxK here)
       k_dense_refine_cut<<<blocks_for(nb, RW), RW * 32, rsm, s>>>(R);
+      R.unit = 1;
+      k_dense_refine_scan<<<1, 1024, 0, s>>>(R);
+      static int val_blocks = 0;                      // persistent: every block resident at once
+      if (!val_blocks) {
+        int per_sm = 0, sms = 0;
+        DK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dense_values_flat, VW * 32, 0));
+        DK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, D->device));
+        val_blocks = std::max(1, per_sm * sms);
+      }
+      const bool cos = (method == COSINE);
+      k_dense_values_flat<<<val_blocks, VW * 32, 0, s>>>(method, D->d, cos ? D->u64 : D->x64, cos ? Q->u64 : Q->x64,
+                                                         cand, cap, c0, nb, off, vals);
+    } else {
+      k_dense_values_plain<<<blocks_for(nb, 8), 256, 0, s>>>(method, S, ldS, D->norm2, Q->norm2, cand, count, cap,
+                                                             c0, nb, vals);
     }
-    k_dense_values<<<blocks_for(nb, 8), 256, 0, s>>>(method, smode, D->d, D->x64, D->u64, Q->x64, Q->u64, S, ldS,
-                                                     D->norm2, Q->norm2, cand, count, cap, c0, nb, vals);
     SelectArgs sa;
     sa.vals = vals; sa.seg_stride = cap; sa.elem_stride = 1; sa.nseg = nb;
     sa.cand = cand; sa.cand_count = count; sa.cand_ld = cap;
@@ -896,10 +959,11 @@ int dense_search(sdg_ctx* ctx, const sdg_dense* Q, int64_t q0, int64_t nq, const
   DK(cudaStreamSynchronize(s));
   ctx_add_overflow(ctx, (int64_t)overflow.size());
   // kernels per chunk: the screen (fused: key init, weights, k_dense_tc, merge;
-  // slab: the GEMM, segtop, thresh, keep, overflow), the FP32 cut, the exact
-  // values and the selection; two more per overflowing query
+  // slab: the GEMM, segtop, thresh, keep, overflow), the FP32 cut (scan, dot,
+  // cut) and the scan of the exact values, the exact values and the
+  // selection; two more per overflowing query
   const int64_t chunks = (nq + chunk - 1) / chunk;
-  ctx_stats_add(ctx, 3, chunks * ((fused ? 4 : 5) + (smode == 0 ? 3 : 0) + 2) + 2 * (int64_t)overflow.size());
+  ctx_stats_add(ctx, 3, chunks * ((fused ? 4 : 5) + (smode == 0 ? 4 : 0) + 2) + 2 * (int64_t)overflow.size());
   return SDG_OK;
 }
 
