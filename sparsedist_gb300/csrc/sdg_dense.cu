@@ -666,7 +666,12 @@ namespace {
 // squares and degenerate flags.  `async` takes the buffers from the stream's
 // pool (a per-request query matrix) instead of cudaMalloc (a resident
 // reference); `blas` creates the cuBLAS handle of the slab and plain modes.
-int dense_build(sdg_ctx* ctx, const float* X, int32_t d, int64_t n, bool async, bool blas, sdg_dense** out) {
+// keep_err (stream-ordered builds only): instead of reading the finiteness
+// flag back (a stream synchronisation), hand the device flag to the caller,
+// who reads it with its own results and frees it; n_empty is then not counted
+// (a query block needs only the device flags).
+int dense_build(sdg_ctx* ctx, const float* X, int32_t d, int64_t n, bool async, bool blas, sdg_dense** out,
+                int** keep_err = nullptr) {
   cudaStream_t s = ctx_stream(ctx);
   DK(cudaSetDevice(ctx_device(ctx)));
   auto D = new sdg_dense();
@@ -722,6 +727,12 @@ int dense_build(sdg_ctx* ctx, const float* X, int32_t d, int64_t n, bool async, 
                           cudaMemcpyDeviceToDevice, s));
   }
   chk(cudaGetLastError());
+  if (keep_err && async) {
+    if (e != cudaSuccess) { cudaFreeAsync(err, s); sdg_dense_free(D); return cuda_fail(e); }
+    *keep_err = err;
+    *out = D;
+    return SDG_OK;
+  }
   int herr = 0;
   std::vector<uint8_t> he((size_t)n);
   chk(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -743,9 +754,12 @@ int dense_build(sdg_ctx* ctx, const float* X, int32_t d, int64_t n, bool async, 
 // Rows q0 .. q0+nq-1 (query columns of Q) of sparseKNN(Q, R, k, method) with
 // drop_degenerate = TRUE: the self-search with include_self = FALSE when self
 // (Q is R), else the two-matrix search.  See sdg_dense_knn_block for modes.
+// build_err: the query build's device finiteness flag (dense_build's
+// keep_err), read back with the first chunk's counts; NULL when the queries
+// were checked already.
 int dense_search(sdg_ctx* ctx, const sdg_dense* Q, int64_t q0, int64_t nq, const sdg_dense* D, bool self,
                  int method, int k, int mode, int32_t* idx, double* dist_out, int device_out, int* k_eff,
-                 int* flags) {
+                 int* flags, const int* build_err = nullptr) {
   if (!ctx || !Q || !D || !idx || !dist_out || !k_eff || !flags) return fail_with(SDG_E_ARG, "NULL argument");
   if (method != COSINE && method != EUCLIDEAN) return fail_with(SDG_E_UNSUPPORTED, "dense kNN supports cosine and euclidean");
   if (mode < 0 || mode > 3)
@@ -795,7 +809,10 @@ int dense_search(sdg_ctx* ctx, const sdg_dense* Q, int64_t q0, int64_t nq, const
       DK(cudaFreeAsync(o_val, s));
     }
     DK(cudaFreeAsync(row, s));
+    int h_build = 0;
+    if (build_err) DK(cudaMemcpyAsync(&h_build, build_err, sizeof(int), cudaMemcpyDeviceToHost, s));
     DK(cudaStreamSynchronize(s));
+    if (h_build) return fail_with(SDG_E_NONFINITE, "Cosine requires finite input (found NA, NaN or Inf).");
     ctx_stats_add(ctx, 1, n * nq);
     ctx_stats_add(ctx, 3, 2 * nq);
     return SDG_OK;
@@ -814,6 +831,7 @@ int dense_search(sdg_ctx* ctx, const sdg_dense* Q, int64_t q0, int64_t nq, const
   float *segtop = nullptr, *cut = nullptr;
   int32_t *cand = nullptr, *count = nullptr, *over = nullptr, *o_idx = idx;
   int64_t* off = nullptr;
+  int* tc_status = nullptr;                            // the fused screen's wait status (0 = ok)
   double *vals = nullptr, *o_val = dist_out, *row = nullptr;
   if (!fused) {
     DK(cudaMallocAsync(&S, sizeof(float) * (size_t)(chunk * ldS), s));
@@ -825,6 +843,10 @@ int dense_search(sdg_ctx* ctx, const sdg_dense* Q, int64_t q0, int64_t nq, const
   DK(cudaMallocAsync(&over, sizeof(int32_t) * (size_t)chunk, s));
   DK(cudaMallocAsync(&vals, sizeof(double) * (size_t)(chunk * cap), s));
   if (smode == 0) DK(cudaMallocAsync(&off, sizeof(int64_t) * (size_t)(chunk + 1), s));
+  if (fused) {
+    DK(cudaMallocAsync(&tc_status, sizeof(int), s));
+    DK(cudaMemsetAsync(tc_status, 0, sizeof(int), s));
+  }
   if (!device_out) {
     DK(cudaMallocAsync(&o_idx, sizeof(int32_t) * (size_t)(nq * k), s));
     DK(cudaMallocAsync(&o_val, sizeof(double) * (size_t)(nq * k), s));
@@ -842,7 +864,7 @@ int dense_search(sdg_ctx* ctx, const sdg_dense* Q, int64_t q0, int64_t nq, const
   for (int64_t c0 = q0; c0 < q0 + nq; c0 += chunk) {
     const int64_t nb = std::min(chunk, q0 + nq - c0);
     if (fused) {
-      const int st = tc_screen(ctx, Q, D, self, method, k, c0, nb, cand, count, over, cap, s, mode == 3);
+      const int st = tc_screen(ctx, Q, D, self, method, k, c0, nb, cand, count, over, cap, s, mode == 3, tc_status);
       if (st != SDG_OK) return st;
       ctx_stats_add(ctx, 6, 2 * (int64_t)D->dpad * n * nb);
     } else {
@@ -922,9 +944,23 @@ int dense_search(sdg_ctx* ctx, const sdg_dense* Q, int64_t q0, int64_t nq, const
     launch_select(sa, s);
     DK(cudaGetLastError());
     std::vector<int32_t> h_over((size_t)nb), h_count((size_t)nb);
+    int h_status = 0, h_build = 0;
     DK(cudaMemcpyAsync(h_over.data(), over, sizeof(int32_t) * nb, cudaMemcpyDeviceToHost, s));
     DK(cudaMemcpyAsync(h_count.data(), count, sizeof(int32_t) * nb, cudaMemcpyDeviceToHost, s));
+    if (tc_status) DK(cudaMemcpyAsync(&h_status, tc_status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (build_err) DK(cudaMemcpyAsync(&h_build, build_err, sizeof(int), cudaMemcpyDeviceToHost, s));
     DK(cudaStreamSynchronize(s));
+    if (h_build || h_status) {
+      // the flags were raised before this chunk's kernels ran on the results;
+      // nothing is returned
+      for (void* p : {(void*)S, (void*)segtop, (void*)cut, (void*)cand, (void*)count, (void*)over, (void*)vals,
+                      (void*)off, (void*)tc_status, (void*)(device_out ? nullptr : o_idx),
+                      (void*)(device_out ? nullptr : o_val)})
+        if (p) cudaFreeAsync(p, s);
+      cudaStreamSynchronize(s);
+      if (h_build) return fail_with(SDG_E_NONFINITE, "Cosine requires finite input (found NA, NaN or Inf).");
+      return fail_with(SDG_E_CUDA, "tensor-core screen: a pipeline wait timed out");
+    }
     for (int64_t t = 0; t < nb; ++t) {
       if (h_over[(size_t)t]) overflow.push_back(c0 + t);
       ctx_stats_add(ctx, 1, h_over[(size_t)t] ? n : h_count[(size_t)t]);   // pairs valued exactly
@@ -954,6 +990,7 @@ int dense_search(sdg_ctx* ctx, const sdg_dense* Q, int64_t q0, int64_t nq, const
   DK(cudaFreeAsync(cand, s)); DK(cudaFreeAsync(count, s));
   DK(cudaFreeAsync(over, s)); DK(cudaFreeAsync(vals, s));
   if (off) DK(cudaFreeAsync(off, s));
+  if (tc_status) DK(cudaFreeAsync(tc_status, s));
   if (row) DK(cudaFreeAsync(row, s));
   if (!device_out) { DK(cudaFreeAsync(o_idx, s)); DK(cudaFreeAsync(o_val, s)); }
   DK(cudaStreamSynchronize(s));
@@ -987,10 +1024,20 @@ int dense_query(sdg_ctx* ctx, const sdg_dense* D, const float* Q, int32_t d, int
   if (d != D->d) return fail_with(SDG_E_ROWS, "'X' and 'Y' must have the same number of rows.");
   if (nq < 1) return fail_with(SDG_E_ARG, "'X' must have at least one column.");
   sdg_dense* QD = nullptr;
-  int st = dense_build(ctx, Q, d, nq, true, false, &QD);
+  int* berr = nullptr;
+  int st = dense_build(ctx, Q, d, nq, true, false, &QD, &berr);
   if (st != SDG_OK) return st;
-  st = dense_search(ctx, QD, 0, nq, D, false, method, k, mode, idx, dist_out, device_out, k_eff, flags);
+  st = dense_search(ctx, QD, 0, nq, D, false, method, k, mode, idx, dist_out, device_out, k_eff, flags, berr);
   if (st == SDG_OK) ctx_stats_add(ctx, 3, 4);        // the query block's prep, unit columns, cast, error norms
+  if (st != SDG_OK && st != SDG_E_NONFINITE) {
+    // an argument error found before the flag was read: non-finite input
+    // still takes precedence, as when the build checked it at once
+    int h = 0;
+    if (cudaMemcpyAsync(&h, berr, sizeof(int), cudaMemcpyDeviceToHost, QD->stream) == cudaSuccess &&
+        cudaStreamSynchronize(QD->stream) == cudaSuccess && h)
+      st = fail_with(SDG_E_NONFINITE, "Cosine requires finite input (found NA, NaN or Inf).");
+  }
+  cudaFreeAsync(berr, QD->stream);
   sdg_dense_free(QD);
   return st;
 }

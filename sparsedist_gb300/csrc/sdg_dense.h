@@ -75,9 +75,11 @@ __device__ __forceinline__ float dense_cut(float T) {
 // and each query's own column is skipped).
 bool tc_screen_supported(const sdg_dense* D, int method, int k);
 // allow_pairs: run CTA pairs (cta_group::2, M = 256) where the block has more
-// than one 128-query group; otherwise one CTA per query group
+// than one 128-query group; otherwise one CTA per query group.  status: a
+// device int that a pipeline wait which ran out sets to 1; the call returns
+// without synchronising and the caller reads it with the results.
 int tc_screen(sdg_ctx* ctx, const sdg_dense* Q, const sdg_dense* D, bool self, int method, int k, int64_t q0,
               int64_t nq, int32_t* cand, int32_t* count, int32_t* over, int cap, cudaStream_t s,
-              bool allow_pairs);
+              bool allow_pairs, int* status);
 
 }  // namespace sdg

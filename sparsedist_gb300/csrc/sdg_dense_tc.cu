@@ -782,7 +782,8 @@ bool tc_screen_supported(const sdg_dense* R, int method, int k) {
 }
 
 int tc_screen(sdg_ctx* ctx, const sdg_dense* Q, const sdg_dense* D, bool self, int method, int k, int64_t q0,
-              int64_t nq, int32_t* cand, int32_t* count, int32_t* over, int cap, cudaStream_t s, bool allow_pairs) {
+              int64_t nq, int32_t* cand, int32_t* count, int32_t* over, int cap, cudaStream_t s, bool allow_pairs,
+              int* status) {
   EncodeTiledFn enc = encode_fn();
   if (!enc) return fail(SDG_E_CUDA, "cuTensorMapEncodeTiled is unavailable");
   if (Q->dpad != D->dpad || Q->n >= (int64_t)1 << 30) return fail(SDG_E_ARG, "query and reference shapes differ");
@@ -858,7 +859,6 @@ int tc_screen(sdg_ctx* ctx, const sdg_dense* Q, const sdg_dense* D, bool self, i
   float *w = nullptr, *lists = nullptr, *es = nullptr, *cand_s = nullptr;
   int32_t *ecount = nullptr, *eidx = nullptr;
   unsigned* tshared = nullptr;
-  int* status = nullptr;
   cudaError_t e = cudaSuccess;
   auto chk = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
   const int64_t nw = ntiles * BN;
@@ -868,10 +868,8 @@ int tc_screen(sdg_ctx* ctx, const sdg_dense* Q, const sdg_dense* D, bool self, i
   chk(cudaMallocAsync(&eidx, sizeof(int32_t) * (size_t)(nq * nslots * ecap), s));
   chk(cudaMallocAsync(&es, sizeof(float) * (size_t)(nq * nslots * ecap), s));
   chk(cudaMallocAsync(&cand_s, sizeof(float) * (size_t)(nq * cap), s));
-  chk(cudaMallocAsync(&status, sizeof(int), s));
   chk(cudaMallocAsync(&tshared, sizeof(unsigned) * (size_t)nq, s));
   if (e == cudaSuccess) {
-    chk(cudaMemsetAsync(status, 0, sizeof(int), s));
     // every query's shared key starts at fkey(-inf)
     k_tc_key_init<<<(unsigned)((nq + 255) / 256), 256, 0, s>>>(nq, tshared);
     chk(cudaMemsetAsync(ecount, 0, sizeof(int32_t) * (size_t)(nq * nslots), s));
@@ -917,17 +915,13 @@ int tc_screen(sdg_ctx* ctx, const sdg_dense* Q, const sdg_dense* D, bool self, i
     k_tc_merge<<<(unsigned)((nq + MW - 1) / MW), MW * 32, 0, s>>>(M);
     chk(cudaGetLastError());
   }
-  int hstatus = 0;
-  if (e == cudaSuccess) chk(cudaMemcpyAsync(&hstatus, status, sizeof(int), cudaMemcpyDeviceToHost, s));
-  if (e == cudaSuccess) chk(cudaStreamSynchronize(s));
-  for (void* p : {(void*)w, (void*)lists, (void*)ecount, (void*)eidx, (void*)es, (void*)cand_s, (void*)status,
-                  (void*)tshared})
+  // stream-ordered frees: the caller reads *status with its own results
+  for (void* p : {(void*)w, (void*)lists, (void*)ecount, (void*)eidx, (void*)es, (void*)cand_s, (void*)tshared})
     if (p) cudaFreeAsync(p, s);
   if (e != cudaSuccess) {
     set_error(cudaGetErrorString(e));
     return e == cudaErrorMemoryAllocation ? SDG_E_NOMEM : SDG_E_CUDA;
   }
-  if (hstatus) return fail(SDG_E_CUDA, "tensor-core screen: a pipeline wait timed out");
   return SDG_OK;
 }
 

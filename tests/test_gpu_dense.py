@@ -175,6 +175,34 @@ def test_fp32_cut_near_ties_equal_oracle(method, code, mode):
     torch.cuda.synchronize()
 
 
+@pytest.mark.parametrize("k,mode", [(10, 0), (10, 3), (10, 2), (1100, 0), (0, 0)])
+def test_nonfinite_query_block_fails_and_context_recovers(k, mode):
+    """A query block holding a NaN (or an Inf) fails with SDG_E_NONFINITE and
+    returns nothing, whatever the path: the fused screen (the build's
+    finiteness flag is read with the first chunk's counts), the slab screen,
+    the exact rows of k > 1,024, and an argument error (k = 0) found before
+    the flag was read; the next query on the same context is exact."""
+    import ctypes as C
+    import torch
+    from sparsedist_gb300 import _lib, synth
+    d, n, nq = 64, 5000, 200
+    X = synth.dense_embeddings(d=d, n=n, centres=20, seed=11)
+    ctx = _lib.Context()
+    h = C.c_void_p()
+    _lib.check(ctx.lib.sdg_dense_upload(ctx.handle, X.data_ptr(), d, n, C.byref(h)))
+    Q = np.ascontiguousarray(synth.dense_embeddings(d=d, n=nq, centres=20, seed=12).cpu().numpy())
+    bad = Q.copy()
+    bad[57, 3] = np.nan if k != 1100 else np.inf
+    with pytest.raises(_lib.SdgError) as ei:
+        dense_query(ctx, h, bad, 1, k, mode)
+    assert ei.value.code == -2                      # SDG_E_NONFINITE
+    got = dense_query(ctx, h, Q, 1, 10, mode)
+    ctx.lib.sdg_dense_free(h)
+    want = OracleBackend().knn(as_csc(torch.from_numpy(Q)), as_csc(X), k=10, method="cosine")
+    assert same_bits(got[0], want[0]) and same_bits(got[1], want[1])
+    torch.cuda.synchronize()
+
+
 @pytest.mark.parametrize("mode", [0, 2])
 def test_unit_columns_of_wide_ragged_columns_equal_oracle(mode):
     """The dense unit columns (unit_csc's recurrence, 8 and 32 columns per
