@@ -1,14 +1,17 @@
-// sdg_dense.cu -- kNN over dense embedding columns (d <= 256 FP32 embeddings).
+// sdg_dense.cu -- kNN over dense embedding columns (FP32 embeddings, d x n).
 //
 // Columns are dense (d values each).  A cosine / euclidean slab between
 // dense columns is a true contraction, so the screen runs on the tensor
-// cores: BF16 GEMM tiles with FP32 accumulation (cuBLAS GemmEx) write the
-// screen slab S[q][r] = <col q, col r>; the select kernel keeps every
-// reference whose optimistic bound reaches the k-th pessimistic bound (the
-// BF16 rounding bound below); the kept pairs are re-ranked in exact FP64 with
-// the reference's arithmetic (unit_csc normalisation and a sequential dot for
-// cosine, a sequential sum of squared differences for euclidean), so the
-// returned idx and distances are those of sparseKNN on the same data.
+// cores: the fused tcgen05 kernel of sdg_dense_tc.cu (modes 0 and 3), or
+// BF16 GEMM tiles with FP32 accumulation (cuBLAS GemmEx, mode 2) that write
+// the screen slab S[q][r] = <col q, col r> for the segmented selection here.
+// Either keeps every reference whose optimistic bound reaches the k-th
+// pessimistic bound (the BF16 rounding bound below); an FP32 cut with a
+// rigorous bound (k_dense_refine_*) leaves about k of them per query, and
+// those are valued in exact FP64 with the reference's arithmetic (unit_csc
+// normalisation and a sequential dot for cosine, a sequential sum of squared
+// differences for euclidean), so the returned idx and distances are those of
+// sparseKNN on the same data.
 //
 // The plain path (mode 1) is the FP32 baseline: an FP32 SGEMM on the CUDA
 // cores and the top-k taken directly on the FP32 values (no re-rank).
