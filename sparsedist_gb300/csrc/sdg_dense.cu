@@ -860,6 +860,13 @@ int dense_search(sdg_ctx* ctx, const sdg_dense* Q, int64_t q0, int64_t nq, const
     blas_lock.lock();
     DB(cublasSetStream(D->blas, s));
   }
+  // stream-ordered frees of this call's buffers (the error returns below)
+  auto release_all = [&]() {
+    for (void* p : {(void*)S, (void*)segtop, (void*)cut, (void*)cand, (void*)count, (void*)over, (void*)vals,
+                    (void*)off, (void*)tc_status, (void*)(device_out ? nullptr : o_idx),
+                    (void*)(device_out ? nullptr : o_val)})
+      if (p) cudaFreeAsync(p, s);
+  };
   const float one = 1.f, zero = 0.f;
   std::vector<int64_t> overflow;
   ctx_stats_reset(ctx);
@@ -868,7 +875,7 @@ int dense_search(sdg_ctx* ctx, const sdg_dense* Q, int64_t q0, int64_t nq, const
     const int64_t nb = std::min(chunk, q0 + nq - c0);
     if (fused) {
       const int st = tc_screen(ctx, Q, D, self, method, k, c0, nb, cand, count, over, cap, s, mode == 3, tc_status);
-      if (st != SDG_OK) return st;
+      if (st != SDG_OK) { release_all(); return st; }
       ctx_stats_add(ctx, 6, 2 * (int64_t)D->dpad * n * nb);
     } else {
     // S (n x nb, column-major, leading dimension ldS) = R^T Q:
@@ -956,10 +963,7 @@ int dense_search(sdg_ctx* ctx, const sdg_dense* Q, int64_t q0, int64_t nq, const
     if (h_build || h_status) {
       // the flags were raised before this chunk's kernels ran on the results;
       // nothing is returned
-      for (void* p : {(void*)S, (void*)segtop, (void*)cut, (void*)cand, (void*)count, (void*)over, (void*)vals,
-                      (void*)off, (void*)tc_status, (void*)(device_out ? nullptr : o_idx),
-                      (void*)(device_out ? nullptr : o_val)})
-        if (p) cudaFreeAsync(p, s);
+      release_all();
       cudaStreamSynchronize(s);
       if (h_build) return fail_with(SDG_E_NONFINITE, "Cosine requires finite input (found NA, NaN or Inf).");
       return fail_with(SDG_E_CUDA, "tensor-core screen: a pipeline wait timed out");
