@@ -53,7 +53,7 @@ typedef enum {
   SDG_E_NOMEM = -5,        /* device or host allocation failed */
   SDG_E_INDEX = -6,        /* SNN index out of range */
   SDG_E_CUDA = -7,         /* CUDA runtime error */
-  SDG_E_UNSUPPORTED = -8,  /* outside this build's limits (message says which) */
+  SDG_E_UNSUPPORTED = -8,  /* outside the library's limits (message says which) */
   SDG_E_CANCELLED = -9     /* sdg_ctx_cancel() was called */
 } sdg_status;
 

@@ -1,7 +1,7 @@
 /*
  * sdg_oracle.c -- CPU oracle for the blocked exact-kNN path of sparseDist.
  *
- * TEST INFRASTRUCTURE ONLY: the checker that the GPU library is compared
+ * TEST INFRASTRUCTURE ONLY: the results that the GPU library is compared
  * against, and the scalar CPU baseline ("port") that bench.py times.  It is
  * never linked into, or called by, libsdgpu.so.
  *

@@ -5,12 +5,12 @@
  * plain C, the reference's column-pair distance slabs, the per-column top-k,
  * the running per-row top-k, the SNN overlap weights and the R orchestration
  * around them.  Only tests/, __graft_entry__.smoke() and bench.py's
- * cpu_baseline / --impl reference legs load it, as the checker or as the timed
+ * cpu_baseline / --impl reference legs load it, as the oracle or as the timed
  * CPU baseline.  The product (libsdgpu.so) never links or calls it.
  *
  * Pinning: binary, cosine, euclidean, manhattan, topKBlock, topKRowsAccum and
  * snnJaccard are checked bit-for-bit against the reference's own unmodified
- * C++ (compiled by oracle/build_ref.sh against a project-written API shim into
+ * C++ (compiled by oracle/build.py (build_ref) against a project-written API shim into
  * oracle/_ref/) and against the literal fixtures of the reference's tests.
  * pearson and js take their arithmetic from Armadillo (arma::cor, arma::accu),
  * a third-party dependency that the reference does not vendor or pin; for

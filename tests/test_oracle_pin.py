@@ -1,4 +1,4 @@
-"""Pins the CPU oracle before it is trusted as the checker:
+"""Pins the CPU oracle before the GPU results are compared with it:
 
 * against the committed outputs of the reference's own kernels
   (tests/golden, made by tests/golden/make_golden.py from oracle/_ref);
