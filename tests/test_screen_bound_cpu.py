@@ -445,3 +445,58 @@ def test_dense_fp32_cut_bound():
         worst = max(worst, _refine_cosine_case(vq, vr))
         worst = max(worst, _refine_euclid_case(vq * 3.0, vr * 3.0))
     assert worst < 1.0
+
+
+def _rd32(x):
+    """An FP32 value at or below the real x (round to nearest, then one step
+    down when that went up): the kernel's __fsub_rd / __fadd_rd stand-in."""
+    f = np.float32(x)
+    return f if float(f) <= x else np.nextafter(f, np.float32(-np.inf))
+
+
+def _ru32(x):
+    f = np.float32(x)
+    return f if float(f) >= x else np.nextafter(f, np.float32(np.inf))
+
+
+def _dense_cut32(T):
+    T = np.float32(T)
+    return np.float32(T - np.float32(np.float32(abs(T)) * np.float32(2.0 ** -21) + np.float32(1e-30)))
+
+
+def test_dense_fp32_cut_keeps_the_exact_top_k_with_near_ties():
+    """k_dense_refine_cut's selection on candidates the FP32 products cannot
+    separate: 150 references at relative offsets 2^-25 .. 2^-12 from the
+    query and 4 exact copies (distance ties broken by index); T3 = the k-th
+    largest lower bound, every candidate with hi >= dense_cut(T3) kept.  Every
+    reference whose FP64 distance is at most the k-th smallest must be kept."""
+    rng = np.random.default_rng(31)
+    d, k = 256, 20
+    C = _refine_constant(True, d)
+    for trial in range(3):
+        q = rng.standard_normal(d)
+        R = [q * (1 + s * rng.standard_normal(d)) for s in np.exp2(rng.uniform(-25, -12, 150))]
+        R += [q.copy() for _ in range(4)]
+        R += [rng.standard_normal(d) for _ in range(30)]
+        R = np.asarray(R, np.float32).astype(np.float64)          # FP32 inputs, as the dense path takes
+        q = q.astype(np.float32).astype(np.float64)
+        uq = q / np.linalg.norm(q)
+        U = R / np.linalg.norm(R, axis=1)[:, None]
+        bq = _bf16(uq)
+        Nq = ru32(ru32(np.linalg.norm(bq) * (1 + 1e-12)) + ru32(np.linalg.norm(uq - bq) * (1 + 1e-12)))
+        lo, hi, dist = [], [], []
+        for ur in U:
+            c = _seq64(ur, uq, False)
+            dist.append(1.0 - min(1.0, max(-1.0, c)))
+            s = _warp_dot(ur.astype(np.float32), uq.astype(np.float32), False)
+            br = _bf16(ur)
+            Nr = ru32(ru32(np.linalg.norm(br) * (1 + 1e-12)) + ru32(np.linalg.norm(ur - br) * (1 + 1e-12)))
+            E = float(_ru32(C * float(_ru32(Nq * Nr)) + 1e-15))
+            lo.append(_rd32(s - E))
+            hi.append(_ru32(s + E))
+        lo, hi, dist = np.array(lo), np.array(hi), np.array(dist)
+        cut = _dense_cut32(np.sort(lo)[::-1][k - 1])
+        kept = hi >= cut
+        kth = np.sort(dist)[k - 1]
+        assert np.all(kept[dist <= kth]), trial
+        assert k <= kept.sum() < len(kept)                          # the unrelated references go
