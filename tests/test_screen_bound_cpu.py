@@ -500,3 +500,33 @@ def test_dense_fp32_cut_keeps_the_exact_top_k_with_near_ties():
         kth = np.sort(dist)[k - 1]
         assert np.all(kept[dist <= kth]), trial
         assert k <= kept.sum() < len(kept)                          # the unrelated references go
+
+
+def test_dense_fp32_cut_keeps_the_exact_top_k_euclidean():
+    """The same selection for euclidean: key -m with m the FP32 sum of squared
+    FP32 differences of the inputs, allowance C m + 1e-36; references at
+    relative offsets 2^-24 .. 2^-10 from the query, exact copies (distance 0,
+    ties) and unrelated references."""
+    rng = np.random.default_rng(37)
+    d, k = 256, 20
+    C = _refine_constant(False, d)
+    for trial in range(3):
+        q = (rng.standard_normal(d) * 3.0).astype(np.float32)
+        R = [q * (1 + s * rng.standard_normal(d)) for s in np.exp2(rng.uniform(-24, -10, 150))]
+        R += [q.copy() for _ in range(3)]
+        R += [rng.standard_normal(d) * 3.0 for _ in range(30)]
+        R = np.asarray(R, np.float32)
+        lo, hi, dist = [], [], []
+        for r in R:
+            num = _seq64(r.astype(np.float64), q.astype(np.float64), True)
+            dist.append(np.sqrt(num))
+            m = _warp_dot(r, q, True)
+            E = float(_ru32(C * m + 1e-36))
+            lo.append(_rd32(-m - E))
+            hi.append(_ru32(-m + E))
+        lo, hi, dist = np.array(lo), np.array(hi), np.array(dist)
+        cut = _dense_cut32(np.sort(lo)[::-1][k - 1])
+        kept = hi >= cut
+        kth = np.sort(dist)[k - 1]
+        assert np.all(kept[dist <= kth]), trial
+        assert k <= kept.sum() < len(kept)
