@@ -919,28 +919,20 @@ int dense_search(sdg_ctx* ctx, const sdg_dense* Q, int64_t q0, int64_t nq, const
       R.off = off;
       R.unit = RG;
       k_dense_refine_scan<<<1, 1024, 0, s>>>(R);
-      static int dot_blocks = 0;                      // persistent: every block resident at once
-      if (!dot_blocks) {
-        int per_sm = 0, sms = 0;
-        DK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dense_refine_dot, 128, 0));
-        DK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, D->device));
-        dot_blocks = std::max(1, per_sm * sms);
-      }
-      k_dense_refine_dot<<<dot_blocks, 128, 0, s>>>(R);
+      // persistent grids: every block resident at once on this device (asked
+      // per call: a host-side query, no state shared between threads)
+      int sms = 0, per_sm = 0;
+      DK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, D->device));
+      DK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dense_refine_dot, 128, 0));
+      k_dense_refine_dot<<<std::max(1, per_sm * sms), 128, 0, s>>>(R);
       const size_t rsm = sizeof(float) * (size_t)RW * k;   // <= 32 KB (k <= kMaxK here)
       k_dense_refine_cut<<<blocks_for(nb, RW), RW * 32, rsm, s>>>(R);
       R.unit = 1;
       k_dense_refine_scan<<<1, 1024, 0, s>>>(R);
-      static int val_blocks = 0;                      // persistent: every block resident at once
-      if (!val_blocks) {
-        int per_sm = 0, sms = 0;
-        DK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dense_values_flat, VW * 32, 0));
-        DK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, D->device));
-        val_blocks = std::max(1, per_sm * sms);
-      }
+      DK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dense_values_flat, VW * 32, 0));
       const bool cos = (method == COSINE);
-      k_dense_values_flat<<<val_blocks, VW * 32, 0, s>>>(method, D->d, cos ? D->u64 : D->x64, cos ? Q->u64 : Q->x64,
-                                                         cand, cap, c0, nb, off, vals);
+      k_dense_values_flat<<<std::max(1, per_sm * sms), VW * 32, 0, s>>>(
+          method, D->d, cos ? D->u64 : D->x64, cos ? Q->u64 : Q->x64, cand, cap, c0, nb, off, vals);
     } else {
       k_dense_values_plain<<<blocks_for(nb, 8), 256, 0, s>>>(method, S, ldS, D->norm2, Q->norm2, cand, count, cap,
                                                              c0, nb, vals);
