@@ -242,10 +242,10 @@ SDG_API int sdg_knn_resident(sdg_ctx* ctx, const sdg_matrix* X, const sdg_matrix
  * embedding.  sdg_dense_knn_block returns rows q0 .. q0+nq-1 of the
  * self-search sparseKNN(X, k, method) (include_self = FALSE,
  * drop_degenerate = TRUE) for cosine (dist) or euclidean.  mode 0: BF16
- * tensor-core screen with a rigorous bound and exact FP64 re-rank (the
- * reference's idx and distances), fused in one tcgen05 kernel (no slab in
- * HBM, one CTA per 128-query group) for k <= 64 and d <= 256, else as
- * mode 2; mode 3: the fused screen on CTA pairs (clusters of two CTAs sharing
+ * tensor-core screen with a rigorous bound, a second FP32 cut with a rigorous
+ * bound, and exact FP64 values of the survivors (the reference's idx and
+ * distances), the screen fused in one tcgen05 kernel (no slab in HBM, one
+ * CTA per 128-query group) for k <= 64 and d <= 256, else as mode 2; mode 3: the fused screen on CTA pairs (clusters of two CTAs sharing
  * cta_group::2 UMMAs of 256 queries; the same results) when the block has
  * more than 128 queries; mode 2: the same screen through a cuBLAS BF16 GEMM slab; mode 1:
  * the plain FP32 path (FP32 GEMM, top-k on FP32 values, no re-rank).  k above
@@ -264,8 +264,10 @@ SDG_API int sdg_dense_knn_block(sdg_ctx* ctx, const sdg_dense* D, int64_t q0, in
  * (drop_degenerate = TRUE; no self-exclusion, as in the reference's
  * two-matrix form, R/sparseKNN.R:183-301 with Y given).  Same modes, outputs
  * and clamp as sdg_dense_knn_block; idx are 1-based columns of D.  The
- * queries' FP64 / unit / BF16 forms are built on the context's stream from
- * its memory pool and released when the call returns. */
+ * queries' FP64 / unit / FP32 / BF16 forms are built on the context's stream
+ * from its memory pool and released when the call returns.  A non-finite
+ * query value fails the call with SDG_E_NONFINITE: host outputs are left
+ * untouched, device outputs (device_out) may hold partial values. */
 SDG_API int sdg_dense_knn_query(sdg_ctx* ctx, const sdg_dense* D, const float* Q, int32_t d, int64_t nq,
                                 int method, int k, int mode, int32_t* idx, double* dist_out,
                                 int device_out, int* k_eff, int* flags);
