@@ -266,8 +266,8 @@ SDG_API int sdg_dense_knn_block(sdg_ctx* ctx, const sdg_dense* D, int64_t q0, in
  * and clamp as sdg_dense_knn_block; idx are 1-based columns of D.  The
  * queries' FP64 / unit / FP32 / BF16 forms are built on the context's stream
  * from its memory pool and released when the call returns.  A non-finite
- * query value fails the call with SDG_E_NONFINITE: host outputs are left
- * untouched, device outputs (device_out) may hold partial values. */
+ * query value fails the call with SDG_E_NONFINITE (the outputs' contents are
+ * then unspecified). */
 SDG_API int sdg_dense_knn_query(sdg_ctx* ctx, const sdg_dense* D, const float* Q, int32_t d, int64_t nq,
                                 int method, int k, int mode, int32_t* idx, double* dist_out,
                                 int device_out, int* k_eff, int* flags);
